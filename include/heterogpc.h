@@ -1,0 +1,180 @@
+/*
+ * heterogpc.h -- C ABI of the GB300 PC-stable skeleton library (libheterogpc.so).
+ *
+ * PC-stable skeleton discovery with Gaussian (Fisher-z partial-correlation)
+ * conditional-independence tests on one GPU. Every entry point takes plain
+ * pointers and sizes, returns an hpc_status and never exits the process
+ * (the reference calls exit() on every CUDA error, src/util/cuda_util.cuh:28-50).
+ *
+ * Each function names the reference interface it replaces (paths are relative
+ * to the milanpro/Masterthesis-Heterogeneous-PC source tree).
+ *
+ * Threading: a context is used by one host thread at a time; all its work is
+ * ordered on the context's own CUDA stream.
+ */
+#ifndef HETEROGPC_H
+#define HETEROGPC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HPC_ABI_VERSION 1
+/* Highest conditioning-set size the kernels accept. */
+#define HPC_MAX_LEVEL 16
+
+typedef enum hpc_status {
+  HPC_OK = 0,
+  HPC_ERR_INVALID_ARG = 1, /* bad pointer, size or option */
+  HPC_ERR_OOM = 2,         /* device or host allocation failed */
+  HPC_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  HPC_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  HPC_ERR_NUMERIC = 5,     /* non-finite input where finite values are required */
+  HPC_ERR_STATE = 6,       /* call out of order (e.g. run before correlation) */
+  HPC_ERR_CAPACITY = 7,    /* a device work or record buffer would overflow */
+  HPC_ERR_NO_DEVICE = 8    /* no CUDA device / extension not usable */
+} hpc_status;
+
+typedef enum hpc_precision {
+  /* Plain path: FP64 correlation, every CI test in FP64. */
+  HPC_PREC_FP64 = 0,
+  /* FP64 correlation, CI tests in FP32; tests whose |z| lies within the margin
+   * of z_crit, and ill-conditioned or non-finite ones, are re-run in FP64. */
+  HPC_PREC_MIXED = 1,
+  /* Split-BF16 tensor-core Gram (FP32 accumulation) for the FP32 correlation,
+   * FP32 tests, FP64 re-tests on exact FP64 correlation entries computed on
+   * demand from the FP64-standardised data. */
+  HPC_PREC_MIXED_TC = 2
+} hpc_precision;
+
+typedef struct hpc_opts {
+  int device;            /* CUDA device ordinal (default 0) */
+  double alpha;          /* significance level; an edge is removed iff p >= alpha (default 0.05) */
+  int max_level;         /* highest level run; -1 = until no edge has enough neighbours (default 4) */
+  int precision;         /* hpc_precision (default HPC_PREC_MIXED) */
+  double retest_margin;  /* relative |z| band around z_crit re-tested in FP64 (default 1e-3) */
+  int ref_compat_sd;     /* 1: standard deviation rounded through float like src/correlation/corHelper.cu:75 */
+  int verbose;           /* 1: per-level lines on stdout */
+} hpc_opts;
+
+typedef struct hpc_level_stats {
+  int level;
+  int max_degree;             /* largest neighbour count at the level start */
+  int64_t rows;               /* rows with at least `level` neighbours */
+  int64_t potential_tests;    /* T_l = sum over directed edges of C(d_i - 1, l) */
+  int64_t executed_tests;     /* CI tests actually evaluated on the device */
+  int64_t retests;            /* tests re-run in FP64 (band, conditioning, non-finite) */
+  int64_t edges_before;       /* undirected edges at the level start */
+  int64_t edges_after;        /* undirected edges after the level */
+  double ms;                  /* device time of the level (compaction + tests), CUDA events */
+} hpc_level_stats;
+
+typedef struct hpc_sepset_record {
+  int32_t i, j;               /* i < j, the removed edge */
+  int32_t level;              /* conditioning-set size; 0 = marginal (reference marker -2) */
+  int32_t pad;
+  double pmax;                /* FP64 p-value of the removing test */
+  int32_t ids[HPC_MAX_LEVEL]; /* ascending separating variables, `level` of them */
+} hpc_sepset_record;
+
+typedef struct hpc_ctx hpc_ctx;
+
+/* ---- errors ------------------------------------------------------------ */
+/* Message for the last failing call on this host thread. */
+const char *hpc_last_error_string(void);
+/* Short name of a status code. */
+const char *hpc_status_string(hpc_status s);
+
+/* ---- context ------------------------------------------------------------
+ * Replaces MMState's constructor (src/util/state.cu:3-44, struct at
+ * src/util/state.cuh:29-56): all p x p state lives in device memory owned by
+ * the context, not in managed memory. */
+hpc_status hpc_opts_default(hpc_opts *opts);
+hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n_obs, const hpc_opts *opts);
+hpc_status hpc_ctx_destroy(hpc_ctx *ctx);
+/* Resets adjacency (complete graph minus diagonal) and separation sets, keeping
+ * the correlation matrix (src/util/state.cu:31-43). */
+hpc_status hpc_ctx_reset(hpc_ctx *ctx);
+/* Device bytes held by a context of this shape (admission control). */
+hpc_status hpc_ctx_footprint(int64_t p, int64_t n_obs, const hpc_opts *opts, int64_t *bytes);
+
+/* ---- correlation --------------------------------------------------------
+ * Replaces gpuPMCC(h_mat, n, dim, cors, deviceId, verbose)
+ * (src/correlation/corOwn.cuh:3, src/correlation/corOwn.cu:10-48).
+ * X is column-major n_obs x p (each variable's samples contiguous), exactly the
+ * arma::mat layout returned by CSVParser::read_csv_to_mat (src/util/csv_parser.cpp:64-77).
+ * Host pointers are copied to the device inside the call; *_device variants take
+ * device pointers already resident in HBM. */
+hpc_status hpc_correlation_f64(hpc_ctx *ctx, const double *X_host);
+hpc_status hpc_correlation_f32(hpc_ctx *ctx, const float *X_host);
+hpc_status hpc_correlation_device_f64(hpc_ctx *ctx, const double *X_dev);
+hpc_status hpc_correlation_device_f32(hpc_ctx *ctx, const float *X_dev);
+/* Replaces SkeletonCalculator::add_correlation_matrix's memcpy into state.cor
+ * (src/independence/skeleton.cpp:60-65). C is row-major p x p. */
+hpc_status hpc_load_correlation(hpc_ctx *ctx, const double *C_host);
+hpc_status hpc_load_correlation_device(hpc_ctx *ctx, const double *C_dev);
+/* Copies the FP64 correlation matrix (row-major p x p) to the host. */
+hpc_status hpc_get_correlation(hpc_ctx *ctx, double *C_host);
+
+/* ---- skeleton levels ----------------------------------------------------
+ * hpc_run_level replaces SkeletonCalculator::calcLevel (src/independence/skeleton.cpp:104-150):
+ * for level >= 1 it first snapshots the neighbour lists (callCompact,
+ * src/independence/compact.cu:91-99), then runs every CI test of the level
+ * (GPUExecutor::executeLevel, src/executor/gpuExecutor.cu:9-122, and the
+ * testRowL0/L1/LN kernels, src/executor/testing/gpuRowTests.cu) for any level,
+ * not only 0..3. Levels must be run in order 0, 1, 2, ...
+ * Returns HPC_OK with stats->potential_tests == 0 when no edge has enough neighbours. */
+hpc_status hpc_run_level(hpc_ctx *ctx, int level, hpc_level_stats *stats);
+/* Replaces SkeletonCalculator::run's level loop (src/independence/skeleton.cpp:152-190):
+ * levels 0..max_level (opts.max_level, -1 = until exhausted), stopping early once a
+ * level has no tests. `stats` receives up to `cap` per-level records. */
+hpc_status hpc_run_skeleton(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_run);
+
+/* ---- results ------------------------------------------------------------ */
+/* adj (row-major p x p, 1 = edge kept), the reference's state.adj. */
+hpc_status hpc_get_adjacency(hpc_ctx *ctx, uint8_t *adj_host);
+/* Number of undirected edges left (printSepsets' count, src/util/sepset_util.hpp:9-60). */
+hpc_status hpc_edge_count(hpc_ctx *ctx, int64_t *edges);
+/* Separation sets in the reference layout (src/util/state.cu:7,25 and
+ * src/executor/testing/cpuUtil.cpp:3-48): out[(i*p + j)*max_cond + k] for i < j,
+ * -1 = none, -2 in slot 0 = removed at level 0. out holds p*p*max_cond ints. */
+hpc_status hpc_get_sepsets(hpc_ctx *ctx, int32_t *out, int max_cond);
+/* Records of every edge removed at level >= 1 (level-0 removals are implied by
+ * the adjacency): *count receives the number available; at most cap are copied. */
+hpc_status hpc_get_sepset_records(hpc_ctx *ctx, hpc_sepset_record *out, int64_t cap, int64_t *count);
+
+/* ---- independence statistics (FP64) -------------------------------------
+ * Same semantics as CPU::calcPValue / CPU::pValL1 / CPU::pValLN
+ * (src/executor/independence/cpuInd.hpp:3-10, cpuInd.cpp:8-38). M is the
+ * row-major k x k correlation submatrix ordered (i, j, S...). These are the
+ * device FP64 re-test formulas compiled for the host, for callers of that API. */
+double hpc_calc_pvalue(double r, int n_obs);
+double hpc_pval_l1(double x1, double x2, double x3, int n_obs);
+double hpc_pval_ln(const double *M, int k, int n_obs);
+/* z_crit = Phi^-1(1 - alpha/2): p >= alpha  <=>  |z| <= z_crit. */
+double hpc_z_crit(double alpha);
+
+/* ---- synthetic data ------------------------------------------------------
+ * Seeded linear-Gaussian SEM (no reference counterpart; the reference reads
+ * CSV files only). Bit-identical output on every host. */
+typedef enum hpc_graph_kind { HPC_GRAPH_ER = 0, HPC_GRAPH_PA = 1 } hpc_graph_kind;
+typedef struct hpc_sem_params {
+  int64_t p, n;       /* variables, samples */
+  int graph;          /* hpc_graph_kind */
+  double degree;      /* ER: expected degree (edge probability degree/(p-1)) */
+  int pa_parents;     /* PA: parents per new node */
+  double w_lo, w_hi;  /* |weight| ~ U[w_lo, w_hi], random sign */
+  uint64_t seed;
+} hpc_sem_params;
+/* X (n x p column-major, FP64) and/or X32 (FP32 copy); dag (p x p, parent->child)
+ * and weights (p x p) optional; any output may be NULL. */
+hpc_status hpc_sem_generate(const hpc_sem_params *prm, double *X, float *X32, uint8_t *dag,
+                            double *weights);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HETEROGPC_H */

@@ -1,0 +1,298 @@
+// Level-l conditional-independence tests (l >= 1) on a persistent grid.
+//
+// Replaces testRowL1 / testRowLN<l+2,l> (src/executor/testing/gpuRowTests.cu:29-205),
+// their workstealing twins (src/executor/testing/gpuWorkstealingTests.cu) and the
+// CPU/GPU balancer (src/loadbalance/balancer.cpp): the reference launches one
+// 64-thread block per (row, neighbour slot) with grid y = the maximum degree and has
+// each thread unrank a subset and run a 30-iteration FP64 SVD in local memory.
+//
+// Here every test of the level is one index of a flattened space
+//   t in [0, T_l),  T_l = sum_i d_i * C(d_i - 1, l)
+// ordered by (row i, neighbour slot s, lexicographic subset rank). Warps claim
+// tiles of 32 * m consecutive tests with one atomicAdd on a device-wide counter;
+// each lane takes m consecutive tests, unranks its first subset once
+// (the order of ithCombination, src/util/cuda_util.cu:34-50) and then steps to
+// the lexicographic successor. Lanes stop testing an edge as soon as its live bit
+// is cleared (the reference's `adj == 0` early exit, gpuRowTests.cu:166-168).
+//
+// The partial correlation of (i, j) given S comes from a Cholesky factorisation
+// of the S block and forward solves for r_iS and r_jS:
+//   r = (r_ij - w_i . w_j) / sqrt((1 - |w_i|^2)(1 - |w_j|^2)),  w = L_S^-1 r_S.
+// In mixed precision this runs in FP32 on cor32; a test is decided in FP32 only
+// when |z| is outside the re-test band around z_crit (the configured relative
+// margin plus an error bound from the smallest pivot); every other test, and
+// every removal, is re-evaluated in FP64 on cor64 with the reference's formula
+// (closed form at l = 1 as cpuInd.cpp:16-27; pinv semantics at l >= 2 as
+// cpuInd.cpp:29-38: Cholesky when well conditioned, Jacobi pseudoinverse with
+// arma::pinv's tolerance otherwise). The decision is p >= alpha in FP64.
+//
+// Removal (src/executor/testing/cpuUtil.cpp:23-48, gpuRowTests.cu:172-201): the
+// lane clearing the (min, max) bit with atomicAnd owns the edge, clears the mirror
+// bit and appends one separation-set record.
+#include <cuda_runtime.h>
+
+#include "internal.cuh"
+#include "stats.cuh"
+
+namespace hpc {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, int64_t j) {
+  const volatile uint32_t *w = adj + i * W + (j >> 5);
+  return (*w >> (j & 31)) & 1u;
+}
+
+// FP64 p-value of the test (i, j | ids) with the reference's semantics.
+template <int LA>
+__device__ __noinline__ double exact_pvalue(const double *__restrict__ C, int64_t p, int n_obs, int64_t i, int64_t j,
+                                            const int *ids, int l) {
+  if (l == 1) return pval_l1_64(C[i * p + j], C[i * p + ids[0]], C[j * p + ids[0]], n_obs);
+  const int k = l + 2;
+  double M[(LA + 2) * (LA + 2)];
+  for (int q = 0; q < k * k; ++q) M[q] = 0.0;
+  for (int q = 0; q < k; ++q) M[q * k + q] = 1.0;
+  M[1] = M[k] = C[i * p + j];
+  for (int q = 2; q < k; ++q) {
+    M[q] = M[q * k] = C[i * p + ids[q - 2]];
+    M[k + q] = M[q * k + 1] = C[j * p + ids[q - 2]];
+  }
+  for (int r = 2; r < k; ++r)
+    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = C[(int64_t)ids[r - 2] * p + ids[c - 2]];
+  for (int q = 0; q < k * k; ++q)
+    if (isnan(M[q])) return nan("");  // cpuInd.cpp:31-33: NaN p-value, edge kept
+  // Cholesky of the S block (rows/cols 2..k-1), forward solves for x = M[0][S], y = M[1][S]
+  double Lm[LA * (LA + 1) / 2], wx[LA], wy[LA];
+  double dmin = 1.0;
+  for (int r = 0; r < l; ++r) {
+    for (int c = 0; c < r; ++c) {
+      double v = M[(c + 2) * k + (r + 2)];
+      for (int q = 0; q < c; ++q) v -= Lm[r * (r + 1) / 2 + q] * Lm[c * (c + 1) / 2 + q];
+      Lm[r * (r + 1) / 2 + c] = v / Lm[c * (c + 1) / 2 + c];
+    }
+    double d = 1.0;
+    for (int q = 0; q < r; ++q) d -= Lm[r * (r + 1) / 2 + q] * Lm[r * (r + 1) / 2 + q];
+    dmin = fmin(dmin, d);
+    if (!(d > 1e-10)) break;
+    const double lrr = sqrt(d);
+    Lm[r * (r + 1) / 2 + r] = lrr;
+    double vx = M[r + 2], vy = M[k + r + 2];
+    for (int q = 0; q < r; ++q) { vx -= Lm[r * (r + 1) / 2 + q] * wx[q]; vy -= Lm[r * (r + 1) / 2 + q] * wy[q]; }
+    wx[r] = vx / lrr;
+    wy[r] = vy / lrr;
+  }
+  double r_partial;
+  if (dmin > 1e-10) {
+    double ax = 1.0, ay = 1.0, b = M[1];
+    for (int q = 0; q < l; ++q) { ax -= wx[q] * wx[q]; ay -= wy[q] * wy[q]; b -= wx[q] * wy[q]; }
+    if (ax > 1e-10 && ay > 1e-10) {
+      r_partial = b / sqrt(ax * ay);
+      return calc_pvalue64(r_partial, n_obs);
+    }
+  }
+  // ill-conditioned: pseudoinverse semantics
+  double V[(LA + 2) * (LA + 2)];
+  double p00, p01, p11;
+  pinv_sym64_corner(M, k, V, &p00, &p01, &p11);
+  r_partial = -p01 / sqrt(p00 * p11);
+  return calc_pvalue64(r_partial, n_obs);
+}
+
+// FP32 test. Returns 1 = remove, 0 = keep, 2 = undecided (re-test in FP64).
+template <int LA>
+__device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l) {
+  const float *__restrict__ C = a.cor32;
+  const int64_t p = a.p;
+  const float rij = __ldg(C + i * p + j);
+  float Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1];
+  float invd[LA], wx[LA], wy[LA];
+  float dmin = 1.0f;
+  float sx = 0.f, sy = 0.f, sxy = 0.f;
+#pragma unroll
+  for (int r = 0; r < LA; ++r) {
+    if (r < l) {
+      const int idr = ids[r];
+      float vx = __ldg(C + i * p + idr);
+      float vy = __ldg(C + j * p + idr);
+      float d = 1.0f;
+#pragma unroll
+      for (int c = 0; c < LA; ++c) {
+        if (c < r) {
+          float v = __ldg(C + (int64_t)ids[c] * p + idr);
+#pragma unroll
+          for (int q = 0; q < LA; ++q)
+            if (q < c) v -= Lm[r * (r + 1) / 2 + q] * Lm[c * (c + 1) / 2 + q];
+          v *= invd[c];
+          Lm[r * (r + 1) / 2 + c] = v;
+          d -= v * v;
+          vx -= v * wx[c];
+          vy -= v * wy[c];
+        }
+      }
+      dmin = fminf(dmin, d);
+      float id = rsqrtf(fmaxf(d, 1e-30f));
+      invd[r] = id;
+      wx[r] = vx * id;
+      wy[r] = vy * id;
+      sx += wx[r] * wx[r];
+      sy += wy[r] * wy[r];
+      sxy += wx[r] * wy[r];
+    }
+  }
+  const float ax = 1.0f - sx, ay = 1.0f - sy;
+  const float cond = fminf(dmin, fminf(ax, ay));
+  if (!(cond > 1e-3f)) return 2;
+  const float r = (rij - sxy) * rsqrtf(ax * ay);
+  if (!isfinite(r)) return 2;
+  const float rr = fminf(fabsf(r), 0.9999999f);
+  const float z = (float)a.sqrt_n3 * atanhf(rr);
+  // error bound of z from the input rounding and the factorisation
+  const float er = (4.0f * a.eps_in + (float)(l + 2) * 2.4e-7f) / cond * (1.0f + rr);
+  const float ez = (float)a.sqrt_n3 * er / fmaxf(1.0f - rr * rr, 1e-6f);
+  if (fabsf(z - a.zc32) <= a.margin_abs + 8.0f * ez) return 2;
+  return z < a.zc32 ? 1 : 0;
+}
+
+__device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, int64_t p, unsigned long long t) {
+  // largest i with row_work[i] <= t (row_work is non-decreasing, row_work[p] > t)
+  int64_t lo = 0, hi = p;
+  while (hi - lo > 1) {
+    int64_t mid = (lo + hi) >> 1;
+    if (row_work[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void record_removal(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l, double pv) {
+  const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+  const uint32_t bit = 1u << (hi & 31);
+  const uint32_t old = atomicAnd(a.adj + lo * a.W + (hi >> 5), ~bit);
+  if (!(old & bit)) return;  // another lane removed it first
+  atomicAnd(a.adj + hi * a.W + (lo >> 5), ~(1u << (lo & 31)));
+  atomicAdd(&a.ctr->deleted, 1ull);
+  const unsigned long long slot = atomicAdd(&a.ctr->rec_count, 1ull);
+  if ((long long)slot >= a.rec_cap) {
+    atomicOr(&a.ctr->err, kErrRecOverflow);
+    return;
+  }
+  hpc_sepset_record *rec = a.recs + slot;
+  rec->i = (int32_t)lo;
+  rec->j = (int32_t)hi;
+  rec->level = l;
+  rec->pad = 0;
+  rec->pmax = pv;
+  for (int q = 0; q < HPC_MAX_LEVEL; ++q) rec->ids[q] = q < l ? ids[q] : -1;
+}
+
+template <int LT, bool MIXED>
+__global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
+  constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
+  const int l = LT > 0 ? LT : a.level;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long total = a.ctr->work_total;
+  const int m = a.tile_tests;
+  const unsigned long long per_tile = 32ull * (unsigned long long)m;
+  int pos[LA], ids[LA];
+  for (;;) {
+    unsigned long long tile = 0;
+    if (lane == 0) tile = atomicAdd(&a.ctr->tile_next, 1ull);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    const unsigned long long t0 = tile * per_tile;
+    if (t0 >= total) break;
+    unsigned long long t = t0 + (unsigned long long)lane * m;
+    const unsigned long long tend = min(t + (unsigned long long)m, total);
+    unsigned executed = 0, retests = 0;
+    if (t < tend) {
+      int64_t i = find_row(a.row_work, a.p, t);
+      int d = a.deg[i];
+      unsigned long long c = binom_sat(d - 1, l);
+      unsigned long long off = t - a.row_work[i];
+      int s = (int)(off / c);
+      unsigned long long rank = off - (unsigned long long)s * c;
+      int base = a.rowptr[i];
+      unrank_lex(rank, l, d - 1, pos);
+      int64_t j = a.colidx[base + s];
+      bool alive = live_bit(a.adj, a.W, i, j);
+      for (;;) {
+        if (alive) {
+#pragma unroll
+          for (int q = 0; q < LA; ++q)
+            if (q < l) ids[q] = a.colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
+          int res = 2;
+          if (MIXED) res = test_f32<LA>(a, i, j, ids, l);
+          ++executed;
+          if (res != 0) {
+            if (MIXED && res == 2) ++retests;
+            const double pv = exact_pvalue<LA>(a.cor64, a.p, a.n_obs, i, j, ids, l);
+            if (pv >= a.alpha) {
+              record_removal(a, i, j, ids, l, pv);
+              alive = false;
+            }
+          }
+        }
+        if (++t >= tend) break;
+        if (++rank == c) {
+          rank = 0;
+          if (++s == d) {
+            i = find_row(a.row_work, a.p, t);
+            d = a.deg[i];
+            c = binom_sat(d - 1, l);
+            base = a.rowptr[i];
+            s = 0;
+          }
+#pragma unroll
+          for (int q = 0; q < LA; ++q)
+            if (q < l) pos[q] = q;
+          j = a.colidx[base + s];
+          alive = live_bit(a.adj, a.W, i, j);
+        } else {
+          next_lex(l, d - 1, pos);
+          if (alive && (executed & 3u) == 0) alive = live_bit(a.adj, a.W, i, j);
+        }
+      }
+    }
+    executed = __reduce_add_sync(0xffffffffu, executed);
+    retests = __reduce_add_sync(0xffffffffu, retests);
+    if (lane == 0) {
+      if (executed) atomicAdd(&a.ctr->tests, (unsigned long long)executed);
+      if (retests) atomicAdd(&a.ctr->retests, (unsigned long long)retests);
+    }
+  }
+}
+
+template <bool MIXED>
+void *kernel_for(int level) {
+  switch (level) {
+    case 1: return (void *)citest_kernel<1, MIXED>;
+    case 2: return (void *)citest_kernel<2, MIXED>;
+    case 3: return (void *)citest_kernel<3, MIXED>;
+    case 4: return (void *)citest_kernel<4, MIXED>;
+    case 5: return (void *)citest_kernel<5, MIXED>;
+    case 6: return (void *)citest_kernel<6, MIXED>;
+    case 7: return (void *)citest_kernel<7, MIXED>;
+    case 8: return (void *)citest_kernel<8, MIXED>;
+    default: return (void *)citest_kernel<0, MIXED>;
+  }
+}
+
+}  // namespace
+
+int citest_grid(int precision, int level, int device) {
+  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(level) : kernel_for<true>(level);
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) sms = 1;
+  return per_sm * sms;
+}
+
+hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s) {
+  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(a.level) : kernel_for<true>(a.level);
+  LevelArgs args = a;
+  void *params[] = {&args};
+  HPC_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), params, 0, s));
+  return HPC_OK;
+}
+
+}  // namespace hpc

@@ -1,0 +1,576 @@
+// C ABI of libheterogpc: contexts, correlation entry points, the level loop and
+// result retrieval. The reference equivalents are named beside each function in
+// include/heterogpc.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+#include "stats.cuh"
+
+namespace hpc {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+hpc_status cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+  set_error("CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(e), cudaGetErrorString(e), what, file, line);
+  if (e == cudaErrorMemoryAllocation) return HPC_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return HPC_ERR_NO_DEVICE;
+  return HPC_ERR_CUDA;
+}
+
+namespace {
+
+// z with erfc(z / sqrt 2) == alpha, by bisection in FP64 (host set-up only)
+double z_crit_of(double alpha) {
+  double lo = 0.0, hi = 40.0;
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (std::erfc(mid / 1.41421356237309504880) >= alpha) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// |r| with calc_pvalue64(r) == alpha (p is decreasing in |r|)
+double r_crit_of(double alpha, int n) {
+  double lo = 0.0, hi = kCutThr;
+  if (calc_pvalue64(hi, n) >= alpha) return 2.0;  // every finite r is removed
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (calc_pvalue64(mid, n) >= alpha) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+template <typename T>
+hpc_status dev_alloc(T **ptr, int64_t count, const char *what) {
+  if (count <= 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (size_t)count);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    cudaGetLastError();
+    set_error("device allocation of %s (%lld bytes) failed: %s", what, (long long)(sizeof(T) * count),
+              cudaGetErrorString(e));
+    return HPC_ERR_OOM;
+  }
+  return HPC_OK;
+}
+
+template <typename T>
+void dev_free(T *&ptr) {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+}
+
+LevelArgs make_args(hpc_ctx *c, int level) {
+  LevelArgs a{};
+  a.p = c->p;
+  a.W = c->W;
+  a.level = level;
+  a.n_obs = (int)c->n;
+  a.alpha = c->opts.alpha;
+  a.sqrt_n3 = std::sqrt((double)c->n - 3.0);
+  a.zc32 = (float)c->zc;
+  a.margin_abs = (float)(c->opts.retest_margin * c->zc);
+  a.eps_in = c->opts.precision == HPC_PREC_MIXED_TC ? 4e-6f : 1.2e-7f;
+  a.cor64 = c->cor64;
+  a.cor32 = c->cor32;
+  a.adj = c->adj;
+  a.deg = c->deg;
+  a.rowptr = c->rowptr;
+  a.colidx = c->colidx;
+  a.row_work = c->row_work;
+  a.recs = c->recs;
+  a.rec_cap = c->rec_cap;
+  a.ctr = c->ctr;
+  a.tile_tests = 8;
+  return a;
+}
+
+hpc_status check_ctx(hpc_ctx *c) {
+  if (!c) {
+    set_error("null context");
+    return HPC_ERR_INVALID_ARG;
+  }
+  HPC_CUDA(cudaSetDevice(c->device));
+  return HPC_OK;
+}
+
+hpc_status pull_counters(hpc_ctx *c) {
+  HPC_CUDA(cudaMemcpyAsync(c->ctr_host, c->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
+hpc_status after_correlation(hpc_ctx *c) {
+  if (c->opts.precision != HPC_PREC_FP64) {
+    hpc_status s = launch_to_f32(c->cor64, c->p * c->p, c->cor32, c->stream);
+    if (s != HPC_OK) return s;
+  }
+  c->have_cor = true;
+  return hpc_ctx_reset(c);
+}
+
+template <typename T>
+hpc_status correlation_device(hpc_ctx *c, const T *X) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!X) {
+    set_error("null observation pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  const int64_t elems = c->n * c->p;
+  if (c->Z_elems < elems) {
+    dev_free(c->Z);
+    if ((s = dev_alloc(&c->Z, elems, "standardised data")) != HPC_OK) return s;
+    c->Z_elems = elems;
+  }
+  if (sizeof(T) == 8)
+    s = launch_standardise_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
+  else
+    s = launch_standardise_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
+  if (s != HPC_OK) return s;
+  const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
+  if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
+  return after_correlation(c);
+}
+
+template <typename T>
+hpc_status correlation_host(hpc_ctx *c, const T *X) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!X) {
+    set_error("null observation pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  const int64_t bytes = c->n * c->p * (int64_t)sizeof(T);
+  if (c->X_stage_bytes < bytes) {
+    if (c->X_stage) cudaFree(c->X_stage);
+    c->X_stage = nullptr;
+    uint8_t *buf = nullptr;
+    if ((s = dev_alloc(&buf, bytes, "observation staging")) != HPC_OK) return s;
+    c->X_stage = buf;
+    c->X_stage_bytes = bytes;
+  }
+  HPC_CUDA(cudaMemcpyAsync(c->X_stage, X, (size_t)bytes, cudaMemcpyHostToDevice, c->stream));
+  return correlation_device(c, (const T *)c->X_stage);
+}
+
+}  // namespace
+}  // namespace hpc
+
+using namespace hpc;
+
+extern "C" {
+
+const char *hpc_last_error_string(void) { return g_last_error.c_str(); }
+
+const char *hpc_status_string(hpc_status s) {
+  switch (s) {
+    case HPC_OK: return "HPC_OK";
+    case HPC_ERR_INVALID_ARG: return "HPC_ERR_INVALID_ARG";
+    case HPC_ERR_OOM: return "HPC_ERR_OOM";
+    case HPC_ERR_CUDA: return "HPC_ERR_CUDA";
+    case HPC_ERR_TIMEOUT: return "HPC_ERR_TIMEOUT";
+    case HPC_ERR_NUMERIC: return "HPC_ERR_NUMERIC";
+    case HPC_ERR_STATE: return "HPC_ERR_STATE";
+    case HPC_ERR_CAPACITY: return "HPC_ERR_CAPACITY";
+    case HPC_ERR_NO_DEVICE: return "HPC_ERR_NO_DEVICE";
+  }
+  return "HPC_ERR_UNKNOWN";
+}
+
+hpc_status hpc_opts_default(hpc_opts *o) {
+  if (!o) return HPC_ERR_INVALID_ARG;
+  std::memset(o, 0, sizeof(*o));
+  o->device = 0;
+  o->alpha = 0.05;  // src/main.cpp:26
+  o->max_level = 4; // src/main.cpp:31
+  o->precision = HPC_PREC_MIXED;
+  o->retest_margin = 1e-3;
+  o->ref_compat_sd = 0;
+  o->verbose = 0;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *bytes) {
+  if (!o || !bytes || p < 2 || n < 4) return HPC_ERR_INVALID_ARG;
+  const int64_t W = (p + 31) / 32;
+  int64_t b = p * p * 8;                                  // cor64
+  if (o->precision != HPC_PREC_FP64) b += p * p * 4;      // cor32
+  b += p * W * 4;                                         // adjacency bits
+  b += (p + 1) * (4 + 4 + 8);                             // deg, rowptr, row_work
+  b += n * p * 8;                                         // standardised data
+  // neighbour lists and records are sized at level 1 from the surviving edges;
+  // budget them for an average degree of 64
+  const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
+  b += 2 * e * 4 + e * (int64_t)sizeof(hpc_sepset_record);
+  *bytes = b;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n, const hpc_opts *opts) {
+  if (!out) {
+    set_error("null output pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  hpc_opts o;
+  if (opts) o = *opts; else hpc_opts_default(&o);
+  if (p < 2 || p > 46340) {
+    set_error("p = %lld out of range [2, 46340]", (long long)p);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (n < 4 || n > 0x7fffffff) {
+    set_error("n_obs = %lld out of range [4, 2^31)", (long long)n);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (!(o.alpha > 0.0 && o.alpha <= 1.0)) {
+    set_error("alpha = %g outside (0, 1]", o.alpha);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (o.precision < HPC_PREC_FP64 || o.precision > HPC_PREC_MIXED_TC) {
+    set_error("unknown precision %d", o.precision);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (o.max_level > HPC_MAX_LEVEL) {
+    set_error("max_level %d above HPC_MAX_LEVEL %d", o.max_level, HPC_MAX_LEVEL);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (!(o.retest_margin >= 0.0)) o.retest_margin = 1e-3;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device available: %s", cudaGetErrorString(e));
+    return HPC_ERR_NO_DEVICE;
+  }
+  if (o.device < 0 || o.device >= ndev) {
+    set_error("device %d not present (%d devices)", o.device, ndev);
+    return HPC_ERR_INVALID_ARG;
+  }
+  hpc_ctx *c = new hpc_ctx();
+  c->p = p;
+  c->n = n;
+  c->opts = o;
+  c->device = o.device;
+  c->W = (int)((p + 31) / 32);
+  c->zc = z_crit_of(o.alpha);
+  c->r_crit = r_crit_of(o.alpha, (int)n);
+  hpc_status s = HPC_OK;
+  auto fail = [&](hpc_status st) {
+    hpc_ctx_destroy(c);
+    return st;
+  };
+  if (cudaSetDevice(c->device) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaSetDevice(%d) failed", c->device);
+    delete c;
+    return HPC_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("stream/event creation failed");
+    return fail(HPC_ERR_CUDA);
+  }
+  if ((s = dev_alloc(&c->cor64, p * p, "cor64")) != HPC_OK) return fail(s);
+  if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, p * p, "cor32")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->adj, p * (int64_t)c->W, "adjacency")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->deg, p, "degrees")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->rowptr, p + 1, "row offsets")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->row_work, p + 1, "row work")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->ctr, 1, "counters")) != HPC_OK) return fail(s);
+  if (cudaMallocHost((void **)&c->ctr_host, sizeof(DevCounters)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("pinned counter allocation failed");
+    return fail(HPC_ERR_OOM);
+  }
+  if (cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream) != cudaSuccess) return fail(HPC_ERR_CUDA);
+  *out = c;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_destroy(hpc_ctx *c) {
+  if (!c) return HPC_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  dev_free(c->cor64);
+  dev_free(c->cor32);
+  dev_free(c->Z);
+  if (c->X_stage) cudaFree(c->X_stage);
+  dev_free(c->adj);
+  dev_free(c->deg);
+  dev_free(c->rowptr);
+  dev_free(c->colidx);
+  dev_free(c->row_work);
+  dev_free(c->recs);
+  dev_free(c->ctr);
+  if (c->ctr_host) cudaFreeHost(c->ctr_host);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  cudaGetLastError();
+  delete c;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_reset(hpc_ctx *c) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream));
+  c->next_level = 0;
+  c->edges = c->p * (c->p - 1) / 2;
+  return HPC_OK;
+}
+
+hpc_status hpc_correlation_f64(hpc_ctx *c, const double *X) { return correlation_host(c, X); }
+hpc_status hpc_correlation_f32(hpc_ctx *c, const float *X) { return correlation_host(c, X); }
+hpc_status hpc_correlation_device_f64(hpc_ctx *c, const double *X) { return correlation_device(c, X); }
+hpc_status hpc_correlation_device_f32(hpc_ctx *c, const float *X) { return correlation_device(c, X); }
+
+hpc_status hpc_load_correlation(hpc_ctx *c, const double *C) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!C) {
+    set_error("null correlation pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyHostToDevice, c->stream));
+  return after_correlation(c);
+}
+
+hpc_status hpc_load_correlation_device(hpc_ctx *c, const double *C) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!C) {
+    set_error("null correlation pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToDevice, c->stream));
+  return after_correlation(c);
+}
+
+hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!C || !c->have_cor) {
+    set_error(!C ? "null output pointer" : "no correlation matrix yet");
+    return !C ? HPC_ERR_INVALID_ARG : HPC_ERR_STATE;
+  }
+  HPC_CUDA(cudaMemcpyAsync(C, c->cor64, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
+hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!c->have_cor) {
+    set_error("run before a correlation matrix was computed or loaded");
+    return HPC_ERR_STATE;
+  }
+  if (level != c->next_level) {
+    set_error("level %d requested, next level is %d", level, c->next_level);
+    return HPC_ERR_STATE;
+  }
+  if (level > HPC_MAX_LEVEL) {
+    set_error("level %d above HPC_MAX_LEVEL", level);
+    return HPC_ERR_INVALID_ARG;
+  }
+  hpc_level_stats out{};
+  out.level = level;
+  out.edges_before = c->edges;
+  LevelArgs a = make_args(c, level);
+  HPC_CUDA(cudaEventRecord(c->ev0, c->stream));
+  if (level == 0) {
+    const double rc = c->r_crit;
+    const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
+    if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
+    if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
+    if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, c->ctr, c->stream)) != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->ev1, c->stream));
+    if ((s = pull_counters(c)) != HPC_OK) return s;
+    out.max_degree = (int)(c->p - 1);
+    out.rows = c->p;
+    out.potential_tests = out.executed_tests = c->p * (c->p - 1) / 2;
+    out.edges_after = (int64_t)(c->ctr_host->edges2 / 2);
+  } else {
+    if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
+    if ((s = launch_scan(c->p, level, c->deg, c->rowptr, c->row_work, c->ctr, c->stream)) != HPC_OK) return s;
+    if ((s = pull_counters(c)) != HPC_OK) return s;
+    const DevCounters h = *c->ctr_host;
+    if (h.err & kErrWorkOverflow) {
+      set_error("level %d: number of CI tests overflows 64 bits (max degree %d)", level, h.max_deg);
+      return HPC_ERR_CAPACITY;
+    }
+    out.max_degree = h.max_deg;
+    out.rows = h.rows;
+    out.potential_tests = (int64_t)h.work_total;
+    if (h.work_total > 0) {
+      if ((int64_t)h.edges2 > c->colidx_cap) {
+        dev_free(c->colidx);
+        if ((s = dev_alloc(&c->colidx, (int64_t)h.edges2, "neighbour lists")) != HPC_OK) return s;
+        c->colidx_cap = (int64_t)h.edges2;
+      }
+      if (level == 1 && c->rec_cap < (int64_t)(h.edges2 / 2)) {
+        // every removal from level 1 on is one of the edges alive now
+        dev_free(c->recs);
+        const int64_t cap = std::max<int64_t>(1, (int64_t)(h.edges2 / 2));
+        if ((s = dev_alloc(&c->recs, cap, "separation-set records")) != HPC_OK) return s;
+        c->rec_cap = cap;
+      }
+      a = make_args(c, level);
+      if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
+      const int grid = citest_grid(c->opts.precision, level, c->device);
+      const unsigned long long lanes = (unsigned long long)grid * 256ull;
+      unsigned long long m = h.work_total / (lanes * 4ull);
+      a.tile_tests = (int)std::max<unsigned long long>(1ull, std::min<unsigned long long>(64ull, m));
+      if ((s = launch_citest(a, c->opts.precision, grid, c->stream)) != HPC_OK) return s;
+    }
+    HPC_CUDA(cudaEventRecord(c->ev1, c->stream));
+    if ((s = pull_counters(c)) != HPC_OK) return s;
+    const DevCounters h2 = *c->ctr_host;
+    if (h2.err & kErrRecOverflow) {
+      set_error("level %d: separation-set record buffer overflow", level);
+      return HPC_ERR_CAPACITY;
+    }
+    out.executed_tests = (int64_t)h2.tests;
+    out.retests = (int64_t)h2.retests;
+    out.edges_after = out.edges_before - (int64_t)h2.deleted;
+  }
+  float ms = 0.f;
+  HPC_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  out.ms = ms;
+  c->edges = out.edges_after;
+  c->next_level = level + 1;
+  if (c->opts.verbose)
+    printf("level %d: max degree %d, tests %lld of %lld, FP64 re-tests %lld, edges %lld -> %lld, %.3f ms\n", level,
+           out.max_degree, (long long)out.executed_tests, (long long)out.potential_tests, (long long)out.retests,
+           (long long)out.edges_before, (long long)out.edges_after, out.ms);
+  if (st) *st = out;
+  return HPC_OK;
+}
+
+hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  const int top = c->opts.max_level < 0 ? HPC_MAX_LEVEL : c->opts.max_level;
+  int ran = 0;
+  for (int l = c->next_level; l <= top; ++l) {
+    hpc_level_stats st{};
+    if ((s = hpc_run_level(c, l, &st)) != HPC_OK) return s;
+    if (stats && ran < cap) stats[ran] = st;
+    ++ran;
+    if (l >= 1 && st.potential_tests == 0) break;
+  }
+  if (levels_run) *levels_run = ran;
+  return HPC_OK;
+}
+
+hpc_status hpc_get_adjacency(hpc_ctx *c, uint8_t *out) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!out) {
+    set_error("null output pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  std::vector<uint32_t> bits((size_t)(c->p * c->W));
+  if (c->next_level == 0) {
+    for (int64_t i = 0; i < c->p; ++i)
+      for (int64_t j = 0; j < c->p; ++j) out[i * c->p + j] = (uint8_t)(i != j);
+    return HPC_OK;
+  }
+  HPC_CUDA(cudaMemcpyAsync(bits.data(), c->adj, bits.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int64_t i = 0; i < c->p; ++i)
+    for (int64_t j = 0; j < c->p; ++j) out[i * c->p + j] = (uint8_t)((bits[i * c->W + (j >> 5)] >> (j & 31)) & 1u);
+  return HPC_OK;
+}
+
+hpc_status hpc_edge_count(hpc_ctx *c, int64_t *edges) {
+  if (!c || !edges) {
+    set_error("null argument");
+    return HPC_ERR_INVALID_ARG;
+  }
+  *edges = c->edges;
+  return HPC_OK;
+}
+
+hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t cap, int64_t *count) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!count) {
+    set_error("null count pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  unsigned long long n = 0;
+  HPC_CUDA(cudaMemcpyAsync(&n, &c->ctr->rec_count, sizeof(n), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  n = std::min<unsigned long long>(n, (unsigned long long)std::max<int64_t>(c->rec_cap, 0));
+  *count = (int64_t)n;
+  if (out && cap > 0 && n > 0) {
+    const int64_t k = std::min<int64_t>(cap, (int64_t)n);
+    HPC_CUDA(cudaMemcpyAsync(out, c->recs, sizeof(hpc_sepset_record) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
+    HPC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return HPC_OK;
+}
+
+hpc_status hpc_get_sepsets(hpc_ctx *c, int32_t *out, int max_cond) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!out || max_cond < 1) {
+    set_error("null output or max_cond < 1");
+    return HPC_ERR_INVALID_ARG;
+  }
+  const int64_t p = c->p;
+  std::fill(out, out + p * p * max_cond, -1);
+  if (c->next_level == 0) return HPC_OK;
+  std::vector<uint8_t> adj((size_t)(p * p));
+  if ((s = hpc_get_adjacency(c, adj.data())) != HPC_OK) return s;
+  int64_t nrec = 0;
+  if ((s = hpc_get_sepset_records(c, nullptr, 0, &nrec)) != HPC_OK) return s;
+  std::vector<hpc_sepset_record> recs((size_t)nrec);
+  if (nrec && (s = hpc_get_sepset_records(c, recs.data(), nrec, &nrec)) != HPC_OK) return s;
+  std::vector<uint8_t> later((size_t)(p * p), 0);
+  for (const auto &r : recs) {
+    later[(int64_t)r.i * p + r.j] = 1;
+    for (int k = 0; k < std::min(r.level, max_cond); ++k) out[((int64_t)r.i * p + r.j) * max_cond + k] = r.ids[k];
+  }
+  for (int64_t i = 0; i < p; ++i)
+    for (int64_t j = i + 1; j < p; ++j)
+      if (!adj[i * p + j] && !later[i * p + j]) out[(i * p + j) * max_cond] = -2;
+  return HPC_OK;
+}
+
+double hpc_calc_pvalue(double r, int n) { return calc_pvalue64(r, n); }
+double hpc_pval_l1(double x1, double x2, double x3, int n) { return pval_l1_64(x1, x2, x3, n); }
+double hpc_pval_ln(const double *M, int k, int n) {
+  if (!M || k < 2 || k > HPC_MAX_LEVEL + 2) return std::nan("");
+  for (int i = 0; i < k * k; ++i)
+    if (std::isnan(M[i])) return std::nan("");
+  std::vector<double> a(M, M + k * k), v((size_t)(k * k));
+  double p00, p01, p11;
+  pinv_sym64_corner(a.data(), k, v.data(), &p00, &p01, &p11);
+  return calc_pvalue64(-p01 / std::sqrt(p00 * p11), n);
+}
+double hpc_z_crit(double alpha) { return z_crit_of(alpha); }
+
+}  // extern "C"

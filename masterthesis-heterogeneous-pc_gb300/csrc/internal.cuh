@@ -1,0 +1,124 @@
+// Internal declarations shared by the CUDA translation units of libheterogpc.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/heterogpc.h"
+
+namespace hpc {
+
+// ---------------------------------------------------------------------------
+// error plumbing (thread-local last error, never exit())
+void set_error(const char *fmt, ...);
+hpc_status cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define HPC_CUDA(call)                                                   \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) return hpc::cuda_fail(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define HPC_LAUNCH_CHECK(what)                                           \
+  do {                                                                   \
+    cudaError_t e_ = cudaGetLastError();                                 \
+    if (e_ != cudaSuccess) return hpc::cuda_fail(e_, what, __FILE__, __LINE__); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// constants of the statistic (src/executor/independence/cpuInd.cpp:6)
+constexpr double kCutThr = 0.9999999;
+
+// Device counters of one context. Reset per level where noted.
+struct DevCounters {
+  unsigned long long tests;        // executed CI tests (per level)
+  unsigned long long retests;      // FP64 re-tests (per level)
+  unsigned long long deleted;      // edges removed (per level)
+  unsigned long long rec_count;    // sepset records written (cumulative)
+  unsigned long long tile_next;    // work-queue head (per level)
+  unsigned long long work_total;   // T_l (per level)
+  unsigned long long edges2;       // sum of degrees at level start
+  int max_deg;                     // at level start
+  int rows;                        // rows with work at this level
+  int err;                         // error bits (kErr*)
+  int pad;
+};
+constexpr int kErrRecOverflow = 1;
+constexpr int kErrWorkOverflow = 2;
+
+// Everything a level kernel needs, passed by value.
+struct LevelArgs {
+  int64_t p;
+  int W;                 // 32-bit words per adjacency row
+  int level;
+  int n_obs;
+  double alpha;
+  double sqrt_n3;        // sqrt(n - 3)
+  float zc32;            // z_crit in FP32
+  float margin_abs;      // absolute |z| band re-tested in FP64
+  float eps_in;          // relative error bound of cor32 entries
+  const double *cor64;   // p x p row-major (FP64 correlation)
+  const float *cor32;    // p x p row-major (FP32 copy) or null in plain mode
+  uint32_t *adj;         // live bitmask p x W
+  const int *deg;        // snapshot degrees
+  const int *rowptr;     // snapshot CSR offsets (p+1)
+  const int *colidx;     // snapshot neighbour ids, ascending per row
+  const unsigned long long *row_work;  // exclusive prefix of tests per row (p+1)
+  hpc_sepset_record *recs;
+  long long rec_cap;
+  DevCounters *ctr;
+  int tile_tests;        // tests per lane per tile
+};
+
+// ---------------------------------------------------------------------------
+// kernels' host launchers (defined in the .cu files)
+hpc_status launch_standardise_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z,
+                                  cudaStream_t s);
+hpc_status launch_standardise_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z,
+                                  cudaStream_t s);
+hpc_status launch_gram_f64(const double *Z, int64_t n, int64_t p, double inv_denom, double *C,
+                           cudaStream_t s);
+hpc_status launch_to_f32(const double *C, int64_t count, float *C32, cudaStream_t s);
+hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStream_t s);
+hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s);
+hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
+                       DevCounters *ctr, cudaStream_t s);
+hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s);
+hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s);
+int citest_grid(int precision, int level, int device);
+
+}  // namespace hpc
+
+// ---------------------------------------------------------------------------
+// The context (opaque to callers).
+struct hpc_ctx {
+  int64_t p = 0, n = 0;
+  hpc_opts opts{};
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  int W = 0;
+  double *cor64 = nullptr;
+  float *cor32 = nullptr;
+  double *Z = nullptr;          // standardised data (n x p), transient
+  int64_t Z_elems = 0;
+  void *X_stage = nullptr;      // device copy of host observations
+  int64_t X_stage_bytes = 0;
+  uint32_t *adj = nullptr;
+  int *deg = nullptr;
+  int *rowptr = nullptr;
+  int *colidx = nullptr;
+  int64_t colidx_cap = 0;
+  unsigned long long *row_work = nullptr;
+  hpc_sepset_record *recs = nullptr;
+  int64_t rec_cap = 0;
+  hpc::DevCounters *ctr = nullptr;      // device
+  hpc::DevCounters *ctr_host = nullptr; // pinned mirror
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool have_cor = false;
+  int next_level = 0;
+  int64_t edges = 0;           // undirected edges after the last level
+  double zc = 0.0;             // z_crit (FP64)
+  double r_crit = 0.0;         // |r| at which p == alpha
+};

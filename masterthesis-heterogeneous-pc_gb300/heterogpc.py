@@ -1,0 +1,253 @@
+"""Python binding of libheterogpc (ctypes over the C ABI in include/heterogpc.h).
+
+Mirrors the reference's skeleton interface (src/independence/skeleton.hpp:10-73):
+``SkeletonCalculator(max_level, alpha, ...)`` with ``add_observations`` /
+``add_correlation_matrix`` / ``calc_level`` / ``run``, backed by one GPU context.
+There is no CPU fallback: importing works without a GPU, but every compute call
+goes to the CUDA library and raises ``HpcError`` when no device is usable.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libheterogpc.so")
+
+HPC_MAX_LEVEL = 16
+PREC_FP64, PREC_MIXED, PREC_MIXED_TC = 0, 1, 2
+GRAPH_ER, GRAPH_PA = 0, 1
+
+STATUS = {0: "HPC_OK", 1: "HPC_ERR_INVALID_ARG", 2: "HPC_ERR_OOM", 3: "HPC_ERR_CUDA", 4: "HPC_ERR_TIMEOUT",
+          5: "HPC_ERR_NUMERIC", 6: "HPC_ERR_STATE", 7: "HPC_ERR_CAPACITY", 8: "HPC_ERR_NO_DEVICE"}
+
+
+class HpcError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int), ("alpha", C.c_double), ("max_level", C.c_int), ("precision", C.c_int),
+                ("retest_margin", C.c_double), ("ref_compat_sd", C.c_int), ("verbose", C.c_int)]
+
+
+class LevelStats(C.Structure):
+    _fields_ = [("level", C.c_int), ("max_degree", C.c_int), ("rows", C.c_int64), ("potential_tests", C.c_int64),
+                ("executed_tests", C.c_int64), ("retests", C.c_int64), ("edges_before", C.c_int64),
+                ("edges_after", C.c_int64), ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class SepsetRecord(C.Structure):
+    _fields_ = [("i", C.c_int32), ("j", C.c_int32), ("level", C.c_int32), ("pad", C.c_int32),
+                ("pmax", C.c_double), ("ids", C.c_int32 * HPC_MAX_LEVEL)]
+
+
+class SemParams(C.Structure):
+    _fields_ = [("p", C.c_int64), ("n", C.c_int64), ("graph", C.c_int), ("degree", C.c_double),
+                ("pa_parents", C.c_int), ("w_lo", C.c_double), ("w_hi", C.c_double), ("seed", C.c_uint64)]
+
+
+_lib = None
+
+# symbol -> (restype, argtypes)
+_SIGS = {
+    "hpc_last_error_string": (C.c_char_p, []),
+    "hpc_status_string": (C.c_char_p, [C.c_int]),
+    "hpc_opts_default": (C.c_int, [C.POINTER(Opts)]),
+    "hpc_ctx_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int64, C.c_int64, C.POINTER(Opts)]),
+    "hpc_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "hpc_ctx_reset": (C.c_int, [C.c_void_p]),
+    "hpc_ctx_footprint": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(Opts), C.POINTER(C.c_int64)]),
+    "hpc_correlation_f64": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_correlation_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_correlation_device_f64": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_correlation_device_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_load_correlation": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_load_correlation_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_get_correlation": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_run_level": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LevelStats)]),
+    "hpc_run_skeleton": (C.c_int, [C.c_void_p, C.POINTER(LevelStats), C.c_int, C.POINTER(C.c_int)]),
+    "hpc_get_adjacency": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_edge_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "hpc_get_sepsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "hpc_get_sepset_records": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "hpc_calc_pvalue": (C.c_double, [C.c_double, C.c_int]),
+    "hpc_pval_l1": (C.c_double, [C.c_double, C.c_double, C.c_double, C.c_int]),
+    "hpc_pval_ln": (C.c_double, [C.c_void_p, C.c_int, C.c_int]),
+    "hpc_z_crit": (C.c_double, [C.c_double]),
+    "hpc_sem_generate": (C.c_int, [C.POINTER(SemParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+
+def lib():
+    """Load libheterogpc.so (built in-tree); raise if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libheterogpc.so not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def _check(status):
+    if status != 0:
+        msg = lib().hpc_last_error_string()
+        raise HpcError(status, msg.decode() if msg else "")
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+# ---- independence statistics (CPU::calcPValue / pValL1 / pValLN, cpuInd.hpp:3-10)
+def calcPValue(r, n):
+    return lib().hpc_calc_pvalue(float(r), int(n))
+
+
+def pValL1(x1, x2, x3, n):
+    return lib().hpc_pval_l1(float(x1), float(x2), float(x3), int(n))
+
+
+def pValLN(M, n):
+    M = np.ascontiguousarray(M, dtype=np.float64)
+    return lib().hpc_pval_ln(_ptr(M), int(M.shape[0]), int(n))
+
+
+def z_crit(alpha):
+    return lib().hpc_z_crit(float(alpha))
+
+
+# ---- synthetic data
+def sem_generate(p, n, graph=GRAPH_ER, degree=2.0, pa_parents=2, w_lo=0.1, w_hi=1.0, seed=1, dtype=np.float64,
+                 want_dag=False):
+    """Seeded linear-Gaussian SEM; returns X with shape (p, n) (each variable's samples
+    contiguous, i.e. the column-major n x p layout of the C ABI) and optionally the DAG."""
+    prm = SemParams(p, n, graph, degree, pa_parents, w_lo, w_hi, seed)
+    X64 = np.empty((p, n), np.float64) if dtype == np.float64 else None
+    X32 = np.empty((p, n), np.float32) if dtype == np.float32 else None
+    dag = np.empty((p, p), np.uint8) if want_dag else None
+    _check(lib().hpc_sem_generate(C.byref(prm), _ptr(X64) if X64 is not None else None,
+                                  _ptr(X32) if X32 is not None else None,
+                                  _ptr(dag) if dag is not None else None, None))
+    X = X64 if X64 is not None else X32
+    return (X, dag) if want_dag else X
+
+
+class SkeletonCalculator:
+    """One skeleton problem on one GPU (src/independence/skeleton.hpp:10-73).
+
+    alpha: edges are removed iff p >= alpha; max_level: highest level (-1 = until no
+    edge has enough neighbours); precision: PREC_FP64 (plain path), PREC_MIXED or
+    PREC_MIXED_TC."""
+
+    def __init__(self, p, n_obs, alpha=0.05, max_level=4, precision=PREC_MIXED, device=0, retest_margin=1e-3,
+                 ref_compat_sd=False, verbose=False):
+        self.p, self.n = int(p), int(n_obs)
+        o = Opts()
+        lib().hpc_opts_default(C.byref(o))
+        o.device, o.alpha, o.max_level, o.precision = device, alpha, max_level, precision
+        o.retest_margin, o.ref_compat_sd, o.verbose = retest_margin, int(ref_compat_sd), int(verbose)
+        self.opts = o
+        h = C.c_void_p()
+        _check(lib().hpc_ctx_create(C.byref(h), self.p, self.n, C.byref(o)))
+        self._h = h
+        self.level_stats = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hpc_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # add_observations (skeleton.cpp:53-58); X shape (p, n), FP64 or FP32
+    def add_observations(self, X):
+        X = np.asarray(X)
+        assert X.shape == (self.p, self.n), X.shape
+        if X.dtype == np.float32:
+            X = np.ascontiguousarray(X)
+            _check(lib().hpc_correlation_f32(self._h, _ptr(X)))
+        else:
+            X = np.ascontiguousarray(X, dtype=np.float64)
+            _check(lib().hpc_correlation_f64(self._h, _ptr(X)))
+        self.level_stats = []
+
+    # add_correlation_matrix (skeleton.cpp:60-65)
+    def add_correlation_matrix(self, Cm):
+        Cm = np.ascontiguousarray(Cm, dtype=np.float64)
+        assert Cm.shape == (self.p, self.p)
+        _check(lib().hpc_load_correlation(self._h, _ptr(Cm)))
+        self.level_stats = []
+
+    def reset(self):
+        _check(lib().hpc_ctx_reset(self._h))
+        self.level_stats = []
+
+    def calc_level(self, level):
+        st = LevelStats()
+        _check(lib().hpc_run_level(self._h, int(level), C.byref(st)))
+        self.level_stats.append(st.as_dict())
+        return st.as_dict()
+
+    def run(self):
+        cap = HPC_MAX_LEVEL + 1
+        arr = (LevelStats * cap)()
+        ran = C.c_int(0)
+        _check(lib().hpc_run_skeleton(self._h, arr, cap, C.byref(ran)))
+        self.level_stats.extend(arr[i].as_dict() for i in range(ran.value))
+        return self.level_stats
+
+    def correlation(self):
+        out = np.empty((self.p, self.p), np.float64)
+        _check(lib().hpc_get_correlation(self._h, _ptr(out)))
+        return out
+
+    def adjacency(self):
+        out = np.empty((self.p, self.p), np.uint8)
+        _check(lib().hpc_get_adjacency(self._h, _ptr(out)))
+        return out
+
+    def edge_count(self):
+        e = C.c_int64(0)
+        _check(lib().hpc_edge_count(self._h, C.byref(e)))
+        return e.value
+
+    def sepsets(self, max_cond):
+        out = np.empty((self.p, self.p, max_cond), np.int32)
+        _check(lib().hpc_get_sepsets(self._h, _ptr(out), int(max_cond)))
+        return out
+
+    def sepset_records(self):
+        n = C.c_int64(0)
+        _check(lib().hpc_get_sepset_records(self._h, None, 0, C.byref(n)))
+        recs = (SepsetRecord * max(1, n.value))()
+        _check(lib().hpc_get_sepset_records(self._h, recs, n.value, C.byref(n)))
+        return [(r.i, r.j, r.level, tuple(r.ids[:r.level]), r.pmax) for r in recs[:n.value]]
