@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""Benchmark of the PC-stable skeleton path on one GB300 (or N replicas).
+
+Workload (default, "c2"): linear-Gaussian SEM on a seeded Erdos-Renyi DAG, p=2000
+variables, expected degree 4, weights +-[0.1, 1.0], N(0,1) noise, n=5000 FP32 samples,
+alpha=0.01, levels 0..6, FP64-accurate correlation computed on the device.
+
+A step is one skeleton discovery on a correlation matrix resident in HBM: levels
+0..6 (snapshots, CI tests, removals, separation sets), i.e. the region the reference
+times (src/independence/skeleton.cpp:167-180). The correlation of the step's data is
+computed once beforehand on the device and reported separately.
+
+  value   skeletons/s with the correlation resident in HBM (CUDA events, L2 flushed
+          before every step because the 48 MB of correlation fits in L2)
+  e2e     the same through the C ABI from pinned host memory: H2D of the FP64
+          correlation, all levels, D2H of the adjacency bitmask
+  --impl reference   the reference's CPU path (the oracle restatement, all host cores)
+
+Multi-GPU: replicas only (the skeleton does not shard without an exchange step);
+under torchrun every rank runs the workload and rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "masterthesis-heterogeneous-pc_gb300")
+for _d in (PKG, ROOT):
+    if _d not in sys.path:
+        sys.path.insert(0, _d)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "c2": dict(p=2000, n=5000, graph=0, degree=4.0, pa_parents=2, w_lo=0.1, w_hi=1.0, seed=2, alpha=0.01,
+               max_level=6, dtype="f32"),
+}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def citest_bytes(adjs, levels_stats, lane_bytes=4):
+    """Algorithmic bytes of the CI-test kernel per level: l(l+3)/2 correlation entries
+    per executed test, plus (2 + d_i) words per directed edge that has tests."""
+    out = []
+    for st, adj in zip(levels_stats, adjs):
+        l = st["level"]
+        if l == 0 or adj is None:
+            out.append(0)
+            continue
+        d = adj.sum(1).astype(np.int64)
+        has = d - 1 >= l
+        edge_bytes = int((d[has] * (2 + d[has])).sum()) * 4
+        out.append(st["executed_tests"] * lane_bytes * l * (l + 3) // 2 + edge_bytes)
+    return out
+
+
+def traffic_from_profile(kernel):
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    ent = d.get(kernel)
+    return ent.get("dram_bytes_per_launch") if ent else None
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    import heterogpc as hg
+    from oracle import oracle as orc
+
+    import hpc_build
+    hpc_build.build_oracle()
+    X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
+                        wl["seed"], dtype=np.float32)
+    Cm = orc.correlation(X.astype(np.float64))
+    cores = os.cpu_count()
+    for _ in range(args.warmup):
+        orc.run(Cm, wl["n"], wl["alpha"], wl["max_level"], threads=cores)
+    times, tests = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        res = orc.run(Cm, wl["n"], wl["alpha"], wl["max_level"], threads=cores)
+        times.append(time.perf_counter() - t0)
+        tests = sum(l["executed_tests"] for l in res.levels)
+    total = sum(times)
+    value = args.steps / total
+    line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded linear-Gaussian SEM)", "impl": "reference",
+            "config": dict(workload=args.workload, **{k: wl[k] for k in ("p", "n", "degree", "alpha", "max_level")},
+                           parallelism="replicas"),
+            "ci_tests_per_step": tests, "ci_tests_per_sec": tests * args.steps / total,
+            "cpu_baseline": {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
+                             "sample": "the full skeleton phase (levels 0-%d) of the workload per step"
+                                       % wl["max_level"]},
+            "e2e": {"value": value, "unit": "skeletons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, wl, rank, world)
+        return
+
+    import torch
+
+    import heterogpc as hg
+    import hpc_build
+
+    if not os.path.exists(hg.LIB_PATH):
+        hpc_build.build_library()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    # data: generated on the host, then resident in HBM
+    X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
+                        wl["seed"] + 1000 * rank * 0, dtype=np.float32)
+    Xd = torch.from_numpy(X).to(dev)
+    p, n = wl["p"], wl["n"]
+
+    def make(precision):
+        sk = hg.SkeletonCalculator(p, n, alpha=wl["alpha"], max_level=wl["max_level"], precision=precision,
+                                   device=local)
+        sk.set_stream(stream.cuda_stream)
+        return sk
+
+    sk = make(hg.PREC_MIXED)
+    # correlation once (FP64-accurate), timed separately
+    for _ in range(2):
+        sk.add_observations_device(Xd.data_ptr(), np.float32)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sk.add_observations_device(Xd.data_ptr(), np.float32)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cor_ms = e0.elapsed_time(e1)
+    cor_t = sk.timings()
+    Cdev = torch.empty((p, p), dtype=torch.float64, device=dev)
+    sk_plain = make(hg.PREC_FP64)
+    sk_plain.add_observations_device(Xd.data_ptr(), np.float32)
+    torch.cuda.synchronize()
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def timed_steps(s, k):
+        ms, stats, t_tests = [], None, None
+        test_ms_acc = np.zeros(hg.HPC_MAX_LEVEL + 1)
+        launches0 = s.timings()["launches"]
+        for _ in range(k):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.reset()
+            s.run()
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+            stats = s.level_stats
+            t = s.timings()
+            test_ms_acc += np.array(t["test_ms"])
+        launches = s.timings()["launches"] - launches0
+        return ms, stats, test_ms_acc / k, launches
+
+    for _ in range(args.warmup):
+        sk.reset()
+        sk.run()
+        sk_plain.reset()
+        sk_plain.run()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    step_ms, stats, test_ms, launches = timed_steps(sk, args.steps)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    plain_ms, plain_stats, plain_test_ms, _ = timed_steps(sk_plain, args.steps)
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1e3)
+
+    # e2e through the C ABI from pinned host memory
+    Ch = torch.empty((p, p), dtype=torch.float64, pin_memory=True)
+    Cdev.copy_(torch.from_numpy(sk.correlation()))
+    Ch.copy_(Cdev.cpu())
+    adj_h = torch.empty((p, p), dtype=torch.uint8, pin_memory=True)
+    for _ in range(args.warmup):
+        sk.add_correlation_matrix_ptr(Ch.data_ptr())
+        sk.run()
+        sk.adjacency_into(adj_h.data_ptr())
+    torch.cuda.synchronize()
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sk.add_correlation_matrix_ptr(Ch.data_ptr())
+        sk.run()
+        sk.adjacency_into(adj_h.data_ptr())
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_t)
+    if dist:
+        t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    W = (p + 31) // 32
+    e2e = {"value": world * args.steps / e2e_total, "unit": "skeletons/s", "h2d_bytes_per_step": p * p * 8,
+           "d2h_bytes_per_step": p * W * 4}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # algorithmic bytes of the CI-test kernel: degree sequences per level from one
+    # instrumented replay (the level-by-level edge sets are deterministic)
+    sk.reset()
+    adjs, lst = [], []
+    for lv in range(wl["max_level"] + 1):
+        adj_before = sk.adjacency() if lv >= 1 else None
+        st = sk.calc_level(lv)
+        lst.append(st)
+        adjs.append(adj_before)
+        if lv >= 1 and st["potential_tests"] == 0:
+            break
+    peaks = load_peaks()
+    # executed-test counts of the timed steps (they vary slightly between runs)
+    for a_, b_ in zip(lst, stats):
+        a_["executed_tests"] = b_["executed_tests"]
+    bytes_l = citest_bytes(adjs, lst)
+    kern_ms = sum(test_ms[1:len(lst)])
+    launches_ct = sum(1 for s_ in lst[1:] if s_["potential_tests"] > 0)
+    achieved_gbs = (sum(bytes_l) / 1e9) / (kern_ms / 1e3) if kern_ms > 0 else 0.0
+    tests_per_step = sum(s_["executed_tests"] for s_ in stats)
+    roofline = {"kernel": "citest_kernel (levels 1-%d)" % wl["max_level"], "bound": "hbm",
+                "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                "traffic": traffic_from_profile("citest_kernel"),
+                "algorithmic_bytes_per_step": int(sum(bytes_l)), "kernel_ms_per_step": kern_ms,
+                "launches_per_step": launches_ct}
+    gram_flops = n * p * (p + 1)  # FP64 Gram, upper triangle incl. diagonal
+    line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded linear-Gaussian SEM)",
+            "config": dict(workload=args.workload, p=p, n=n, degree=wl["degree"], alpha=wl["alpha"],
+                           max_level=wl["max_level"], precision="mixed (FP32 tests, FP64 re-tests)",
+                           l2="flushed before every step (256 MB write)", parallelism="replicas"),
+            "ci_tests_per_step": tests_per_step, "ci_tests_per_sec": tests_per_step * args.steps * world / (total_ms / 1e3),
+            "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+            "levels": [{k: s_[k] for k in ("level", "max_degree", "potential_tests", "executed_tests", "retests",
+                                           "edges_after")} for s_ in stats],
+            "plain_gpu_path": {"skeletons_per_sec": args.steps / (sum(plain_ms) / 1e3),
+                               "ms_per_step": sum(plain_ms) / args.steps, "precision": "fp64"},
+            "correlation": {"ms": cor_ms, "gram_ms": cor_t["gram_ms"], "standardise_ms": cor_t["standardise_ms"],
+                            "kernel": "gram_f64_kernel", "fp64_gflops": gram_flops / (cor_t["gram_ms"] / 1e3) / 1e9},
+            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        hpc_build.build_oracle()
+        Cm = Ch.numpy().copy()
+        cores = os.cpu_count()
+        t0 = time.perf_counter()
+        res = orc.run(Cm, n, wl["alpha"], wl["max_level"], threads=cores)
+        dt = time.perf_counter() - t0
+        same = bool(np.array_equal(res.adj, adj_h.numpy()))
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "skeletons/s", "cores": cores, "kind": "port",
+                                "sample": "one full skeleton phase (levels 0-%d) of the workload" % wl["max_level"],
+                                "ci_tests_per_sec": sum(l["executed_tests"] for l in res.levels) / dt,
+                                "same_skeleton_as_gpu": same}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

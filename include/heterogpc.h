@@ -80,6 +80,17 @@ typedef struct hpc_sepset_record {
   int32_t ids[HPC_MAX_LEVEL]; /* ascending separating variables, `level` of them */
 } hpc_sepset_record;
 
+/* Device-time breakdown of the last calls, from CUDA events on the context stream. */
+typedef struct hpc_timings {
+  double standardise_ms;                 /* last correlation: column standardisation */
+  double gram_ms;                        /* last correlation: Gram */
+  double convert_ms;                     /* last correlation: FP32 copy */
+  double level_ms[HPC_MAX_LEVEL + 1];    /* whole level (snapshot + tests) */
+  double compact_ms[HPC_MAX_LEVEL + 1];  /* neighbour-list snapshot of the level */
+  double test_ms[HPC_MAX_LEVEL + 1];     /* CI-test kernel of the level */
+  int64_t launches;                      /* kernels launched by this context so far */
+} hpc_timings;
+
 typedef struct hpc_ctx hpc_ctx;
 
 /* ---- errors ------------------------------------------------------------ */
@@ -98,6 +109,11 @@ hpc_status hpc_ctx_destroy(hpc_ctx *ctx);
 /* Resets adjacency (complete graph minus diagonal) and separation sets, keeping
  * the correlation matrix (src/util/state.cu:31-43). */
 hpc_status hpc_ctx_reset(hpc_ctx *ctx);
+/* Orders all of the context's work on `stream` (a cudaStream_t of the same device,
+ * owned by the caller) instead of the context's own stream; NULL restores it. */
+hpc_status hpc_ctx_set_stream(hpc_ctx *ctx, void *stream);
+/* Device-time breakdown of the context's last correlation and levels. */
+hpc_status hpc_get_timings(hpc_ctx *ctx, hpc_timings *out);
 /* Device bytes held by a context of this shape (admission control). */
 hpc_status hpc_ctx_footprint(int64_t p, int64_t n_obs, const hpc_opts *opts, int64_t *bytes);
 

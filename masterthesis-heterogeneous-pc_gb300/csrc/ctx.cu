@@ -121,6 +121,7 @@ hpc_status after_correlation(hpc_ctx *c) {
   if (c->opts.precision != HPC_PREC_FP64) {
     hpc_status s = launch_to_f32(c->cor64, c->p * c->p, c->cor32, c->stream);
     if (s != HPC_OK) return s;
+    c->timings.launches += 1;
   }
   c->have_cor = true;
   return hpc_ctx_reset(c);
@@ -140,14 +141,21 @@ hpc_status correlation_device(hpc_ctx *c, const T *X) {
     if ((s = dev_alloc(&c->Z, elems, "standardised data")) != HPC_OK) return s;
     c->Z_elems = elems;
   }
+  HPC_CUDA(cudaEventRecord(c->evc[0], c->stream));
   if (sizeof(T) == 8)
     s = launch_standardise_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
   else
     s = launch_standardise_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
   if (s != HPC_OK) return s;
+  HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
   const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
   if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
-  return after_correlation(c);
+  HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+  c->timings.launches += 2;
+  if ((s = after_correlation(c)) != HPC_OK) return s;
+  HPC_CUDA(cudaEventRecord(c->evc[3], c->stream));
+  c->cor_timed = true;
+  return HPC_OK;
 }
 
 template <typename T>
@@ -284,12 +292,16 @@ hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n, const hpc_opts *o
     return HPC_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+  c->stream = nullptr;
+  bool ev_ok = cudaEventCreate(&c->ev0) == cudaSuccess && cudaEventCreate(&c->ev1) == cudaSuccess;
+  for (auto &e : c->evc) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
+  for (auto &e : c->evt) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess || !ev_ok) {
     cudaGetLastError();
     set_error("stream/event creation failed");
     return fail(HPC_ERR_CUDA);
   }
+  c->stream = c->own_stream;
   if ((s = dev_alloc(&c->cor64, p * p, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, p * p, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, p * (int64_t)c->W, "adjacency")) != HPC_OK) return fail(s);
@@ -325,9 +337,42 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   if (c->ctr_host) cudaFreeHost(c->ctr_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  for (auto &e : c->evc)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : c->evt)
+    if (e) cudaEventDestroy(e);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
   cudaGetLastError();
   delete c;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_set_stream(hpc_ctx *c, void *stream) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return HPC_OK;
+}
+
+hpc_status hpc_get_timings(hpc_ctx *c, hpc_timings *out) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!out) {
+    set_error("null output pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (c->cor_timed) {
+    HPC_CUDA(cudaEventSynchronize(c->evc[3]));
+    float a = 0.f, b = 0.f, d = 0.f;
+    HPC_CUDA(cudaEventElapsedTime(&a, c->evc[0], c->evc[1]));
+    HPC_CUDA(cudaEventElapsedTime(&b, c->evc[1], c->evc[2]));
+    HPC_CUDA(cudaEventElapsedTime(&d, c->evc[2], c->evc[3]));
+    c->timings.standardise_ms = a;
+    c->timings.gram_ms = b;
+    c->timings.convert_ms = d;
+  }
+  *out = c->timings;
   return HPC_OK;
 }
 
@@ -403,10 +448,16 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     const double rc = c->r_crit;
     const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
     if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->evt[1], c->stream));
     if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
     if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, c->ctr, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->ev1, c->stream));
+    c->timings.launches += 4;
     if ((s = pull_counters(c)) != HPC_OK) return s;
+    float t0 = 0.f;
+    HPC_CUDA(cudaEventElapsedTime(&t0, c->ev0, c->evt[1]));
+    c->timings.test_ms[0] = t0;
+    c->timings.compact_ms[0] = 0.0;
     out.max_degree = (int)(c->p - 1);
     out.rows = c->p;
     out.potential_tests = out.executed_tests = c->p * (c->p - 1) / 2;
@@ -414,8 +465,10 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
   } else {
     if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
     if ((s = launch_scan(c->p, level, c->deg, c->rowptr, c->row_work, c->ctr, c->stream)) != HPC_OK) return s;
+    c->timings.launches += 2;
     if ((s = pull_counters(c)) != HPC_OK) return s;
     const DevCounters h = *c->ctr_host;
+    c->timings.test_ms[level] = 0.0;
     if (h.err & kErrWorkOverflow) {
       set_error("level %d: number of CI tests overflows 64 bits (max degree %d)", level, h.max_deg);
       return HPC_ERR_CAPACITY;
@@ -438,14 +491,24 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
       }
       a = make_args(c, level);
       if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
+      HPC_CUDA(cudaEventRecord(c->evt[0], c->stream));
       const int grid = citest_grid(c->opts.precision, level, c->device);
       const unsigned long long lanes = (unsigned long long)grid * 256ull;
       unsigned long long m = h.work_total / (lanes * 4ull);
       a.tile_tests = (int)std::max<unsigned long long>(1ull, std::min<unsigned long long>(64ull, m));
       if ((s = launch_citest(a, c->opts.precision, grid, c->stream)) != HPC_OK) return s;
+      HPC_CUDA(cudaEventRecord(c->evt[1], c->stream));
+      c->timings.launches += 2;
     }
     HPC_CUDA(cudaEventRecord(c->ev1, c->stream));
     if ((s = pull_counters(c)) != HPC_OK) return s;
+    if (h.work_total > 0) {
+      float tt = 0.f, tc = 0.f;
+      HPC_CUDA(cudaEventElapsedTime(&tt, c->evt[0], c->evt[1]));
+      HPC_CUDA(cudaEventElapsedTime(&tc, c->ev0, c->evt[0]));
+      c->timings.test_ms[level] = tt;
+      c->timings.compact_ms[level] = tc;
+    }
     const DevCounters h2 = *c->ctr_host;
     if (h2.err & kErrRecOverflow) {
       set_error("level %d: separation-set record buffer overflow", level);
@@ -458,6 +521,7 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
   float ms = 0.f;
   HPC_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   out.ms = ms;
+  c->timings.level_ms[level] = ms;
   c->edges = out.edges_after;
   c->next_level = level + 1;
   if (c->opts.verbose)

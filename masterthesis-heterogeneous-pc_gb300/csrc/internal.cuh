@@ -115,7 +115,12 @@ struct hpc_ctx {
   int64_t rec_cap = 0;
   hpc::DevCounters *ctr = nullptr;      // device
   hpc::DevCounters *ctr_host = nullptr; // pinned mirror
+  cudaStream_t own_stream = nullptr; // the context's stream; `stream` may be a caller's
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
+  cudaEvent_t evt[2] = {nullptr, nullptr};                    // CI-test kernel
+  bool cor_timed = false;
+  hpc_timings timings{};
   bool have_cor = false;
   int next_level = 0;
   int64_t edges = 0;           // undirected edges after the last level

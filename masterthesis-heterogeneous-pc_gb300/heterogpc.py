@@ -47,6 +47,17 @@ class SepsetRecord(C.Structure):
                 ("pmax", C.c_double), ("ids", C.c_int32 * HPC_MAX_LEVEL)]
 
 
+class Timings(C.Structure):
+    _fields_ = [("standardise_ms", C.c_double), ("gram_ms", C.c_double), ("convert_ms", C.c_double),
+                ("level_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("compact_ms", C.c_double * (HPC_MAX_LEVEL + 1)),
+                ("test_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("launches", C.c_int64)]
+
+    def as_dict(self):
+        return {"standardise_ms": self.standardise_ms, "gram_ms": self.gram_ms, "convert_ms": self.convert_ms,
+                "level_ms": list(self.level_ms), "compact_ms": list(self.compact_ms), "test_ms": list(self.test_ms),
+                "launches": self.launches}
+
+
 class SemParams(C.Structure):
     _fields_ = [("p", C.c_int64), ("n", C.c_int64), ("graph", C.c_int), ("degree", C.c_double),
                 ("pa_parents", C.c_int), ("w_lo", C.c_double), ("w_hi", C.c_double), ("seed", C.c_uint64)]
@@ -63,6 +74,8 @@ _SIGS = {
     "hpc_ctx_destroy": (C.c_int, [C.c_void_p]),
     "hpc_ctx_reset": (C.c_int, [C.c_void_p]),
     "hpc_ctx_footprint": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(Opts), C.POINTER(C.c_int64)]),
+    "hpc_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_get_timings": (C.c_int, [C.c_void_p, C.POINTER(Timings)]),
     "hpc_correlation_f64": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_correlation_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_correlation_device_f64": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -224,6 +237,34 @@ class SkeletonCalculator:
         _check(lib().hpc_run_skeleton(self._h, arr, cap, C.byref(ran)))
         self.level_stats.extend(arr[i].as_dict() for i in range(ran.value))
         return self.level_stats
+
+    def set_stream(self, stream_handle):
+        """Run on a caller-owned cudaStream_t (an int handle, e.g. torch's cuda_stream)."""
+        _check(lib().hpc_ctx_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None))
+
+    def timings(self):
+        t = Timings()
+        _check(lib().hpc_get_timings(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def add_observations_device(self, ptr, dtype):
+        """Observations already in device memory (pointer to a column-major n x p array)."""
+        fn = lib().hpc_correlation_device_f32 if dtype == np.float32 else lib().hpc_correlation_device_f64
+        _check(fn(self._h, C.c_void_p(ptr)))
+        self.level_stats = []
+
+    def add_correlation_matrix_device(self, ptr):
+        _check(lib().hpc_load_correlation_device(self._h, C.c_void_p(ptr)))
+        self.level_stats = []
+
+    def add_correlation_matrix_ptr(self, ptr):
+        """Host pointer (e.g. pinned memory) to a row-major p x p FP64 matrix."""
+        _check(lib().hpc_load_correlation(self._h, C.c_void_p(ptr)))
+        self.level_stats = []
+
+    def adjacency_into(self, ptr):
+        """Copy the p x p uint8 adjacency into caller memory at ptr."""
+        _check(lib().hpc_get_adjacency(self._h, C.c_void_p(ptr)))
 
     def correlation(self):
         out = np.empty((self.p, self.p), np.float64)
