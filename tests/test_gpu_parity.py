@@ -135,11 +135,14 @@ def test_call_order_errors():
     assert sk.edge_count() == 0  # identity: every pair independent
 
 
-def test_alpha_one_removes_everything_and_tiny_alpha_keeps():
+@pytest.mark.parametrize("alpha,max_level", [(1.0, 3), (0.999, 2), (1e-300, 0), (1e-12, 3)])
+def test_extreme_alpha(alpha, max_level):
+    """alpha = 1 removes only pairs with p == 1 exactly (r == 0 or NaN, cpuInd.cpp:10-13);
+    tiny alpha removes almost nothing."""
     X = gen(dict(p=30, n=200, graph=hg.GRAPH_ER, degree=3.0, seed=66))
     Cm = orc.correlation(X)
-    sk = run_gpu(Cm, 200, 1.0, 3, hg.PREC_MIXED)
-    assert sk.edge_count() == 0
-    sk = run_gpu(Cm, 200, 1e-300, 0, hg.PREC_MIXED)
-    want = orc.run(Cm, 200, 1e-300, 0)
-    assert np.array_equal(sk.adjacency(), want.adj)
+    Cm[3, 1] = Cm[1, 3] = 0.0  # p == 1 exactly at level 0
+    want = orc.run(Cm, 200, alpha, max_level)
+    for precision in PRECISIONS:
+        sk = run_gpu(Cm, 200, alpha, max_level, precision)
+        assert np.array_equal(sk.adjacency(), want.adj)
