@@ -135,6 +135,24 @@ hpc_status hpc_load_correlation_device(hpc_ctx *ctx, const double *C_dev);
 /* Copies the FP64 correlation matrix (row-major p x p) to the host. */
 hpc_status hpc_get_correlation(hpc_ctx *ctx, double *C_host);
 
+/* Allocation-free correlation. No counterpart in the reference: it serves callers
+ * that cannot allocate device memory when they need the matrix, such as a plugin
+ * in a host application that owns all GPU memory through its own pool, or a
+ * latency-critical caller that cannot afford the device-wide synchronisation that
+ * cudaMalloc/cudaFree may cause. No context is needed. X_dev (column-major n_obs x p
+ * FP64, device) and C_dev (row-major p x p FP64, device) are the caller's; the
+ * standardised data lives in one library-wide __device__ array of
+ * HPC_NOALLOC_MAX_ELEMS doubles (32 MiB, held by every GPU that loads the library
+ * until the process exits), so n_obs * p above that limit returns HPC_ERR_CAPACITY.
+ * Work is queued on `stream` (a cudaStream_t, NULL = default stream) and is not
+ * waited for. The first call on a device looks up the array's device address;
+ * make it before any stream capture. All calls share the array: calls that
+ * overlap on the GPU race, so order them on one stream. Results equal those of
+ * hpc_correlation_device_f64. */
+#define HPC_NOALLOC_MAX_ELEMS (4LL * 1024 * 1024)
+hpc_status hpc_correlation_noalloc_f64(const double *X_dev, int64_t n_obs, int64_t p, int ref_compat_sd,
+                                       double *C_dev, void *stream);
+
 /* ---- skeleton levels ----------------------------------------------------
  * hpc_run_level replaces SkeletonCalculator::calcLevel (src/independence/skeleton.cpp:104-150):
  * for level >= 1 it first snapshots the neighbour lists (callCompact,

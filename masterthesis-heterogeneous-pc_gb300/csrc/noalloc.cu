@@ -1,0 +1,92 @@
+// Correlation matrix without any device allocation.
+//
+// Some callers cannot allocate device memory at the moment they need a
+// correlation matrix: a plugin inside a host application that owns all of the
+// GPU's memory through its own pool and forbids other allocations, or a
+// latency-critical caller that cannot afford cudaMalloc / cudaFree, which may
+// synchronise the whole device. hpc_correlation_noalloc_f64 serves them: the
+// caller passes the observations and the output matrix (device memory it
+// already owns), and the standardised copy of the data that the Gram reads
+// lives in one file-scope __device__ array instead of a cudaMalloc'd buffer.
+//
+// Limits and rules:
+//  * n_obs * p <= HPC_NOALLOC_MAX_ELEMS (4,194,304 FP64 values, 32 MiB). The
+//    array is part of the library image, so every GPU that loads the library
+//    holds these 32 MiB until the process exits. Larger inputs are rejected
+//    with HPC_ERR_CAPACITY before anything is launched.
+//  * Host code cannot use the array's name as a device address (on the host it
+//    names a host-side stand-in). The first call on each device looks the
+//    address up with cudaGetSymbolAddress, with that device current, and
+//    caches it; make that first call on a device before any stream capture.
+//  * Every call shares the one array and it keeps the last call's contents.
+//    Nothing here needs it cleared: the standardisation writes every one of the
+//    n_obs * p values the Gram then reads. Calls whose work overlaps on the GPU
+//    (different streams, or different host threads) race on the array; order
+//    them on one stream or serialise them.
+//  * No cudaMalloc, cudaFree or allocating library routine is called.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace hpc {
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) double g_corr_scratch[HPC_NOALLOC_MAX_ELEMS];
+
+std::mutex g_scratch_mu;
+double *g_scratch_addr[kMaxDevices] = {};
+
+hpc_status scratch_for_current_device(double **out) {
+  int dev = -1;
+  HPC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("device ordinal %d outside the supported range [0, %d)", dev, kMaxDevices);
+    return HPC_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> g(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_corr_scratch);
+    if (e != cudaSuccess || !ptr) {
+      cudaGetLastError();
+      set_error("cudaGetSymbolAddress of the correlation scratch failed on device %d: %s", dev,
+                cudaGetErrorString(e));
+      return HPC_ERR_CUDA;
+    }
+    g_scratch_addr[dev] = (double *)ptr;
+  }
+  *out = g_scratch_addr[dev];
+  return HPC_OK;
+}
+
+}  // namespace
+}  // namespace hpc
+
+extern "C" hpc_status hpc_correlation_noalloc_f64(const double *X_dev, int64_t n_obs, int64_t p, int ref_compat_sd,
+                                                  double *C_dev, void *stream) {
+  using namespace hpc;
+  if (!X_dev || !C_dev) {
+    set_error("null observation or output pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (p < 1 || n_obs < 2) {
+    set_error("p = %lld, n_obs = %lld: need p >= 1 and n_obs >= 2", (long long)p, (long long)n_obs);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (n_obs > HPC_NOALLOC_MAX_ELEMS / p) {
+    set_error("n_obs * p = %lld exceeds the allocation-free limit of %lld values; use hpc_correlation_device_f64",
+              (long long)n_obs * (long long)p, (long long)HPC_NOALLOC_MAX_ELEMS);
+    return HPC_ERR_CAPACITY;
+  }
+  double *Z = nullptr;
+  hpc_status s = scratch_for_current_device(&Z);
+  if (s != HPC_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((s = launch_standardise_f64(X_dev, n_obs, p, ref_compat_sd, Z, st)) != HPC_OK) return s;
+  const double denom = ref_compat_sd ? (double)((float)n_obs - 1.f) : (double)(n_obs - 1);
+  return launch_gram_f64(Z, n_obs, p, denom, C_dev, st);
+}

@@ -83,6 +83,7 @@ _SIGS = {
     "hpc_load_correlation": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_load_correlation_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_get_correlation": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_correlation_noalloc_f64": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
     "hpc_run_level": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LevelStats)]),
     "hpc_run_skeleton": (C.c_int, [C.c_void_p, C.POINTER(LevelStats), C.c_int, C.POINTER(C.c_int)]),
     "hpc_get_adjacency": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -1,0 +1,68 @@
+"""The allocation-free correlation entry point, through the C ABI.
+
+hpc_correlation_noalloc_f64 is for callers that cannot allocate device memory when
+they need a correlation matrix (a plugin whose host application owns all GPU memory
+through its own pool, or a latency-critical caller that cannot afford the
+device-wide synchronisation of cudaMalloc/cudaFree). It keeps its scratch in one
+library-wide __device__ array shared by every call, so this test checks two calls
+in a row, of different shapes, against the allocating entry point
+(hpc_correlation_device_f64 read back with hpc_get_correlation), and the size limit.
+
+This file is collected last so that a run stopping at the first failure has already
+run every other test; it also passes when run alone in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import heterogpc as hg
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # the correlation tolerance used by the other GPU tests
+
+
+def _reference_correlation(Xd, p, n):
+    sk = hg.SkeletonCalculator(p, n, precision=hg.PREC_FP64)
+    sk.add_observations_device(Xd.data_ptr(), np.float64)
+    out = sk.correlation()
+    sk.close()
+    return out
+
+
+def _noalloc(Xd, p, n, Cd, stream):
+    return hg.lib().hpc_correlation_noalloc_f64(C.c_void_p(Xd.data_ptr()), n, p, 0, C.c_void_p(Cd.data_ptr()),
+                                                C.c_void_p(stream))
+
+
+def test_noalloc_matches_allocating_entry_point_twice():
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    shapes = [(48, 700, 3), (96, 1500, 4)]  # (p, n, seed): the second call reuses the scratch
+    for p, n, seed in shapes:
+        X = hg.sem_generate(p, n, hg.GRAPH_ER, 3.0, seed=seed)  # (p, n): column-major n x p
+        Xd = torch.from_numpy(X).to(dev)
+        Cd = torch.full((p, p), float("nan"), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        st = _noalloc(Xd, p, n, Cd, stream.cuda_stream)
+        assert st == 0, hg.lib().hpc_last_error_string()
+        stream.synchronize()
+        got = Cd.cpu().numpy()
+        want = _reference_correlation(Xd, p, n)
+        assert np.isfinite(got).all()
+        assert np.abs(got - want).max() <= TOL
+
+
+def test_noalloc_rejects_oversize_inputs():
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    limit = 4 * 1024 * 1024
+    p, n = 1024, limit // 1024 + 1
+    Xd = torch.zeros(8, dtype=torch.float64, device=dev)  # never read: the call is refused first
+    Cd = torch.zeros(8, dtype=torch.float64, device=dev)
+    st = hg.lib().hpc_correlation_noalloc_f64(C.c_void_p(Xd.data_ptr()), n, p, 0, C.c_void_p(Cd.data_ptr()), None)
+    assert st == 7  # HPC_ERR_CAPACITY
+    assert b"allocation-free limit" in hg.lib().hpc_last_error_string()
