@@ -199,7 +199,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the library captures its level sequence into a CUDA graph
+    # (not possible on the legacy default stream) and our events bracket its work
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
 
     # data: generated on the host, then resident in HBM
     X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],

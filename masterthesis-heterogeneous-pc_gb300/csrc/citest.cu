@@ -143,15 +143,12 @@ __device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j
   const float ax = 1.0f - sx, ay = 1.0f - sy;
   const float cond = fminf(dmin, fminf(ax, ay));
   if (!(cond > 1e-3f)) return 2;
-  const float r = (rij - sxy) * rsqrtf(ax * ay);
-  if (!isfinite(r)) return 2;
-  const float rr = fminf(fabsf(r), 0.9999999f);
-  const float z = (float)a.sqrt_n3 * atanhf(rr);
-  // error bound of z from the input rounding and the factorisation
-  const float er = (4.0f * a.eps_in + (float)(l + 2) * 2.4e-7f) / cond * (1.0f + rr);
-  const float ez = (float)a.sqrt_n3 * er / fmaxf(1.0f - rr * rr, 1e-6f);
-  if (fabsf(z - a.zc32) <= a.margin_abs + 8.0f * ez) return 2;
-  return z < a.zc32 ? 1 : 0;
+  // |r| = |b| / sqrt(ax * ay) against r_c: no transcendental on this path
+  const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
+  const float dist = rr - a.r_c;
+  const float band = a.margin_r + 8.0f * __fdividef(a.ke, cond);
+  if (!(fabsf(dist) > band)) return 2;  // inside the band, or NaN
+  return dist < 0.0f ? 1 : 0;
 }
 
 __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, int64_t p, unsigned long long t) {
@@ -164,6 +161,8 @@ __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, 
   return lo;
 }
 
+// pv < 0 marks a removal decided in FP32; its FP64 p-value is filled in by the
+// finalize_records post-pass.
 __device__ __forceinline__ void record_removal(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l, double pv) {
   const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
   const uint32_t bit = 1u << (hi & 31);
@@ -171,9 +170,9 @@ __device__ __forceinline__ void record_removal(const LevelArgs &a, int64_t i, in
   if (!(old & bit)) return;  // another lane removed it first
   atomicAnd(a.adj + hi * a.W + (lo >> 5), ~(1u << (lo & 31)));
   atomicAdd(&a.ctr->deleted, 1ull);
-  const unsigned long long slot = atomicAdd(&a.ctr->rec_count, 1ull);
+  const unsigned long long slot = atomicAdd(&a.gctr->rec_count, 1ull);
   if ((long long)slot >= a.rec_cap) {
-    atomicOr(&a.ctr->err, kErrRecOverflow);
+    atomicOr(&a.gctr->err, kErrRecOverflow);
     return;
   }
   hpc_sepset_record *rec = a.recs + slot;
@@ -191,7 +190,10 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
   const int l = LT > 0 ? LT : a.level;
   const int lane = threadIdx.x & 31;
   const unsigned long long total = a.ctr->work_total;
-  const int m = a.tile_tests;
+  if (total == 0) return;
+  // tests per lane per tile: about four tiles per lane of the grid, 1..64
+  const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
+  const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
   int pos[LA], ids[LA];
   for (;;) {
@@ -222,8 +224,11 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
           int res = 2;
           if (MIXED) res = test_f32<LA>(a, i, j, ids, l);
           ++executed;
-          if (res != 0) {
-            if (MIXED && res == 2) ++retests;
+          if (res == 1) {
+            record_removal(a, i, j, ids, l, -1.0);
+            alive = false;
+          } else if (res == 2) {
+            if (MIXED) ++retests;
             const double pv = exact_pvalue<LA>(a.cor64, a.p, a.n_obs, i, j, ids, l);
             if (pv >= a.alpha) {
               record_removal(a, i, j, ids, l, pv);
@@ -261,6 +266,23 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
   }
 }
 
+// FP64 p-values of the removals a level decided in FP32 (records [rec_begin, rec_count)),
+// thread per record; a removal whose FP64 p-value is below alpha is counted as a
+// band violation (the FP32 error bound did not hold).
+__global__ void finalize_records_kernel(LevelArgs a) {
+  const unsigned long long begin = a.ctr->rec_begin;
+  unsigned long long end = a.gctr->rec_count;
+  if (end > (unsigned long long)a.rec_cap) end = (unsigned long long)a.rec_cap;
+  for (unsigned long long r = begin + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; r < end;
+       r += (unsigned long long)gridDim.x * blockDim.x) {
+    hpc_sepset_record *rec = a.recs + r;
+    if (!(rec->pmax < 0.0)) continue;
+    const double pv = exact_pvalue<HPC_MAX_LEVEL>(a.cor64, a.p, a.n_obs, rec->i, rec->j, rec->ids, rec->level);
+    rec->pmax = pv;
+    if (!(pv >= a.alpha)) atomicAdd(&a.ctr->band_violations, 1ull);
+  }
+}
+
 template <bool MIXED>
 void *kernel_for(int level) {
   switch (level) {
@@ -285,6 +307,12 @@ int citest_grid(int precision, int level, int device) {
     per_sm = 1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) sms = 1;
   return per_sm * sms;
+}
+
+hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s) {
+  finalize_records_kernel<<<152 * 2, 128, 0, s>>>(a);
+  HPC_LAUNCH_CHECK("finalize_records_kernel");
+  return HPC_OK;
 }
 
 hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s) {

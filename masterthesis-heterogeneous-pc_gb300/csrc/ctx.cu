@@ -85,9 +85,15 @@ LevelArgs make_args(hpc_ctx *c, int level) {
   a.n_obs = (int)c->n;
   a.alpha = c->opts.alpha;
   a.sqrt_n3 = std::sqrt((double)c->n - 3.0);
-  a.zc32 = (float)c->zc;
-  a.margin_abs = (float)(c->opts.retest_margin * c->zc);
-  a.eps_in = c->opts.precision == HPC_PREC_MIXED_TC ? 4e-6f : 1.2e-7f;
+  // FP32 decision: |r| against r_crit with a band of the configured relative |z|
+  // margin (mapped to |r| through dz/dr = sqrt(n-3) / (1 - r^2)) plus an error bound
+  // ke / (smallest pivot) from the rounding of the FP32 correlation entries and of
+  // the factorisation
+  const double rc = c->r_crit >= 1.5 ? 2.0 : c->r_crit;
+  a.r_c = (float)rc;
+  a.margin_r = rc >= 1.5 ? 0.f : (float)(c->opts.retest_margin * c->zc * (1.0 - rc * rc) / a.sqrt_n3);
+  const double eps_in = c->opts.precision == HPC_PREC_MIXED_TC ? 4e-6 : 1.2e-7;
+  a.ke = (float)((4.0 * eps_in + (level + 2) * 2.4e-7) * (1.0 + std::min(rc, 1.0)));
   a.cor64 = c->cor64;
   a.cor32 = c->cor32;
   a.adj = c->adj;
@@ -97,8 +103,9 @@ LevelArgs make_args(hpc_ctx *c, int level) {
   a.row_work = c->row_work;
   a.recs = c->recs;
   a.rec_cap = c->rec_cap;
-  a.ctr = c->ctr;
-  a.tile_tests = 8;
+  a.colidx_cap = c->colidx_cap;
+  a.ctr = c->ctr + level;
+  a.gctr = c->gctr;
   return a;
 }
 
@@ -112,8 +119,116 @@ hpc_status check_ctx(hpc_ctx *c) {
 }
 
 hpc_status pull_counters(hpc_ctx *c) {
-  HPC_CUDA(cudaMemcpyAsync(c->ctr_host, c->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaMemcpyAsync(c->ctr_host, c->ctr, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1), cudaMemcpyDeviceToHost,
+                           c->stream));
+  HPC_CUDA(cudaMemcpyAsync(c->gctr_host, c->gctr, sizeof(DevGlobal), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
+// Queue all device work of one level on the context stream (no host sync).
+hpc_status enqueue_level(hpc_ctx *c, int level) {
+  hpc_status s;
+  LevelArgs a = make_args(c, level);
+  cudaEvent_t *ev = c->evl[level];
+  HPC_CUDA(cudaEventRecord(ev[0], c->stream));
+  if (level == 0) {
+    const double rc = c->r_crit;
+    const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
+    HPC_CUDA(cudaEventRecord(ev[1], c->stream));
+    if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(ev[2], c->stream));
+    if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
+    if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
+    c->timings.launches += 4;
+    return HPC_OK;
+  }
+  if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
+  if ((s = launch_scan(c->p, level, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
+  if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
+  HPC_CUDA(cudaEventRecord(ev[1], c->stream));
+  if ((s = launch_citest(a, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
+  HPC_CUDA(cudaEventRecord(ev[2], c->stream));
+  c->timings.launches += 4;
+  if (c->opts.precision != HPC_PREC_FP64) {
+    if ((s = launch_finalize_records(a, c->stream)) != HPC_OK) return s;
+    c->timings.launches += 1;
+  }
+  return HPC_OK;
+}
+
+// Neighbour-list and record buffers sized from the level-0 result (counters pulled).
+hpc_status ensure_capacity(hpc_ctx *c, bool *changed) {
+  const int64_t e2 = (int64_t)c->ctr_host[0].edges2;
+  hpc_status s;
+  *changed = false;
+  if (e2 > c->colidx_cap) {
+    dev_free(c->colidx);
+    c->colidx_cap = 0;
+    if ((s = dev_alloc(&c->colidx, std::max<int64_t>(1, e2), "neighbour lists")) != HPC_OK) return s;
+    c->colidx_cap = std::max<int64_t>(1, e2);
+    *changed = true;
+  }
+  if (e2 / 2 > c->rec_cap) {
+    dev_free(c->recs);
+    c->rec_cap = 0;
+    if ((s = dev_alloc(&c->recs, std::max<int64_t>(1, e2 / 2), "separation-set records")) != HPC_OK) return s;
+    c->rec_cap = std::max<int64_t>(1, e2 / 2);
+    *changed = true;
+  }
+  return HPC_OK;
+}
+
+// Per-level statistics and timings from the pulled counters and events.
+hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
+  const DevCounters &h = c->ctr_host[level];
+  hpc_level_stats st{};
+  st.level = level;
+  st.edges_before = c->edges;
+  st.max_degree = level == 0 ? (int)(c->p - 1) : h.max_deg;
+  st.rows = level == 0 ? c->p : h.rows;
+  if (level == 0) {
+    st.potential_tests = st.executed_tests = c->p * (c->p - 1) / 2;
+    st.edges_after = (int64_t)(h.edges2 / 2);
+  } else {
+    st.potential_tests = (int64_t)h.work_total;
+    st.executed_tests = (int64_t)h.tests;
+    st.retests = (int64_t)h.retests;
+    st.edges_after = st.edges_before - (int64_t)h.deleted;
+  }
+  float t_all = 0.f, t_snap = 0.f, t_test = 0.f;
+  HPC_CUDA(cudaEventElapsedTime(&t_snap, c->evl[level][0], c->evl[level][1]));
+  HPC_CUDA(cudaEventElapsedTime(&t_test, c->evl[level][1], c->evl[level][2]));
+  HPC_CUDA(cudaEventElapsedTime(&t_all, c->evl[level][0], level < HPC_MAX_LEVEL && level + 1 < c->next_level
+                                                              ? c->evl[level + 1][0] : c->evl[level][2]));
+  st.ms = t_all;
+  c->timings.level_ms[level] = t_all;
+  c->timings.compact_ms[level] = t_snap;
+  c->timings.test_ms[level] = t_test;
+  c->edges = st.edges_after;
+  if (h.band_violations) {
+    set_error("level %d: %llu FP32 removals not confirmed in FP64 (error bound violated)", level,
+              (unsigned long long)h.band_violations);
+    return HPC_ERR_NUMERIC;
+  }
+  if (c->opts.verbose)
+    printf("level %d: max degree %d, tests %lld of %lld, FP64 re-tests %lld, edges %lld -> %lld, %.3f ms\n", level,
+           st.max_degree, (long long)st.executed_tests, (long long)st.potential_tests, (long long)st.retests,
+           (long long)st.edges_before, (long long)st.edges_after, st.ms);
+  if (out) *out = st;
+  return HPC_OK;
+}
+
+hpc_status global_errors(hpc_ctx *c) {
+  const int err = c->gctr_host->err;
+  if (err & kErrWorkOverflow) {
+    set_error("the number of CI tests of a level overflows 64 bits");
+    return HPC_ERR_CAPACITY;
+  }
+  if (err & kErrRecOverflow) {
+    set_error("separation-set record buffer overflow");
+    return HPC_ERR_CAPACITY;
+  }
   return HPC_OK;
 }
 
@@ -293,28 +408,34 @@ hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n, const hpc_opts *o
   }
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
   c->stream = nullptr;
-  bool ev_ok = cudaEventCreate(&c->ev0) == cudaSuccess && cudaEventCreate(&c->ev1) == cudaSuccess;
+  bool ev_ok = true;
   for (auto &e : c->evc) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
-  for (auto &e : c->evt) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
+  for (auto &lv : c->evl)
+    for (auto &e : lv) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess || !ev_ok) {
     cudaGetLastError();
     set_error("stream/event creation failed");
     return fail(HPC_ERR_CUDA);
   }
   c->stream = c->own_stream;
+  for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
   if ((s = dev_alloc(&c->cor64, p * p, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, p * p, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, p * (int64_t)c->W, "adjacency")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->deg, p, "degrees")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->rowptr, p + 1, "row offsets")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->row_work, p + 1, "row work")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->ctr, 1, "counters")) != HPC_OK) return fail(s);
-  if (cudaMallocHost((void **)&c->ctr_host, sizeof(DevCounters)) != cudaSuccess) {
+  if ((s = dev_alloc(&c->ctr, HPC_MAX_LEVEL + 1, "level counters")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->gctr, 1, "counters")) != HPC_OK) return fail(s);
+  if (cudaMallocHost((void **)&c->ctr_host, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1)) != cudaSuccess ||
+      cudaMallocHost((void **)&c->gctr_host, sizeof(DevGlobal)) != cudaSuccess) {
     cudaGetLastError();
     set_error("pinned counter allocation failed");
     return fail(HPC_ERR_OOM);
   }
-  if (cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream) != cudaSuccess) return fail(HPC_ERR_CUDA);
+  if (cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1), c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal), c->stream) != cudaSuccess)
+    return fail(HPC_ERR_CUDA);
   *out = c;
   return HPC_OK;
 }
@@ -334,13 +455,15 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->row_work);
   dev_free(c->recs);
   dev_free(c->ctr);
+  dev_free(c->gctr);
   if (c->ctr_host) cudaFreeHost(c->ctr_host);
-  if (c->ev0) cudaEventDestroy(c->ev0);
-  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->gctr_host) cudaFreeHost(c->gctr_host);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
   for (auto &e : c->evc)
     if (e) cudaEventDestroy(e);
-  for (auto &e : c->evt)
-    if (e) cudaEventDestroy(e);
+  for (auto &lv : c->evl)
+    for (auto &e : lv)
+      if (e) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   cudaGetLastError();
   delete c;
@@ -379,7 +502,8 @@ hpc_status hpc_get_timings(hpc_ctx *c, hpc_timings *out) {
 hpc_status hpc_ctx_reset(hpc_ctx *c) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
-  HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream));
+  HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1), c->stream));
+  HPC_CUDA(cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal), c->stream));
   c->next_level = 0;
   c->edges = c->p * (c->p - 1) / 2;
   return HPC_OK;
@@ -439,113 +563,143 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     set_error("level %d above HPC_MAX_LEVEL", level);
     return HPC_ERR_INVALID_ARG;
   }
-  hpc_level_stats out{};
-  out.level = level;
-  out.edges_before = c->edges;
-  LevelArgs a = make_args(c, level);
-  HPC_CUDA(cudaEventRecord(c->ev0, c->stream));
-  if (level == 0) {
-    const double rc = c->r_crit;
-    const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
-    if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
-    HPC_CUDA(cudaEventRecord(c->evt[1], c->stream));
-    if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
-    if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, c->ctr, c->stream)) != HPC_OK) return s;
-    HPC_CUDA(cudaEventRecord(c->ev1, c->stream));
-    c->timings.launches += 4;
-    if ((s = pull_counters(c)) != HPC_OK) return s;
-    float t0 = 0.f;
-    HPC_CUDA(cudaEventElapsedTime(&t0, c->ev0, c->evt[1]));
-    c->timings.test_ms[0] = t0;
-    c->timings.compact_ms[0] = 0.0;
-    out.max_degree = (int)(c->p - 1);
-    out.rows = c->p;
-    out.potential_tests = out.executed_tests = c->p * (c->p - 1) / 2;
-    out.edges_after = (int64_t)(c->ctr_host->edges2 / 2);
-  } else {
-    if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
-    if ((s = launch_scan(c->p, level, c->deg, c->rowptr, c->row_work, c->ctr, c->stream)) != HPC_OK) return s;
-    c->timings.launches += 2;
-    if ((s = pull_counters(c)) != HPC_OK) return s;
-    const DevCounters h = *c->ctr_host;
-    c->timings.test_ms[level] = 0.0;
-    if (h.err & kErrWorkOverflow) {
-      set_error("level %d: number of CI tests overflows 64 bits (max degree %d)", level, h.max_deg);
-      return HPC_ERR_CAPACITY;
-    }
-    out.max_degree = h.max_deg;
-    out.rows = h.rows;
-    out.potential_tests = (int64_t)h.work_total;
-    if (h.work_total > 0) {
-      if ((int64_t)h.edges2 > c->colidx_cap) {
-        dev_free(c->colidx);
-        if ((s = dev_alloc(&c->colidx, (int64_t)h.edges2, "neighbour lists")) != HPC_OK) return s;
-        c->colidx_cap = (int64_t)h.edges2;
-      }
-      if (level == 1 && c->rec_cap < (int64_t)(h.edges2 / 2)) {
-        // every removal from level 1 on is one of the edges alive now
-        dev_free(c->recs);
-        const int64_t cap = std::max<int64_t>(1, (int64_t)(h.edges2 / 2));
-        if ((s = dev_alloc(&c->recs, cap, "separation-set records")) != HPC_OK) return s;
-        c->rec_cap = cap;
-      }
-      a = make_args(c, level);
-      if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
-      HPC_CUDA(cudaEventRecord(c->evt[0], c->stream));
-      const int grid = citest_grid(c->opts.precision, level, c->device);
-      const unsigned long long lanes = (unsigned long long)grid * 256ull;
-      unsigned long long m = h.work_total / (lanes * 4ull);
-      a.tile_tests = (int)std::max<unsigned long long>(1ull, std::min<unsigned long long>(64ull, m));
-      if ((s = launch_citest(a, c->opts.precision, grid, c->stream)) != HPC_OK) return s;
-      HPC_CUDA(cudaEventRecord(c->evt[1], c->stream));
-      c->timings.launches += 2;
-    }
-    HPC_CUDA(cudaEventRecord(c->ev1, c->stream));
-    if ((s = pull_counters(c)) != HPC_OK) return s;
-    if (h.work_total > 0) {
-      float tt = 0.f, tc = 0.f;
-      HPC_CUDA(cudaEventElapsedTime(&tt, c->evt[0], c->evt[1]));
-      HPC_CUDA(cudaEventElapsedTime(&tc, c->ev0, c->evt[0]));
-      c->timings.test_ms[level] = tt;
-      c->timings.compact_ms[level] = tc;
-    }
-    const DevCounters h2 = *c->ctr_host;
-    if (h2.err & kErrRecOverflow) {
-      set_error("level %d: separation-set record buffer overflow", level);
-      return HPC_ERR_CAPACITY;
-    }
-    out.executed_tests = (int64_t)h2.tests;
-    out.retests = (int64_t)h2.retests;
-    out.edges_after = out.edges_before - (int64_t)h2.deleted;
+  if (level == 1) {
+    bool changed = false;
+    if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
   }
-  float ms = 0.f;
-  HPC_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-  out.ms = ms;
-  c->timings.level_ms[level] = ms;
-  c->edges = out.edges_after;
+  if ((s = enqueue_level(c, level)) != HPC_OK) return s;
+  if ((s = pull_counters(c)) != HPC_OK) return s;
+  if ((s = global_errors(c)) != HPC_OK) return s;
   c->next_level = level + 1;
-  if (c->opts.verbose)
-    printf("level %d: max degree %d, tests %lld of %lld, FP64 re-tests %lld, edges %lld -> %lld, %.3f ms\n", level,
-           out.max_degree, (long long)out.executed_tests, (long long)out.potential_tests, (long long)out.retests,
-           (long long)out.edges_before, (long long)out.edges_after, out.ms);
-  if (st) *st = out;
-  return HPC_OK;
+  return collect_level(c, level, st);
 }
+
+namespace {
+bool capturable(cudaStream_t s) {
+  return s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
+}
+
+// Run levels first..last (already validated) with one host sync at the end; the
+// whole sequence 0..last is captured once into a CUDA graph and replayed.
+hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
+  hpc_status s;
+  if (use_graph && first == 0 && capturable(c->stream)) {
+    const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
+                       c->graph_colidx_cap == c->colidx_cap && c->graph_rec_cap == c->rec_cap;
+    if (!valid) {
+      if (c->graph) cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+      cudaGraph_t g = nullptr;
+      HPC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      const int64_t launches = c->timings.launches;
+      for (int l = first; l <= last; ++l) {
+        if ((s = enqueue_level(c, l)) != HPC_OK) {
+          cudaStreamEndCapture(c->stream, &g);
+          if (g) cudaGraphDestroy(g);
+          return s;
+        }
+      }
+      c->timings.launches = launches;  // counted when the graph runs
+      HPC_CUDA(cudaStreamEndCapture(c->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        c->graph = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+      }
+      c->graph_top = last;
+      c->graph_stream = c->stream;
+      c->graph_colidx_cap = c->colidx_cap;
+      c->graph_rec_cap = c->rec_cap;
+      // launches of one replay
+      c->graph_launches = 0;
+      for (int l = first; l <= last; ++l) c->graph_launches += l == 0 ? 4 : (c->opts.precision != HPC_PREC_FP64 ? 5 : 4);
+    }
+    HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    c->timings.launches += c->graph_launches;
+  } else {
+    for (int l = first; l <= last; ++l)
+      if ((s = enqueue_level(c, l)) != HPC_OK) return s;
+  }
+  return pull_counters(c);
+}
+}  // namespace
 
 hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if (!c->have_cor) {
+    set_error("run before a correlation matrix was computed or loaded");
+    return HPC_ERR_STATE;
+  }
   const int top = c->opts.max_level < 0 ? HPC_MAX_LEVEL : c->opts.max_level;
   int ran = 0;
-  for (int l = c->next_level; l <= top; ++l) {
+  auto emit = [&](int l) -> hpc_status {
     hpc_level_stats st{};
-    if ((s = hpc_run_level(c, l, &st)) != HPC_OK) return s;
+    hpc_status e = collect_level(c, l, &st);
+    if (e != HPC_OK) return e;
     if (stats && ran < cap) stats[ran] = st;
     ++ran;
-    if (l >= 1 && st.potential_tests == 0) break;
+    return HPC_OK;
+  };
+  // levels run one by one through hpc_run_level before: continue the same way
+  if (c->next_level != 0) {
+    for (int l = c->next_level; l <= top; ++l) {
+      if ((s = hpc_run_level(c, l, nullptr)) != HPC_OK) return s;
+      if ((s = emit(l)) != HPC_OK) return s;
+      if (l >= 1 && c->ctr_host[l].work_total == 0) break;
+    }
+    if (levels_run) *levels_run = ran;
+    return HPC_OK;
   }
-  if (levels_run) *levels_run = ran;
-  return HPC_OK;
+  // A known max level runs as one sequence (one graph replay, one sync); "until
+  // exhausted" runs in chunks of four levels with a check in between.
+  const bool known = c->opts.max_level >= 0;
+  const int chunk = known ? top + 1 : 4;
+  const int64_t edges0 = c->edges;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    ran = 0;
+    c->edges = edges0;
+    bool sized = c->colidx_cap > 0 && c->rec_cap > 0;
+    int first = 0;
+    if (!sized) {
+      // first run: level 0 alone sizes the neighbour-list and record buffers
+      if ((s = run_levels(c, 0, 0, false)) != HPC_OK) return s;
+      bool changed;
+      if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
+      first = 1;
+    }
+    bool overflow = false, done = false;
+    int last_run = first - 1;
+    while (!done && first <= top) {
+      const int last = std::min(top, first + chunk - 1);
+      if ((s = run_levels(c, first, last, known)) != HPC_OK) return s;
+      last_run = last;
+      if (c->gctr_host->err & kErrCsrOverflow) {
+        overflow = true;
+        break;
+      }
+      if ((s = global_errors(c)) != HPC_OK) return s;
+      done = last >= 1 && c->ctr_host[last].work_total == 0;
+      first = last + 1;
+    }
+    if (overflow) {
+      // the data changed since the buffers were sized: resize from level 0 and rerun
+      bool changed;
+      if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
+      if ((s = hpc_ctx_reset(c)) != HPC_OK) return s;
+      continue;
+    }
+    c->next_level = last_run + 1;
+    for (int l = 0; l <= last_run; ++l) {
+      if ((s = emit(l)) != HPC_OK) return s;
+      if (l >= 1 && c->ctr_host[l].work_total == 0) break;
+    }
+    if (levels_run) *levels_run = ran;
+    return HPC_OK;
+  }
+  set_error("neighbour-list buffer still too small after resizing");
+  return HPC_ERR_CAPACITY;
 }
 
 hpc_status hpc_get_adjacency(hpc_ctx *c, uint8_t *out) {
@@ -585,7 +739,7 @@ hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t ca
     return HPC_ERR_INVALID_ARG;
   }
   unsigned long long n = 0;
-  HPC_CUDA(cudaMemcpyAsync(&n, &c->ctr->rec_count, sizeof(n), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaMemcpyAsync(&n, &c->gctr->rec_count, sizeof(n), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   n = std::min<unsigned long long>(n, (unsigned long long)std::max<int64_t>(c->rec_cap, 0));
   *count = (int64_t)n;

@@ -99,7 +99,7 @@ constexpr int kScanThreads = 1024;
 __global__ void __launch_bounds__(kScanThreads) scan_rows_kernel(int64_t p, int level, const int *__restrict__ deg,
                                                                  int *__restrict__ rowptr,
                                                                  unsigned long long *__restrict__ row_work,
-                                                                 DevCounters *ctr) {
+                                                                 DevCounters *ctr, DevGlobal *g) {
   __shared__ unsigned long long s_deg[kScanThreads];
   __shared__ unsigned long long s_work[kScanThreads];
   __shared__ int s_max[kScanThreads / 32];
@@ -154,25 +154,38 @@ __global__ void __launch_bounds__(kScanThreads) scan_rows_kernel(int64_t p, int 
   if (tid == kScanThreads - 1) {
     rowptr[p] = (int)s_deg[kScanThreads - 1];
     row_work[p] = s_work[kScanThreads - 1];
-    ctr->edges2 = s_deg[kScanThreads - 1];
-    ctr->work_total = s_work[kScanThreads - 1];
   }
   if (tid == 0) {
+    ctr->edges2 = s_deg[kScanThreads - 1];
+    ctr->work_total = s_work[kScanThreads - 1];
     int m = 0, r = 0;
     for (int w = 0; w < kScanThreads / 32; ++w) { m = max(m, s_max[w]); r += s_rows[w]; }
     ctr->max_deg = m;
     ctr->rows = r;
-    if (s_over) atomicOr(&ctr->err, kErrWorkOverflow);
+    if (s_over) {
+      atomicOr(&g->err, kErrWorkOverflow);
+      ctr->work_total = 0;  // nothing of this level runs
+    }
     ctr->tile_next = 0;
     ctr->tests = 0;
     ctr->retests = 0;
     ctr->deleted = 0;
+    ctr->band_violations = 0;
+    ctr->rec_begin = g->rec_count;
   }
 }
 
 __global__ void fill_csr_kernel(const uint32_t *__restrict__ adj, int64_t p, int W, const int *__restrict__ rowptr,
-                                int *__restrict__ colidx) {
+                                int *__restrict__ colidx, long long cap, DevCounters *ctr, DevGlobal *g) {
   const int lane = threadIdx.x & 31;
+  if ((long long)ctr->edges2 > cap) {
+    // the neighbour-list buffer is too small for this level: flag it, test nothing
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicOr(&g->err, kErrCsrOverflow);
+      ctr->work_total = 0;
+    }
+    return;
+  }
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = warp; i < p; i += nwarps) {
@@ -219,15 +232,15 @@ hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s) {
 }
 
 hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
-                       DevCounters *ctr, cudaStream_t s) {
-  scan_rows_kernel<<<1, kScanThreads, 0, s>>>(p, level, deg, rowptr, row_work, ctr);
+                       DevCounters *ctr, DevGlobal *g, cudaStream_t s) {
+  scan_rows_kernel<<<1, kScanThreads, 0, s>>>(p, level, deg, rowptr, row_work, ctr, g);
   HPC_LAUNCH_CHECK("scan_rows_kernel");
   return HPC_OK;
 }
 
 hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s) {
   int blocks = (int)std::min<int64_t>((a.p + 7) / 8, 152 * 16);
-  fill_csr_kernel<<<blocks, 256, 0, s>>>(a.adj, a.p, a.W, a.rowptr, colidx);
+  fill_csr_kernel<<<blocks, 256, 0, s>>>(a.adj, a.p, a.W, a.rowptr, colidx, a.colidx_cap, a.ctr, a.gctr);
   HPC_LAUNCH_CHECK("fill_csr_kernel");
   return HPC_OK;
 }

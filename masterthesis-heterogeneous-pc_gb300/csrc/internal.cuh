@@ -30,22 +30,29 @@ hpc_status cuda_fail(cudaError_t e, const char *what, const char *file, int line
 // constants of the statistic (src/executor/independence/cpuInd.cpp:6)
 constexpr double kCutThr = 0.9999999;
 
-// Device counters of one context. Reset per level where noted.
+// Device counters of one level (one slot per level, written by that level's kernels).
 struct DevCounters {
-  unsigned long long tests;        // executed CI tests (per level)
-  unsigned long long retests;      // FP64 re-tests (per level)
-  unsigned long long deleted;      // edges removed (per level)
-  unsigned long long rec_count;    // sepset records written (cumulative)
-  unsigned long long tile_next;    // work-queue head (per level)
-  unsigned long long work_total;   // T_l (per level)
-  unsigned long long edges2;       // sum of degrees at level start
-  int max_deg;                     // at level start
+  unsigned long long tests;        // executed CI tests
+  unsigned long long retests;      // tests re-run in FP64 (band, conditioning, non-finite)
+  unsigned long long deleted;      // edges removed
+  unsigned long long tile_next;    // work-queue head
+  unsigned long long work_total;   // T_l
+  unsigned long long edges2;       // sum of degrees at the level start
+  unsigned long long rec_begin;    // first separation-set record of the level
+  unsigned long long band_violations;  // FP32 removals the FP64 post-pass did not confirm
+  int max_deg;                     // at the level start
   int rows;                        // rows with work at this level
+  int pad[2];
+};
+// Context-wide device counters.
+struct DevGlobal {
+  unsigned long long rec_count;    // separation-set records written (cumulative)
   int err;                         // error bits (kErr*)
   int pad;
 };
 constexpr int kErrRecOverflow = 1;
 constexpr int kErrWorkOverflow = 2;
+constexpr int kErrCsrOverflow = 4;
 
 // Everything a level kernel needs, passed by value.
 struct LevelArgs {
@@ -55,9 +62,9 @@ struct LevelArgs {
   int n_obs;
   double alpha;
   double sqrt_n3;        // sqrt(n - 3)
-  float zc32;            // z_crit in FP32
-  float margin_abs;      // absolute |z| band re-tested in FP64
-  float eps_in;          // relative error bound of cor32 entries
+  float r_c;             // |r| at which p == alpha (FP32)
+  float margin_r;        // |r| half-width of the fixed re-test band
+  float ke;              // error-bound coefficient: |r| error <= ke / (smallest pivot)
   const double *cor64;   // p x p row-major (FP64 correlation)
   const float *cor32;    // p x p row-major (FP32 copy) or null in plain mode
   uint32_t *adj;         // live bitmask p x W
@@ -67,8 +74,9 @@ struct LevelArgs {
   const unsigned long long *row_work;  // exclusive prefix of tests per row (p+1)
   hpc_sepset_record *recs;
   long long rec_cap;
-  DevCounters *ctr;
-  int tile_tests;        // tests per lane per tile
+  long long colidx_cap;
+  DevCounters *ctr;      // this level's counters
+  DevGlobal *gctr;
 };
 
 // ---------------------------------------------------------------------------
@@ -83,9 +91,10 @@ hpc_status launch_to_f32(const double *C, int64_t count, float *C32, cudaStream_
 hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStream_t s);
 hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s);
 hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
-                       DevCounters *ctr, cudaStream_t s);
+                       DevCounters *ctr, DevGlobal *g, cudaStream_t s);
 hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s);
 hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s);
+hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s);
 int citest_grid(int precision, int level, int device);
 
 }  // namespace hpc
@@ -113,12 +122,21 @@ struct hpc_ctx {
   unsigned long long *row_work = nullptr;
   hpc_sepset_record *recs = nullptr;
   int64_t rec_cap = 0;
-  hpc::DevCounters *ctr = nullptr;      // device
+  hpc::DevCounters *ctr = nullptr;      // device, one slot per level (HPC_MAX_LEVEL + 1)
   hpc::DevCounters *ctr_host = nullptr; // pinned mirror
+  hpc::DevGlobal *gctr = nullptr;       // device
+  hpc::DevGlobal *gctr_host = nullptr;  // pinned mirror
   cudaStream_t own_stream = nullptr; // the context's stream; `stream` may be a caller's
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
-  cudaEvent_t evt[2] = {nullptr, nullptr};                    // CI-test kernel
+  cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
+  // CUDA graph of the whole level sequence 0..graph_top, replayed while the
+  // buffers it was captured with stay in place
+  cudaGraphExec_t graph = nullptr;
+  int graph_top = -1;
+  cudaStream_t graph_stream = nullptr;
+  int64_t graph_colidx_cap = 0, graph_rec_cap = 0;
+  int64_t graph_launches = 0;
+  int citest_grid[HPC_MAX_LEVEL + 1] = {};  // persistent grid size per level
   bool cor_timed = false;
   hpc_timings timings{};
   bool have_cor = false;

@@ -146,3 +146,21 @@ def test_extreme_alpha(alpha, max_level):
     for precision in PRECISIONS:
         sk = run_gpu(Cm, 200, alpha, max_level, precision)
         assert np.array_equal(sk.adjacency(), want.adj)
+
+
+def test_graph_replays_and_changing_data():
+    """Repeated runs replay the captured level sequence; loading denser data afterwards
+    outgrows the neighbour-list buffer, which is detected on the device, resized and rerun."""
+    p, n = 150, 1000
+    Xa = gen(dict(p=p, n=n, graph=hg.GRAPH_ER, degree=1.5, seed=71))
+    Xb = gen(dict(p=p, n=n, graph=hg.GRAPH_ER, degree=8.0, seed=72))
+    sk = hg.SkeletonCalculator(p, n, alpha=0.05, max_level=5, precision=hg.PREC_MIXED)
+    for X in (Xa, Xa, Xa, Xb, Xb, Xa):
+        Cm = orc.correlation(X)
+        want = orc.run(Cm, n, 0.05, 5)
+        sk.add_correlation_matrix(Cm)
+        sk.run()
+        assert np.array_equal(sk.adjacency(), want.adj)
+        assert len(sk.sepset_records()) == len(want.records)
+        for got, exp in zip(sk.level_stats, want.levels):
+            assert got["edges_after"] == exp["edges_after"]
