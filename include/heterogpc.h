@@ -89,6 +89,7 @@ typedef struct hpc_timings {
   double compact_ms[HPC_MAX_LEVEL + 1];  /* neighbour-list snapshot of the level */
   double test_ms[HPC_MAX_LEVEL + 1];     /* CI-test kernel of the level */
   int64_t launches;                      /* kernels launched by this context so far */
+  double skeleton_ms;                    /* last hpc_run_skeleton as a whole */
 } hpc_timings;
 
 typedef struct hpc_ctx hpc_ctx;
@@ -112,6 +113,10 @@ hpc_status hpc_ctx_reset(hpc_ctx *ctx);
 /* Orders all of the context's work on `stream` (a cudaStream_t of the same device,
  * owned by the caller) instead of the context's own stream; NULL restores it. */
 hpc_status hpc_ctx_set_stream(hpc_ctx *ctx, void *stream);
+/* hpc_run_skeleton captures its level sequence into a CUDA graph and replays it on
+ * later runs (enable = 1, the default); 0 runs it kernel by kernel, which also
+ * records the per-level kernel timings (graph replays time the whole skeleton only). */
+hpc_status hpc_ctx_set_graphs(hpc_ctx *ctx, int enable);
 /* Device-time breakdown of the context's last correlation and levels. */
 hpc_status hpc_get_timings(hpc_ctx *ctx, hpc_timings *out);
 /* Device bytes held by a context of this shape (admission control). */
@@ -134,6 +139,9 @@ hpc_status hpc_load_correlation(hpc_ctx *ctx, const double *C_host);
 hpc_status hpc_load_correlation_device(hpc_ctx *ctx, const double *C_dev);
 /* Copies the FP64 correlation matrix (row-major p x p) to the host. */
 hpc_status hpc_get_correlation(hpc_ctx *ctx, double *C_host);
+/* Copies the FP32 correlation the mixed-precision tests read (row-major p x p):
+ * the tensor-core split-BF16 Gram in HPC_PREC_MIXED_TC, else the FP32 rounding. */
+hpc_status hpc_get_correlation_f32(hpc_ctx *ctx, float *C_host);
 
 /* Allocation-free correlation. No counterpart in the reference: it serves callers
  * that cannot allocate device memory when they need the matrix, such as a plugin

@@ -92,7 +92,7 @@ LevelArgs make_args(hpc_ctx *c, int level) {
   const double rc = c->r_crit >= 1.5 ? 2.0 : c->r_crit;
   a.r_c = (float)rc;
   a.margin_r = rc >= 1.5 ? 0.f : (float)(c->opts.retest_margin * c->zc * (1.0 - rc * rc) / a.sqrt_n3);
-  const double eps_in = c->opts.precision == HPC_PREC_MIXED_TC ? 4e-6 : 1.2e-7;
+  const double eps_in = c->cor32_rounded ? 1.2e-7 : 4e-6;
   a.ke = (float)((4.0 * eps_in + (level + 2) * 2.4e-7) * (1.0 + std::min(rc, 1.0)));
   a.cor64 = c->cor64;
   a.cor32 = c->cor32;
@@ -127,17 +127,19 @@ hpc_status pull_counters(hpc_ctx *c) {
 }
 
 // Queue all device work of one level on the context stream (no host sync).
-hpc_status enqueue_level(hpc_ctx *c, int level) {
+// `timed` records the per-level events (not inside a graph capture: events
+// recorded by graph nodes cannot be timed).
+hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   hpc_status s;
   LevelArgs a = make_args(c, level);
   cudaEvent_t *ev = c->evl[level];
-  HPC_CUDA(cudaEventRecord(ev[0], c->stream));
+  if (timed) HPC_CUDA(cudaEventRecord(ev[0], c->stream));
   if (level == 0) {
     const double rc = c->r_crit;
     const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
-    HPC_CUDA(cudaEventRecord(ev[1], c->stream));
+    if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
     if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
-    HPC_CUDA(cudaEventRecord(ev[2], c->stream));
+    if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
     if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
     if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
     c->timings.launches += 4;
@@ -146,9 +148,9 @@ hpc_status enqueue_level(hpc_ctx *c, int level) {
   if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
   if ((s = launch_scan(c->p, level, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
   if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
-  HPC_CUDA(cudaEventRecord(ev[1], c->stream));
+  if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
   if ((s = launch_citest(a, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
-  HPC_CUDA(cudaEventRecord(ev[2], c->stream));
+  if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += 4;
   if (c->opts.precision != HPC_PREC_FP64) {
     if ((s = launch_finalize_records(a, c->stream)) != HPC_OK) return s;
@@ -197,10 +199,12 @@ hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
     st.edges_after = st.edges_before - (int64_t)h.deleted;
   }
   float t_all = 0.f, t_snap = 0.f, t_test = 0.f;
-  HPC_CUDA(cudaEventElapsedTime(&t_snap, c->evl[level][0], c->evl[level][1]));
-  HPC_CUDA(cudaEventElapsedTime(&t_test, c->evl[level][1], c->evl[level][2]));
-  HPC_CUDA(cudaEventElapsedTime(&t_all, c->evl[level][0], level < HPC_MAX_LEVEL && level + 1 < c->next_level
-                                                              ? c->evl[level + 1][0] : c->evl[level][2]));
+  if (!c->last_run_graph) {
+    HPC_CUDA(cudaEventElapsedTime(&t_snap, c->evl[level][0], c->evl[level][1]));
+    HPC_CUDA(cudaEventElapsedTime(&t_test, c->evl[level][1], c->evl[level][2]));
+    HPC_CUDA(cudaEventElapsedTime(&t_all, c->evl[level][0], level < HPC_MAX_LEVEL && level + 1 < c->next_level
+                                                                ? c->evl[level + 1][0] : c->evl[level][2]));
+  }
   st.ms = t_all;
   c->timings.level_ms[level] = t_all;
   c->timings.compact_ms[level] = t_snap;
@@ -233,12 +237,25 @@ hpc_status global_errors(hpc_ctx *c) {
 }
 
 hpc_status after_correlation(hpc_ctx *c) {
+  if (c->opts.precision == HPC_PREC_MIXED) {
+    hpc_status s = launch_to_f32(c->cor64, c->p * c->p, c->cor32, c->stream);
+    if (s != HPC_OK) return s;
+    c->timings.launches += 1;
+  }
+  c->have_cor = true;
+  c->cor32_rounded = c->opts.precision != HPC_PREC_MIXED_TC;
+  return hpc_ctx_reset(c);
+}
+
+// A loaded FP64 matrix: every mixed mode tests on its FP32 rounding.
+hpc_status after_loaded_correlation(hpc_ctx *c) {
   if (c->opts.precision != HPC_PREC_FP64) {
     hpc_status s = launch_to_f32(c->cor64, c->p * c->p, c->cor32, c->stream);
     if (s != HPC_OK) return s;
     c->timings.launches += 1;
   }
   c->have_cor = true;
+  c->cor32_rounded = true;
   return hpc_ctx_reset(c);
 }
 
@@ -257,16 +274,44 @@ hpc_status correlation_device(hpc_ctx *c, const T *X) {
     c->Z_elems = elems;
   }
   HPC_CUDA(cudaEventRecord(c->evc[0], c->stream));
-  if (sizeof(T) == 8)
-    s = launch_standardise_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
-  else
-    s = launch_standardise_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
-  if (s != HPC_OK) return s;
-  HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
   const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
-  if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
-  HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
-  c->timings.launches += 2;
+  if (c->opts.precision == HPC_PREC_MIXED_TC) {
+    // split-BF16 operands + FP64 standardised copy, tensor-core Gram into cor32
+    const int64_t tc = tc_p_pad(c->p) * 3 * tc_n_pad(c->n);
+    if (c->tc_elems < tc) {
+      dev_free(c->tcP);
+      dev_free(c->tcQ);
+      c->tc_elems = 0;
+      if ((s = dev_alloc(&c->tcP, tc, "tensor-core operand P")) != HPC_OK) return s;
+      if ((s = dev_alloc(&c->tcQ, tc, "tensor-core operand Q")) != HPC_OK) return s;
+      HPC_CUDA(cudaMemsetAsync(c->tcP, 0, sizeof(__nv_bfloat16) * tc, c->stream));
+      HPC_CUDA(cudaMemsetAsync(c->tcQ, 0, sizeof(__nv_bfloat16) * tc, c->stream));
+      c->tc_elems = tc;
+    }
+    if (sizeof(T) == 8)
+      s = launch_standardise_split_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->tcP, c->tcQ,
+                                       c->stream);
+    else
+      s = launch_standardise_split_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->tcP, c->tcQ,
+                                       c->stream);
+    if (s != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
+    if ((s = launch_gram_tc(c->tcP, c->tcQ, c->n, c->p, c->cor32, &c->gctr->err, c->stream)) != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+    // FP64 entries for the exact path
+    if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
+    c->timings.launches += 3;
+  } else {
+    if (sizeof(T) == 8)
+      s = launch_standardise_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
+    else
+      s = launch_standardise_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
+    if (s != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
+    if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+    c->timings.launches += 2;
+  }
   if ((s = after_correlation(c)) != HPC_OK) return s;
   HPC_CUDA(cudaEventRecord(c->evc[3], c->stream));
   c->cor_timed = true;
@@ -410,6 +455,7 @@ hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n, const hpc_opts *o
   c->stream = nullptr;
   bool ev_ok = true;
   for (auto &e : c->evc) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
+  for (auto &e : c->evr) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
   for (auto &lv : c->evl)
     for (auto &e : lv) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess || !ev_ok) {
@@ -447,6 +493,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->cor64);
   dev_free(c->cor32);
   dev_free(c->Z);
+  dev_free(c->tcP);
+  dev_free(c->tcQ);
   if (c->X_stage) cudaFree(c->X_stage);
   dev_free(c->adj);
   dev_free(c->deg);
@@ -460,6 +508,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   if (c->gctr_host) cudaFreeHost(c->gctr_host);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (auto &e : c->evc)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : c->evr)
     if (e) cudaEventDestroy(e);
   for (auto &lv : c->evl)
     for (auto &e : lv)
@@ -475,6 +525,13 @@ hpc_status hpc_ctx_set_stream(hpc_ctx *c, void *stream) {
   if (s != HPC_OK) return s;
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_set_graphs(hpc_ctx *c, int enable) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  c->graphs_enabled = enable != 0;
   return HPC_OK;
 }
 
@@ -522,7 +579,7 @@ hpc_status hpc_load_correlation(hpc_ctx *c, const double *C) {
     return HPC_ERR_INVALID_ARG;
   }
   HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyHostToDevice, c->stream));
-  return after_correlation(c);
+  return after_loaded_correlation(c);
 }
 
 hpc_status hpc_load_correlation_device(hpc_ctx *c, const double *C) {
@@ -533,7 +590,7 @@ hpc_status hpc_load_correlation_device(hpc_ctx *c, const double *C) {
     return HPC_ERR_INVALID_ARG;
   }
   HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToDevice, c->stream));
-  return after_correlation(c);
+  return after_loaded_correlation(c);
 }
 
 hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
@@ -544,6 +601,18 @@ hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
     return !C ? HPC_ERR_INVALID_ARG : HPC_ERR_STATE;
   }
   HPC_CUDA(cudaMemcpyAsync(C, c->cor64, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
+hpc_status hpc_get_correlation_f32(hpc_ctx *c, float *C) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!C || !c->have_cor || !c->cor32) {
+    set_error(!C ? "null output pointer" : "no FP32 correlation (plain FP64 precision or none computed)");
+    return !C ? HPC_ERR_INVALID_ARG : HPC_ERR_STATE;
+  }
+  HPC_CUDA(cudaMemcpyAsync(C, c->cor32, sizeof(float) * (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   return HPC_OK;
 }
@@ -567,7 +636,8 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     bool changed = false;
     if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
   }
-  if ((s = enqueue_level(c, level)) != HPC_OK) return s;
+  if ((s = enqueue_level(c, level, true)) != HPC_OK) return s;
+  c->last_run_graph = false;
   if ((s = pull_counters(c)) != HPC_OK) return s;
   if ((s = global_errors(c)) != HPC_OK) return s;
   c->next_level = level + 1;
@@ -583,7 +653,7 @@ bool capturable(cudaStream_t s) {
 // whole sequence 0..last is captured once into a CUDA graph and replayed.
 hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
   hpc_status s;
-  if (use_graph && first == 0 && capturable(c->stream)) {
+  if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
                        c->graph_colidx_cap == c->colidx_cap && c->graph_rec_cap == c->rec_cap;
     if (!valid) {
@@ -593,7 +663,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
       HPC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
       const int64_t launches = c->timings.launches;
       for (int l = first; l <= last; ++l) {
-        if ((s = enqueue_level(c, l)) != HPC_OK) {
+        if ((s = enqueue_level(c, l, false)) != HPC_OK) {
           cudaStreamEndCapture(c->stream, &g);
           if (g) cudaGraphDestroy(g);
           return s;
@@ -617,9 +687,11 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
     }
     HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
     c->timings.launches += c->graph_launches;
+    c->last_run_graph = true;
   } else {
     for (int l = first; l <= last; ++l)
-      if ((s = enqueue_level(c, l)) != HPC_OK) return s;
+      if ((s = enqueue_level(c, l, true)) != HPC_OK) return s;
+    c->last_run_graph = false;
   }
   return pull_counters(c);
 }
@@ -657,6 +729,7 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
   const bool known = c->opts.max_level >= 0;
   const int chunk = known ? top + 1 : 4;
   const int64_t edges0 = c->edges;
+  HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
   for (int attempt = 0; attempt < 2; ++attempt) {
     ran = 0;
     c->edges = edges0;
@@ -691,6 +764,13 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
       continue;
     }
     c->next_level = last_run + 1;
+    HPC_CUDA(cudaEventRecord(c->evr[1], c->stream));
+    HPC_CUDA(cudaEventSynchronize(c->evr[1]));
+    float tr = 0.f;
+    HPC_CUDA(cudaEventElapsedTime(&tr, c->evr[0], c->evr[1]));
+    c->timings.skeleton_ms = tr;
+    // a first run sized its buffers with level 0 alone: the events of that part
+    // are of the eager kind, the rest may be a graph replay
     for (int l = 0; l <= last_run; ++l) {
       if ((s = emit(l)) != HPC_OK) return s;
       if (l >= 1 && c->ctr_host[l].work_total == 0) break;

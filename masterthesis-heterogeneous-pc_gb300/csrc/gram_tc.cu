@@ -1,0 +1,404 @@
+// Split-BF16 correlation Gram on the 5th-generation tensor cores (tcgen05 + TMA).
+//
+// Replaces the reference's gpuPMCC (src/correlation/corHelper.cu:79-116), which
+// spends one 64-thread block of FP64 SIMT work per (i, j) pair, with the one dense
+// contraction of the path done on the tensor cores:
+//
+//   z  = (x - mean) / sd / sqrt(n - 1)          (FP64, per variable)
+//   hi = bf16(z),  lo = bf16(z - hi)
+//   P  = [hi | hi | lo],  Q = [hi | lo | hi]    (K' = 3 * n_pad, K-major rows)
+//   C  = P Q^T = hi.hi + hi.lo + lo.hi          (FP32 accumulation in TMEM)
+//
+// so one BF16 GEMM with K' = 3n gives the three products of the split. Only
+// upper-triangle 128 x 128 tiles are computed; each is written twice (direct and
+// mirrored), diagonal tiles from their upper half only, so C is exactly symmetric.
+//
+// Kernel structure (one CTA of 4 warps per tile, 6-stage shared-memory ring):
+//   warp 0 lane 0   TMA producer: cp.async.bulk.tensor of the A (rows of P) and B
+//                   (rows of Q) 128 x 64 tiles, 128-byte swizzle, into stage s,
+//                   completion counted on full[s] (expect_tx)
+//   warp 1 lane 0   MMA issuer: 4 x tcgen05.mma.kind::f16 (M=128, N=128, K=16) per
+//                   stage, accumulator in 128 TMEM columns, tcgen05.commit to
+//                   empty[s] (frees the stage) and finally to `done`
+//   warps 0-3       epilogue: tcgen05.ld 32x32b of their 32 TMEM lanes (rows)
+// Every mbarrier wait is bounded by a %globaltimer deadline; on time-out the CTA
+// records kErrTimeout, stops issuing, waits (bounded) for what it already issued,
+// frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "internal.cuh"
+
+namespace hpc {
+namespace {
+
+constexpr int TM = 128, TN = 128, TK = 64;  // tile: 128 x 128 outputs, 64 bf16 (128 B) of K per stage
+constexpr int kStages = 6;
+constexpr int kStageBytesA = TM * TK * 2;   // 16 KB
+constexpr int kStageBytesB = TN * TK * 2;   // 16 KB
+constexpr int kStageBytes = kStageBytesA + kStageBytesB;
+constexpr int kTmemCols = 128;
+constexpr int kThreadsTc = 128;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on the phase with the given parity; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (stride byte offset), descriptor version bits 46-48 = 0b001.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(16u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor of tcgen05.mma.kind::f16: D = F32, A = B = BF16, both
+// K-major, N = 128, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                            ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct alignas(1024) TcSmem {
+  uint8_t stage[kStages][kStageBytes];
+  uint64_t full[kStages];
+  uint64_t empty[kStages];
+  uint64_t done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__global__ void __launch_bounds__(kThreadsTc, 1)
+    gram_tc_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapQ, int64_t p,
+                   int nb, int kblocks, float *__restrict__ C, int *__restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  TcSmem &sm = *reinterpret_cast<TcSmem *>((((uintptr_t)smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // tile (bi, bj), bi <= bj, from the linear block index over the upper triangle
+  int64_t t = blockIdx.x;
+  int bi = 0;
+  while (t >= nb - bi) {
+    t -= nb - bi;
+    ++bi;
+  }
+  const int bj = bi + (int)t;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], 1);
+    }
+    mbar_init(&sm.done, 1);
+    sm.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = sm.tmem_base;
+
+  int issued = 0;  // producer: stage fills issued
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % kStages;
+      if (kb >= kStages && !mbar_wait(&sm.empty[s], ((kb / kStages) + 1) & 1)) {
+        atomicOr(err, kErrTimeout);
+        atomicExch(&sm.abort, 1);
+        break;
+      }
+      if (*(volatile int *)&sm.abort) break;
+      mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
+      tma_load_2d(sm.stage[s], &mapP, kb * TK, bi * TM, &sm.full[s]);
+      tma_load_2d(sm.stage[s] + kStageBytesA, &mapQ, kb * TK, bj * TN, &sm.full[s]);
+      ++issued;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    int kb = 0;
+    for (; kb < kblocks; ++kb) {
+      const int s = kb % kStages;
+      if (!mbar_wait(&sm.full[s], (kb / kStages) & 1)) {
+        atomicOr(err, kErrTimeout);
+        atomicExch(&sm.abort, 1);
+        break;
+      }
+      if (*(volatile int *)&sm.abort) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(sm.stage[s]), b0 = a0 + kStageBytesA;
+#pragma unroll
+      for (int k = 0; k < TK / 16; ++k) {
+        // 16 bf16 = 32 bytes further along K inside the 128-byte swizzled row
+        mma_bf16(tmem, smem_desc_sw128(a0 + k * 32), smem_desc_sw128(b0 + k * 32), (kb > 0 || k > 0) ? 1u : 0u);
+      }
+      mma_commit(&sm.empty[s]);
+    }
+    mma_commit(&sm.done);  // arrives once every MMA issued above has completed
+  }
+  // everyone: wait for the accumulator (bounded)
+  const bool ok = mbar_wait(&sm.done, 0);
+  if (!ok) atomicOr(err, kErrTimeout);
+  __syncwarp();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok && !sm.abort) {
+    const int r = warp * 32 + lane;  // TMEM lane = tile row
+    const int64_t row = (int64_t)bi * TM + r;
+    const bool diag = bi == bj;
+#pragma unroll 1
+    for (int c0 = 0; c0 < TN; c0 += 32) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int cc = c0 + q;
+        const int64_t col = (int64_t)bj * TN + cc;
+        if (row < p && col < p && (!diag || cc >= r)) {
+          C[row * p + col] = v[q];
+          C[col * p + row] = v[q];
+        }
+      }
+    }
+  }
+  // before freeing TMEM and exiting, the producer's copies must have landed: wait
+  // (bounded) for the last phase of every stage it filled
+  if (warp == 0 && lane == 0 && sm.abort) {
+    for (int s = 0; s < kStages; ++s) {
+      const int fills = issued / kStages + (s < issued % kStages ? 1 : 0);
+      if (fills > 0) mbar_wait(&sm.full[s], (fills - 1) & 1);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// standardisation into the split operands (and the FP64 copy used for exact re-tests)
+template <typename TIn>
+__global__ void __launch_bounds__(256) standardise_split_kernel(const TIn *__restrict__ X, int64_t n, int64_t p,
+                                                               int64_t n_pad, int ref_compat,
+                                                               double *__restrict__ Z64,
+                                                               __nv_bfloat16 *__restrict__ P,
+                                                               __nv_bfloat16 *__restrict__ Q) {
+  const int64_t v = blockIdx.x;
+  if (v >= p) return;
+  const TIn *x = X + v * n;
+  __shared__ double red[8];
+  __shared__ long long redc[8];
+  __shared__ double mean_s, sd_s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double s = 0.0;
+  long long c = 0;
+  for (int64_t k = threadIdx.x; k < n; k += 256) {
+    double a = (double)x[k];
+    if (!isnan(a)) { s += a; ++c; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if (lane == 0) { red[wid] = s; redc[wid] = c; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    long long tc = 0;
+    for (int w = 0; w < 8; ++w) { t += red[w]; tc += redc[w]; }
+    mean_s = t / (double)tc;
+  }
+  __syncthreads();
+  const double mean = mean_s;
+  double ss = 0.0;
+  for (int64_t k = threadIdx.x; k < n; k += 256) {
+    double a = (double)x[k];
+    if (!isnan(a)) { double d = a - mean; ss += d * d; }
+  }
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  __syncthreads();
+  if (lane == 0) red[wid] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    sd_s = ref_compat ? (double)sqrtf((float)(t / (double)((float)n - 1.f))) : sqrt(t / (double)(n - 1));
+  }
+  __syncthreads();
+  const double sd = sd_s;
+  const double denom = ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
+  const double scale = 1.0 / sqrt(denom);
+  const int64_t K = 3 * n_pad;
+  __nv_bfloat16 *pr = P + v * K, *qr = Q + v * K;
+  for (int64_t k = threadIdx.x; k < n_pad; k += 256) {
+    double z = 0.0;
+    if (k < n) {
+      double a = (double)x[k];
+      z = isnan(a) ? 0.0 : (a - mean) / sd;
+      Z64[v * n + k] = z;
+    }
+    const double zs = z * scale;
+    const __nv_bfloat16 hi = __double2bfloat16(zs);
+    const __nv_bfloat16 lo = __double2bfloat16(zs - (double)__bfloat162float(hi));
+    pr[k] = hi;
+    pr[n_pad + k] = hi;
+    pr[2 * n_pad + k] = lo;
+    qr[k] = hi;
+    qr[n_pad + k] = lo;
+    qr[2 * n_pad + k] = hi;
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+hpc_status make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int64_t K, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return HPC_ERR_CUDA;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(K * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return HPC_ERR_CUDA;
+  }
+  return HPC_OK;
+}
+
+}  // namespace
+
+int64_t tc_n_pad(int64_t n) { return (n + TK - 1) / TK * TK; }
+int64_t tc_p_pad(int64_t p) { return (p + TM - 1) / TM * TM; }
+
+hpc_status launch_standardise_split_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z64,
+                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s) {
+  standardise_split_kernel<double><<<(unsigned)p, 256, 0, s>>>(X, n, p, tc_n_pad(n), ref_compat, Z64, P, Q);
+  HPC_LAUNCH_CHECK("standardise_split_kernel<double>");
+  return HPC_OK;
+}
+
+hpc_status launch_standardise_split_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z64,
+                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s) {
+  standardise_split_kernel<float><<<(unsigned)p, 256, 0, s>>>(X, n, p, tc_n_pad(n), ref_compat, Z64, P, Q);
+  HPC_LAUNCH_CHECK("standardise_split_kernel<float>");
+  return HPC_OK;
+}
+
+// C (p x p FP32, row-major) = P Q^T over upper-triangle tiles, mirrored.
+// P and Q: tc_p_pad(p) rows of 3 * tc_n_pad(n) bf16, zero padded.
+hpc_status launch_gram_tc(const __nv_bfloat16 *P, const __nv_bfloat16 *Q, int64_t n, int64_t p, float *C, int *err,
+                          cudaStream_t s) {
+  const int64_t rows = tc_p_pad(p), K = 3 * tc_n_pad(n);
+  CUtensorMap mp, mq;
+  hpc_status st;
+  if ((st = make_map(&mp, P, rows, K, TM)) != HPC_OK) return st;
+  if ((st = make_map(&mq, Q, rows, K, TN)) != HPC_OK) return st;
+  const int nb = (int)(rows / TM);
+  const int64_t tiles = (int64_t)nb * (nb + 1) / 2;
+  const int smem = (int)sizeof(TcSmem) + 1024;
+  HPC_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  gram_tc_kernel<<<(unsigned)tiles, kThreadsTc, smem, s>>>(mp, mq, p, nb, (int)(K / TK), C, err);
+  HPC_LAUNCH_CHECK("gram_tc_kernel");
+  return HPC_OK;
+}
+
+}  // namespace hpc

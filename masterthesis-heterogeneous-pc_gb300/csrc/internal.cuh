@@ -1,5 +1,6 @@
 // Internal declarations shared by the CUDA translation units of libheterogpc.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -53,6 +54,7 @@ struct DevGlobal {
 constexpr int kErrRecOverflow = 1;
 constexpr int kErrWorkOverflow = 2;
 constexpr int kErrCsrOverflow = 4;
+constexpr int kErrTimeout = 8;
 
 // Everything a level kernel needs, passed by value.
 struct LevelArgs {
@@ -88,6 +90,14 @@ hpc_status launch_standardise_f32(const float *X, int64_t n, int64_t p, int ref_
 hpc_status launch_gram_f64(const double *Z, int64_t n, int64_t p, double inv_denom, double *C,
                            cudaStream_t s);
 hpc_status launch_to_f32(const double *C, int64_t count, float *C32, cudaStream_t s);
+int64_t tc_n_pad(int64_t n);
+int64_t tc_p_pad(int64_t p);
+hpc_status launch_standardise_split_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z64,
+                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
+hpc_status launch_standardise_split_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z64,
+                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
+hpc_status launch_gram_tc(const __nv_bfloat16 *P, const __nv_bfloat16 *Q, int64_t n, int64_t p, float *C, int *err,
+                          cudaStream_t s);
 hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStream_t s);
 hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s);
 hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
@@ -110,8 +120,10 @@ struct hpc_ctx {
   int W = 0;
   double *cor64 = nullptr;
   float *cor32 = nullptr;
-  double *Z = nullptr;          // standardised data (n x p), transient
+  double *Z = nullptr;          // standardised data (n x p)
   int64_t Z_elems = 0;
+  __nv_bfloat16 *tcP = nullptr, *tcQ = nullptr;  // split-BF16 operands of the tensor-core Gram
+  int64_t tc_elems = 0;
   void *X_stage = nullptr;      // device copy of host observations
   int64_t X_stage_bytes = 0;
   uint32_t *adj = nullptr;
@@ -136,10 +148,14 @@ struct hpc_ctx {
   cudaStream_t graph_stream = nullptr;
   int64_t graph_colidx_cap = 0, graph_rec_cap = 0;
   int64_t graph_launches = 0;
+  bool graphs_enabled = true;
+  bool last_run_graph = false;
+  cudaEvent_t evr[2] = {nullptr, nullptr};  // whole skeleton run
   int citest_grid[HPC_MAX_LEVEL + 1] = {};  // persistent grid size per level
   bool cor_timed = false;
   hpc_timings timings{};
   bool have_cor = false;
+  bool cor32_rounded = true;   // cor32 is the FP32 rounding of cor64 (else the tensor-core Gram)
   int next_level = 0;
   int64_t edges = 0;           // undirected edges after the last level
   double zc = 0.0;             // z_crit (FP64)

@@ -50,12 +50,13 @@ class SepsetRecord(C.Structure):
 class Timings(C.Structure):
     _fields_ = [("standardise_ms", C.c_double), ("gram_ms", C.c_double), ("convert_ms", C.c_double),
                 ("level_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("compact_ms", C.c_double * (HPC_MAX_LEVEL + 1)),
-                ("test_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("launches", C.c_int64)]
+                ("test_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("launches", C.c_int64),
+                ("skeleton_ms", C.c_double)]
 
     def as_dict(self):
         return {"standardise_ms": self.standardise_ms, "gram_ms": self.gram_ms, "convert_ms": self.convert_ms,
                 "level_ms": list(self.level_ms), "compact_ms": list(self.compact_ms), "test_ms": list(self.test_ms),
-                "launches": self.launches}
+                "launches": self.launches, "skeleton_ms": self.skeleton_ms}
 
 
 class SemParams(C.Structure):
@@ -76,6 +77,7 @@ _SIGS = {
     "hpc_ctx_footprint": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(Opts), C.POINTER(C.c_int64)]),
     "hpc_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_get_timings": (C.c_int, [C.c_void_p, C.POINTER(Timings)]),
+    "hpc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "hpc_correlation_f64": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_correlation_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_correlation_device_f64": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -83,6 +85,7 @@ _SIGS = {
     "hpc_load_correlation": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_load_correlation_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_get_correlation": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_get_correlation_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_correlation_noalloc_f64": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
     "hpc_run_level": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LevelStats)]),
     "hpc_run_skeleton": (C.c_int, [C.c_void_p, C.POINTER(LevelStats), C.c_int, C.POINTER(C.c_int)]),
@@ -243,6 +246,9 @@ class SkeletonCalculator:
         """Run on a caller-owned cudaStream_t (an int handle, e.g. torch's cuda_stream)."""
         _check(lib().hpc_ctx_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None))
 
+    def set_graphs(self, enable):
+        _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
+
     def timings(self):
         t = Timings()
         _check(lib().hpc_get_timings(self._h, C.byref(t)))
@@ -270,6 +276,11 @@ class SkeletonCalculator:
     def correlation(self):
         out = np.empty((self.p, self.p), np.float64)
         _check(lib().hpc_get_correlation(self._h, _ptr(out)))
+        return out
+
+    def correlation_f32(self):
+        out = np.empty((self.p, self.p), np.float32)
+        _check(lib().hpc_get_correlation_f32(self._h, _ptr(out)))
         return out
 
     def adjacency(self):
