@@ -312,7 +312,7 @@ def main():
         e2e_total = float(t.item())
     W = (p + 31) // 32
     e2e = {"value": world * args.steps / e2e_total, "unit": "skeletons/s", "h2d_bytes_per_step": p * p * 8,
-           "d2h_bytes_per_step": p * W * 4}
+           "d2h_bytes_per_step": p * p}
 
     if rank != 0:
         if dist:

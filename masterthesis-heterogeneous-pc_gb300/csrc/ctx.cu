@@ -497,6 +497,7 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->tcQ);
   if (c->X_stage) cudaFree(c->X_stage);
   dev_free(c->adj);
+  dev_free(c->adj_bytes);
   dev_free(c->deg);
   dev_free(c->rowptr);
   dev_free(c->colidx);
@@ -789,16 +790,16 @@ hpc_status hpc_get_adjacency(hpc_ctx *c, uint8_t *out) {
     set_error("null output pointer");
     return HPC_ERR_INVALID_ARG;
   }
-  std::vector<uint32_t> bits((size_t)(c->p * c->W));
   if (c->next_level == 0) {
     for (int64_t i = 0; i < c->p; ++i)
       for (int64_t j = 0; j < c->p; ++j) out[i * c->p + j] = (uint8_t)(i != j);
     return HPC_OK;
   }
-  HPC_CUDA(cudaMemcpyAsync(bits.data(), c->adj, bits.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (!c->adj_bytes && (s = dev_alloc(&c->adj_bytes, c->p * c->p, "adjacency bytes")) != HPC_OK) return s;
+  if ((s = launch_expand_adjacency(c->adj, c->p, c->W, c->adj_bytes, c->stream)) != HPC_OK) return s;
+  c->timings.launches += 1;
+  HPC_CUDA(cudaMemcpyAsync(out, c->adj_bytes, (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
-  for (int64_t i = 0; i < c->p; ++i)
-    for (int64_t j = 0; j < c->p; ++j) out[i * c->p + j] = (uint8_t)((bits[i * c->W + (j >> 5)] >> (j & 31)) & 1u);
   return HPC_OK;
 }
 

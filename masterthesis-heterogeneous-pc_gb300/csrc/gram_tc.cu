@@ -13,14 +13,23 @@
 // upper-triangle 128 x 128 tiles are computed; each is written twice (direct and
 // mirrored), diagonal tiles from their upper half only, so C is exactly symmetric.
 //
-// Kernel structure (one CTA of 4 warps per tile, 6-stage shared-memory ring):
+// The tensor core rounds its FP32 accumulator once per MMA; along K = 3n that is
+// thousands of roundings with a systematic bias (measured about 3e-5 on sums of
+// magnitude 1). So the accumulation restarts every kGroup k-blocks in one of two
+// TMEM buffers while the epilogue warps drain the other into FP32 registers
+// (round-to-nearest adds): about 3n/256 register additions per output instead.
+//
+// Kernel structure (one CTA of 6 warps per tile, 6-stage shared-memory ring):
 //   warp 0 lane 0   TMA producer: cp.async.bulk.tensor of the A (rows of P) and B
 //                   (rows of Q) 128 x 64 tiles, 128-byte swizzle, into stage s,
 //                   completion counted on full[s] (expect_tx)
 //   warp 1 lane 0   MMA issuer: 4 x tcgen05.mma.kind::f16 (M=128, N=128, K=16) per
-//                   stage, accumulator in 128 TMEM columns, tcgen05.commit to
-//                   empty[s] (frees the stage) and finally to `done`
-//   warps 0-3       epilogue: tcgen05.ld 32x32b of their 32 TMEM lanes (rows)
+//                   stage into TMEM buffer g % 2 (128 columns each), tcgen05.commit
+//                   to empty[s] (frees the stage) and, after each group of kGroup
+//                   stages, to acc_full[g % 2]
+//   warps 2-5       accumulate: tcgen05.ld 32x32b of their TMEM lane quadrant
+//                   (warp % 4), add into 128 registers per thread, arrive on
+//                   acc_empty[g % 2]; finally write the tile
 // Every mbarrier wait is bounded by a %globaltimer deadline; on time-out the CTA
 // records kErrTimeout, stops issuing, waits (bounded) for what it already issued,
 // frees its TMEM and returns.
@@ -38,8 +47,9 @@ constexpr int kStages = 6;
 constexpr int kStageBytesA = TM * TK * 2;   // 16 KB
 constexpr int kStageBytesB = TN * TK * 2;   // 16 KB
 constexpr int kStageBytes = kStageBytesA + kStageBytesB;
-constexpr int kTmemCols = 128;
-constexpr int kThreadsTc = 128;
+constexpr int kTmemCols = 256;   // two 128-column accumulators
+constexpr int kGroup = 4;        // k-blocks (16 MMAs) per accumulation group
+constexpr int kThreadsTc = 192;  // producer warp, MMA warp, 4 accumulator warps
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -133,14 +143,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 struct alignas(1024) TcSmem {
   uint8_t stage[kStages][kStageBytes];
   uint64_t full[kStages];
   uint64_t empty[kStages];
-  uint64_t done;
+  uint64_t acc_full[2];
+  uint64_t acc_empty[2];
+  uint64_t drain;
   uint32_t tmem_base;
   int abort;
 };
+
+__device__ __forceinline__ bool aborted(TcSmem &sm) { return *(volatile int *)&sm.abort != 0; }
+__device__ __forceinline__ void fail(TcSmem &sm, int *err) {
+  atomicOr(err, kErrTimeout);
+  atomicExch(&sm.abort, 1);
+}
 
 __global__ void __launch_bounds__(kThreadsTc, 1)
     gram_tc_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapQ, int64_t p,
@@ -163,7 +185,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       mbar_init(&sm.full[s], 1);
       mbar_init(&sm.empty[s], 1);
     }
-    mbar_init(&sm.done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.acc_full[b], 1);
+      mbar_init(&sm.acc_empty[b], 4);  // one arrival per accumulator warp
+    }
+    mbar_init(&sm.drain, 1);
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -182,58 +208,85 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     for (int kb = 0; kb < kblocks; ++kb) {
       const int s = kb % kStages;
       if (kb >= kStages && !mbar_wait(&sm.empty[s], ((kb / kStages) + 1) & 1)) {
-        atomicOr(err, kErrTimeout);
-        atomicExch(&sm.abort, 1);
+        fail(sm, err);
         break;
       }
-      if (*(volatile int *)&sm.abort) break;
+      if (aborted(sm)) break;
       mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
       tma_load_2d(sm.stage[s], &mapP, kb * TK, bi * TM, &sm.full[s]);
       tma_load_2d(sm.stage[s] + kStageBytesA, &mapQ, kb * TK, bj * TN, &sm.full[s]);
       ++issued;
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    int kb = 0;
-    for (; kb < kblocks; ++kb) {
-      const int s = kb % kStages;
-      if (!mbar_wait(&sm.full[s], (kb / kStages) & 1)) {
-        atomicOr(err, kErrTimeout);
-        atomicExch(&sm.abort, 1);
+    // MMA issuer: group g accumulates k-blocks [g*kGroup, (g+1)*kGroup) into buffer g % 2
+    const int groups = (kblocks + kGroup - 1) / kGroup;
+    for (int g = 0; g < groups && !aborted(sm); ++g) {
+      const int b = g & 1;
+      if (g >= 2 && !mbar_wait(&sm.acc_empty[b], ((g >> 1) + 1) & 1)) {
+        fail(sm, err);
         break;
       }
-      if (*(volatile int *)&sm.abort) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = smem_u32(sm.stage[s]), b0 = a0 + kStageBytesA;
+      const uint32_t dcol = tmem + (uint32_t)(b * 128);
+      const int kb_end = min(kblocks, (g + 1) * kGroup);
+      for (int kb = g * kGroup; kb < kb_end; ++kb) {
+        const int s = kb % kStages;
+        if (!mbar_wait(&sm.full[s], (kb / kStages) & 1)) {
+          fail(sm, err);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a0 = smem_u32(sm.stage[s]), b0 = a0 + kStageBytesA;
 #pragma unroll
-      for (int k = 0; k < TK / 16; ++k) {
-        // 16 bf16 = 32 bytes further along K inside the 128-byte swizzled row
-        mma_bf16(tmem, smem_desc_sw128(a0 + k * 32), smem_desc_sw128(b0 + k * 32), (kb > 0 || k > 0) ? 1u : 0u);
+        for (int k = 0; k < TK / 16; ++k) {
+          // 16 bf16 = 32 bytes further along K inside the 128-byte swizzled row
+          mma_bf16(dcol, smem_desc_sw128(a0 + k * 32), smem_desc_sw128(b0 + k * 32),
+                   (kb > g * kGroup || k > 0) ? 1u : 0u);
+        }
+        mma_commit(&sm.empty[s]);
       }
-      mma_commit(&sm.empty[s]);
+      mma_commit(&sm.acc_full[b]);  // arrives when this group's MMAs have completed
     }
-    mma_commit(&sm.done);  // arrives once every MMA issued above has completed
-  }
-  // everyone: wait for the accumulator (bounded)
-  const bool ok = mbar_wait(&sm.done, 0);
-  if (!ok) atomicOr(err, kErrTimeout);
-  __syncwarp();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok && !sm.abort) {
-    const int r = warp * 32 + lane;  // TMEM lane = tile row
-    const int64_t row = (int64_t)bi * TM + r;
-    const bool diag = bi == bj;
-#pragma unroll 1
-    for (int c0 = 0; c0 < TN; c0 += 32) {
-      float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+    // every MMA issued above has completed before TMEM is freed
+    mma_commit(&sm.drain);
+    if (!mbar_wait(&sm.drain, 0)) fail(sm, err);
+  } else if (warp >= 2) {
+    // accumulator warps: TMEM lane quadrant warp % 4 = rows 32*(warp%4) .. +31
+    const int quad = warp & 3;
+    float acc[TN];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int cc = c0 + q;
+    for (int q = 0; q < TN; ++q) acc[q] = 0.f;
+    const int groups = (kblocks + kGroup - 1) / kGroup;
+    bool ok = true;
+    for (int g = 0; g < groups; ++g) {
+      const int b = g & 1;
+      if (!mbar_wait(&sm.acc_full[b], (g >> 1) & 1)) {
+        fail(sm, err);
+        ok = false;
+        break;
+      }
+      __syncwarp();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c0 = 0; c0 < TN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * 128 + c0), v);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) acc[c0 + q] += v[q];
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[b]);
+    }
+    if (ok && !aborted(sm)) {
+      const int r = quad * 32 + lane;  // tile row
+      const int64_t row = (int64_t)bi * TM + r;
+      const bool diag = bi == bj;
+#pragma unroll
+      for (int cc = 0; cc < TN; ++cc) {
         const int64_t col = (int64_t)bj * TN + cc;
         if (row < p && col < p && (!diag || cc >= r)) {
-          C[row * p + col] = v[q];
-          C[col * p + row] = v[q];
+          C[row * p + col] = acc[cc];
+          C[col * p + row] = acc[cc];
         }
       }
     }

@@ -15,6 +15,8 @@
 // warp-per-row ballot/scan that writes the ascending neighbour ids.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.cuh"
 #include "stats.cuh"
 
@@ -210,7 +212,31 @@ __global__ void fill_csr_kernel(const uint32_t *__restrict__ adj, int64_t p, int
   }
 }
 
+// p x p bytes (1 = edge) from the bitmask, 4 bytes per thread
+__global__ void expand_adjacency_kernel(const uint32_t *__restrict__ adj, int64_t p, int W, uint8_t *__restrict__ out) {
+  const int64_t total = p * p;
+  for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 4; t < total;
+       t += (int64_t)gridDim.x * blockDim.x * 4) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t e = t + k;
+      if (e < total) {
+        const int64_t i = e / p, j = e - i * p;
+        out[e] = (uint8_t)((adj[i * W + (j >> 5)] >> (j & 31)) & 1u);
+      }
+    }
+  }
+}
+
 }  // namespace
+
+hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s) {
+  const int64_t total = p * p;
+  int blocks = (int)std::min<int64_t>((total / 4 + 255) / 256 + 1, 152 * 32);
+  expand_adjacency_kernel<<<blocks, 256, 0, s>>>(adj, p, W, out);
+  HPC_LAUNCH_CHECK("expand_adjacency_kernel");
+  return HPC_OK;
+}
 
 hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStream_t s) {
   const int64_t total = a.p * (int64_t)a.W;

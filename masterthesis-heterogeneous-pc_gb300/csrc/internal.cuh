@@ -103,6 +103,7 @@ hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s);
 hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
                        DevCounters *ctr, DevGlobal *g, cudaStream_t s);
 hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s);
+hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
 hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s);
 hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s);
 int citest_grid(int precision, int level, int device);
@@ -127,6 +128,7 @@ struct hpc_ctx {
   void *X_stage = nullptr;      // device copy of host observations
   int64_t X_stage_bytes = 0;
   uint32_t *adj = nullptr;
+  uint8_t *adj_bytes = nullptr;  // p x p expansion for hpc_get_adjacency
   int *deg = nullptr;
   int *rowptr = nullptr;
   int *colidx = nullptr;

@@ -42,6 +42,7 @@ def _newer(out, deps):
 def _headers():
     hs = [os.path.join(INCLUDE, "heterogpc.h")]
     hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hs += [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".hpp", ".h"))]
     return hs
 
 
@@ -75,7 +76,20 @@ def build_library(jobs=8):
     so = os.path.join(LIB, "libheterogpc.so")
     if not _newer(so, objs):
         _run([NVCC, "-shared", *ARCH, "-o", so, *objs, "-cudart", "shared", "-lpthread"])
+    build_cli(so)
     return so
+
+
+CLI_SOURCES = ["main.cpp", "skeleton.cpp", "csv.cpp"]
+
+
+def build_cli(so):
+    """The heterogpc command line, linked against libheterogpc.so (rpath to lib/)."""
+    objs = [_compile_host(os.path.join(HOST, f), extra=("-I", HOST)) for f in CLI_SOURCES]
+    exe = os.path.join(LIB, "heterogpc")
+    if not _newer(exe, objs + [so]):
+        _run(["g++", "-o", exe, *objs, "-L", LIB, "-lheterogpc", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+    return exe
 
 
 def build_oracle():
