@@ -44,25 +44,38 @@ __device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, 
   return (*w >> (j & 31)) & 1u;
 }
 
-// FP64 p-value of the test (i, j | ids) with the reference's semantics.
-template <int LA>
-__device__ __noinline__ double exact_pvalue(const double *__restrict__ C, int64_t p, int n_obs, int64_t i, int64_t j,
-                                            const int *ids, int l) {
-  if (l == 1) return pval_l1_64(C[i * p + j], C[i * p + ids[0]], C[j * p + ids[0]], n_obs);
-  const int k = l + 2;
-  double M[(LA + 2) * (LA + 2)];
-  for (int q = 0; q < k * k; ++q) M[q] = 0.0;
-  for (int q = 0; q < k; ++q) M[q * k + q] = 1.0;
-  M[1] = M[k] = C[i * p + j];
-  for (int q = 2; q < k; ++q) {
-    M[q] = M[q * k] = C[i * p + ids[q - 2]];
-    M[k + q] = M[q * k + 1] = C[j * p + ids[q - 2]];
+// FP64 correlation entries: read from the FP64 matrix when there is one, else
+// the dot product of the FP64-standardised columns (the tensor-core mode keeps no
+// p x p FP64 matrix). Index order as the reference reads cor[row * p + col].
+struct ExactSrc {
+  const double *cor64;
+  const double *Z;
+  int64_t p, n;
+  double denom;
+  __device__ double entry(int64_t x, int64_t y) const {
+    if (cor64) return cor64[x * p + y];
+    const double *a = Z + x * n, *b = Z + y * n;
+    double s = 0.0;
+    for (int64_t k = 0; k < n; ++k) s = fma(a[k], b[k], s);
+    return s / denom;
   }
-  for (int r = 2; r < k; ++r)
-    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = C[(int64_t)ids[r - 2] * p + ids[c - 2]];
+};
+
+__device__ __forceinline__ ExactSrc exact_src(const LevelArgs &a) {
+  return ExactSrc{a.cor64, a.Z, a.p, a.n_z, a.denom};
+}
+
+// FP64 p-value of a k x k submatrix M (row-major, ordered i, j, S; overwritten)
+// with the reference's semantics: closed form at l = 1 (cpuInd.cpp:16-27); at
+// l >= 2 NaN -> no removal, else the pseudoinverse partial correlation
+// (cpuInd.cpp:29-38), by Cholesky when well conditioned, by Jacobi pinv with
+// arma::pinv's tolerance otherwise.
+template <int LA>
+__device__ __noinline__ double pvalue_of_matrix(double *M, int l, int n_obs) {
+  const int k = l + 2;
+  if (l == 1) return pval_l1_64(M[1], M[2], M[k + 2], n_obs);
   for (int q = 0; q < k * k; ++q)
     if (isnan(M[q])) return nan("");  // cpuInd.cpp:31-33: NaN p-value, edge kept
-  // Cholesky of the S block (rows/cols 2..k-1), forward solves for x = M[0][S], y = M[1][S]
   double Lm[LA * (LA + 1) / 2], wx[LA], wy[LA];
   double dmin = 1.0;
   for (int r = 0; r < l; ++r) {
@@ -82,26 +95,38 @@ __device__ __noinline__ double exact_pvalue(const double *__restrict__ C, int64_
     wx[r] = vx / lrr;
     wy[r] = vy / lrr;
   }
-  double r_partial;
   if (dmin > 1e-10) {
     double ax = 1.0, ay = 1.0, b = M[1];
     for (int q = 0; q < l; ++q) { ax -= wx[q] * wx[q]; ay -= wy[q] * wy[q]; b -= wx[q] * wy[q]; }
-    if (ax > 1e-10 && ay > 1e-10) {
-      r_partial = b / sqrt(ax * ay);
-      return calc_pvalue64(r_partial, n_obs);
-    }
+    if (ax > 1e-10 && ay > 1e-10) return calc_pvalue64(b / sqrt(ax * ay), n_obs);
   }
-  // ill-conditioned: pseudoinverse semantics
   double V[(LA + 2) * (LA + 2)];
   double p00, p01, p11;
   pinv_sym64_corner(M, k, V, &p00, &p01, &p11);
-  r_partial = -p01 / sqrt(p00 * p11);
-  return calc_pvalue64(r_partial, n_obs);
+  return calc_pvalue64(-p01 / sqrt(p00 * p11), n_obs);
+}
+
+// FP64 p-value of the test (i, j | ids), entries from `src`.
+template <int LA>
+__device__ __noinline__ double exact_pvalue(const ExactSrc &src, int n_obs, int64_t i, int64_t j, const int *ids,
+                                            int l) {
+  const int k = l + 2;
+  double M[(LA + 2) * (LA + 2)];
+  for (int q = 0; q < k * k; ++q) M[q] = 0.0;
+  for (int q = 0; q < k; ++q) M[q * k + q] = 1.0;
+  M[1] = M[k] = src.entry(i, j);
+  for (int q = 2; q < k; ++q) {
+    M[q] = M[q * k] = src.entry(i, ids[q - 2]);
+    M[k + q] = M[q * k + 1] = src.entry(j, ids[q - 2]);
+  }
+  for (int r = 2; r < k; ++r)
+    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = src.entry(ids[r - 2], ids[c - 2]);
+  return pvalue_of_matrix<LA>(M, l, n_obs);
 }
 
 // FP32 test. Returns 1 = remove, 0 = keep, 2 = undecided (re-test in FP64).
 template <int LA>
-__device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l) {
+__device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l, float *rr_out) {
   const float *__restrict__ C = a.cor32;
   const int64_t p = a.p;
   const float rij = __ldg(C + i * p + j);
@@ -145,6 +170,7 @@ __device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j
   if (!(cond > 1e-3f)) return 2;
   // |r| = |b| / sqrt(ax * ay) against r_c: no transcendental on this path
   const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
+  *rr_out = rr;
   const float dist = rr - a.r_c;
   const float band = a.margin_r + 8.0f * __fdividef(a.ke, cond);
   if (!(fabsf(dist) > band)) return 2;  // inside the band, or NaN
@@ -182,6 +208,19 @@ __device__ __forceinline__ void record_removal(const LevelArgs &a, int64_t i, in
   rec->pad = 0;
   rec->pmax = pv;
   for (int q = 0; q < HPC_MAX_LEVEL; ++q) rec->ids[q] = q < l ? ids[q] : -1;
+}
+
+// Defer an undecided test to the FP64 re-test kernel; false when the queue is full.
+__device__ __forceinline__ bool push_retest(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l) {
+  const unsigned long long slot = atomicAdd(&a.ctr->rq_count, 1ull);
+  if ((long long)slot >= a.rq_cap) return false;
+  RetestItem *it = a.rq + slot;
+  it->i = (int32_t)i;
+  it->j = (int32_t)j;
+  it->level = l;
+  it->pad = 0;
+  for (int q = 0; q < HPC_MAX_LEVEL; ++q) it->ids[q] = q < l ? ids[q] : -1;
+  return true;
 }
 
 template <int LT, bool MIXED>
@@ -222,17 +261,25 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
           for (int q = 0; q < LA; ++q)
             if (q < l) ids[q] = a.colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
           int res = 2;
-          if (MIXED) res = test_f32<LA>(a, i, j, ids, l);
+          float rr = 0.f;
+          if (MIXED) res = test_f32<LA>(a, i, j, ids, l, &rr);
           ++executed;
           if (res == 1) {
-            record_removal(a, i, j, ids, l, -1.0);
+            // decided in FP32; the p-value is filled in by the post-pass (the
+            // negative value carries |r| for the mode without an FP64 matrix)
+            record_removal(a, i, j, ids, l, -1.0 - (double)rr);
             alive = false;
           } else if (res == 2) {
             if (MIXED) ++retests;
-            const double pv = exact_pvalue<LA>(a.cor64, a.p, a.n_obs, i, j, ids, l);
-            if (pv >= a.alpha) {
-              record_removal(a, i, j, ids, l, pv);
-              alive = false;
+            // without an FP64 matrix the FP64 re-test is deferred to the warp-
+            // cooperative re-test kernel; inline (serial dot products) only if
+            // its queue is full
+            if (!(MIXED && !a.cor64 && push_retest(a, i, j, ids, l))) {
+              const double pv = exact_pvalue<LA>(exact_src(a), a.n_obs, i, j, ids, l);
+              if (pv >= a.alpha) {
+                record_removal(a, i, j, ids, l, pv);
+                alive = false;
+              }
             }
           }
         }
@@ -277,9 +324,70 @@ __global__ void finalize_records_kernel(LevelArgs a) {
        r += (unsigned long long)gridDim.x * blockDim.x) {
     hpc_sepset_record *rec = a.recs + r;
     if (!(rec->pmax < 0.0)) continue;
-    const double pv = exact_pvalue<HPC_MAX_LEVEL>(a.cor64, a.p, a.n_obs, rec->i, rec->j, rec->ids, rec->level);
+    if (!a.cor64) {
+      // no FP64 matrix: the p-value of the FP32 partial correlation
+      rec->pmax = calc_pvalue64(-1.0 - rec->pmax, a.n_obs);
+      continue;
+    }
+    const double pv = exact_pvalue<HPC_MAX_LEVEL>(exact_src(a), a.n_obs, rec->i, rec->j, rec->ids, rec->level);
     rec->pmax = pv;
     if (!(pv >= a.alpha)) atomicAdd(&a.ctr->band_violations, 1ull);
+  }
+}
+
+__device__ __forceinline__ double warp_dot(const double *__restrict__ x, const double *__restrict__ y, int64_t n) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int64_t k = lane; k < n; k += 32) s = fma(x[k], y[k], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// FP64 re-tests deferred by the level kernels (tensor-core mode): one warp per
+// queued test computes the FP64 correlation entries it needs as dot products of
+// the FP64-standardised columns, lane 0 evaluates the reference formula. Level-0
+// items set the kept lower-triangle bit; level >= 1 items remove the edge.
+constexpr int kRetestWarps = 8;
+__global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(LevelArgs a) {
+  __shared__ double Ms[kRetestWarps][(HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2)];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double *M = Ms[wib];
+  unsigned long long count = a.ctr->rq_count;
+  if (count > (unsigned long long)a.rq_cap) count = (unsigned long long)a.rq_cap;
+  const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+  const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  const double *Z = a.Z;
+  const int64_t n = a.n_z;
+  for (unsigned long long q = warp; q < count; q += nwarps) {
+    const RetestItem it = a.rq[q];
+    const int64_t i = it.i, j = it.j;
+    const int l = it.level;
+    if (l == 0) {
+      const double r = warp_dot(Z + i * n, Z + j * n, n) / a.denom;
+      if (lane == 0 && !(calc_pvalue64(r, a.n_obs) >= a.alpha))
+        atomicOr(a.adj + i * a.W + (j >> 5), 1u << (j & 31));  // kept: lower-triangle bit (i > j)
+      continue;
+    }
+    if (!live_bit(a.adj, a.W, i, j)) continue;  // removed by another test meanwhile
+    const int k = l + 2;
+    int V[HPC_MAX_LEVEL + 2];
+    V[0] = (int)i;
+    V[1] = (int)j;
+    for (int t = 0; t < l; ++t) V[2 + t] = it.ids[t];
+    for (int r = 0; r < k; ++r) {
+      if (lane == 0) M[r * k + r] = 1.0;
+      for (int c = r + 1; c < k; ++c) {
+        const double v = warp_dot(Z + (int64_t)V[r] * n, Z + (int64_t)V[c] * n, n) / a.denom;
+        if (lane == 0) M[r * k + c] = M[c * k + r] = v;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const double pv = pvalue_of_matrix<HPC_MAX_LEVEL>(M, l, a.n_obs);
+      if (pv >= a.alpha) record_removal(a, i, j, it.ids, l, pv);
+    }
+    __syncwarp();
   }
 }
 
@@ -307,6 +415,12 @@ int citest_grid(int precision, int level, int device) {
     per_sm = 1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) sms = 1;
   return per_sm * sms;
+}
+
+hpc_status launch_retest(const LevelArgs &a, int sms, cudaStream_t s) {
+  retest_kernel<<<sms * 4, kRetestWarps * 32, 0, s>>>(a);
+  HPC_LAUNCH_CHECK("retest_kernel");
+  return HPC_OK;
 }
 
 hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s) {

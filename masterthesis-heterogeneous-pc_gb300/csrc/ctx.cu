@@ -77,6 +77,12 @@ void dev_free(T *&ptr) {
   ptr = nullptr;
 }
 
+// Absolute error bound of the tensor-core (split-BF16, FP32-accumulated) correlation
+// entries used by the FP32 decision bands: the rounding of the low halves (2^-17
+// relative per value) averages over the n samples, plus the FP32 accumulation;
+// four times the model, which bounds the measured errors of tests/test_gpu_tensorcore.py.
+double tc_entry_err(int64_t n) { return 4.0 * (1.6e-5 / std::sqrt((double)n) + 1e-7); }
+
 LevelArgs make_args(hpc_ctx *c, int level) {
   LevelArgs a{};
   a.p = c->p;
@@ -92,10 +98,15 @@ LevelArgs make_args(hpc_ctx *c, int level) {
   const double rc = c->r_crit >= 1.5 ? 2.0 : c->r_crit;
   a.r_c = (float)rc;
   a.margin_r = rc >= 1.5 ? 0.f : (float)(c->opts.retest_margin * c->zc * (1.0 - rc * rc) / a.sqrt_n3);
-  const double eps_in = c->cor32_rounded ? 1.2e-7 : 4e-6;
+  const double eps_in = c->cor32_rounded ? 1.2e-7 : tc_entry_err(c->n);
   a.ke = (float)((4.0 * eps_in + (level + 2) * 2.4e-7) * (1.0 + std::min(rc, 1.0)));
-  a.cor64 = c->cor64;
+  a.cor64 = c->cor64_valid ? c->cor64 : nullptr;
   a.cor32 = c->cor32;
+  a.Z = c->Z;
+  a.n_z = c->n;
+  a.denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
+  a.rq = c->rq;
+  a.rq_cap = c->rq_cap;
   a.adj = c->adj;
   a.deg = c->deg;
   a.rowptr = c->rowptr;
@@ -136,9 +147,20 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   if (timed) HPC_CUDA(cudaEventRecord(ev[0], c->stream));
   if (level == 0) {
     const double rc = c->r_crit;
-    const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
     if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-    if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
+    if (c->cor64_valid) {
+      const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
+      if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
+    } else {
+      // FP32 tensor-core entries: band of the entry error bound, FP64 re-tests queued
+      const double d0 = tc_entry_err(c->n) + 1e-6 * rc;
+      const float lo = rc >= 1.5 ? 2.f : (float)(rc - d0), hi = rc >= 1.5 ? 2.f : (float)(rc + d0);
+      HPC_CUDA(cudaMemsetAsync(&a.ctr->rq_count, 0, sizeof(unsigned long long), c->stream));
+      if ((s = launch_level0_f32(a, lo, hi, c->stream)) != HPC_OK) return s;
+      if ((s = launch_retest(a, c->sm_count, c->stream)) != HPC_OK) return s;
+      if ((s = launch_mirror(a, c->stream)) != HPC_OK) return s;
+      c->timings.launches += 1;
+    }
     if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
     if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
     if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
@@ -150,6 +172,10 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
   if ((s = launch_citest(a, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
+  if (!c->cor64_valid) {
+    if ((s = launch_retest(a, c->sm_count, c->stream)) != HPC_OK) return s;
+    c->timings.launches += 1;
+  }
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += 4;
   if (c->opts.precision != HPC_PREC_FP64) {
@@ -256,6 +282,7 @@ hpc_status after_loaded_correlation(hpc_ctx *c) {
   }
   c->have_cor = true;
   c->cor32_rounded = true;
+  c->cor64_valid = true;
   return hpc_ctx_reset(c);
 }
 
@@ -277,7 +304,7 @@ hpc_status correlation_device(hpc_ctx *c, const T *X) {
   const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
   if (c->opts.precision == HPC_PREC_MIXED_TC) {
     // split-BF16 operands + FP64 standardised copy, tensor-core Gram into cor32
-    const int64_t tc = tc_p_pad(c->p) * 3 * tc_n_pad(c->n);
+    const int64_t tc = tc_p_pad(c->p) * tc_k(c->n);
     if (c->tc_elems < tc) {
       dev_free(c->tcP);
       dev_free(c->tcQ);
@@ -298,9 +325,14 @@ hpc_status correlation_device(hpc_ctx *c, const T *X) {
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
     if ((s = launch_gram_tc(c->tcP, c->tcQ, c->n, c->p, c->cor32, &c->gctr->err, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
-    // FP64 entries for the exact path
-    if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
-    c->timings.launches += 3;
+    // FP64 entries come from dot products of Z in the re-test kernels: no FP64 matrix
+    if (!c->rq) {
+      const int64_t cap = 1 << 20;
+      if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
+      c->rq_cap = cap;
+    }
+    c->cor64_valid = false;
+    c->timings.launches += 2;
   } else {
     if (sizeof(T) == 8)
       s = launch_standardise_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
@@ -310,6 +342,7 @@ hpc_status correlation_device(hpc_ctx *c, const T *X) {
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
     if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+    c->cor64_valid = true;
     c->timings.launches += 2;
   }
   if ((s = after_correlation(c)) != HPC_OK) return s;
@@ -465,7 +498,7 @@ hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n, const hpc_opts *o
   }
   c->stream = c->own_stream;
   for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
-  if ((s = dev_alloc(&c->cor64, p * p, "cor64")) != HPC_OK) return fail(s);
+  if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, p * p, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, p * p, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, p * (int64_t)c->W, "adjacency")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->deg, p, "degrees")) != HPC_OK) return fail(s);
@@ -498,6 +531,7 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   if (c->X_stage) cudaFree(c->X_stage);
   dev_free(c->adj);
   dev_free(c->adj_bytes);
+  dev_free(c->rq);
   dev_free(c->deg);
   dev_free(c->rowptr);
   dev_free(c->colidx);
@@ -579,6 +613,7 @@ hpc_status hpc_load_correlation(hpc_ctx *c, const double *C) {
     set_error("null correlation pointer");
     return HPC_ERR_INVALID_ARG;
   }
+  if (!c->cor64 && (s = dev_alloc(&c->cor64, c->p * c->p, "cor64")) != HPC_OK) return s;
   HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyHostToDevice, c->stream));
   return after_loaded_correlation(c);
 }
@@ -590,6 +625,7 @@ hpc_status hpc_load_correlation_device(hpc_ctx *c, const double *C) {
     set_error("null correlation pointer");
     return HPC_ERR_INVALID_ARG;
   }
+  if (!c->cor64 && (s = dev_alloc(&c->cor64, c->p * c->p, "cor64")) != HPC_OK) return s;
   HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToDevice, c->stream));
   return after_loaded_correlation(c);
 }
@@ -600,6 +636,13 @@ hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
   if (!C || !c->have_cor) {
     set_error(!C ? "null output pointer" : "no correlation matrix yet");
     return !C ? HPC_ERR_INVALID_ARG : HPC_ERR_STATE;
+  }
+  if (!c->cor64_valid) {
+    // tensor-core mode keeps no FP64 matrix: form it from the standardised data
+    if (!c->cor64 && (s = dev_alloc(&c->cor64, c->p * c->p, "cor64")) != HPC_OK) return s;
+    const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
+    if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
+    c->cor64_valid = true;
   }
   HPC_CUDA(cudaMemcpyAsync(C, c->cor64, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
@@ -656,6 +699,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
   hpc_status s;
   if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
+                       c->graph_cor64_valid == c->cor64_valid &&
                        c->graph_colidx_cap == c->colidx_cap && c->graph_rec_cap == c->rec_cap;
     if (!valid) {
       if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -680,6 +724,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
       }
       c->graph_top = last;
       c->graph_stream = c->stream;
+      c->graph_cor64_valid = c->cor64_valid;
       c->graph_colidx_cap = c->colidx_cap;
       c->graph_rec_cap = c->rec_cap;
       // launches of one replay

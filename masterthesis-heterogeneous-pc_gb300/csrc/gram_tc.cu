@@ -6,10 +6,13 @@
 //
 //   z  = (x - mean) / sd / sqrt(n - 1)          (FP64, per variable)
 //   hi = bf16(z),  lo = bf16(z - hi)
-//   P  = [hi | hi | lo],  Q = [hi | lo | hi]    (K' = 3 * n_pad, K-major rows)
-//   C  = P Q^T = hi.hi + hi.lo + lo.hi          (FP32 accumulation in TMEM)
+//   P  = [hi | hi | lo | lo],  Q = [hi | lo | hi | lo]    (K' = 4 * n_pad, K-major rows)
+//   C  = P Q^T = hi.hi + hi.lo + lo.hi + lo.lo            (FP32 accumulation in TMEM)
 //
-// so one BF16 GEMM with K' = 3n gives the three products of the split. Only
+// so one BF16 GEMM with K' = 4n gives the products of the split. With lo.lo the
+// product of the two 16-bit representations is complete and what is left is the
+// rounding of lo (2^-17 relative per value), which averages out over n samples;
+// without it a systematic error of about 2^-18 |r| remains. Only
 // upper-triangle 128 x 128 tiles are computed; each is written twice (direct and
 // mirrored), diagonal tiles from their upper half only, so C is exactly symmetric.
 //
@@ -44,6 +47,7 @@ namespace {
 
 constexpr int TM = 128, TN = 128, TK = 64;  // tile: 128 x 128 outputs, 64 bf16 (128 B) of K per stage
 constexpr int kStages = 6;
+constexpr int kSlices = 4;       // K' = kSlices * n_pad: hi.hi, hi.lo, lo.hi, lo.lo
 constexpr int kStageBytesA = TM * TK * 2;   // 16 KB
 constexpr int kStageBytesB = TN * TK * 2;   // 16 KB
 constexpr int kStageBytes = kStageBytesA + kStageBytesB;
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(256) standardise_split_kernel(const TIn *__res
   const double sd = sd_s;
   const double denom = ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
   const double scale = 1.0 / sqrt(denom);
-  const int64_t K = 3 * n_pad;
+  const int64_t K = kSlices * n_pad;
   __nv_bfloat16 *pr = P + v * K, *qr = Q + v * K;
   for (int64_t k = threadIdx.x; k < n_pad; k += 256) {
     double z = 0.0;
@@ -373,9 +377,11 @@ __global__ void __launch_bounds__(256) standardise_split_kernel(const TIn *__res
     pr[k] = hi;
     pr[n_pad + k] = hi;
     pr[2 * n_pad + k] = lo;
+    pr[3 * n_pad + k] = lo;
     qr[k] = hi;
     qr[n_pad + k] = lo;
     qr[2 * n_pad + k] = hi;
+    qr[3 * n_pad + k] = lo;
   }
 }
 
@@ -421,6 +427,7 @@ hpc_status make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int
 
 int64_t tc_n_pad(int64_t n) { return (n + TK - 1) / TK * TK; }
 int64_t tc_p_pad(int64_t p) { return (p + TM - 1) / TM * TM; }
+int64_t tc_k(int64_t n) { return kSlices * tc_n_pad(n); }
 
 hpc_status launch_standardise_split_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z64,
                                         __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s) {
@@ -437,10 +444,10 @@ hpc_status launch_standardise_split_f32(const float *X, int64_t n, int64_t p, in
 }
 
 // C (p x p FP32, row-major) = P Q^T over upper-triangle tiles, mirrored.
-// P and Q: tc_p_pad(p) rows of 3 * tc_n_pad(n) bf16, zero padded.
+// P and Q: tc_p_pad(p) rows of tc_k(n) bf16, zero padded.
 hpc_status launch_gram_tc(const __nv_bfloat16 *P, const __nv_bfloat16 *Q, int64_t n, int64_t p, float *C, int *err,
                           cudaStream_t s) {
-  const int64_t rows = tc_p_pad(p), K = 3 * tc_n_pad(n);
+  const int64_t rows = tc_p_pad(p), K = kSlices * tc_n_pad(n);
   CUtensorMap mp, mq;
   hpc_status st;
   if ((st = make_map(&mp, P, rows, K, TM)) != HPC_OK) return st;

@@ -52,6 +52,48 @@ __global__ void level0_lower_kernel(LevelArgs a, double r_lo, double r_hi) {
   }
 }
 
+// Level 0 on the FP32 correlation of the tensor-core mode (no FP64 matrix): pairs
+// clear of the band [lo, hi] around r_crit are decided here; pairs inside it, and
+// non-finite ones, are queued for the FP64 re-test kernel, which sets the kept bits
+// (inline serial dot product only when the queue is full).
+__global__ void level0_lower_f32_kernel(LevelArgs a, float lo, float hi) {
+  const int64_t total = a.p * (int64_t)a.W;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / a.W;
+    const int w = (int)(t % a.W);
+    const int64_t j0 = (int64_t)w * 32;
+    uint32_t bits = 0;
+    if (j0 < i) {
+      const float *row = a.cor32 + i * a.p;
+      const int jend = (i - j0) < 32 ? (int)(i - j0) : 32;
+      for (int b = 0; b < jend; ++b) {
+        const float av = fabsf(row[j0 + b]);
+        if (av < lo) continue;             // removed
+        if (av > hi) {                     // kept
+          bits |= 1u << b;
+          continue;
+        }
+        const int64_t j = j0 + b;          // in the band, or NaN
+        const unsigned long long slot = atomicAdd(&a.ctr->rq_count, 1ull);
+        if ((long long)slot < a.rq_cap) {
+          RetestItem *it = a.rq + slot;
+          it->i = (int32_t)i;
+          it->j = (int32_t)j;
+          it->level = 0;
+          it->pad = 0;
+        } else {
+          const double *x = a.Z + i * a.n_z, *y = a.Z + j * a.n_z;
+          double s = 0.0;
+          for (int64_t k = 0; k < a.n_z; ++k) s = fma(x[k], y[k], s);
+          if (!(calc_pvalue64(s / a.denom, a.n_obs) >= a.alpha)) bits |= 1u << b;
+        }
+      }
+    }
+    a.adj[t] = bits;
+  }
+}
+
 // Mirror the lower triangle into the upper: warp per 32x32 bit tile (I, w) with w <= I.
 __global__ void mirror_bits_kernel(uint32_t *adj, int64_t p, int W) {
   const int lane = threadIdx.x & 31;
@@ -243,6 +285,22 @@ hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStrea
   int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
   level0_lower_kernel<<<blocks, 256, 0, s>>>(a, r_lo, r_hi);
   HPC_LAUNCH_CHECK("level0_lower_kernel");
+  const int64_t tiles = (int64_t)a.W * (a.W + 1) / 2;
+  int mblocks = (int)std::min<int64_t>((tiles + 7) / 8, 152 * 32);
+  mirror_bits_kernel<<<mblocks, 256, 0, s>>>(a.adj, a.p, a.W);
+  HPC_LAUNCH_CHECK("mirror_bits_kernel");
+  return HPC_OK;
+}
+
+hpc_status launch_level0_f32(const LevelArgs &a, float lo, float hi, cudaStream_t s) {
+  const int64_t total = a.p * (int64_t)a.W;
+  int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  level0_lower_f32_kernel<<<blocks, 256, 0, s>>>(a, lo, hi);
+  HPC_LAUNCH_CHECK("level0_lower_f32_kernel");
+  return HPC_OK;
+}
+
+hpc_status launch_mirror(const LevelArgs &a, cudaStream_t s) {
   const int64_t tiles = (int64_t)a.W * (a.W + 1) / 2;
   int mblocks = (int)std::min<int64_t>((tiles + 7) / 8, 152 * 32);
   mirror_bits_kernel<<<mblocks, 256, 0, s>>>(a.adj, a.p, a.W);

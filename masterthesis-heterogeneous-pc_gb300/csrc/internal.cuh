@@ -41,6 +41,7 @@ struct DevCounters {
   unsigned long long edges2;       // sum of degrees at the level start
   unsigned long long rec_begin;    // first separation-set record of the level
   unsigned long long band_violations;  // FP32 removals the FP64 post-pass did not confirm
+  unsigned long long rq_count;     // FP64 re-tests queued (tensor-core mode)
   int max_deg;                     // at the level start
   int rows;                        // rows with work at this level
   int pad[2];
@@ -55,6 +56,12 @@ constexpr int kErrRecOverflow = 1;
 constexpr int kErrWorkOverflow = 2;
 constexpr int kErrCsrOverflow = 4;
 constexpr int kErrTimeout = 8;
+
+// One deferred FP64 re-test: edge (i, j) given ids[0..level), or a level-0 pair (i > j).
+struct RetestItem {
+  int32_t i, j, level, pad;
+  int32_t ids[HPC_MAX_LEVEL];
+};
 
 // Everything a level kernel needs, passed by value.
 struct LevelArgs {
@@ -79,6 +86,12 @@ struct LevelArgs {
   long long colidx_cap;
   DevCounters *ctr;      // this level's counters
   DevGlobal *gctr;
+  // FP64 entries without an FP64 matrix: dot products of the standardised columns
+  const double *Z;       // n_z x p column-major (each variable contiguous) or null
+  int64_t n_z;
+  double denom;          // n - 1 (the Gram's divisor)
+  RetestItem *rq;        // deferred FP64 re-tests (tensor-core mode)
+  long long rq_cap;
 };
 
 // ---------------------------------------------------------------------------
@@ -92,6 +105,7 @@ hpc_status launch_gram_f64(const double *Z, int64_t n, int64_t p, double inv_den
 hpc_status launch_to_f32(const double *C, int64_t count, float *C32, cudaStream_t s);
 int64_t tc_n_pad(int64_t n);
 int64_t tc_p_pad(int64_t p);
+int64_t tc_k(int64_t n);
 hpc_status launch_standardise_split_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z64,
                                         __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
 hpc_status launch_standardise_split_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z64,
@@ -106,6 +120,9 @@ hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s);
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
 hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s);
 hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s);
+hpc_status launch_retest(const LevelArgs &a, int sms, cudaStream_t s);
+hpc_status launch_level0_f32(const LevelArgs &a, float lo, float hi, cudaStream_t s);
+hpc_status launch_mirror(const LevelArgs &a, cudaStream_t s);
 int citest_grid(int precision, int level, int device);
 
 }  // namespace hpc
@@ -129,6 +146,9 @@ struct hpc_ctx {
   int64_t X_stage_bytes = 0;
   uint32_t *adj = nullptr;
   uint8_t *adj_bytes = nullptr;  // p x p expansion for hpc_get_adjacency
+  hpc::RetestItem *rq = nullptr;  // deferred FP64 re-tests (tensor-core mode)
+  int64_t rq_cap = 0;
+  bool cor64_valid = false;       // cor64 holds the current FP64 matrix
   int *deg = nullptr;
   int *rowptr = nullptr;
   int *colidx = nullptr;
@@ -150,6 +170,7 @@ struct hpc_ctx {
   cudaStream_t graph_stream = nullptr;
   int64_t graph_colidx_cap = 0, graph_rec_cap = 0;
   int64_t graph_launches = 0;
+  bool graph_cor64_valid = false;
   bool graphs_enabled = true;
   bool last_run_graph = false;
   cudaEvent_t evr[2] = {nullptr, nullptr};  // whole skeleton run
