@@ -58,7 +58,8 @@ def test_tensorcore_mode_without_fp64_matrix(graph, p, n, alpha, ml, seed):
         sk.reset()
         st = sk.run()
         assert np.array_equal(sk.adjacency(), want.adj)
-        assert [s["edges_after"] for s in st] == [l["edges_after"] for l in want.levels][:len(st)]
+        ran = [s_ for s_ in st if s_["level"] == 0 or s_["potential_tests"] > 0]  # the oracle omits the empty last level
+        assert [s_["edges_after"] for s_ in ran] == [l["edges_after"] for l in want.levels]
     recs = sk.sepset_records()
     assert len(recs) == len(want.records)
     for i, j, lev, ids, pmax in recs[:2000]:
