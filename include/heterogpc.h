@@ -188,6 +188,27 @@ hpc_status hpc_get_sepsets(hpc_ctx *ctx, int32_t *out, int max_cond);
  * the adjacency): *count receives the number available; at most cap are copied. */
 hpc_status hpc_get_sepset_records(hpc_ctx *ctx, hpc_sepset_record *out, int64_t cap, int64_t *count);
 
+/* ---- batches ----------------------------------------------------------------
+ * Many independent skeleton problems (uneven p, n and alpha) in one context; no
+ * counterpart in the reference, which runs one problem per process. Each kernel of
+ * each level runs once for all instances (one shared launch per kernel), so
+ * hundreds of small problems fill the GPU together. The correlation and run calls
+ * above act on every instance of a batch: observations are packed (instance b's
+ * column-major n_b x p_b block starts at element obs_offsets[b]) and loaded
+ * correlation matrices likewise (row-major p_b x p_b at cor_offsets[b]); the
+ * single-instance result calls act on instance 0. */
+hpc_status hpc_batch_create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n_obs, const double *alpha,
+                            const hpc_opts *opts);
+hpc_status hpc_batch_size(hpc_ctx *ctx, int *count);
+/* count + 1 offsets each (the last is the total); either pointer may be NULL */
+hpc_status hpc_batch_offsets(hpc_ctx *ctx, int64_t *obs_offsets, int64_t *cor_offsets);
+/* per-level statistics of instance idx of the last run */
+hpc_status hpc_batch_level_stats(hpc_ctx *ctx, int idx, hpc_level_stats *out, int cap, int *levels);
+hpc_status hpc_batch_get_adjacency(hpc_ctx *ctx, int idx, uint8_t *adj_host);
+hpc_status hpc_batch_edge_count(hpc_ctx *ctx, int idx, int64_t *edges);
+hpc_status hpc_batch_get_sepset_records(hpc_ctx *ctx, int idx, hpc_sepset_record *out, int64_t cap,
+                                        int64_t *count);
+
 /* ---- independence statistics (FP64) -------------------------------------
  * Same semantics as CPU::calcPValue / CPU::pValL1 / CPU::pValLN
  * (src/executor/independence/cpuInd.hpp:3-10, cpuInd.cpp:8-38). M is the

@@ -1,4 +1,5 @@
-// Level-l conditional-independence tests (l >= 1) on a persistent grid.
+// Level-l conditional-independence tests (l >= 1) on a persistent grid, over all
+// instances of a context in one launch.
 //
 // Replaces testRowL1 / testRowLN<l+2,l> (src/executor/testing/gpuRowTests.cu:29-205),
 // their workstealing twins (src/executor/testing/gpuWorkstealingTests.cu) and the
@@ -7,28 +8,31 @@
 // each thread unrank a subset and run a 30-iteration FP64 SVD in local memory.
 //
 // Here every test of the level is one index of a flattened space
-//   t in [0, T_l),  T_l = sum_i d_i * C(d_i - 1, l)
-// ordered by (row i, neighbour slot s, lexicographic subset rank). Warps claim
-// tiles of 32 * m consecutive tests with one atomicAdd on a device-wide counter;
-// each lane takes m consecutive tests, unranks its first subset once
-// (the order of ithCombination, src/util/cuda_util.cu:34-50) and then steps to
-// the lexicographic successor. Lanes stop testing an edge as soon as its live bit
-// is cleared (the reference's `adj == 0` early exit, gpuRowTests.cu:166-168).
+//   t in [0, sum_b T_l(b)),  T_l(b) = sum_i d_i * C(d_i - 1, l)
+// ordered by (instance b, row i, neighbour slot s, lexicographic subset rank). Warps
+// claim tiles of 32 * m consecutive tests with one atomicAdd on a device-wide counter;
+// each lane takes m consecutive tests, finds its instance and row by binary search,
+// unranks its first subset once (the order of ithCombination,
+// src/util/cuda_util.cu:34-50) and then steps to the lexicographic successor. Lanes
+// stop testing an edge as soon as its live bit is cleared (the reference's
+// `adj == 0` early exit, gpuRowTests.cu:166-168).
 //
-// The partial correlation of (i, j) given S comes from a Cholesky factorisation
-// of the S block and forward solves for r_iS and r_jS:
+// The partial correlation of (i, j) given S comes from a Cholesky factorisation of
+// the S block and forward solves for r_iS and r_jS:
 //   r = (r_ij - w_i . w_j) / sqrt((1 - |w_i|^2)(1 - |w_j|^2)),  w = L_S^-1 r_S.
-// In mixed precision this runs in FP32 on cor32; a test is decided in FP32 only
-// when |z| is outside the re-test band around z_crit (the configured relative
-// margin plus an error bound from the smallest pivot); every other test, and
-// every removal, is re-evaluated in FP64 on cor64 with the reference's formula
-// (closed form at l = 1 as cpuInd.cpp:16-27; pinv semantics at l >= 2 as
-// cpuInd.cpp:29-38: Cholesky when well conditioned, Jacobi pseudoinverse with
-// arma::pinv's tolerance otherwise). The decision is p >= alpha in FP64.
+// In mixed precision this runs in FP32 on cor32; a test is decided in FP32 only when
+// |r| is outside the re-test band around r_crit (the configured relative |z| margin
+// plus an error bound from the smallest pivot); every other test is re-evaluated in
+// FP64 with the reference's formula (closed form at l = 1 as cpuInd.cpp:16-27; pinv
+// semantics at l >= 2 as cpuInd.cpp:29-38: Cholesky when well conditioned, Jacobi
+// pseudoinverse with arma::pinv's tolerance otherwise). The decision is p >= alpha in
+// FP64. With an FP64 matrix the re-test runs inline; without one (tensor-core mode)
+// it is queued for retest_kernel, which forms the FP64 entries as warp-cooperative
+// dot products of the standardised data.
 //
-// Removal (src/executor/testing/cpuUtil.cpp:23-48, gpuRowTests.cu:172-201): the
-// lane clearing the (min, max) bit with atomicAnd owns the edge, clears the mirror
-// bit and appends one separation-set record.
+// Removal (src/executor/testing/cpuUtil.cpp:23-48, gpuRowTests.cu:172-201): the lane
+// clearing the (min, max) bit with atomicAnd owns the edge, clears the mirror bit and
+// appends one separation-set record.
 #include <cuda_runtime.h>
 
 #include "internal.cuh"
@@ -44,32 +48,19 @@ __device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, 
   return (*w >> (j & 31)) & 1u;
 }
 
-// FP64 correlation entries: read from the FP64 matrix when there is one, else
-// the dot product of the FP64-standardised columns (the tensor-core mode keeps no
-// p x p FP64 matrix). Index order as the reference reads cor[row * p + col].
-struct ExactSrc {
-  const double *cor64;
-  const double *Z;
-  int64_t p, n;
-  double denom;
-  __device__ double entry(int64_t x, int64_t y) const {
-    if (cor64) return cor64[x * p + y];
-    const double *a = Z + x * n, *b = Z + y * n;
-    double s = 0.0;
-    for (int64_t k = 0; k < n; ++k) s = fma(a[k], b[k], s);
-    return s / denom;
-  }
-};
-
-__device__ __forceinline__ ExactSrc exact_src(const LevelArgs &a) {
-  return ExactSrc{a.cor64, a.Z, a.p, a.n_z, a.denom};
+// FP64 correlation entries of one instance: read from its FP64 matrix when there is
+// one, else the dot product of its FP64-standardised columns. Index order as the
+// reference reads cor[row * p + col].
+__device__ __forceinline__ double exact_entry(const Inst &I, int64_t x, int64_t y) {
+  if (I.cor64) return I.cor64[x * I.p + y];
+  const double *a = I.Z + x * I.n_z, *b = I.Z + y * I.n_z;
+  double s = 0.0;
+  for (int64_t k = 0; k < I.n_z; ++k) s = fma(a[k], b[k], s);
+  return s / I.denom;
 }
 
-// FP64 p-value of a k x k submatrix M (row-major, ordered i, j, S; overwritten)
-// with the reference's semantics: closed form at l = 1 (cpuInd.cpp:16-27); at
-// l >= 2 NaN -> no removal, else the pseudoinverse partial correlation
-// (cpuInd.cpp:29-38), by Cholesky when well conditioned, by Jacobi pinv with
-// arma::pinv's tolerance otherwise.
+// FP64 p-value of a k x k submatrix M (row-major, ordered i, j, S; overwritten) with
+// the reference's semantics.
 template <int LA>
 __device__ __noinline__ double pvalue_of_matrix(double *M, int l, int n_obs) {
   const int k = l + 2;
@@ -91,13 +82,20 @@ __device__ __noinline__ double pvalue_of_matrix(double *M, int l, int n_obs) {
     const double lrr = sqrt(d);
     Lm[r * (r + 1) / 2 + r] = lrr;
     double vx = M[r + 2], vy = M[k + r + 2];
-    for (int q = 0; q < r; ++q) { vx -= Lm[r * (r + 1) / 2 + q] * wx[q]; vy -= Lm[r * (r + 1) / 2 + q] * wy[q]; }
+    for (int q = 0; q < r; ++q) {
+      vx -= Lm[r * (r + 1) / 2 + q] * wx[q];
+      vy -= Lm[r * (r + 1) / 2 + q] * wy[q];
+    }
     wx[r] = vx / lrr;
     wy[r] = vy / lrr;
   }
   if (dmin > 1e-10) {
     double ax = 1.0, ay = 1.0, b = M[1];
-    for (int q = 0; q < l; ++q) { ax -= wx[q] * wx[q]; ay -= wy[q] * wy[q]; b -= wx[q] * wy[q]; }
+    for (int q = 0; q < l; ++q) {
+      ax -= wx[q] * wx[q];
+      ay -= wy[q] * wy[q];
+      b -= wx[q] * wy[q];
+    }
     if (ax > 1e-10 && ay > 1e-10) return calc_pvalue64(b / sqrt(ax * ay), n_obs);
   }
   double V[(LA + 2) * (LA + 2)];
@@ -106,29 +104,29 @@ __device__ __noinline__ double pvalue_of_matrix(double *M, int l, int n_obs) {
   return calc_pvalue64(-p01 / sqrt(p00 * p11), n_obs);
 }
 
-// FP64 p-value of the test (i, j | ids), entries from `src`.
+// FP64 p-value of the test (i, j | ids) of instance I.
 template <int LA>
-__device__ __noinline__ double exact_pvalue(const ExactSrc &src, int n_obs, int64_t i, int64_t j, const int *ids,
-                                            int l) {
+__device__ __noinline__ double exact_pvalue(const Inst &I, int64_t i, int64_t j, const int *ids, int l) {
   const int k = l + 2;
   double M[(LA + 2) * (LA + 2)];
   for (int q = 0; q < k * k; ++q) M[q] = 0.0;
   for (int q = 0; q < k; ++q) M[q * k + q] = 1.0;
-  M[1] = M[k] = src.entry(i, j);
+  M[1] = M[k] = exact_entry(I, i, j);
   for (int q = 2; q < k; ++q) {
-    M[q] = M[q * k] = src.entry(i, ids[q - 2]);
-    M[k + q] = M[q * k + 1] = src.entry(j, ids[q - 2]);
+    M[q] = M[q * k] = exact_entry(I, i, ids[q - 2]);
+    M[k + q] = M[q * k + 1] = exact_entry(I, j, ids[q - 2]);
   }
   for (int r = 2; r < k; ++r)
-    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = src.entry(ids[r - 2], ids[c - 2]);
-  return pvalue_of_matrix<LA>(M, l, n_obs);
+    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = exact_entry(I, ids[r - 2], ids[c - 2]);
+  return pvalue_of_matrix<LA>(M, l, I.n_obs);
 }
 
-// FP32 test. Returns 1 = remove, 0 = keep, 2 = undecided (re-test in FP64).
+// FP32 test. Returns 1 = remove, 0 = keep, 2 = undecided (re-test in FP64); *rr_out
+// receives |r|.
 template <int LA>
-__device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l, float *rr_out) {
-  const float *__restrict__ C = a.cor32;
-  const int64_t p = a.p;
+__device__ __forceinline__ int test_f32(const Inst &I, int64_t i, int64_t j, const int *ids, int l, float *rr_out) {
+  const float *__restrict__ C = I.cor32;
+  const int64_t p = I.p;
   const float rij = __ldg(C + i * p + j);
   float Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1];
   float invd[LA], wx[LA], wy[LA];
@@ -156,7 +154,7 @@ __device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j
         }
       }
       dmin = fminf(dmin, d);
-      float id = rsqrtf(fmaxf(d, 1e-30f));
+      const float id = rsqrtf(fmaxf(d, 1e-30f));
       invd[r] = id;
       wx[r] = vx * id;
       wy[r] = vy * id;
@@ -171,8 +169,9 @@ __device__ __forceinline__ int test_f32(const LevelArgs &a, int64_t i, int64_t j
   // |r| = |b| / sqrt(ax * ay) against r_c: no transcendental on this path
   const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
   *rr_out = rr;
-  const float dist = rr - a.r_c;
-  const float band = a.margin_r + 8.0f * __fdividef(a.ke, cond);
+  const float dist = rr - I.r_c;
+  const float ke = I.ke_a + (float)(l + 2) * I.ke_b;
+  const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
   if (!(fabsf(dist) > band)) return 2;  // inside the band, or NaN
   return dist < 0.0f ? 1 : 0;
 }
@@ -181,27 +180,27 @@ __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, 
   // largest i with row_work[i] <= t (row_work is non-decreasing, row_work[p] > t)
   int64_t lo = 0, hi = p;
   while (hi - lo > 1) {
-    int64_t mid = (lo + hi) >> 1;
+    const int64_t mid = (lo + hi) >> 1;
     if (row_work[mid] <= t) lo = mid; else hi = mid;
   }
   return lo;
 }
 
-// pv < 0 marks a removal decided in FP32; its FP64 p-value is filled in by the
-// finalize_records post-pass.
-__device__ __forceinline__ void record_removal(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l, double pv) {
+// pv < 0 marks a removal decided in FP32; finalize_records fills in its p-value.
+__device__ __forceinline__ void record_removal(const Inst &I, int level, int64_t i, int64_t j, const int *ids, int l,
+                                               double pv) {
   const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
   const uint32_t bit = 1u << (hi & 31);
-  const uint32_t old = atomicAnd(a.adj + lo * a.W + (hi >> 5), ~bit);
+  const uint32_t old = atomicAnd(I.adj + lo * I.W + (hi >> 5), ~bit);
   if (!(old & bit)) return;  // another lane removed it first
-  atomicAnd(a.adj + hi * a.W + (lo >> 5), ~(1u << (lo & 31)));
-  atomicAdd(&a.ctr->deleted, 1ull);
-  const unsigned long long slot = atomicAdd(&a.gctr->rec_count, 1ull);
-  if ((long long)slot >= a.rec_cap) {
-    atomicOr(&a.gctr->err, kErrRecOverflow);
+  atomicAnd(I.adj + hi * I.W + (lo >> 5), ~(1u << (lo & 31)));
+  atomicAdd(&I.ctr[level].deleted, 1ull);
+  const unsigned long long slot = atomicAdd(&I.g->rec_count, 1ull);
+  if ((long long)slot >= I.rec_cap) {
+    atomicOr(&I.g->err, kErrRecOverflow);
     return;
   }
-  hpc_sepset_record *rec = a.recs + slot;
+  hpc_sepset_record *rec = I.recs + slot;
   rec->i = (int32_t)lo;
   rec->j = (int32_t)hi;
   rec->level = l;
@@ -211,24 +210,25 @@ __device__ __forceinline__ void record_removal(const LevelArgs &a, int64_t i, in
 }
 
 // Defer an undecided test to the FP64 re-test kernel; false when the queue is full.
-__device__ __forceinline__ bool push_retest(const LevelArgs &a, int64_t i, int64_t j, const int *ids, int l) {
-  const unsigned long long slot = atomicAdd(&a.ctr->rq_count, 1ull);
-  if ((long long)slot >= a.rq_cap) return false;
-  RetestItem *it = a.rq + slot;
+__device__ __forceinline__ bool push_retest(const Launch &L, int b, int64_t i, int64_t j, const int *ids, int l) {
+  const unsigned long long slot = atomicAdd(&L.lc->rq_count, 1ull);
+  if ((long long)slot >= L.rq_cap) return false;
+  RetestItem *it = L.rq + slot;
   it->i = (int32_t)i;
   it->j = (int32_t)j;
   it->level = l;
-  it->pad = 0;
+  it->inst = b;
   for (int q = 0; q < HPC_MAX_LEVEL; ++q) it->ids[q] = q < l ? ids[q] : -1;
   return true;
 }
 
 template <int LT, bool MIXED>
-__global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
+__global__ void __launch_bounds__(kThreads) citest_kernel(Launch L) {
   constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
-  const int l = LT > 0 ? LT : a.level;
+  const int l = LT > 0 ? LT : L.level;
+  const int level = L.level;
   const int lane = threadIdx.x & 31;
-  const unsigned long long total = a.ctr->work_total;
+  const unsigned long long total = L.work_prefix[L.count];
   if (total == 0) return;
   // tests per lane per tile: about four tiles per lane of the grid, 1..64
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
@@ -237,47 +237,50 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
   int pos[LA], ids[LA];
   for (;;) {
     unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(&a.ctr->tile_next, 1ull);
+    if (lane == 0) tile = atomicAdd(&L.lc->tile_next, 1ull);
     tile = __shfl_sync(0xffffffffu, tile, 0);
     const unsigned long long t0 = tile * per_tile;
     if (t0 >= total) break;
     unsigned long long t = t0 + (unsigned long long)lane * m;
     const unsigned long long tend = min(t + (unsigned long long)m, total);
     unsigned executed = 0, retests = 0;
+    int b_last = -1;
     if (t < tend) {
-      int64_t i = find_row(a.row_work, a.p, t);
-      int d = a.deg[i];
+      int b = find_inst_u(L.work_prefix, L.count, t);
+      const Inst *I = L.inst + b;
+      unsigned long long base_t = L.work_prefix[b];
+      int64_t i = find_row(I->row_work, I->p, t - base_t);
+      int d = I->deg[i];
       unsigned long long c = binom_sat(d - 1, l);
-      unsigned long long off = t - a.row_work[i];
+      const unsigned long long off = t - base_t - I->row_work[i];
       int s = (int)(off / c);
       unsigned long long rank = off - (unsigned long long)s * c;
-      int base = a.rowptr[i];
+      int base = I->rowptr[i];
       unrank_lex(rank, l, d - 1, pos);
-      int64_t j = a.colidx[base + s];
-      bool alive = live_bit(a.adj, a.W, i, j);
+      int64_t j = I->colidx[base + s];
+      bool alive = live_bit(I->adj, I->W, i, j);
+      unsigned tested_edge = 0;
       for (;;) {
         if (alive) {
 #pragma unroll
           for (int q = 0; q < LA; ++q)
-            if (q < l) ids[q] = a.colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
+            if (q < l) ids[q] = I->colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
           int res = 2;
           float rr = 0.f;
-          if (MIXED) res = test_f32<LA>(a, i, j, ids, l, &rr);
+          if (MIXED) res = test_f32<LA>(*I, i, j, ids, l, &rr);
           ++executed;
+          ++tested_edge;
           if (res == 1) {
-            // decided in FP32; the p-value is filled in by the post-pass (the
-            // negative value carries |r| for the mode without an FP64 matrix)
-            record_removal(a, i, j, ids, l, -1.0 - (double)rr);
+            // decided in FP32; the post-pass fills in the p-value (the negative
+            // value carries |r| for instances without an FP64 matrix)
+            record_removal(*I, level, i, j, ids, l, -1.0 - (double)rr);
             alive = false;
           } else if (res == 2) {
             if (MIXED) ++retests;
-            // without an FP64 matrix the FP64 re-test is deferred to the warp-
-            // cooperative re-test kernel; inline (serial dot products) only if
-            // its queue is full
-            if (!(MIXED && !a.cor64 && push_retest(a, i, j, ids, l))) {
-              const double pv = exact_pvalue<LA>(exact_src(a), a.n_obs, i, j, ids, l);
-              if (pv >= a.alpha) {
-                record_removal(a, i, j, ids, l, pv);
+            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, ids, l))) {
+              const double pv = exact_pvalue<LA>(*I, i, j, ids, l);
+              if (pv >= I->alpha) {
+                record_removal(*I, level, i, j, ids, l, pv);
                 alive = false;
               }
             }
@@ -287,51 +290,64 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(LevelArgs a) {
         if (++rank == c) {
           rank = 0;
           if (++s == d) {
-            i = find_row(a.row_work, a.p, t);
-            d = a.deg[i];
+            // next row with tests, possibly of the next instance
+            if (t >= L.work_prefix[b + 1]) {
+              b = find_inst_u(L.work_prefix, L.count, t);
+              I = L.inst + b;
+              base_t = L.work_prefix[b];
+            }
+            i = find_row(I->row_work, I->p, t - base_t);
+            d = I->deg[i];
             c = binom_sat(d - 1, l);
-            base = a.rowptr[i];
+            base = I->rowptr[i];
             s = 0;
           }
 #pragma unroll
           for (int q = 0; q < LA; ++q)
             if (q < l) pos[q] = q;
-          j = a.colidx[base + s];
-          alive = live_bit(a.adj, a.W, i, j);
+          j = I->colidx[base + s];
+          alive = live_bit(I->adj, I->W, i, j);
+          tested_edge = 0;
         } else {
           next_lex(l, d - 1, pos);
-          if (alive && (executed & 3u) == 0) alive = live_bit(a.adj, a.W, i, j);
+          if (alive && (tested_edge & 3u) == 0) alive = live_bit(I->adj, I->W, i, j);
         }
       }
+      b_last = b;
     }
-    executed = __reduce_add_sync(0xffffffffu, executed);
-    retests = __reduce_add_sync(0xffffffffu, retests);
-    if (lane == 0) {
-      if (executed) atomicAdd(&a.ctr->tests, (unsigned long long)executed);
-      if (retests) atomicAdd(&a.ctr->retests, (unsigned long long)retests);
+    // per-instance test counts, one atomic per instance present in the warp (a
+    // lane's range rarely crosses instances: its counts go to its last instance)
+    const unsigned grp = __match_any_sync(0xffffffffu, b_last);
+    const unsigned ex = __reduce_add_sync(grp, executed);
+    const unsigned rt = __reduce_add_sync(grp, retests);
+    if (b_last >= 0 && lane == __ffs(grp) - 1) {
+      atomicAdd(&L.inst[b_last].ctr[level].tests, (unsigned long long)ex);
+      if (rt) atomicAdd(&L.inst[b_last].ctr[level].retests, (unsigned long long)rt);
     }
   }
 }
 
-// FP64 p-values of the removals a level decided in FP32 (records [rec_begin, rec_count)),
-// thread per record; a removal whose FP64 p-value is below alpha is counted as a
-// band violation (the FP32 error bound did not hold).
-__global__ void finalize_records_kernel(LevelArgs a) {
-  const unsigned long long begin = a.ctr->rec_begin;
-  unsigned long long end = a.gctr->rec_count;
-  if (end > (unsigned long long)a.rec_cap) end = (unsigned long long)a.rec_cap;
-  for (unsigned long long r = begin + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; r < end;
-       r += (unsigned long long)gridDim.x * blockDim.x) {
-    hpc_sepset_record *rec = a.recs + r;
-    if (!(rec->pmax < 0.0)) continue;
-    if (!a.cor64) {
-      // no FP64 matrix: the p-value of the FP32 partial correlation
-      rec->pmax = calc_pvalue64(-1.0 - rec->pmax, a.n_obs);
-      continue;
+// p-values of the removals a level decided in FP32 (records [rec_begin, rec_count) of
+// each instance): FP64 re-evaluation where the instance has an FP64 matrix (a result
+// below alpha is counted as a band violation: the FP32 error bound did not hold),
+// else the FP64 formula on the stored FP32 |r|.
+__global__ void finalize_records_kernel(Launch L) {
+  for (int b = blockIdx.x; b < L.count; b += gridDim.x) {
+    const Inst &I = L.inst[b];
+    const unsigned long long begin = I.ctr[L.level].rec_begin;
+    unsigned long long end = I.g->rec_count;
+    if (end > (unsigned long long)I.rec_cap) end = (unsigned long long)I.rec_cap;
+    for (unsigned long long r = begin + threadIdx.x; r < end; r += blockDim.x) {
+      hpc_sepset_record *rec = I.recs + r;
+      if (!(rec->pmax < 0.0)) continue;
+      if (!I.cor64) {
+        rec->pmax = calc_pvalue64(-1.0 - rec->pmax, I.n_obs);
+        continue;
+      }
+      const double pv = exact_pvalue<HPC_MAX_LEVEL>(I, rec->i, rec->j, rec->ids, rec->level);
+      rec->pmax = pv;
+      if (!(pv >= I.alpha)) atomicAdd(&I.ctr[L.level].band_violations, 1ull);
     }
-    const double pv = exact_pvalue<HPC_MAX_LEVEL>(exact_src(a), a.n_obs, rec->i, rec->j, rec->ids, rec->level);
-    rec->pmax = pv;
-    if (!(pv >= a.alpha)) atomicAdd(&a.ctr->band_violations, 1ull);
   }
 }
 
@@ -344,32 +360,31 @@ __device__ __forceinline__ double warp_dot(const double *__restrict__ x, const d
   return s;
 }
 
-// FP64 re-tests deferred by the level kernels (tensor-core mode): one warp per
-// queued test computes the FP64 correlation entries it needs as dot products of
-// the FP64-standardised columns, lane 0 evaluates the reference formula. Level-0
-// items set the kept lower-triangle bit; level >= 1 items remove the edge.
+// FP64 re-tests deferred by the level kernels (instances without an FP64 matrix):
+// one warp per queued test forms the FP64 correlation entries it needs as dot
+// products of the FP64-standardised columns, lane 0 evaluates the reference formula.
+// Level-0 items set the kept lower-triangle bit; level >= 1 items remove the edge.
 constexpr int kRetestWarps = 8;
-__global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(LevelArgs a) {
+__global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
   __shared__ double Ms[kRetestWarps][(HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2)];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   double *M = Ms[wib];
-  unsigned long long count = a.ctr->rq_count;
-  if (count > (unsigned long long)a.rq_cap) count = (unsigned long long)a.rq_cap;
+  unsigned long long count = L.lc->rq_count;
+  if (count > (unsigned long long)L.rq_cap) count = (unsigned long long)L.rq_cap;
   const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-  const double *Z = a.Z;
-  const int64_t n = a.n_z;
   for (unsigned long long q = warp; q < count; q += nwarps) {
-    const RetestItem it = a.rq[q];
-    const int64_t i = it.i, j = it.j;
+    const RetestItem it = L.rq[q];
+    const Inst &I = L.inst[it.inst];
+    const int64_t i = it.i, j = it.j, n = I.n_z;
     const int l = it.level;
     if (l == 0) {
-      const double r = warp_dot(Z + i * n, Z + j * n, n) / a.denom;
-      if (lane == 0 && !(calc_pvalue64(r, a.n_obs) >= a.alpha))
-        atomicOr(a.adj + i * a.W + (j >> 5), 1u << (j & 31));  // kept: lower-triangle bit (i > j)
+      const double r = warp_dot(I.Z + i * n, I.Z + j * n, n) / I.denom;
+      if (lane == 0 && !(calc_pvalue64(r, I.n_obs) >= I.alpha))
+        atomicOr(I.adj + i * I.W + (j >> 5), 1u << (j & 31));  // kept: lower-triangle bit (i > j)
       continue;
     }
-    if (!live_bit(a.adj, a.W, i, j)) continue;  // removed by another test meanwhile
+    if (!live_bit(I.adj, I.W, i, j)) continue;  // removed by another test meanwhile
     const int k = l + 2;
     int V[HPC_MAX_LEVEL + 2];
     V[0] = (int)i;
@@ -377,15 +392,15 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(LevelArgs a) 
     for (int t = 0; t < l; ++t) V[2 + t] = it.ids[t];
     for (int r = 0; r < k; ++r) {
       if (lane == 0) M[r * k + r] = 1.0;
-      for (int c = r + 1; c < k; ++c) {
-        const double v = warp_dot(Z + (int64_t)V[r] * n, Z + (int64_t)V[c] * n, n) / a.denom;
-        if (lane == 0) M[r * k + c] = M[c * k + r] = v;
+      for (int c2 = r + 1; c2 < k; ++c2) {
+        const double v = warp_dot(I.Z + (int64_t)V[r] * n, I.Z + (int64_t)V[c2] * n, n) / I.denom;
+        if (lane == 0) M[r * k + c2] = M[c2 * k + r] = v;
       }
     }
     __syncwarp();
     if (lane == 0) {
-      const double pv = pvalue_of_matrix<HPC_MAX_LEVEL>(M, l, a.n_obs);
-      if (pv >= a.alpha) record_removal(a, i, j, it.ids, l, pv);
+      const double pv = pvalue_of_matrix<HPC_MAX_LEVEL>(M, l, I.n_obs);
+      if (pv >= I.alpha) record_removal(I, L.level, i, j, it.ids, l, pv);
     }
     __syncwarp();
   }
@@ -417,21 +432,22 @@ int citest_grid(int precision, int level, int device) {
   return per_sm * sms;
 }
 
-hpc_status launch_retest(const LevelArgs &a, int sms, cudaStream_t s) {
-  retest_kernel<<<sms * 4, kRetestWarps * 32, 0, s>>>(a);
+hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
+  retest_kernel<<<sms * 4, kRetestWarps * 32, 0, s>>>(L);
   HPC_LAUNCH_CHECK("retest_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s) {
-  finalize_records_kernel<<<152 * 2, 128, 0, s>>>(a);
+hpc_status launch_finalize_records(const Launch &L, cudaStream_t s) {
+  const int blocks = L.count < 304 ? L.count : 304;
+  finalize_records_kernel<<<blocks, 128, 0, s>>>(L);
   HPC_LAUNCH_CHECK("finalize_records_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s) {
-  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(a.level) : kernel_for<true>(a.level);
-  LevelArgs args = a;
+hpc_status launch_citest(const Launch &L, int precision, int grid, cudaStream_t s) {
+  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(L.level) : kernel_for<true>(L.level);
+  Launch args = L;
   void *params[] = {&args};
   HPC_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), params, 0, s));
   return HPC_OK;

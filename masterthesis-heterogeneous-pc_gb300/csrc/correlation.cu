@@ -1,13 +1,15 @@
-// Correlation: column standardisation and the FP64 Gram.
+// Correlation: column standardisation and the FP64 Gram, grouped over the instances
+// of a context.
 //
 // Replaces gpuMeans / gpuSD / gpuPMCC (src/correlation/corHelper.cu:8-116), which
-// launch one 64-thread block per (i, j) pair and re-read both columns for every
-// pair. Here one block per variable standardises its column once (NaN-skipping
-// mean, SD with the n-1 denominator, z = (x - mean) / sd, missing samples as 0 so
-// that a product with a missing sample contributes nothing -- the reference's
-// pairwise NaN skip, corHelper.cu:101), and the correlation is the register- and
-// shared-memory-tiled Gram C = Z^T Z / (n - 1) over upper-triangle tiles only,
-// mirrored on write.
+// launch one 64-thread block per (i, j) pair and re-read both columns for every pair.
+// Here one block per variable standardises its column once (NaN-skipping mean, SD with
+// the n-1 denominator, z = (x - mean) / sd, missing samples as 0 so that a product with
+// a missing sample contributes nothing -- the reference's pairwise NaN skip,
+// corHelper.cu:101) into the FP64 copy Z and, for the tensor-core Gram, into the
+// split-BF16 operands; the FP64 correlation is the register- and shared-memory-tiled
+// Gram C = Z^T Z / (n - 1) over upper-triangle 64 x 64 tiles, mirrored on write.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -20,14 +22,18 @@ namespace {
 
 constexpr int kStdThreads = 256;
 
-template <typename TIn>
-__global__ void __launch_bounds__(kStdThreads) standardise_kernel(const TIn *__restrict__ X, int64_t n,
-                                                                  int64_t p, int ref_compat,
-                                                                  double *__restrict__ Z) {
-  const int64_t v = blockIdx.x;
-  if (v >= p) return;
-  const TIn *x = X + v * n;
-  double *z = Z + v * n;
+// grid: one block per variable of every instance (flattened over row_prefix)
+template <typename TIn, bool SPLIT>
+__global__ void __launch_bounds__(kStdThreads) standardise_kernel(const TIn *__restrict__ X, StdArgs a,
+                                                                  double *__restrict__ Z,
+                                                                  __nv_bfloat16 *__restrict__ P,
+                                                                  __nv_bfloat16 *__restrict__ Q) {
+  const long long t = blockIdx.x;
+  const int b = find_inst(a.row_prefix, a.count, t);
+  const long long v = t - a.row_prefix[b];
+  const long long n = a.n[b];
+  const TIn *x = X + a.x_off[b] + v * n;
+  double *z = Z + a.z_off[b] + v * n;
   __shared__ double red[kStdThreads / 32];
   __shared__ long long redc[kStdThreads / 32];
   __shared__ double mean_s, sd_s;
@@ -35,66 +41,110 @@ __global__ void __launch_bounds__(kStdThreads) standardise_kernel(const TIn *__r
 
   double s = 0.0;
   long long c = 0;
-  for (int64_t k = threadIdx.x; k < n; k += kStdThreads) {
-    double a = (double)x[k];
-    if (!isnan(a)) { s += a; ++c; }
+  for (long long k = threadIdx.x; k < n; k += kStdThreads) {
+    const double xv = (double)x[k];
+    if (!isnan(xv)) {
+      s += xv;
+      ++c;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     s += __shfl_xor_sync(0xffffffffu, s, o);
     c += __shfl_xor_sync(0xffffffffu, c, o);
   }
-  if (lane == 0) { red[wid] = s; redc[wid] = c; }
+  if (lane == 0) {
+    red[wid] = s;
+    redc[wid] = c;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
+    double tt = 0.0;
     long long tc = 0;
-    for (int w = 0; w < kStdThreads / 32; ++w) { t += red[w]; tc += redc[w]; }
-    mean_s = t / (double)tc;
+    for (int w = 0; w < kStdThreads / 32; ++w) {
+      tt += red[w];
+      tc += redc[w];
+    }
+    mean_s = tt / (double)tc;
   }
   __syncthreads();
   const double mean = mean_s;
   double ss = 0.0;
-  for (int64_t k = threadIdx.x; k < n; k += kStdThreads) {
-    double a = (double)x[k];
-    if (!isnan(a)) { double d = a - mean; ss += d * d; }
+  for (long long k = threadIdx.x; k < n; k += kStdThreads) {
+    const double xv = (double)x[k];
+    if (!isnan(xv)) {
+      const double d = xv - mean;
+      ss += d * d;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
   __syncthreads();
   if (lane == 0) red[wid] = ss;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kStdThreads / 32; ++w) t += red[w];
-    if (ref_compat)  // corHelper.cu:75: sqrtf of (sum / (dim - 1.f))
-      sd_s = (double)sqrtf((float)(t / (double)((float)n - 1.f)));
+    double tt = 0.0;
+    for (int w = 0; w < kStdThreads / 32; ++w) tt += red[w];
+    if (a.ref_compat)  // corHelper.cu:75: sqrtf of (sum / (dim - 1.f))
+      sd_s = (double)sqrtf((float)(tt / (double)((float)n - 1.f)));
     else
-      sd_s = sqrt(t / (double)(n - 1));
+      sd_s = sqrt(tt / (double)(n - 1));
   }
   __syncthreads();
   const double sd = sd_s;
-  for (int64_t k = threadIdx.x; k < n; k += kStdThreads) {
-    double a = (double)x[k];
-    z[k] = isnan(a) ? 0.0 : (a - mean) / sd;
+  if (!SPLIT) {
+    for (long long k = threadIdx.x; k < n; k += kStdThreads) {
+      const double xv = (double)x[k];
+      z[k] = isnan(xv) ? 0.0 : (xv - mean) / sd;
+    }
+    return;
+  }
+  // split-BF16 operands of the tensor-core Gram: P = [hi|hi|lo|lo], Q = [hi|lo|hi|lo]
+  // of z / sqrt(n - 1), so that P Q^T is the correlation
+  const double denom = a.ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
+  const double scale = 1.0 / sqrt(denom);
+  const long long n_pad = a.n_pad[b], K = a.kdim[b];
+  __nv_bfloat16 *pr = P + a.tc_off[b] + v * K, *qr = Q + a.tc_off[b] + v * K;
+  for (long long k = threadIdx.x; k < n_pad; k += kStdThreads) {
+    double zz = 0.0;
+    if (k < n) {
+      const double xv = (double)x[k];
+      zz = isnan(xv) ? 0.0 : (xv - mean) / sd;
+      z[k] = zz;
+    }
+    const double zs = zz * scale;
+    const __nv_bfloat16 hi = __double2bfloat16(zs);
+    const __nv_bfloat16 lo = __double2bfloat16(zs - (double)__bfloat162float(hi));
+    pr[k] = hi;
+    pr[n_pad + k] = hi;
+    pr[2 * n_pad + k] = lo;
+    pr[3 * n_pad + k] = lo;
+    qr[k] = hi;
+    qr[n_pad + k] = lo;
+    qr[2 * n_pad + k] = hi;
+    qr[3 * n_pad + k] = lo;
   }
 }
 
 // FP64 Gram, 64 x 64 output tile per block, K staged 16 at a time through shared
-// memory, 4 x 4 outputs per thread.
+// memory, 4 x 4 outputs per thread; blocks flattened over all instances' tiles.
 constexpr int BM = 64, BK = 16, GT = 256;
 
-__global__ void __launch_bounds__(GT) gram_f64_kernel(const double *__restrict__ Z, int64_t n, int64_t p,
-                                                      int nb, double denom, double *__restrict__ C) {
-  // linear block id -> (bi, bj) with bi <= bj over the upper triangle of tiles
-  int64_t t = blockIdx.x;
+__global__ void __launch_bounds__(GT) gram_f64_kernel(const double *__restrict__ Zall, double *__restrict__ Call,
+                                                      GramArgs g) {
+  const long long tt = blockIdx.x;
+  const int b = find_inst(g.tile_prefix, g.count, tt);
+  long long t = tt - g.tile_prefix[b];
+  const long long p = g.p[b], n = g.n[b];
+  const int nb = (int)((p + BM - 1) / BM);
+  const double *Z = Zall + g.z_off[b];
+  double *C = Call + g.c_off[b];
+  const double denom = g.denom[b];
   int bi = 0;
-  {
-    // row bi holds nb - bi tiles
-    int64_t rem = t;
-    while (rem >= nb - bi) { rem -= nb - bi; ++bi; }
-    t = rem;
+  while (t >= nb - bi) {  // (bi, bj), bi <= bj, row-major over the upper triangle of tiles
+    t -= nb - bi;
+    ++bi;
   }
   const int bj = bi + (int)t;
-  const int64_t a0 = (int64_t)bi * BM, b0 = (int64_t)bj * BM;
+  const long long a0 = (long long)bi * BM, b0 = (long long)bj * BM;
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BM + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -103,15 +153,13 @@ __global__ void __launch_bounds__(GT) gram_f64_kernel(const double *__restrict__
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-
-  for (int64_t k0 = 0; k0 < n; k0 += BK) {
-    // 64 columns x 16 k = 1024 values per operand, 4 per thread
+  for (long long k0 = 0; k0 < n; k0 += BK) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      int idx = threadIdx.x + r * GT;  // 0..1023
-      int col = idx >> 4, kk = idx & 15;
-      int64_t k = k0 + kk;
-      int64_t va = a0 + col, vb = b0 + col;
+      const int idx = threadIdx.x + r * GT;  // 0..1023: 64 columns x 16 k per operand
+      const int col = idx >> 4, kk = idx & 15;
+      const long long k = k0 + kk;
+      const long long va = a0 + col, vb = b0 + col;
       As[kk][col] = (va < p && k < n) ? Z[va * n + k] : 0.0;
       Bs[kk][col] = (vb < p && k < n) ? Z[vb * n + k] : 0.0;
     }
@@ -132,14 +180,14 @@ __global__ void __launch_bounds__(GT) gram_f64_kernel(const double *__restrict__
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    int64_t a = a0 + ty + 16 * i;
+    const long long ra = a0 + ty + 16 * i;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      int64_t b = b0 + tx + 16 * j;
-      if (a < p && b < p && a <= b) {
-        double v = acc[i][j] / denom;
-        C[a * p + b] = v;
-        C[b * p + a] = v;
+      const long long cb = b0 + tx + 16 * j;
+      if (ra < p && cb < p && ra <= cb) {
+        const double v = acc[i][j] / denom;
+        C[ra * p + cb] = v;
+        C[cb * p + ra] = v;
       }
     }
   }
@@ -152,30 +200,38 @@ __global__ void to_f32_kernel(const double *__restrict__ C, int64_t count, float
 
 }  // namespace
 
-hpc_status launch_standardise_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z,
-                                  cudaStream_t s) {
-  standardise_kernel<double><<<(unsigned)p, kStdThreads, 0, s>>>(X, n, p, ref_compat, Z);
-  HPC_LAUNCH_CHECK("standardise_kernel<double>");
+long long gram_f64_tiles(int64_t p) {
+  const long long nb = (p + BM - 1) / BM;
+  return nb * (nb + 1) / 2;
+}
+
+hpc_status launch_standardise(const void *X, bool f32, const StdArgs &a, long long total_rows, double *Z,
+                              __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s) {
+  const bool split = P != nullptr;
+  const unsigned grid = (unsigned)total_rows;
+  if (f32) {
+    if (split)
+      standardise_kernel<float, true><<<grid, kStdThreads, 0, s>>>((const float *)X, a, Z, P, Q);
+    else
+      standardise_kernel<float, false><<<grid, kStdThreads, 0, s>>>((const float *)X, a, Z, P, Q);
+  } else {
+    if (split)
+      standardise_kernel<double, true><<<grid, kStdThreads, 0, s>>>((const double *)X, a, Z, P, Q);
+    else
+      standardise_kernel<double, false><<<grid, kStdThreads, 0, s>>>((const double *)X, a, Z, P, Q);
+  }
+  HPC_LAUNCH_CHECK("standardise_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_standardise_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z,
-                                  cudaStream_t s) {
-  standardise_kernel<float><<<(unsigned)p, kStdThreads, 0, s>>>(X, n, p, ref_compat, Z);
-  HPC_LAUNCH_CHECK("standardise_kernel<float>");
-  return HPC_OK;
-}
-
-hpc_status launch_gram_f64(const double *Z, int64_t n, int64_t p, double denom, double *C, cudaStream_t s) {
-  const int nb = (int)((p + BM - 1) / BM);
-  const int64_t tiles = (int64_t)nb * (nb + 1) / 2;
-  gram_f64_kernel<<<(unsigned)tiles, GT, 0, s>>>(Z, n, p, nb, denom, C);
+hpc_status launch_gram_f64(const double *Z, double *C, const GramArgs &a, long long total_tiles, cudaStream_t s) {
+  gram_f64_kernel<<<(unsigned)total_tiles, GT, 0, s>>>(Z, C, a);
   HPC_LAUNCH_CHECK("gram_f64_kernel");
   return HPC_OK;
 }
 
 hpc_status launch_to_f32(const double *C, int64_t count, float *C32, cudaStream_t s) {
-  int blocks = (int)std::min<int64_t>((count + 255) / 256, 152 * 16);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, 152 * 16));
   to_f32_kernel<<<blocks, 256, 0, s>>>(C, count, C32);
   HPC_LAUNCH_CHECK("to_f32_kernel");
   return HPC_OK;

@@ -1,6 +1,6 @@
-// C ABI of libheterogpc: contexts, correlation entry points, the level loop and
-// result retrieval. The reference equivalents are named beside each function in
-// include/heterogpc.h.
+// C ABI of libheterogpc: contexts (one or many skeleton instances), correlation entry
+// points, the level loop and result retrieval. The reference equivalents are named
+// beside each function in include/heterogpc.h.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,31 +36,39 @@ hpc_status cuda_fail(cudaError_t e, const char *what, const char *file, int line
 
 namespace {
 
+constexpr int kLevels = HPC_MAX_LEVEL + 1;
+
 // z with erfc(z / sqrt 2) == alpha, by bisection in FP64 (host set-up only)
 double z_crit_of(double alpha) {
   double lo = 0.0, hi = 40.0;
   for (int it = 0; it < 200; ++it) {
-    double mid = 0.5 * (lo + hi);
+    const double mid = 0.5 * (lo + hi);
     if (std::erfc(mid / 1.41421356237309504880) >= alpha) lo = mid; else hi = mid;
   }
   return 0.5 * (lo + hi);
 }
 
-// |r| with calc_pvalue64(r) == alpha (p is decreasing in |r|)
+// |r| with calc_pvalue64(r) == alpha (p is decreasing in |r|); 2 if every r is removed
 double r_crit_of(double alpha, int n) {
   double lo = 0.0, hi = kCutThr;
-  if (calc_pvalue64(hi, n) >= alpha) return 2.0;  // every finite r is removed
+  if (calc_pvalue64(hi, n) >= alpha) return 2.0;
   for (int it = 0; it < 200; ++it) {
-    double mid = 0.5 * (lo + hi);
+    const double mid = 0.5 * (lo + hi);
     if (calc_pvalue64(mid, n) >= alpha) lo = mid; else hi = mid;
   }
   return 0.5 * (lo + hi);
 }
 
+// Absolute error bound of the tensor-core (split-BF16, FP32-accumulated) correlation
+// entries used by the FP32 decision bands: the rounding of the low halves (2^-17
+// relative per value) averages over the n samples, plus the FP32 accumulation; four
+// times the model, which bounds the measured errors of tests/test_gpu_tensorcore.py.
+double tc_entry_err(int64_t n) { return 4.0 * (1.6e-5 / std::sqrt((double)n) + 1e-7); }
+
 template <typename T>
 hpc_status dev_alloc(T **ptr, int64_t count, const char *what) {
   if (count <= 0) count = 1;
-  cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (size_t)count);
+  const cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (size_t)count);
   if (e != cudaSuccess) {
     *ptr = nullptr;
     cudaGetLastError();
@@ -77,49 +85,6 @@ void dev_free(T *&ptr) {
   ptr = nullptr;
 }
 
-// Absolute error bound of the tensor-core (split-BF16, FP32-accumulated) correlation
-// entries used by the FP32 decision bands: the rounding of the low halves (2^-17
-// relative per value) averages over the n samples, plus the FP32 accumulation;
-// four times the model, which bounds the measured errors of tests/test_gpu_tensorcore.py.
-double tc_entry_err(int64_t n) { return 4.0 * (1.6e-5 / std::sqrt((double)n) + 1e-7); }
-
-LevelArgs make_args(hpc_ctx *c, int level) {
-  LevelArgs a{};
-  a.p = c->p;
-  a.W = c->W;
-  a.level = level;
-  a.n_obs = (int)c->n;
-  a.alpha = c->opts.alpha;
-  a.sqrt_n3 = std::sqrt((double)c->n - 3.0);
-  // FP32 decision: |r| against r_crit with a band of the configured relative |z|
-  // margin (mapped to |r| through dz/dr = sqrt(n-3) / (1 - r^2)) plus an error bound
-  // ke / (smallest pivot) from the rounding of the FP32 correlation entries and of
-  // the factorisation
-  const double rc = c->r_crit >= 1.5 ? 2.0 : c->r_crit;
-  a.r_c = (float)rc;
-  a.margin_r = rc >= 1.5 ? 0.f : (float)(c->opts.retest_margin * c->zc * (1.0 - rc * rc) / a.sqrt_n3);
-  const double eps_in = c->cor32_rounded ? 1.2e-7 : tc_entry_err(c->n);
-  a.ke = (float)((4.0 * eps_in + (level + 2) * 2.4e-7) * (1.0 + std::min(rc, 1.0)));
-  a.cor64 = c->cor64_valid ? c->cor64 : nullptr;
-  a.cor32 = c->cor32;
-  a.Z = c->Z;
-  a.n_z = c->n;
-  a.denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
-  a.rq = c->rq;
-  a.rq_cap = c->rq_cap;
-  a.adj = c->adj;
-  a.deg = c->deg;
-  a.rowptr = c->rowptr;
-  a.colidx = c->colidx;
-  a.row_work = c->row_work;
-  a.recs = c->recs;
-  a.rec_cap = c->rec_cap;
-  a.colidx_cap = c->colidx_cap;
-  a.ctr = c->ctr + level;
-  a.gctr = c->gctr;
-  return a;
-}
-
 hpc_status check_ctx(hpc_ctx *c) {
   if (!c) {
     set_error("null context");
@@ -129,101 +94,194 @@ hpc_status check_ctx(hpc_ctx *c) {
   return HPC_OK;
 }
 
+hpc_status check_index(hpc_ctx *c, int idx) {
+  if (idx < 0 || idx >= c->count) {
+    set_error("instance %d out of range [0, %d)", idx, c->count);
+    return HPC_ERR_INVALID_ARG;
+  }
+  return HPC_OK;
+}
+
+double denom_of(const hpc_ctx *c, int64_t n) {
+  return c->opts.ref_compat_sd ? (double)((float)n - 1.f) : (double)(n - 1);
+}
+
+// The device instance table from the host bookkeeping and the current buffers.
+hpc_status write_inst_table(hpc_ctx *c) {
+  std::vector<Inst> t((size_t)c->count);
+  for (int b = 0; b < c->count; ++b) {
+    const InstHost &h = c->ih[b];
+    Inst &I = t[b];
+    std::memset(&I, 0, sizeof(I));
+    I.p = h.p;
+    I.W = h.W;
+    I.n_obs = (int)h.n;
+    I.alpha = h.alpha;
+    const double rc = h.r_crit >= 1.5 ? 2.0 : h.r_crit;
+    const double sqrt_n3 = std::sqrt((double)h.n - 3.0);
+    I.r_c = (float)rc;
+    I.margin_r = rc >= 1.5 ? 0.f : (float)(c->opts.retest_margin * h.zc * (1.0 - rc * rc) / sqrt_n3);
+    const double eps_in = c->cor32_rounded ? 1.2e-7 : tc_entry_err(h.n);
+    I.ke_a = (float)(4.0 * eps_in * (1.0 + std::min(rc, 1.0)));
+    I.ke_b = (float)(2.4e-7 * (1.0 + std::min(rc, 1.0)));
+    I.r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7);
+    I.r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
+    const double d0 = tc_entry_err(h.n) + 1e-6 * rc;
+    I.lo32 = rc >= 1.5 ? 2.f : (float)(rc - d0);
+    I.hi32 = rc >= 1.5 ? 2.f : (float)(rc + d0);
+    I.cor64 = (c->cor64_valid && c->cor64) ? c->cor64 + h.cor_off : nullptr;
+    I.cor32 = c->cor32 ? c->cor32 + h.cor_off : nullptr;
+    I.Z = c->Z ? c->Z + h.z_off : nullptr;
+    I.n_z = h.n;
+    I.denom = denom_of(c, h.n);
+    I.adj = c->adj + h.adj_off;
+    I.deg = c->deg + h.row_off;
+    I.rowptr = c->rowptr + h.row_off;
+    I.row_work = c->row_work + h.row_off;
+    I.colidx = c->colidx ? c->colidx + h.colidx_off : nullptr;
+    I.colidx_cap = c->colidx ? h.colidx_cap : 0;
+    I.recs = c->recs ? c->recs + h.rec_off : nullptr;
+    I.rec_cap = c->recs ? h.rec_cap : 0;
+    I.ctr = c->ctr + (size_t)b * kLevels;
+    I.g = c->gctr + b;
+  }
+  if (c->inst_host.size() == t.size() && std::memcmp(c->inst_host.data(), t.data(), sizeof(Inst) * t.size()) == 0)
+    return HPC_OK;  // unchanged: captured graphs stay valid
+  c->inst_host = t;
+  HPC_CUDA(cudaMemcpyAsync(c->inst, c->inst_host.data(), sizeof(Inst) * t.size(), cudaMemcpyHostToDevice, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  ++c->inst_version;
+  return HPC_OK;
+}
+
+Launch make_launch(hpc_ctx *c, int level) {
+  Launch L{};
+  L.inst = c->inst;
+  L.count = c->count;
+  L.level = level;
+  L.word_prefix = c->prefixes;
+  L.tile_prefix = c->prefixes + (c->count + 1);
+  L.row_prefix = c->prefixes + 2 * (c->count + 1);
+  L.work_prefix = c->work_prefix + (size_t)level * (c->count + 1);
+  L.lc = c->lc + level;
+  L.rq = c->rq;
+  L.rq_cap = c->rq_cap;
+  return L;
+}
+
 hpc_status pull_counters(hpc_ctx *c) {
-  HPC_CUDA(cudaMemcpyAsync(c->ctr_host, c->ctr, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1), cudaMemcpyDeviceToHost,
+  HPC_CUDA(cudaMemcpyAsync(c->ctr_host, c->ctr, sizeof(DevCounters) * (size_t)c->count * kLevels,
+                           cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaMemcpyAsync(c->gctr_host, c->gctr, sizeof(DevGlobal) * (size_t)c->count, cudaMemcpyDeviceToHost,
                            c->stream));
-  HPC_CUDA(cudaMemcpyAsync(c->gctr_host, c->gctr, sizeof(DevGlobal), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   return HPC_OK;
 }
 
 // Queue all device work of one level on the context stream (no host sync).
-// `timed` records the per-level events (not inside a graph capture: events
-// recorded by graph nodes cannot be timed).
+// `timed` records the per-level events (not inside a graph capture: events recorded
+// by graph nodes cannot be timed).
 hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   hpc_status s;
-  LevelArgs a = make_args(c, level);
+  const Launch L = make_launch(c, level);
   cudaEvent_t *ev = c->evl[level];
+  const bool queue = !c->cor64_valid;  // FP64 re-tests deferred to the re-test kernel
   if (timed) HPC_CUDA(cudaEventRecord(ev[0], c->stream));
   if (level == 0) {
-    const double rc = c->r_crit;
     if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-    if (c->cor64_valid) {
-      const double r_lo = rc >= 1.5 ? 2.0 : rc * (1.0 - 1e-7), r_hi = rc >= 1.5 ? 2.0 : rc * (1.0 + 1e-7);
-      if ((s = launch_level0(a, r_lo, r_hi, c->stream)) != HPC_OK) return s;
-    } else {
-      // FP32 tensor-core entries: band of the entry error bound, FP64 re-tests queued
-      const double d0 = tc_entry_err(c->n) + 1e-6 * rc;
-      const float lo = rc >= 1.5 ? 2.f : (float)(rc - d0), hi = rc >= 1.5 ? 2.f : (float)(rc + d0);
-      HPC_CUDA(cudaMemsetAsync(&a.ctr->rq_count, 0, sizeof(unsigned long long), c->stream));
-      if ((s = launch_level0_f32(a, lo, hi, c->stream)) != HPC_OK) return s;
-      if ((s = launch_retest(a, c->sm_count, c->stream)) != HPC_OK) return s;
-      if ((s = launch_mirror(a, c->stream)) != HPC_OK) return s;
-      c->timings.launches += 1;
-    }
+    if ((s = launch_level0(L, c->total_words, c->stream)) != HPC_OK) return s;
+    if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
+    if ((s = launch_mirror(L, c->total_tiles, c->stream)) != HPC_OK) return s;
     if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
-    if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
-    if ((s = launch_scan(c->p, 0, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
-    c->timings.launches += 4;
+    if ((s = launch_degrees(L, c->total_rows, c->stream)) != HPC_OK) return s;
+    if ((s = launch_scan(L, c->stream)) != HPC_OK) return s;
+    c->timings.launches += queue ? 5 : 4;
     return HPC_OK;
   }
-  if ((s = launch_degrees(a, c->deg, c->stream)) != HPC_OK) return s;
-  if ((s = launch_scan(c->p, level, c->deg, c->rowptr, c->row_work, a.ctr, c->gctr, c->stream)) != HPC_OK) return s;
-  if ((s = launch_fill_csr(a, c->colidx, c->stream)) != HPC_OK) return s;
+  if ((s = launch_degrees(L, c->total_rows, c->stream)) != HPC_OK) return s;
+  if ((s = launch_scan(L, c->stream)) != HPC_OK) return s;
+  if ((s = launch_fill_csr(L, c->total_rows, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  if ((s = launch_citest(a, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
-  if (!c->cor64_valid) {
-    if ((s = launch_retest(a, c->sm_count, c->stream)) != HPC_OK) return s;
-    c->timings.launches += 1;
-  }
+  if ((s = launch_citest(L, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
+  if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
-  c->timings.launches += 4;
+  c->timings.launches += queue ? 5 : 4;
   if (c->opts.precision != HPC_PREC_FP64) {
-    if ((s = launch_finalize_records(a, c->stream)) != HPC_OK) return s;
+    if ((s = launch_finalize_records(L, c->stream)) != HPC_OK) return s;
     c->timings.launches += 1;
   }
   return HPC_OK;
 }
 
-// Neighbour-list and record buffers sized from the level-0 result (counters pulled).
+// Neighbour-list and record buffers sized from the level-0 result (counters pulled):
+// an instance needs room for the edges alive after level 0.
 hpc_status ensure_capacity(hpc_ctx *c, bool *changed) {
-  const int64_t e2 = (int64_t)c->ctr_host[0].edges2;
-  hpc_status s;
   *changed = false;
-  if (e2 > c->colidx_cap) {
+  bool grow = !c->colidx || !c->recs;
+  for (int b = 0; b < c->count && !grow; ++b) {
+    const long long e2 = (long long)c->ctr_host[(size_t)b * kLevels].edges2;
+    if (e2 > c->ih[b].colidx_cap || e2 / 2 > c->ih[b].rec_cap) grow = true;
+  }
+  if (!grow) return HPC_OK;
+  long long ct = 0, rt = 0;
+  for (int b = 0; b < c->count; ++b) {
+    InstHost &h = c->ih[b];
+    const long long e2 = (long long)c->ctr_host[(size_t)b * kLevels].edges2;
+    h.colidx_cap = std::max<long long>(std::max<long long>(h.colidx_cap, e2), 1);
+    h.rec_cap = std::max<long long>(std::max<long long>(h.rec_cap, e2 / 2), 1);
+    h.colidx_off = ct;
+    h.rec_off = rt;
+    ct += h.colidx_cap;
+    rt += h.rec_cap;
+  }
+  hpc_status s;
+  if (ct > c->colidx_total || !c->colidx) {
     dev_free(c->colidx);
-    c->colidx_cap = 0;
-    if ((s = dev_alloc(&c->colidx, std::max<int64_t>(1, e2), "neighbour lists")) != HPC_OK) return s;
-    c->colidx_cap = std::max<int64_t>(1, e2);
-    *changed = true;
+    c->colidx_total = 0;
+    if ((s = dev_alloc(&c->colidx, ct, "neighbour lists")) != HPC_OK) return s;
+    c->colidx_total = ct;
   }
-  if (e2 / 2 > c->rec_cap) {
+  if (rt > c->rec_total || !c->recs) {
     dev_free(c->recs);
-    c->rec_cap = 0;
-    if ((s = dev_alloc(&c->recs, std::max<int64_t>(1, e2 / 2), "separation-set records")) != HPC_OK) return s;
-    c->rec_cap = std::max<int64_t>(1, e2 / 2);
-    *changed = true;
+    c->rec_total = 0;
+    if ((s = dev_alloc(&c->recs, rt, "separation-set records")) != HPC_OK) return s;
+    c->rec_total = rt;
   }
-  return HPC_OK;
+  *changed = true;
+  return write_inst_table(c);
 }
 
-// Per-level statistics and timings from the pulled counters and events.
-hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
-  const DevCounters &h = c->ctr_host[level];
+// Statistics of one level, summed over the instances (or of one instance).
+hpc_level_stats level_stats_of(hpc_ctx *c, int level, int only) {
   hpc_level_stats st{};
   st.level = level;
-  st.edges_before = c->edges;
-  st.max_degree = level == 0 ? (int)(c->p - 1) : h.max_deg;
-  st.rows = level == 0 ? c->p : h.rows;
-  if (level == 0) {
-    st.potential_tests = st.executed_tests = c->p * (c->p - 1) / 2;
-    st.edges_after = (int64_t)(h.edges2 / 2);
-  } else {
-    st.potential_tests = (int64_t)h.work_total;
-    st.executed_tests = (int64_t)h.tests;
-    st.retests = (int64_t)h.retests;
-    st.edges_after = st.edges_before - (int64_t)h.deleted;
+  for (int b = 0; b < c->count; ++b) {
+    if (only >= 0 && b != only) continue;
+    const DevCounters &h = c->ctr_host[(size_t)b * kLevels + level];
+    const InstHost &ih = c->ih[b];
+    const int64_t before = level == 0 ? ih.p * (ih.p - 1) / 2 : 0;
+    st.max_degree = std::max(st.max_degree, level == 0 ? (int)(ih.p - 1) : h.max_deg);
+    if (level == 0) {
+      st.rows += ih.p;
+      st.potential_tests += before;
+      st.executed_tests += before;
+      st.edges_before += before;
+      st.edges_after += (int64_t)(h.edges2 / 2);
+    } else {
+      st.rows += h.rows;
+      st.potential_tests += (int64_t)h.work_total;
+      st.executed_tests += (int64_t)h.tests;
+      st.retests += (int64_t)h.retests;
+      st.edges_before += (int64_t)(h.edges2 / 2);
+      st.edges_after += (int64_t)(h.edges2 / 2) - (int64_t)h.deleted;
+    }
   }
+  return st;
+}
+
+// Per-level statistics and timings after a level ran (counters pulled).
+hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
+  hpc_level_stats st = level_stats_of(c, level, -1);
   float t_all = 0.f, t_snap = 0.f, t_test = 0.f;
   if (!c->last_run_graph) {
     HPC_CUDA(cudaEventElapsedTime(&t_snap, c->evl[level][0], c->evl[level][1]));
@@ -235,11 +293,14 @@ hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
   c->timings.level_ms[level] = t_all;
   c->timings.compact_ms[level] = t_snap;
   c->timings.test_ms[level] = t_test;
-  c->edges = st.edges_after;
-  if (h.band_violations) {
-    set_error("level %d: %llu FP32 removals not confirmed in FP64 (error bound violated)", level,
-              (unsigned long long)h.band_violations);
-    return HPC_ERR_NUMERIC;
+  for (int b = 0; b < c->count; ++b) {
+    const DevCounters &h = c->ctr_host[(size_t)b * kLevels + level];
+    c->ih[b].edges = level == 0 ? (int64_t)(h.edges2 / 2) : (int64_t)(h.edges2 / 2) - (int64_t)h.deleted;
+    if (h.band_violations) {
+      set_error("instance %d level %d: %llu FP32 removals not confirmed in FP64 (error bound violated)", b, level,
+                (unsigned long long)h.band_violations);
+      return HPC_ERR_NUMERIC;
+    }
   }
   if (c->opts.verbose)
     printf("level %d: max degree %d, tests %lld of %lld, FP64 re-tests %lld, edges %lld -> %lld, %.3f ms\n", level,
@@ -250,127 +311,290 @@ hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
 }
 
 hpc_status global_errors(hpc_ctx *c) {
-  const int err = c->gctr_host->err;
-  if (err & kErrWorkOverflow) {
-    set_error("the number of CI tests of a level overflows 64 bits");
-    return HPC_ERR_CAPACITY;
-  }
-  if (err & kErrRecOverflow) {
-    set_error("separation-set record buffer overflow");
-    return HPC_ERR_CAPACITY;
+  for (int b = 0; b < c->count; ++b) {
+    const int err = c->gctr_host[b].err;
+    if (err & kErrWorkOverflow) {
+      set_error("instance %d: the number of CI tests of a level overflows 64 bits", b);
+      return HPC_ERR_CAPACITY;
+    }
+    if (err & kErrRecOverflow) {
+      set_error("instance %d: separation-set record buffer overflow", b);
+      return HPC_ERR_CAPACITY;
+    }
+    if (err & kErrTimeout) {
+      set_error("instance %d: a bounded device wait timed out", b);
+      return HPC_ERR_TIMEOUT;
+    }
   }
   return HPC_OK;
+}
+
+bool any_csr_overflow(hpc_ctx *c) {
+  for (int b = 0; b < c->count; ++b)
+    if (c->gctr_host[b].err & kErrCsrOverflow) return true;
+  return false;
+}
+
+bool any_work(hpc_ctx *c, int level) {
+  for (int b = 0; b < c->count; ++b)
+    if (c->ctr_host[(size_t)b * kLevels + level].work_total) return true;
+  return false;
+}
+
+bool capturable(cudaStream_t s) { return s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread; }
+
+// Run levels first..last with one host sync at the end; the whole sequence 0..last
+// is captured once into a CUDA graph and replayed while the buffers stay in place.
+hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
+  hpc_status s;
+  auto enqueue_all = [&](bool timed) -> hpc_status {
+    HPC_CUDA(cudaMemsetAsync(c->lc + first, 0, sizeof(LaunchCounters) * (size_t)(last - first + 1), c->stream));
+    for (int l = first; l <= last; ++l)
+      if ((s = enqueue_level(c, l, timed)) != HPC_OK) return s;
+    return HPC_OK;
+  };
+  if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
+    const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
+                       c->graph_version == c->inst_version;
+    if (!valid) {
+      if (c->graph) cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+      cudaGraph_t g = nullptr;
+      const int64_t launches = c->timings.launches;
+      HPC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      if ((s = enqueue_all(false)) != HPC_OK) {
+        cudaStreamEndCapture(c->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        return s;
+      }
+      HPC_CUDA(cudaStreamEndCapture(c->stream, &g));
+      c->graph_launches = c->timings.launches - launches;
+      c->timings.launches = launches;  // counted when the graph runs
+      const cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        c->graph = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+      }
+      c->graph_top = last;
+      c->graph_stream = c->stream;
+      c->graph_version = c->inst_version;
+    }
+    HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    c->timings.launches += c->graph_launches;
+    c->last_run_graph = true;
+  } else {
+    if ((s = enqueue_all(true)) != HPC_OK) return s;
+    c->last_run_graph = false;
+  }
+  return pull_counters(c);
+}
+
+// ---- correlation ----------------------------------------------------------
+
+// Shape metadata of the grouped correlation kernels (device arrays), built once.
+hpc_status ensure_meta(hpc_ctx *c) {
+  if (c->meta) return HPC_OK;
+  const int C = c->count;
+  // layout: row_prefix (C+1) | x_off | z_off | n | tc_off | n_pad | kdim | tile64 (C+1) | c_off | p | tiletc (C+1)
+  std::vector<long long> m((size_t)(11 * C + 3), 0);
+  long long *row_prefix = m.data(), *x_off = row_prefix + (C + 1), *z_off = x_off + C, *n = z_off + C;
+  long long *tc_off = n + C, *n_pad = tc_off + C, *kdim = n_pad + C, *tile64 = kdim + C;
+  long long *c_off = tile64 + (C + 1), *p = c_off + C, *tiletc = p + C;
+  long long rows = 0, xo = 0, t64 = 0, ttc = 0;
+  for (int b = 0; b < C; ++b) {
+    const InstHost &h = c->ih[b];
+    row_prefix[b] = rows;
+    rows += h.p;
+    x_off[b] = xo;
+    z_off[b] = h.z_off;
+    xo += h.n * h.p;
+    n[b] = h.n;
+    tc_off[b] = h.tc_off;
+    n_pad[b] = tc_n_pad(h.n);
+    kdim[b] = tc_k(h.n);
+    tile64[b] = t64;
+    t64 += gram_f64_tiles(h.p);
+    c_off[b] = h.cor_off;
+    p[b] = h.p;
+    tiletc[b] = ttc;
+    ttc += gram_tc_tiles(h.p);
+  }
+  row_prefix[C] = rows;
+  tile64[C] = t64;
+  tiletc[C] = ttc;
+  c->tiles64 = t64;
+  c->tiles_tc = ttc;
+  std::vector<double> den((size_t)C);
+  for (int b = 0; b < C; ++b) den[b] = denom_of(c, c->ih[b].n);
+  hpc_status s;
+  if ((s = dev_alloc(&c->meta, (int64_t)m.size(), "correlation metadata")) != HPC_OK) return s;
+  if ((s = dev_alloc(&c->meta_denom, C, "correlation metadata")) != HPC_OK) return s;
+  HPC_CUDA(cudaMemcpyAsync(c->meta, m.data(), sizeof(long long) * m.size(), cudaMemcpyHostToDevice, c->stream));
+  HPC_CUDA(cudaMemcpyAsync(c->meta_denom, den.data(), sizeof(double) * den.size(), cudaMemcpyHostToDevice, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
+StdArgs std_args(hpc_ctx *c) {
+  const int C = c->count;
+  long long *m = c->meta;
+  StdArgs a{};
+  a.count = C;
+  a.row_prefix = m;
+  a.x_off = m + (C + 1);
+  a.z_off = a.x_off + C;
+  a.n = a.z_off + C;
+  a.tc_off = a.n + C;
+  a.n_pad = a.tc_off + C;
+  a.kdim = a.n_pad + C;
+  a.ref_compat = c->opts.ref_compat_sd;
+  return a;
+}
+
+GramArgs gram_args(hpc_ctx *c) {
+  const StdArgs sa = std_args(c);
+  GramArgs g{};
+  g.count = c->count;
+  g.tile_prefix = sa.kdim + c->count;
+  g.z_off = sa.z_off;
+  g.c_off = g.tile_prefix + (c->count + 1);
+  g.n = sa.n;
+  g.p = g.c_off + c->count;
+  g.denom = c->meta_denom;
+  return g;
 }
 
 hpc_status after_correlation(hpc_ctx *c) {
-  if (c->opts.precision == HPC_PREC_MIXED) {
-    hpc_status s = launch_to_f32(c->cor64, c->p * c->p, c->cor32, c->stream);
-    if (s != HPC_OK) return s;
-    c->timings.launches += 1;
-  }
   c->have_cor = true;
-  c->cor32_rounded = c->opts.precision != HPC_PREC_MIXED_TC;
+  hpc_status s = write_inst_table(c);
+  if (s != HPC_OK) return s;
   return hpc_ctx_reset(c);
 }
 
-// A loaded FP64 matrix: every mixed mode tests on its FP32 rounding.
-hpc_status after_loaded_correlation(hpc_ctx *c) {
-  if (c->opts.precision != HPC_PREC_FP64) {
-    hpc_status s = launch_to_f32(c->cor64, c->p * c->p, c->cor32, c->stream);
-    if (s != HPC_OK) return s;
-    c->timings.launches += 1;
-  }
-  c->have_cor = true;
-  c->cor32_rounded = true;
-  c->cor64_valid = true;
-  return hpc_ctx_reset(c);
-}
-
-template <typename T>
-hpc_status correlation_device(hpc_ctx *c, const T *X) {
+hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
   if (!X) {
     set_error("null observation pointer");
     return HPC_ERR_INVALID_ARG;
   }
-  const int64_t elems = c->n * c->p;
-  if (c->Z_elems < elems) {
-    dev_free(c->Z);
-    if ((s = dev_alloc(&c->Z, elems, "standardised data")) != HPC_OK) return s;
-    c->Z_elems = elems;
-  }
+  if ((s = ensure_meta(c)) != HPC_OK) return s;
+  long long ztot = 0;
+  for (const auto &h : c->ih) ztot += h.n * h.p;
+  if (!c->Z && (s = dev_alloc(&c->Z, ztot, "standardised data")) != HPC_OK) return s;
+  const bool tc = c->opts.precision == HPC_PREC_MIXED_TC;
+  StdArgs sa = std_args(c);
   HPC_CUDA(cudaEventRecord(c->evc[0], c->stream));
-  const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
-  if (c->opts.precision == HPC_PREC_MIXED_TC) {
-    // split-BF16 operands + FP64 standardised copy, tensor-core Gram into cor32
-    const int64_t tc = tc_p_pad(c->p) * tc_k(c->n);
-    if (c->tc_elems < tc) {
-      dev_free(c->tcP);
-      dev_free(c->tcQ);
-      c->tc_elems = 0;
-      if ((s = dev_alloc(&c->tcP, tc, "tensor-core operand P")) != HPC_OK) return s;
-      if ((s = dev_alloc(&c->tcQ, tc, "tensor-core operand Q")) != HPC_OK) return s;
-      HPC_CUDA(cudaMemsetAsync(c->tcP, 0, sizeof(__nv_bfloat16) * tc, c->stream));
-      HPC_CUDA(cudaMemsetAsync(c->tcQ, 0, sizeof(__nv_bfloat16) * tc, c->stream));
-      c->tc_elems = tc;
+  if (tc) {
+    if (!c->tcP) {
+      long long tt = 0;
+      for (const auto &h : c->ih) tt += tc_p_pad(h.p) * tc_k(h.n);
+      if ((s = dev_alloc(&c->tcP, tt, "tensor-core operand P")) != HPC_OK) return s;
+      if ((s = dev_alloc(&c->tcQ, tt, "tensor-core operand Q")) != HPC_OK) return s;
+      HPC_CUDA(cudaMemsetAsync(c->tcP, 0, sizeof(__nv_bfloat16) * tt, c->stream));
+      HPC_CUDA(cudaMemsetAsync(c->tcQ, 0, sizeof(__nv_bfloat16) * tt, c->stream));
+      std::vector<CUtensorMap> maps((size_t)(2 * c->count));
+      for (int b = 0; b < c->count; ++b) {
+        const InstHost &h = c->ih[b];
+        if ((s = tc_make_maps(&maps[2 * b], &maps[2 * b + 1], c->tcP + h.tc_off, c->tcQ + h.tc_off, h.p, h.n)) !=
+            HPC_OK)
+          return s;
+      }
+      if ((s = dev_alloc(&c->tc_maps, 2 * c->count, "tensor maps")) != HPC_OK) return s;
+      HPC_CUDA(cudaMemcpyAsync(c->tc_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+      HPC_CUDA(cudaStreamSynchronize(c->stream));
     }
-    if (sizeof(T) == 8)
-      s = launch_standardise_split_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->tcP, c->tcQ,
-                                       c->stream);
-    else
-      s = launch_standardise_split_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->tcP, c->tcQ,
-                                       c->stream);
-    if (s != HPC_OK) return s;
-    HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
-    if ((s = launch_gram_tc(c->tcP, c->tcQ, c->n, c->p, c->cor32, &c->gctr->err, c->stream)) != HPC_OK) return s;
-    HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
-    // FP64 entries come from dot products of Z in the re-test kernels: no FP64 matrix
     if (!c->rq) {
-      const int64_t cap = 1 << 20;
+      const long long cap = 1 << 20;
       if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
       c->rq_cap = cap;
     }
-    c->cor64_valid = false;
+    if ((s = launch_standardise(X, f32, sa, sa.count ? c->total_rows : 0, c->Z, c->tcP, c->tcQ, c->stream)) != HPC_OK)
+      return s;
+    HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
+    TcArgs ta{};
+    ta.count = c->count;
+    ta.tile_prefix = gram_args(c).p + c->count;
+    ta.maps = c->tc_maps;
+    ta.c_off = gram_args(c).c_off;
+    ta.p = gram_args(c).p;
+    ta.n = sa.n;
+    ta.err = &c->gctr[0].err;
+    if ((s = launch_gram_tc(c->cor32, ta, c->tiles_tc, c->stream)) != HPC_OK) return s;
+    HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+    c->cor64_valid = false;  // FP64 entries come from dot products of Z in the re-test kernels
+    c->cor32_rounded = false;
     c->timings.launches += 2;
   } else {
-    if (sizeof(T) == 8)
-      s = launch_standardise_f64((const double *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
-    else
-      s = launch_standardise_f32((const float *)X, c->n, c->p, c->opts.ref_compat_sd, c->Z, c->stream);
-    if (s != HPC_OK) return s;
+    if ((s = launch_standardise(X, f32, sa, c->total_rows, c->Z, nullptr, nullptr, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
-    if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
+    if ((s = launch_gram_f64(c->Z, c->cor64, gram_args(c), c->tiles64, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
-    c->cor64_valid = true;
     c->timings.launches += 2;
+    c->cor64_valid = true;
+    c->cor32_rounded = true;
+    if (c->opts.precision == HPC_PREC_MIXED) {
+      long long tot = 0;
+      for (const auto &h : c->ih) tot += h.p * h.p;
+      if ((s = launch_to_f32(c->cor64, tot, c->cor32, c->stream)) != HPC_OK) return s;
+      c->timings.launches += 1;
+    }
   }
-  if ((s = after_correlation(c)) != HPC_OK) return s;
   HPC_CUDA(cudaEventRecord(c->evc[3], c->stream));
   c->cor_timed = true;
-  return HPC_OK;
+  return after_correlation(c);
 }
 
-template <typename T>
-hpc_status correlation_host(hpc_ctx *c, const T *X) {
+hpc_status correlation_host(hpc_ctx *c, const void *X, bool f32) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
   if (!X) {
     set_error("null observation pointer");
     return HPC_ERR_INVALID_ARG;
   }
-  const int64_t bytes = c->n * c->p * (int64_t)sizeof(T);
+  long long elems = 0;
+  for (const auto &h : c->ih) elems += h.n * h.p;
+  const int64_t bytes = elems * (f32 ? 4 : 8);
   if (c->X_stage_bytes < bytes) {
     if (c->X_stage) cudaFree(c->X_stage);
     c->X_stage = nullptr;
+    c->X_stage_bytes = 0;
     uint8_t *buf = nullptr;
     if ((s = dev_alloc(&buf, bytes, "observation staging")) != HPC_OK) return s;
     c->X_stage = buf;
     c->X_stage_bytes = bytes;
   }
   HPC_CUDA(cudaMemcpyAsync(c->X_stage, X, (size_t)bytes, cudaMemcpyHostToDevice, c->stream));
-  return correlation_device(c, (const T *)c->X_stage);
+  return correlation_device(c, c->X_stage, f32);
 }
+
+// A loaded FP64 matrix (every instance): the mixed modes test on its FP32 rounding.
+hpc_status load_correlation(hpc_ctx *c, const double *C, cudaMemcpyKind kind) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!C) {
+    set_error("null correlation pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  long long tot = 0;
+  for (const auto &h : c->ih) tot += h.p * h.p;
+  if (!c->cor64 && (s = dev_alloc(&c->cor64, tot, "cor64")) != HPC_OK) return s;
+  if (c->opts.precision != HPC_PREC_FP64 && !c->cor32 && (s = dev_alloc(&c->cor32, tot, "cor32")) != HPC_OK)
+    return s;
+  HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)tot, kind, c->stream));
+  if (c->opts.precision != HPC_PREC_FP64) {
+    if ((s = launch_to_f32(c->cor64, tot, c->cor32, c->stream)) != HPC_OK) return s;
+    c->timings.launches += 1;
+  }
+  c->cor64_valid = true;
+  c->cor32_rounded = true;
+  return after_correlation(c);
+}
+
+hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, const double *alpha,
+                  const hpc_opts *opts);
 
 }  // namespace
 }  // namespace hpc
@@ -400,8 +624,8 @@ hpc_status hpc_opts_default(hpc_opts *o) {
   if (!o) return HPC_ERR_INVALID_ARG;
   std::memset(o, 0, sizeof(*o));
   o->device = 0;
-  o->alpha = 0.05;  // src/main.cpp:26
-  o->max_level = 4; // src/main.cpp:31
+  o->alpha = 0.05;   // src/main.cpp:26
+  o->max_level = 4;  // src/main.cpp:31
   o->precision = HPC_PREC_MIXED;
   o->retest_margin = 1e-3;
   o->ref_compat_sd = 0;
@@ -412,13 +636,15 @@ hpc_status hpc_opts_default(hpc_opts *o) {
 hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *bytes) {
   if (!o || !bytes || p < 2 || n < 4) return HPC_ERR_INVALID_ARG;
   const int64_t W = (p + 31) / 32;
-  int64_t b = p * p * 8;                                  // cor64
-  if (o->precision != HPC_PREC_FP64) b += p * p * 4;      // cor32
-  b += p * W * 4;                                         // adjacency bits
-  b += (p + 1) * (4 + 4 + 8);                             // deg, rowptr, row_work
-  b += n * p * 8;                                         // standardised data
-  // neighbour lists and records are sized at level 1 from the surviving edges;
-  // budget them for an average degree of 64
+  int64_t b = 0;
+  if (o->precision != HPC_PREC_MIXED_TC) b += p * p * 8;           // cor64
+  if (o->precision != HPC_PREC_FP64) b += p * p * 4;               // cor32
+  if (o->precision == HPC_PREC_MIXED_TC) b += 2 * tc_p_pad(p) * tc_k(n) * 2;  // split operands
+  b += n * p * 8;                                                  // standardised data
+  b += n * p * 4;                                                  // observation staging
+  b += p * W * 4 + p * p;                                          // adjacency bits + bytes
+  b += (p + 1) * (4 + 4 + 8);                                      // deg, rowptr, row_work
+  // neighbour lists and records are sized after level 0; budget an average degree of 64
   const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
   b += 2 * e * 4 + e * (int64_t)sizeof(hpc_sepset_record);
   *bytes = b;
@@ -426,96 +652,24 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
 }
 
 hpc_status hpc_ctx_create(hpc_ctx **out, int64_t p, int64_t n, const hpc_opts *opts) {
-  if (!out) {
-    set_error("null output pointer");
+  return create(out, 1, &p, &n, nullptr, opts);
+}
+
+hpc_status hpc_batch_create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, const double *alpha,
+                            const hpc_opts *opts) {
+  if (count < 1 || !p || !n) {
+    set_error("batch needs count >= 1 and p, n arrays");
     return HPC_ERR_INVALID_ARG;
   }
-  *out = nullptr;
-  hpc_opts o;
-  if (opts) o = *opts; else hpc_opts_default(&o);
-  if (p < 2 || p > 46340) {
-    set_error("p = %lld out of range [2, 46340]", (long long)p);
+  return create(out, count, p, n, alpha, opts);
+}
+
+hpc_status hpc_batch_size(hpc_ctx *c, int *count) {
+  if (!c || !count) {
+    set_error("null argument");
     return HPC_ERR_INVALID_ARG;
   }
-  if (n < 4 || n > 0x7fffffff) {
-    set_error("n_obs = %lld out of range [4, 2^31)", (long long)n);
-    return HPC_ERR_INVALID_ARG;
-  }
-  if (!(o.alpha > 0.0 && o.alpha <= 1.0)) {
-    set_error("alpha = %g outside (0, 1]", o.alpha);
-    return HPC_ERR_INVALID_ARG;
-  }
-  if (o.precision < HPC_PREC_FP64 || o.precision > HPC_PREC_MIXED_TC) {
-    set_error("unknown precision %d", o.precision);
-    return HPC_ERR_INVALID_ARG;
-  }
-  if (o.max_level > HPC_MAX_LEVEL) {
-    set_error("max_level %d above HPC_MAX_LEVEL %d", o.max_level, HPC_MAX_LEVEL);
-    return HPC_ERR_INVALID_ARG;
-  }
-  if (!(o.retest_margin >= 0.0)) o.retest_margin = 1e-3;
-  int ndev = 0;
-  cudaError_t e = cudaGetDeviceCount(&ndev);
-  if (e != cudaSuccess || ndev == 0) {
-    cudaGetLastError();
-    set_error("no CUDA device available: %s", cudaGetErrorString(e));
-    return HPC_ERR_NO_DEVICE;
-  }
-  if (o.device < 0 || o.device >= ndev) {
-    set_error("device %d not present (%d devices)", o.device, ndev);
-    return HPC_ERR_INVALID_ARG;
-  }
-  hpc_ctx *c = new hpc_ctx();
-  c->p = p;
-  c->n = n;
-  c->opts = o;
-  c->device = o.device;
-  c->W = (int)((p + 31) / 32);
-  c->zc = z_crit_of(o.alpha);
-  c->r_crit = r_crit_of(o.alpha, (int)n);
-  hpc_status s = HPC_OK;
-  auto fail = [&](hpc_status st) {
-    hpc_ctx_destroy(c);
-    return st;
-  };
-  if (cudaSetDevice(c->device) != cudaSuccess) {
-    cudaGetLastError();
-    set_error("cudaSetDevice(%d) failed", c->device);
-    delete c;
-    return HPC_ERR_CUDA;
-  }
-  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
-  c->stream = nullptr;
-  bool ev_ok = true;
-  for (auto &e : c->evc) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
-  for (auto &e : c->evr) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
-  for (auto &lv : c->evl)
-    for (auto &e : lv) ev_ok = ev_ok && cudaEventCreate(&e) == cudaSuccess;
-  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess || !ev_ok) {
-    cudaGetLastError();
-    set_error("stream/event creation failed");
-    return fail(HPC_ERR_CUDA);
-  }
-  c->stream = c->own_stream;
-  for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
-  if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, p * p, "cor64")) != HPC_OK) return fail(s);
-  if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, p * p, "cor32")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->adj, p * (int64_t)c->W, "adjacency")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->deg, p, "degrees")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->rowptr, p + 1, "row offsets")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->row_work, p + 1, "row work")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->ctr, HPC_MAX_LEVEL + 1, "level counters")) != HPC_OK) return fail(s);
-  if ((s = dev_alloc(&c->gctr, 1, "counters")) != HPC_OK) return fail(s);
-  if (cudaMallocHost((void **)&c->ctr_host, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1)) != cudaSuccess ||
-      cudaMallocHost((void **)&c->gctr_host, sizeof(DevGlobal)) != cudaSuccess) {
-    cudaGetLastError();
-    set_error("pinned counter allocation failed");
-    return fail(HPC_ERR_OOM);
-  }
-  if (cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1), c->stream) != cudaSuccess ||
-      cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal), c->stream) != cudaSuccess)
-    return fail(HPC_ERR_CUDA);
-  *out = c;
+  *count = c->count;
   return HPC_OK;
 }
 
@@ -528,17 +682,24 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->Z);
   dev_free(c->tcP);
   dev_free(c->tcQ);
+  dev_free(c->tc_maps);
   if (c->X_stage) cudaFree(c->X_stage);
   dev_free(c->adj);
   dev_free(c->adj_bytes);
-  dev_free(c->rq);
   dev_free(c->deg);
   dev_free(c->rowptr);
-  dev_free(c->colidx);
   dev_free(c->row_work);
+  dev_free(c->colidx);
   dev_free(c->recs);
+  dev_free(c->rq);
   dev_free(c->ctr);
   dev_free(c->gctr);
+  dev_free(c->lc);
+  dev_free(c->inst);
+  dev_free(c->prefixes);
+  dev_free(c->work_prefix);
+  dev_free(c->meta);
+  dev_free(c->meta_denom);
   if (c->ctr_host) cudaFreeHost(c->ctr_host);
   if (c->gctr_host) cudaFreeHost(c->gctr_host);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -552,6 +713,16 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   cudaGetLastError();
   delete c;
+  return HPC_OK;
+}
+
+hpc_status hpc_ctx_reset(hpc_ctx *c) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)c->count * kLevels, c->stream));
+  HPC_CUDA(cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal) * (size_t)c->count, c->stream));
+  c->next_level = 0;
+  for (auto &h : c->ih) h.edges = h.p * (h.p - 1) / 2;
   return HPC_OK;
 }
 
@@ -591,43 +762,29 @@ hpc_status hpc_get_timings(hpc_ctx *c, hpc_timings *out) {
   return HPC_OK;
 }
 
-hpc_status hpc_ctx_reset(hpc_ctx *c) {
-  hpc_status s = check_ctx(c);
-  if (s != HPC_OK) return s;
-  HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (HPC_MAX_LEVEL + 1), c->stream));
-  HPC_CUDA(cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal), c->stream));
-  c->next_level = 0;
-  c->edges = c->p * (c->p - 1) / 2;
-  return HPC_OK;
-}
-
-hpc_status hpc_correlation_f64(hpc_ctx *c, const double *X) { return correlation_host(c, X); }
-hpc_status hpc_correlation_f32(hpc_ctx *c, const float *X) { return correlation_host(c, X); }
-hpc_status hpc_correlation_device_f64(hpc_ctx *c, const double *X) { return correlation_device(c, X); }
-hpc_status hpc_correlation_device_f32(hpc_ctx *c, const float *X) { return correlation_device(c, X); }
-
-hpc_status hpc_load_correlation(hpc_ctx *c, const double *C) {
-  hpc_status s = check_ctx(c);
-  if (s != HPC_OK) return s;
-  if (!C) {
-    set_error("null correlation pointer");
-    return HPC_ERR_INVALID_ARG;
-  }
-  if (!c->cor64 && (s = dev_alloc(&c->cor64, c->p * c->p, "cor64")) != HPC_OK) return s;
-  HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyHostToDevice, c->stream));
-  return after_loaded_correlation(c);
-}
-
+hpc_status hpc_correlation_f64(hpc_ctx *c, const double *X) { return correlation_host(c, X, false); }
+hpc_status hpc_correlation_f32(hpc_ctx *c, const float *X) { return correlation_host(c, X, true); }
+hpc_status hpc_correlation_device_f64(hpc_ctx *c, const double *X) { return correlation_device(c, X, false); }
+hpc_status hpc_correlation_device_f32(hpc_ctx *c, const float *X) { return correlation_device(c, X, true); }
+hpc_status hpc_load_correlation(hpc_ctx *c, const double *C) { return load_correlation(c, C, cudaMemcpyHostToDevice); }
 hpc_status hpc_load_correlation_device(hpc_ctx *c, const double *C) {
-  hpc_status s = check_ctx(c);
-  if (s != HPC_OK) return s;
-  if (!C) {
-    set_error("null correlation pointer");
+  return load_correlation(c, C, cudaMemcpyDeviceToDevice);
+}
+
+hpc_status hpc_batch_offsets(hpc_ctx *c, int64_t *obs_offsets, int64_t *cor_offsets) {
+  if (!c) {
+    set_error("null context");
     return HPC_ERR_INVALID_ARG;
   }
-  if (!c->cor64 && (s = dev_alloc(&c->cor64, c->p * c->p, "cor64")) != HPC_OK) return s;
-  HPC_CUDA(cudaMemcpyAsync(c->cor64, C, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToDevice, c->stream));
-  return after_loaded_correlation(c);
+  long long xo = 0;
+  for (int b = 0; b < c->count; ++b) {
+    if (obs_offsets) obs_offsets[b] = xo;
+    if (cor_offsets) cor_offsets[b] = c->ih[b].cor_off;
+    xo += c->ih[b].n * c->ih[b].p;
+  }
+  if (obs_offsets) obs_offsets[c->count] = xo;
+  if (cor_offsets) cor_offsets[c->count] = c->ih.back().cor_off + c->ih.back().p * c->ih.back().p;
+  return HPC_OK;
 }
 
 hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
@@ -637,14 +794,16 @@ hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
     set_error(!C ? "null output pointer" : "no correlation matrix yet");
     return !C ? HPC_ERR_INVALID_ARG : HPC_ERR_STATE;
   }
+  long long tot = 0;
+  for (const auto &h : c->ih) tot += h.p * h.p;
   if (!c->cor64_valid) {
     // tensor-core mode keeps no FP64 matrix: form it from the standardised data
-    if (!c->cor64 && (s = dev_alloc(&c->cor64, c->p * c->p, "cor64")) != HPC_OK) return s;
-    const double denom = c->opts.ref_compat_sd ? (double)((float)c->n - 1.f) : (double)(c->n - 1);
-    if ((s = launch_gram_f64(c->Z, c->n, c->p, denom, c->cor64, c->stream)) != HPC_OK) return s;
+    if (!c->cor64 && (s = dev_alloc(&c->cor64, tot, "cor64")) != HPC_OK) return s;
+    if ((s = launch_gram_f64(c->Z, c->cor64, gram_args(c), c->tiles64, c->stream)) != HPC_OK) return s;
     c->cor64_valid = true;
+    if ((s = write_inst_table(c)) != HPC_OK) return s;
   }
-  HPC_CUDA(cudaMemcpyAsync(C, c->cor64, sizeof(double) * (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaMemcpyAsync(C, c->cor64, sizeof(double) * (size_t)tot, cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   return HPC_OK;
 }
@@ -656,7 +815,9 @@ hpc_status hpc_get_correlation_f32(hpc_ctx *c, float *C) {
     set_error(!C ? "null output pointer" : "no FP32 correlation (plain FP64 precision or none computed)");
     return !C ? HPC_ERR_INVALID_ARG : HPC_ERR_STATE;
   }
-  HPC_CUDA(cudaMemcpyAsync(C, c->cor32, sizeof(float) * (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
+  long long tot = 0;
+  for (const auto &h : c->ih) tot += h.p * h.p;
+  HPC_CUDA(cudaMemcpyAsync(C, c->cor32, sizeof(float) * (size_t)tot, cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   return HPC_OK;
 }
@@ -680,68 +841,15 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     bool changed = false;
     if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
   }
-  if ((s = enqueue_level(c, level, true)) != HPC_OK) return s;
-  c->last_run_graph = false;
-  if ((s = pull_counters(c)) != HPC_OK) return s;
+  if ((s = run_levels(c, level, level, false)) != HPC_OK) return s;
   if ((s = global_errors(c)) != HPC_OK) return s;
+  if (any_csr_overflow(c)) {
+    set_error("neighbour-list buffer too small");
+    return HPC_ERR_CAPACITY;
+  }
   c->next_level = level + 1;
   return collect_level(c, level, st);
 }
-
-namespace {
-bool capturable(cudaStream_t s) {
-  return s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
-}
-
-// Run levels first..last (already validated) with one host sync at the end; the
-// whole sequence 0..last is captured once into a CUDA graph and replayed.
-hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
-  hpc_status s;
-  if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
-    const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
-                       c->graph_cor64_valid == c->cor64_valid &&
-                       c->graph_colidx_cap == c->colidx_cap && c->graph_rec_cap == c->rec_cap;
-    if (!valid) {
-      if (c->graph) cudaGraphExecDestroy(c->graph);
-      c->graph = nullptr;
-      cudaGraph_t g = nullptr;
-      HPC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      const int64_t launches = c->timings.launches;
-      for (int l = first; l <= last; ++l) {
-        if ((s = enqueue_level(c, l, false)) != HPC_OK) {
-          cudaStreamEndCapture(c->stream, &g);
-          if (g) cudaGraphDestroy(g);
-          return s;
-        }
-      }
-      c->timings.launches = launches;  // counted when the graph runs
-      HPC_CUDA(cudaStreamEndCapture(c->stream, &g));
-      cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) {
-        c->graph = nullptr;
-        return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
-      }
-      c->graph_top = last;
-      c->graph_stream = c->stream;
-      c->graph_cor64_valid = c->cor64_valid;
-      c->graph_colidx_cap = c->colidx_cap;
-      c->graph_rec_cap = c->rec_cap;
-      // launches of one replay
-      c->graph_launches = 0;
-      for (int l = first; l <= last; ++l) c->graph_launches += l == 0 ? 4 : (c->opts.precision != HPC_PREC_FP64 ? 5 : 4);
-    }
-    HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
-    c->timings.launches += c->graph_launches;
-    c->last_run_graph = true;
-  } else {
-    for (int l = first; l <= last; ++l)
-      if ((s = enqueue_level(c, l, true)) != HPC_OK) return s;
-    c->last_run_graph = false;
-  }
-  return pull_counters(c);
-}
-}  // namespace
 
 hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run) {
   hpc_status s = check_ctx(c);
@@ -754,7 +862,7 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
   int ran = 0;
   auto emit = [&](int l) -> hpc_status {
     hpc_level_stats st{};
-    hpc_status e = collect_level(c, l, &st);
+    const hpc_status e = collect_level(c, l, &st);
     if (e != HPC_OK) return e;
     if (stats && ran < cap) stats[ran] = st;
     ++ran;
@@ -765,7 +873,7 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
     for (int l = c->next_level; l <= top; ++l) {
       if ((s = hpc_run_level(c, l, nullptr)) != HPC_OK) return s;
       if ((s = emit(l)) != HPC_OK) return s;
-      if (l >= 1 && c->ctr_host[l].work_total == 0) break;
+      if (l >= 1 && !any_work(c, l)) break;
     }
     if (levels_run) *levels_run = ran;
     return HPC_OK;
@@ -774,12 +882,11 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
   // exhausted" runs in chunks of four levels with a check in between.
   const bool known = c->opts.max_level >= 0;
   const int chunk = known ? top + 1 : 4;
-  const int64_t edges0 = c->edges;
   HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
   for (int attempt = 0; attempt < 2; ++attempt) {
     ran = 0;
-    c->edges = edges0;
-    bool sized = c->colidx_cap > 0 && c->rec_cap > 0;
+    for (auto &h : c->ih) h.edges = h.p * (h.p - 1) / 2;
+    const bool sized = c->colidx && c->recs;
     int first = 0;
     if (!sized) {
       // first run: level 0 alone sizes the neighbour-list and record buffers
@@ -794,12 +901,12 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
       const int last = std::min(top, first + chunk - 1);
       if ((s = run_levels(c, first, last, known)) != HPC_OK) return s;
       last_run = last;
-      if (c->gctr_host->err & kErrCsrOverflow) {
+      if (any_csr_overflow(c)) {
         overflow = true;
         break;
       }
       if ((s = global_errors(c)) != HPC_OK) return s;
-      done = last >= 1 && c->ctr_host[last].work_total == 0;
+      done = last >= 1 && !any_work(c, last);
       first = last + 1;
     }
     if (overflow) {
@@ -815,11 +922,9 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
     float tr = 0.f;
     HPC_CUDA(cudaEventElapsedTime(&tr, c->evr[0], c->evr[1]));
     c->timings.skeleton_ms = tr;
-    // a first run sized its buffers with level 0 alone: the events of that part
-    // are of the eager kind, the rest may be a graph replay
     for (int l = 0; l <= last_run; ++l) {
       if ((s = emit(l)) != HPC_OK) return s;
-      if (l >= 1 && c->ctr_host[l].work_total == 0) break;
+      if (l >= 1 && !any_work(c, l)) break;
     }
     if (levels_run) *levels_run = ran;
     return HPC_OK;
@@ -828,53 +933,85 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
   return HPC_ERR_CAPACITY;
 }
 
-hpc_status hpc_get_adjacency(hpc_ctx *c, uint8_t *out) {
+hpc_status hpc_batch_level_stats(hpc_ctx *c, int idx, hpc_level_stats *out, int cap, int *levels) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = check_index(c, idx)) != HPC_OK) return s;
+  int k = 0;
+  for (int l = 0; l < c->next_level && l <= HPC_MAX_LEVEL; ++l) {
+    if (out && k < cap) out[k] = level_stats_of(c, l, idx);
+    ++k;
+  }
+  if (levels) *levels = k;
+  return HPC_OK;
+}
+
+hpc_status hpc_batch_get_adjacency(hpc_ctx *c, int idx, uint8_t *out) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if ((s = check_index(c, idx)) != HPC_OK) return s;
   if (!out) {
     set_error("null output pointer");
     return HPC_ERR_INVALID_ARG;
   }
+  const InstHost &h = c->ih[idx];
   if (c->next_level == 0) {
-    for (int64_t i = 0; i < c->p; ++i)
-      for (int64_t j = 0; j < c->p; ++j) out[i * c->p + j] = (uint8_t)(i != j);
+    for (int64_t i = 0; i < h.p; ++i)
+      for (int64_t j = 0; j < h.p; ++j) out[i * h.p + j] = (uint8_t)(i != j);
     return HPC_OK;
   }
-  if (!c->adj_bytes && (s = dev_alloc(&c->adj_bytes, c->p * c->p, "adjacency bytes")) != HPC_OK) return s;
-  if ((s = launch_expand_adjacency(c->adj, c->p, c->W, c->adj_bytes, c->stream)) != HPC_OK) return s;
+  if (!c->adj_bytes) {
+    int64_t pm = 0;
+    for (const auto &x : c->ih) pm = std::max(pm, x.p);
+    if ((s = dev_alloc(&c->adj_bytes, pm * pm, "adjacency bytes")) != HPC_OK) return s;
+  }
+  if ((s = launch_expand_adjacency(c->adj + h.adj_off, h.p, h.W, c->adj_bytes, c->stream)) != HPC_OK) return s;
   c->timings.launches += 1;
-  HPC_CUDA(cudaMemcpyAsync(out, c->adj_bytes, (size_t)(c->p * c->p), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaMemcpyAsync(out, c->adj_bytes, (size_t)(h.p * h.p), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
   return HPC_OK;
 }
 
-hpc_status hpc_edge_count(hpc_ctx *c, int64_t *edges) {
+hpc_status hpc_get_adjacency(hpc_ctx *c, uint8_t *out) { return hpc_batch_get_adjacency(c, 0, out); }
+
+hpc_status hpc_batch_edge_count(hpc_ctx *c, int idx, int64_t *edges) {
   if (!c || !edges) {
     set_error("null argument");
     return HPC_ERR_INVALID_ARG;
   }
-  *edges = c->edges;
+  hpc_status s = check_index(c, idx);
+  if (s != HPC_OK) return s;
+  *edges = c->ih[idx].edges;
   return HPC_OK;
 }
 
-hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t cap, int64_t *count) {
+hpc_status hpc_edge_count(hpc_ctx *c, int64_t *edges) { return hpc_batch_edge_count(c, 0, edges); }
+
+hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *out, int64_t cap, int64_t *count) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = check_index(c, idx)) != HPC_OK) return s;
   if (!count) {
     set_error("null count pointer");
     return HPC_ERR_INVALID_ARG;
   }
-  unsigned long long n = 0;
-  HPC_CUDA(cudaMemcpyAsync(&n, &c->gctr->rec_count, sizeof(n), cudaMemcpyDeviceToHost, c->stream));
+  DevGlobal g{};
+  HPC_CUDA(cudaMemcpyAsync(&g, c->gctr + idx, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
-  n = std::min<unsigned long long>(n, (unsigned long long)std::max<int64_t>(c->rec_cap, 0));
-  *count = (int64_t)n;
+  const InstHost &h = c->ih[idx];
+  const long long n = c->recs ? std::min<long long>((long long)g.rec_count, h.rec_cap) : 0;
+  *count = n;
   if (out && cap > 0 && n > 0) {
-    const int64_t k = std::min<int64_t>(cap, (int64_t)n);
-    HPC_CUDA(cudaMemcpyAsync(out, c->recs, sizeof(hpc_sepset_record) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
+    const int64_t k = std::min<int64_t>(cap, n);
+    HPC_CUDA(cudaMemcpyAsync(out, c->recs + h.rec_off, sizeof(hpc_sepset_record) * (size_t)k, cudaMemcpyDeviceToHost,
+                             c->stream));
     HPC_CUDA(cudaStreamSynchronize(c->stream));
   }
   return HPC_OK;
+}
+
+hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t cap, int64_t *count) {
+  return hpc_batch_get_sepset_records(c, 0, out, cap, count);
 }
 
 hpc_status hpc_get_sepsets(hpc_ctx *c, int32_t *out, int max_cond) {
@@ -884,7 +1021,7 @@ hpc_status hpc_get_sepsets(hpc_ctx *c, int32_t *out, int max_cond) {
     set_error("null output or max_cond < 1");
     return HPC_ERR_INVALID_ARG;
   }
-  const int64_t p = c->p;
+  const int64_t p = c->ih[0].p;
   std::fill(out, out + p * p * max_cond, -1);
   if (c->next_level == 0) return HPC_OK;
   std::vector<uint8_t> adj((size_t)(p * p));
@@ -918,3 +1055,150 @@ double hpc_pval_ln(const double *M, int k, int n) {
 double hpc_z_crit(double alpha) { return z_crit_of(alpha); }
 
 }  // extern "C"
+
+namespace hpc {
+namespace {
+
+hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, const double *alpha,
+                  const hpc_opts *opts) {
+  if (!out) {
+    set_error("null output pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  hpc_opts o;
+  if (opts) o = *opts; else hpc_opts_default(&o);
+  if (o.precision < HPC_PREC_FP64 || o.precision > HPC_PREC_MIXED_TC) {
+    set_error("unknown precision %d", o.precision);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (o.max_level > HPC_MAX_LEVEL) {
+    set_error("max_level %d above HPC_MAX_LEVEL %d", o.max_level, HPC_MAX_LEVEL);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (!(o.retest_margin >= 0.0)) o.retest_margin = 1e-3;
+  for (int b = 0; b < count; ++b) {
+    if (p[b] < 2 || p[b] > 46340) {
+      set_error("instance %d: p = %lld out of range [2, 46340]", b, (long long)p[b]);
+      return HPC_ERR_INVALID_ARG;
+    }
+    if (n[b] < 4 || n[b] > 0x7fffffff) {
+      set_error("instance %d: n_obs = %lld out of range [4, 2^31)", b, (long long)n[b]);
+      return HPC_ERR_INVALID_ARG;
+    }
+    const double a = alpha ? alpha[b] : o.alpha;
+    if (!(a > 0.0 && a <= 1.0)) {
+      set_error("instance %d: alpha = %g outside (0, 1]", b, a);
+      return HPC_ERR_INVALID_ARG;
+    }
+  }
+  int ndev = 0;
+  const cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device available: %s", cudaGetErrorString(e));
+    return HPC_ERR_NO_DEVICE;
+  }
+  if (o.device < 0 || o.device >= ndev) {
+    set_error("device %d not present (%d devices)", o.device, ndev);
+    return HPC_ERR_INVALID_ARG;
+  }
+  hpc_ctx *c = new hpc_ctx();
+  c->count = count;
+  c->opts = o;
+  c->device = o.device;
+  c->ih.resize((size_t)count);
+  long long cor = 0, z = 0, adj = 0, rows = 0, tc = 0, words = 0, tiles = 0, nrows = 0;
+  std::vector<long long> pre((size_t)(3 * (count + 1)), 0);
+  for (int b = 0; b < count; ++b) {
+    InstHost &h = c->ih[b];
+    h.p = p[b];
+    h.n = n[b];
+    h.alpha = alpha ? alpha[b] : o.alpha;
+    h.W = (int)((h.p + 31) / 32);
+    h.zc = z_crit_of(h.alpha);
+    h.r_crit = r_crit_of(h.alpha, (int)h.n);
+    h.cor_off = cor;
+    cor += h.p * h.p;
+    h.z_off = z;
+    z += h.n * h.p;
+    h.adj_off = adj;
+    adj += h.p * h.W;
+    h.row_off = rows;
+    rows += h.p + 1;
+    h.tc_off = tc;
+    tc += tc_p_pad(h.p) * tc_k(h.n);
+    h.edges = h.p * (h.p - 1) / 2;
+    pre[b] = words;
+    words += h.p * h.W;
+    pre[(count + 1) + b] = tiles;
+    tiles += (long long)h.W * (h.W + 1) / 2;
+    pre[2 * (count + 1) + b] = nrows;
+    nrows += h.p;
+  }
+  pre[count] = words;
+  pre[(count + 1) + count] = tiles;
+  pre[2 * (count + 1) + count] = nrows;
+  c->total_words = words;
+  c->total_tiles = tiles;
+  c->total_rows = nrows;
+  c->p = c->ih[0].p;
+  c->n = c->ih[0].n;
+  hpc_status s = HPC_OK;
+  auto fail = [&](hpc_status st) {
+    hpc_ctx_destroy(c);
+    return st;
+  };
+  if (cudaSetDevice(c->device) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaSetDevice(%d) failed", c->device);
+    delete c;
+    return HPC_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  bool ev_ok = true;
+  for (auto &ev : c->evc) ev_ok = ev_ok && cudaEventCreate(&ev) == cudaSuccess;
+  for (auto &ev : c->evr) ev_ok = ev_ok && cudaEventCreate(&ev) == cudaSuccess;
+  for (auto &lv : c->evl)
+    for (auto &ev : lv) ev_ok = ev_ok && cudaEventCreate(&ev) == cudaSuccess;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess || !ev_ok) {
+    cudaGetLastError();
+    set_error("stream/event creation failed");
+    return fail(HPC_ERR_CUDA);
+  }
+  c->stream = c->own_stream;
+  for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
+  if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, cor, "cor64")) != HPC_OK) return fail(s);
+  if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, cor, "cor32")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->adj, adj, "adjacency")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->deg, rows, "degrees")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->rowptr, rows, "row offsets")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->row_work, rows, "row work")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->ctr, (int64_t)count * kLevels, "level counters")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->gctr, count, "counters")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->lc, kLevels, "launch counters")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->inst, count, "instance table")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->prefixes, (int64_t)pre.size(), "prefixes")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->work_prefix, (int64_t)kLevels * (count + 1), "work prefixes")) != HPC_OK) return fail(s);
+  if (cudaMallocHost((void **)&c->ctr_host, sizeof(DevCounters) * (size_t)count * kLevels) != cudaSuccess ||
+      cudaMallocHost((void **)&c->gctr_host, sizeof(DevGlobal) * (size_t)count) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("pinned counter allocation failed");
+    return fail(HPC_ERR_OOM);
+  }
+  if (cudaMemcpyAsync(c->prefixes, pre.data(), sizeof(long long) * pre.size(), cudaMemcpyHostToDevice, c->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)count * kLevels, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal) * (size_t)count, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->lc, 0, sizeof(LaunchCounters) * kLevels, c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("context initialisation failed");
+    return fail(HPC_ERR_CUDA);
+  }
+  if ((s = write_inst_table(c)) != HPC_OK) return fail(s);
+  *out = c;
+  return HPC_OK;
+}
+
+}  // namespace
+}  // namespace hpc

@@ -151,6 +151,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+__host__ __device__ __forceinline__ int64_t tc_p_pad_dev(int64_t p) { return (p + TM - 1) / TM * TM; }
+
 struct alignas(1024) TcSmem {
   uint8_t stage[kStages][kStageBytes];
   uint64_t full[kStages];
@@ -169,14 +171,21 @@ __device__ __forceinline__ void fail(TcSmem &sm, int *err) {
 }
 
 __global__ void __launch_bounds__(kThreadsTc, 1)
-    gram_tc_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapQ, int64_t p,
-                   int nb, int kblocks, float *__restrict__ C, int *__restrict__ err) {
+    gram_tc_kernel(float *__restrict__ Call, TcArgs ta) {
   extern __shared__ uint8_t smem_raw[];
   TcSmem &sm = *reinterpret_cast<TcSmem *>((((uintptr_t)smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // tile (bi, bj), bi <= bj, from the linear block index over the upper triangle
-  int64_t t = blockIdx.x;
+  // instance, then tile (bi, bj), bi <= bj, over the upper triangle of its tiles
+  const long long tt = blockIdx.x;
+  const int inst = find_inst(ta.tile_prefix, ta.count, tt);
+  long long t = tt - ta.tile_prefix[inst];
+  const int64_t p = ta.p[inst];
+  const int nb = (int)(tc_p_pad_dev(p) / TM);
+  const int kblocks = (int)(kSlices * ((ta.n[inst] + TK - 1) / TK));
+  const CUtensorMap *mapP = ta.maps + 2 * inst, *mapQ = ta.maps + 2 * inst + 1;
+  float *__restrict__ C = Call + ta.c_off[inst];
+  int *err = ta.err;
   int bi = 0;
   while (t >= nb - bi) {
     t -= nb - bi;
@@ -217,8 +226,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
       if (aborted(sm)) break;
       mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
-      tma_load_2d(sm.stage[s], &mapP, kb * TK, bi * TM, &sm.full[s]);
-      tma_load_2d(sm.stage[s] + kStageBytesA, &mapQ, kb * TK, bj * TN, &sm.full[s]);
+      tma_load_2d(sm.stage[s], mapP, kb * TK, bi * TM, &sm.full[s]);
+      tma_load_2d(sm.stage[s] + kStageBytesA, mapQ, kb * TK, bj * TN, &sm.full[s]);
       ++issued;
     }
   } else if (warp == 1 && lane == 0) {
@@ -310,81 +319,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   }
 }
 
-// standardisation into the split operands (and the FP64 copy used for exact re-tests)
-template <typename TIn>
-__global__ void __launch_bounds__(256) standardise_split_kernel(const TIn *__restrict__ X, int64_t n, int64_t p,
-                                                               int64_t n_pad, int ref_compat,
-                                                               double *__restrict__ Z64,
-                                                               __nv_bfloat16 *__restrict__ P,
-                                                               __nv_bfloat16 *__restrict__ Q) {
-  const int64_t v = blockIdx.x;
-  if (v >= p) return;
-  const TIn *x = X + v * n;
-  __shared__ double red[8];
-  __shared__ long long redc[8];
-  __shared__ double mean_s, sd_s;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double s = 0.0;
-  long long c = 0;
-  for (int64_t k = threadIdx.x; k < n; k += 256) {
-    double a = (double)x[k];
-    if (!isnan(a)) { s += a; ++c; }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    s += __shfl_xor_sync(0xffffffffu, s, o);
-    c += __shfl_xor_sync(0xffffffffu, c, o);
-  }
-  if (lane == 0) { red[wid] = s; redc[wid] = c; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    long long tc = 0;
-    for (int w = 0; w < 8; ++w) { t += red[w]; tc += redc[w]; }
-    mean_s = t / (double)tc;
-  }
-  __syncthreads();
-  const double mean = mean_s;
-  double ss = 0.0;
-  for (int64_t k = threadIdx.x; k < n; k += 256) {
-    double a = (double)x[k];
-    if (!isnan(a)) { double d = a - mean; ss += d * d; }
-  }
-  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-  __syncthreads();
-  if (lane == 0) red[wid] = ss;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < 8; ++w) t += red[w];
-    sd_s = ref_compat ? (double)sqrtf((float)(t / (double)((float)n - 1.f))) : sqrt(t / (double)(n - 1));
-  }
-  __syncthreads();
-  const double sd = sd_s;
-  const double denom = ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
-  const double scale = 1.0 / sqrt(denom);
-  const int64_t K = kSlices * n_pad;
-  __nv_bfloat16 *pr = P + v * K, *qr = Q + v * K;
-  for (int64_t k = threadIdx.x; k < n_pad; k += 256) {
-    double z = 0.0;
-    if (k < n) {
-      double a = (double)x[k];
-      z = isnan(a) ? 0.0 : (a - mean) / sd;
-      Z64[v * n + k] = z;
-    }
-    const double zs = z * scale;
-    const __nv_bfloat16 hi = __double2bfloat16(zs);
-    const __nv_bfloat16 lo = __double2bfloat16(zs - (double)__bfloat162float(hi));
-    pr[k] = hi;
-    pr[n_pad + k] = hi;
-    pr[2 * n_pad + k] = lo;
-    pr[3 * n_pad + k] = lo;
-    qr[k] = hi;
-    qr[n_pad + k] = lo;
-    qr[2 * n_pad + k] = hi;
-    qr[3 * n_pad + k] = lo;
-  }
-}
-
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -429,34 +363,25 @@ int64_t tc_n_pad(int64_t n) { return (n + TK - 1) / TK * TK; }
 int64_t tc_p_pad(int64_t p) { return (p + TM - 1) / TM * TM; }
 int64_t tc_k(int64_t n) { return kSlices * tc_n_pad(n); }
 
-hpc_status launch_standardise_split_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z64,
-                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s) {
-  standardise_split_kernel<double><<<(unsigned)p, 256, 0, s>>>(X, n, p, tc_n_pad(n), ref_compat, Z64, P, Q);
-  HPC_LAUNCH_CHECK("standardise_split_kernel<double>");
-  return HPC_OK;
+long long gram_tc_tiles(int64_t p) {
+  const long long nb = tc_p_pad(p) / TM;
+  return nb * (nb + 1) / 2;
 }
 
-hpc_status launch_standardise_split_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z64,
-                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s) {
-  standardise_split_kernel<float><<<(unsigned)p, 256, 0, s>>>(X, n, p, tc_n_pad(n), ref_compat, Z64, P, Q);
-  HPC_LAUNCH_CHECK("standardise_split_kernel<float>");
-  return HPC_OK;
-}
-
-// C (p x p FP32, row-major) = P Q^T over upper-triangle tiles, mirrored.
-// P and Q: tc_p_pad(p) rows of tc_k(n) bf16, zero padded.
-hpc_status launch_gram_tc(const __nv_bfloat16 *P, const __nv_bfloat16 *Q, int64_t n, int64_t p, float *C, int *err,
-                          cudaStream_t s) {
-  const int64_t rows = tc_p_pad(p), K = kSlices * tc_n_pad(n);
-  CUtensorMap mp, mq;
+// Tensor maps of one instance's operands P and Q (tc_p_pad(p) rows of tc_k(n) bf16).
+hpc_status tc_make_maps(CUtensorMap *mp, CUtensorMap *mq, const __nv_bfloat16 *P, const __nv_bfloat16 *Q,
+                        int64_t p, int64_t n) {
   hpc_status st;
-  if ((st = make_map(&mp, P, rows, K, TM)) != HPC_OK) return st;
-  if ((st = make_map(&mq, Q, rows, K, TN)) != HPC_OK) return st;
-  const int nb = (int)(rows / TM);
-  const int64_t tiles = (int64_t)nb * (nb + 1) / 2;
+  if ((st = make_map(mp, P, tc_p_pad(p), tc_k(n), TM)) != HPC_OK) return st;
+  return make_map(mq, Q, tc_p_pad(p), tc_k(n), TN);
+}
+
+// C (p x p FP32 per instance, row-major) = P Q^T over upper-triangle tiles, mirrored;
+// blocks flattened over all instances' tiles.
+hpc_status launch_gram_tc(float *C, const TcArgs &a, long long total_tiles, cudaStream_t s) {
   const int smem = (int)sizeof(TcSmem) + 1024;
   HPC_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  gram_tc_kernel<<<(unsigned)tiles, kThreadsTc, smem, s>>>(mp, mq, p, nb, (int)(K / TK), C, err);
+  gram_tc_kernel<<<(unsigned)total_tiles, kThreadsTc, smem, s>>>(C, a);
   HPC_LAUNCH_CHECK("gram_tc_kernel");
   return HPC_OK;
 }

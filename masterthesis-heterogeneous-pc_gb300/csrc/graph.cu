@@ -1,18 +1,20 @@
-// Level 0 and the per-level adjacency snapshot.
+// Level 0 and the per-level adjacency snapshot, over all instances of a context.
 //
-// The live adjacency is a symmetric bitmask, p rows of W = ceil(p/32) words
-// (the reference keeps an int32 p x p matrix, src/util/state.cu:21-29).
+// The live adjacency of an instance is a symmetric bitmask, p rows of W = ceil(p/32)
+// words (the reference keeps an int32 p x p matrix, src/util/state.cu:21-29).
 //
-// level0_lower + mirror_bits replace testRowL0 (src/executor/testing/gpuRowTests.cu:4-27)
-// / testRowL0Triangluar (src/executor/testing/cpuRowTests.cpp:5-21): every pair
-// i > j is tested once on cor[i][j] (the lower-triangle entry the reference reads),
-// the kept bits are written for the lower triangle and then mirrored by 32 x 32
+// level0 + mirror replace testRowL0 (src/executor/testing/gpuRowTests.cu:4-27) /
+// testRowL0Triangluar (src/executor/testing/cpuRowTests.cpp:5-21): every pair i > j
+// is tested once on cor[i][j] (the lower-triangle entry the reference reads), the
+// kept bits are written for the lower triangle and then mirrored by 32 x 32
 // bit-tile transposes.
 //
-// degrees + scan_rows + fill_csr replace compactCUTiled (src/independence/compact.cu:4-89):
-// per-row popcounts, one block-wide scan over rows for the CSR offsets and for the
-// number of CI tests each row contributes at the level (d_i * C(d_i - 1, l)), and a
-// warp-per-row ballot/scan that writes the ascending neighbour ids.
+// degrees + scan + fill_csr replace compactCUTiled (src/independence/compact.cu:4-89):
+// per-row popcounts; one block per instance scans its rows for the CSR offsets and
+// for the number of CI tests each row contributes at the level (d_i * C(d_i - 1, l));
+// the last scan block to finish forms the prefix of the instances' test counts that
+// the CI-test kernel flattens over; a warp per row then writes the ascending
+// neighbour ids.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,146 +25,144 @@
 namespace hpc {
 namespace {
 
-// one thread per (row, word): 32 decisions on cor64[i][32w .. 32w+31], j < i only
-__global__ void level0_lower_kernel(LevelArgs a, double r_lo, double r_hi) {
-  const int64_t total = a.p * (int64_t)a.W;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / a.W;
-    const int w = (int)(t % a.W);
+// one thread per (instance, row, word): 32 decisions for j < i
+__global__ void level0_kernel(Launch L, long long total) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int b = find_inst(L.word_prefix, L.count, t);
+    const Inst &I = L.inst[b];
+    const long long lt = t - L.word_prefix[b];
+    const int64_t i = lt / I.W;
+    const int w = (int)(lt % I.W);
     const int64_t j0 = (int64_t)w * 32;
     uint32_t bits = 0;
     if (j0 < i) {
-      const double *row = a.cor64 + i * a.p;
       const int jend = (i - j0) < 32 ? (int)(i - j0) : 32;
-      for (int b = 0; b < jend; ++b) {
-        const double v = row[j0 + b];
-        const double av = fabs(v);
-        bool remove;
-        if (isnan(v) || av < r_lo)
-          remove = true;          // p certainly >= alpha (NaN r is treated as 0)
-        else if (av > r_hi)
-          remove = false;         // p certainly < alpha
-        else
-          remove = calc_pvalue64(v, a.n_obs) >= a.alpha;  // exact reference formula
-        if (!remove) bits |= 1u << b;
-      }
-    }
-    a.adj[t] = bits;
-  }
-}
-
-// Level 0 on the FP32 correlation of the tensor-core mode (no FP64 matrix): pairs
-// clear of the band [lo, hi] around r_crit are decided here; pairs inside it, and
-// non-finite ones, are queued for the FP64 re-test kernel, which sets the kept bits
-// (inline serial dot product only when the queue is full).
-__global__ void level0_lower_f32_kernel(LevelArgs a, float lo, float hi) {
-  const int64_t total = a.p * (int64_t)a.W;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / a.W;
-    const int w = (int)(t % a.W);
-    const int64_t j0 = (int64_t)w * 32;
-    uint32_t bits = 0;
-    if (j0 < i) {
-      const float *row = a.cor32 + i * a.p;
-      const int jend = (i - j0) < 32 ? (int)(i - j0) : 32;
-      for (int b = 0; b < jend; ++b) {
-        const float av = fabsf(row[j0 + b]);
-        if (av < lo) continue;             // removed
-        if (av > hi) {                     // kept
-          bits |= 1u << b;
-          continue;
+      if (I.cor64) {
+        // FP64 entries: the exact formula only inside [r_lo, r_hi]
+        const double *row = I.cor64 + i * I.p;
+        for (int q = 0; q < jend; ++q) {
+          const double v = row[j0 + q];
+          const double av = fabs(v);
+          bool remove;
+          if (isnan(v) || av < I.r_lo)
+            remove = true;  // p certainly >= alpha (NaN r is treated as 0)
+          else if (av > I.r_hi)
+            remove = false;
+          else
+            remove = calc_pvalue64(v, I.n_obs) >= I.alpha;
+          if (!remove) bits |= 1u << q;
         }
-        const int64_t j = j0 + b;          // in the band, or NaN
-        const unsigned long long slot = atomicAdd(&a.ctr->rq_count, 1ull);
-        if ((long long)slot < a.rq_cap) {
-          RetestItem *it = a.rq + slot;
-          it->i = (int32_t)i;
-          it->j = (int32_t)j;
-          it->level = 0;
-          it->pad = 0;
-        } else {
-          const double *x = a.Z + i * a.n_z, *y = a.Z + j * a.n_z;
-          double s = 0.0;
-          for (int64_t k = 0; k < a.n_z; ++k) s = fma(x[k], y[k], s);
-          if (!(calc_pvalue64(s / a.denom, a.n_obs) >= a.alpha)) bits |= 1u << b;
+      } else {
+        // FP32 tensor-core entries: pairs inside the band (or NaN) are queued for
+        // the FP64 re-test kernel, which sets their kept bits
+        const float *row = I.cor32 + i * I.p;
+        for (int q = 0; q < jend; ++q) {
+          const float av = fabsf(row[j0 + q]);
+          if (av < I.lo32) continue;
+          if (av > I.hi32) {
+            bits |= 1u << q;
+            continue;
+          }
+          const int64_t j = j0 + q;
+          const unsigned long long slot = atomicAdd(&L.lc->rq_count, 1ull);
+          if ((long long)slot < L.rq_cap) {
+            RetestItem *it = L.rq + slot;
+            it->i = (int32_t)i;
+            it->j = (int32_t)j;
+            it->level = 0;
+            it->inst = b;
+          } else {  // queue full: serial FP64 dot product here
+            const double *x = I.Z + i * I.n_z, *y = I.Z + j * I.n_z;
+            double s = 0.0;
+            for (int64_t k = 0; k < I.n_z; ++k) s = fma(x[k], y[k], s);
+            if (!(calc_pvalue64(s / I.denom, I.n_obs) >= I.alpha)) bits |= 1u << q;
+          }
         }
       }
     }
-    a.adj[t] = bits;
+    I.adj[lt] = bits;
   }
 }
 
-// Mirror the lower triangle into the upper: warp per 32x32 bit tile (I, w) with w <= I.
-__global__ void mirror_bits_kernel(uint32_t *adj, int64_t p, int W) {
+// Mirror the lower triangle into the upper: warp per 32x32 bit tile (I, w), w <= I.
+__global__ void mirror_bits_kernel(Launch L, long long total) {
   const int lane = threadIdx.x & 31;
-  const int64_t nt = (int64_t)W * (W + 1) / 2;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = warp; t < nt; t += nwarps) {
-    // t -> (I, w), w <= I, row-major over the lower triangle of tiles
-    int64_t I = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (I * (I + 1) / 2 > t) --I;
-    while ((I + 1) * (I + 2) / 2 <= t) ++I;
-    const int64_t w = t - I * (I + 1) / 2;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long t = warp; t < total; t += nwarps) {
+    const int b = find_inst(L.tile_prefix, L.count, t);
+    const Inst &In = L.inst[b];
+    const long long lt = t - L.tile_prefix[b];
+    // lt -> (I, w), w <= I, row-major over the lower triangle of tiles
+    int64_t I = (int64_t)((sqrt(8.0 * (double)lt + 1.0) - 1.0) * 0.5);
+    while (I * (I + 1) / 2 > lt) --I;
+    while ((I + 1) * (I + 2) / 2 <= lt) ++I;
+    const int64_t w = lt - I * (I + 1) / 2;
     const int64_t row = I * 32 + lane;
-    uint32_t word = row < p ? adj[row * W + w] : 0u;
-    // transposed[c] (held by lane c) = bits of column 32w + c over rows 32I .. 32I+31
+    const int W = In.W;
+    uint32_t word = row < In.p ? In.adj[row * W + w] : 0u;
+    // transposed (lane c) = bits of column 32w + c over rows 32I .. 32I+31
     uint32_t tr = 0;
     for (int c = 0; c < 32; ++c) {
-      uint32_t b = __ballot_sync(0xffffffffu, (word >> c) & 1u);
-      if (lane == c) tr = b;
+      uint32_t bb = __ballot_sync(0xffffffffu, (word >> c) & 1u);
+      if (lane == c) tr = bb;
     }
     const int64_t trow = w * 32 + lane;
     if (I == w) {
-      // diagonal tile: symmetric union within the same words
-      if (row < p) adj[row * W + w] = word | tr;
-    } else if (trow < p) {
-      adj[trow * W + I] = tr;
+      if (row < In.p) In.adj[row * W + w] = word | tr;  // diagonal tile: symmetric union
+    } else if (trow < In.p) {
+      In.adj[trow * W + I] = tr;
     }
   }
 }
 
-__global__ void degrees_kernel(const uint32_t *__restrict__ adj, int64_t p, int W, int *__restrict__ deg) {
+__global__ void degrees_kernel(Launch L, long long total) {
   const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < p; i += nwarps) {
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long t = warp; t < total; t += nwarps) {
+    const int b = find_inst(L.row_prefix, L.count, t);
+    const Inst &I = L.inst[b];
+    const int64_t i = t - L.row_prefix[b];
     int c = 0;
-    for (int w = lane; w < W; w += 32) c += __popc(adj[i * W + w]);
+    for (int w = lane; w < I.W; w += 32) c += __popc(I.adj[i * I.W + w]);
     c = __reduce_add_sync(0xffffffffu, c);
-    if (lane == 0) deg[i] = c;
+    if (lane == 0) I.deg[i] = c;
   }
 }
 
-constexpr int kScanThreads = 1024;
+constexpr int kScanThreads = 512;
 
-// Single block: exclusive prefixes of degrees (CSR offsets) and of per-row test
-// counts, plus the level summary in ctr.
-__global__ void __launch_bounds__(kScanThreads) scan_rows_kernel(int64_t p, int level, const int *__restrict__ deg,
-                                                                 int *__restrict__ rowptr,
-                                                                 unsigned long long *__restrict__ row_work,
-                                                                 DevCounters *ctr, DevGlobal *g) {
+// One block per instance: exclusive prefixes of degrees (CSR offsets) and of per-row
+// test counts, the instance's level summary; the last block to finish forms the
+// prefix of test counts over instances (work_prefix) for the CI-test kernel.
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(Launch L) {
   __shared__ unsigned long long s_deg[kScanThreads];
   __shared__ unsigned long long s_work[kScanThreads];
   __shared__ int s_max[kScanThreads / 32];
   __shared__ int s_rows[kScanThreads / 32];
   __shared__ int s_over;
+  __shared__ bool s_last;
+  const int b = blockIdx.x;
+  const Inst &I = L.inst[b];
+  const int level = L.level;
   const int tid = threadIdx.x;
+  const int64_t p = I.p;
   const int64_t per = (p + kScanThreads - 1) / kScanThreads;
   const int64_t lo = tid * per, hi = (lo + per) < p ? (lo + per) : p;
   if (tid == 0) s_over = 0;
+  __syncthreads();
   unsigned long long sd = 0, sw = 0;
   int mx = 0, rows = 0;
   bool over = false;
   for (int64_t i = lo; i < hi; ++i) {
-    int d = deg[i];
+    const int d = I.deg[i];
     sd += (unsigned long long)d;
     mx = max(mx, d);
     if (level >= 1 && d - 1 >= level) {
-      unsigned long long c = binom_sat(d - 1, level);
-      unsigned long long w = (unsigned long long)d * c;
+      const unsigned long long c = binom_sat(d - 1, level);
+      const unsigned long long w = (unsigned long long)d * c;
       if (c == 0xFFFFFFFFFFFFFFFFull || w / (unsigned long long)d != c || sw + w < sw) over = true;
       sw += w;
       ++rows;
@@ -174,79 +174,98 @@ __global__ void __launch_bounds__(kScanThreads) scan_rows_kernel(int64_t p, int 
     mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     rows += __shfl_xor_sync(0xffffffffu, rows, o);
   }
-  if ((tid & 31) == 0) { s_max[tid >> 5] = mx; s_rows[tid >> 5] = rows; }
+  if ((tid & 31) == 0) {
+    s_max[tid >> 5] = mx;
+    s_rows[tid >> 5] = rows;
+  }
   if (over) atomicOr(&s_over, 1);
   __syncthreads();
-  // Hillis-Steele inclusive scan over the 1024 partial sums
-  for (int off = 1; off < kScanThreads; off <<= 1) {
-    unsigned long long a = tid >= off ? s_deg[tid - off] : 0ull;
-    unsigned long long b = tid >= off ? s_work[tid - off] : 0ull;
+  for (int off = 1; off < kScanThreads; off <<= 1) {  // Hillis-Steele inclusive scan
+    const unsigned long long x = tid >= off ? s_deg[tid - off] : 0ull;
+    const unsigned long long y = tid >= off ? s_work[tid - off] : 0ull;
     __syncthreads();
-    s_deg[tid] += a;
-    s_work[tid] += b;
+    s_deg[tid] += x;
+    s_work[tid] += y;
     __syncthreads();
   }
   unsigned long long bd = tid > 0 ? s_deg[tid - 1] : 0ull;
   unsigned long long bw = tid > 0 ? s_work[tid - 1] : 0ull;
   for (int64_t i = lo; i < hi; ++i) {
-    rowptr[i] = (int)bd;
-    row_work[i] = bw;
-    int d = deg[i];
+    I.rowptr[i] = (int)bd;
+    I.row_work[i] = bw;
+    const int d = I.deg[i];
     bd += (unsigned long long)d;
     if (level >= 1 && d - 1 >= level) bw += (unsigned long long)d * binom_sat(d - 1, level);
   }
-  if (tid == kScanThreads - 1) {
-    rowptr[p] = (int)s_deg[kScanThreads - 1];
-    row_work[p] = s_work[kScanThreads - 1];
-  }
   if (tid == 0) {
-    ctr->edges2 = s_deg[kScanThreads - 1];
-    ctr->work_total = s_work[kScanThreads - 1];
+    DevCounters &C = I.ctr[level];
+    const unsigned long long e2 = s_deg[kScanThreads - 1];
+    unsigned long long work = s_work[kScanThreads - 1];
+    I.rowptr[p] = (int)e2;
+    I.row_work[p] = work;
     int m = 0, r = 0;
-    for (int w = 0; w < kScanThreads / 32; ++w) { m = max(m, s_max[w]); r += s_rows[w]; }
-    ctr->max_deg = m;
-    ctr->rows = r;
-    if (s_over) {
-      atomicOr(&g->err, kErrWorkOverflow);
-      ctr->work_total = 0;  // nothing of this level runs
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+      m = max(m, s_max[w]);
+      r += s_rows[w];
     }
-    ctr->tile_next = 0;
-    ctr->tests = 0;
-    ctr->retests = 0;
-    ctr->deleted = 0;
-    ctr->band_violations = 0;
-    ctr->rec_begin = g->rec_count;
+    if (s_over) {
+      atomicOr(&I.g->err, kErrWorkOverflow);
+      work = 0;  // nothing of this level runs for the instance
+    }
+    if (level >= 1 && (long long)e2 > I.colidx_cap) {
+      atomicOr(&I.g->err, kErrCsrOverflow);  // neighbour lists do not fit: resized by the host
+      work = 0;
+    }
+    C.edges2 = e2;
+    C.work_total = work;
+    C.max_deg = m;
+    C.rows = r;
+    C.tests = 0;
+    C.retests = 0;
+    C.deleted = 0;
+    C.band_violations = 0;
+    C.rec_begin = I.g->rec_count;
+    __threadfence();
+    const unsigned int done = atomicAdd(&L.lc->scan_done, 1u);
+    s_last = done == (unsigned int)L.count - 1;
+  }
+  __syncthreads();
+  if (s_last && tid == 0) {
+    // last block: the prefix of the instances' test counts (the other blocks'
+    // counters are visible after their fence and this block's atomic)
+    __threadfence();
+    unsigned long long acc = 0;
+    for (int q = 0; q < L.count; ++q) {
+      L.work_prefix[q] = acc;
+      acc += *(volatile unsigned long long *)&L.inst[q].ctr[level].work_total;
+    }
+    L.work_prefix[L.count] = acc;
   }
 }
 
-__global__ void fill_csr_kernel(const uint32_t *__restrict__ adj, int64_t p, int W, const int *__restrict__ rowptr,
-                                int *__restrict__ colidx, long long cap, DevCounters *ctr, DevGlobal *g) {
+__global__ void fill_csr_kernel(Launch L, long long total) {
   const int lane = threadIdx.x & 31;
-  if ((long long)ctr->edges2 > cap) {
-    // the neighbour-list buffer is too small for this level: flag it, test nothing
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      atomicOr(&g->err, kErrCsrOverflow);
-      ctr->work_total = 0;
-    }
-    return;
-  }
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < p; i += nwarps) {
-    int base = rowptr[i];
-    for (int w0 = 0; w0 < W; w0 += 32) {
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long t = warp; t < total; t += nwarps) {
+    const int b = find_inst(L.row_prefix, L.count, t);
+    const Inst &I = L.inst[b];
+    if ((long long)I.ctr[L.level].edges2 > I.colidx_cap) continue;  // flagged by the scan
+    const int64_t i = t - L.row_prefix[b];
+    int base = I.rowptr[i];
+    for (int w0 = 0; w0 < I.W; w0 += 32) {
       const int w = w0 + lane;
-      uint32_t word = w < W ? adj[i * W + w] : 0u;
-      int c = __popc(word);
+      uint32_t word = w < I.W ? I.adj[i * I.W + w] : 0u;
+      const int c = __popc(word);
       int incl = c;
       for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += v;
       }
       int pos = base + incl - c;
       while (word) {
-        int b = __ffs(word) - 1;
-        colidx[pos++] = w * 32 + b;
+        const int bit = __ffs(word) - 1;
+        I.colidx[pos++] = w * 32 + bit;
         word &= word - 1;
       }
       base += __shfl_sync(0xffffffffu, incl, 31);
@@ -270,62 +289,46 @@ __global__ void expand_adjacency_kernel(const uint32_t *__restrict__ adj, int64_
   }
 }
 
+int blocks_for(long long items, int per_block) {
+  return (int)std::max<long long>(1, std::min<long long>((items + per_block - 1) / per_block, 152LL * 32));
+}
+
 }  // namespace
 
-hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s) {
-  const int64_t total = p * p;
-  int blocks = (int)std::min<int64_t>((total / 4 + 255) / 256 + 1, 152 * 32);
-  expand_adjacency_kernel<<<blocks, 256, 0, s>>>(adj, p, W, out);
-  HPC_LAUNCH_CHECK("expand_adjacency_kernel");
+hpc_status launch_level0(const Launch &L, long long total, cudaStream_t s) {
+  level0_kernel<<<blocks_for(total, 256), 256, 0, s>>>(L, total);
+  HPC_LAUNCH_CHECK("level0_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStream_t s) {
-  const int64_t total = a.p * (int64_t)a.W;
-  int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
-  level0_lower_kernel<<<blocks, 256, 0, s>>>(a, r_lo, r_hi);
-  HPC_LAUNCH_CHECK("level0_lower_kernel");
-  const int64_t tiles = (int64_t)a.W * (a.W + 1) / 2;
-  int mblocks = (int)std::min<int64_t>((tiles + 7) / 8, 152 * 32);
-  mirror_bits_kernel<<<mblocks, 256, 0, s>>>(a.adj, a.p, a.W);
+hpc_status launch_mirror(const Launch &L, long long total, cudaStream_t s) {
+  mirror_bits_kernel<<<blocks_for(total, 8), 256, 0, s>>>(L, total);
   HPC_LAUNCH_CHECK("mirror_bits_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_level0_f32(const LevelArgs &a, float lo, float hi, cudaStream_t s) {
-  const int64_t total = a.p * (int64_t)a.W;
-  int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
-  level0_lower_f32_kernel<<<blocks, 256, 0, s>>>(a, lo, hi);
-  HPC_LAUNCH_CHECK("level0_lower_f32_kernel");
-  return HPC_OK;
-}
-
-hpc_status launch_mirror(const LevelArgs &a, cudaStream_t s) {
-  const int64_t tiles = (int64_t)a.W * (a.W + 1) / 2;
-  int mblocks = (int)std::min<int64_t>((tiles + 7) / 8, 152 * 32);
-  mirror_bits_kernel<<<mblocks, 256, 0, s>>>(a.adj, a.p, a.W);
-  HPC_LAUNCH_CHECK("mirror_bits_kernel");
-  return HPC_OK;
-}
-
-hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s) {
-  int blocks = (int)std::min<int64_t>((a.p + 7) / 8, 152 * 16);
-  degrees_kernel<<<blocks, 256, 0, s>>>(a.adj, a.p, a.W, deg);
+hpc_status launch_degrees(const Launch &L, long long total, cudaStream_t s) {
+  degrees_kernel<<<blocks_for(total, 8), 256, 0, s>>>(L, total);
   HPC_LAUNCH_CHECK("degrees_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
-                       DevCounters *ctr, DevGlobal *g, cudaStream_t s) {
-  scan_rows_kernel<<<1, kScanThreads, 0, s>>>(p, level, deg, rowptr, row_work, ctr, g);
-  HPC_LAUNCH_CHECK("scan_rows_kernel");
+hpc_status launch_scan(const Launch &L, cudaStream_t s) {
+  scan_kernel<<<L.count, kScanThreads, 0, s>>>(L);
+  HPC_LAUNCH_CHECK("scan_kernel");
   return HPC_OK;
 }
 
-hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s) {
-  int blocks = (int)std::min<int64_t>((a.p + 7) / 8, 152 * 16);
-  fill_csr_kernel<<<blocks, 256, 0, s>>>(a.adj, a.p, a.W, a.rowptr, colidx, a.colidx_cap, a.ctr, a.gctr);
+hpc_status launch_fill_csr(const Launch &L, long long total, cudaStream_t s) {
+  fill_csr_kernel<<<blocks_for(total, 8), 256, 0, s>>>(L, total);
   HPC_LAUNCH_CHECK("fill_csr_kernel");
+  return HPC_OK;
+}
+
+hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s) {
+  const int64_t total = p * p;
+  expand_adjacency_kernel<<<blocks_for(total / 4 + 1, 256), 256, 0, s>>>(adj, p, W, out);
+  HPC_LAUNCH_CHECK("expand_adjacency_kernel");
   return HPC_OK;
 }
 

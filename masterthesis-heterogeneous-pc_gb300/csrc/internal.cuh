@@ -1,10 +1,18 @@
 // Internal declarations shared by the CUDA translation units of libheterogpc.
+//
+// A context holds `count` independent skeleton problems ("instances"; a plain
+// context has one). Every device buffer is packed over the instances, and every
+// level kernel runs once per level over all of them: its flattened index space is
+// split by per-launch prefix sums (words, bit tiles, rows, CI tests) and each
+// thread or warp finds its instance by binary search over the prefix.
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/heterogpc.h"
 
@@ -31,25 +39,29 @@ hpc_status cuda_fail(cudaError_t e, const char *what, const char *file, int line
 // constants of the statistic (src/executor/independence/cpuInd.cpp:6)
 constexpr double kCutThr = 0.9999999;
 
-// Device counters of one level (one slot per level, written by that level's kernels).
+// Device counters of one instance and level.
 struct DevCounters {
   unsigned long long tests;        // executed CI tests
   unsigned long long retests;      // tests re-run in FP64 (band, conditioning, non-finite)
   unsigned long long deleted;      // edges removed
-  unsigned long long tile_next;    // work-queue head
-  unsigned long long work_total;   // T_l
+  unsigned long long work_total;   // T_l of the instance
   unsigned long long edges2;       // sum of degrees at the level start
   unsigned long long rec_begin;    // first separation-set record of the level
   unsigned long long band_violations;  // FP32 removals the FP64 post-pass did not confirm
-  unsigned long long rq_count;     // FP64 re-tests queued (tensor-core mode)
   int max_deg;                     // at the level start
   int rows;                        // rows with work at this level
-  int pad[2];
 };
-// Context-wide device counters.
+// Instance-wide device counters.
 struct DevGlobal {
   unsigned long long rec_count;    // separation-set records written (cumulative)
   int err;                         // error bits (kErr*)
+  int pad;
+};
+// Counters of one level's launch over all instances.
+struct LaunchCounters {
+  unsigned long long tile_next;    // CI-test work-queue head
+  unsigned long long rq_count;     // FP64 re-tests queued
+  unsigned int scan_done;          // scan blocks finished (the last one forms the prefix)
   int pad;
 };
 constexpr int kErrRecOverflow = 1;
@@ -57,130 +69,194 @@ constexpr int kErrWorkOverflow = 2;
 constexpr int kErrCsrOverflow = 4;
 constexpr int kErrTimeout = 8;
 
-// One deferred FP64 re-test: edge (i, j) given ids[0..level), or a level-0 pair (i > j).
+// One deferred FP64 re-test: edge (i, j) of instance `inst` given ids[0..level),
+// or a level-0 pair (i > j).
 struct RetestItem {
-  int32_t i, j, level, pad;
+  int32_t i, j, level, inst;
   int32_t ids[HPC_MAX_LEVEL];
 };
 
-// Everything a level kernel needs, passed by value.
-struct LevelArgs {
+// One skeleton problem, as the kernels see it (device-resident table).
+struct Inst {
   int64_t p;
-  int W;                 // 32-bit words per adjacency row
-  int level;
+  int W;                  // 32-bit words per adjacency row
   int n_obs;
   double alpha;
-  double sqrt_n3;        // sqrt(n - 3)
-  float r_c;             // |r| at which p == alpha (FP32)
-  float margin_r;        // |r| half-width of the fixed re-test band
-  float ke;              // error-bound coefficient: |r| error <= ke / (smallest pivot)
-  const double *cor64;   // p x p row-major (FP64 correlation)
-  const float *cor32;    // p x p row-major (FP32 copy) or null in plain mode
-  uint32_t *adj;         // live bitmask p x W
-  const int *deg;        // snapshot degrees
-  const int *rowptr;     // snapshot CSR offsets (p+1)
-  const int *colidx;     // snapshot neighbour ids, ascending per row
-  const unsigned long long *row_work;  // exclusive prefix of tests per row (p+1)
+  // FP32 decision: |r| against r_c with a band margin_r + 8 * ke(l) / pivot,
+  // ke(l) = ke_a + (l + 2) * ke_b
+  float r_c, margin_r, ke_a, ke_b;
+  double r_lo, r_hi;      // level 0 on FP64 entries: exact formula inside [r_lo, r_hi]
+  float lo32, hi32;       // level 0 on FP32 entries: FP64 re-test inside [lo32, hi32]
+  const double *cor64;    // p x p FP64 or null (tensor-core mode: entries from Z)
+  const float *cor32;     // p x p FP32 (mixed modes) or null
+  const double *Z;        // standardised data, n_z x p column-major, or null
+  int64_t n_z;
+  double denom;           // the Gram's divisor n - 1
+  uint32_t *adj;          // live bitmask p x W
+  int *deg;               // snapshot degrees (p)
+  int *rowptr;            // snapshot CSR offsets (p + 1)
+  int *colidx;            // snapshot neighbour ids, ascending per row
+  long long colidx_cap;
+  unsigned long long *row_work;  // exclusive prefix of tests per row (p + 1)
   hpc_sepset_record *recs;
   long long rec_cap;
-  long long colidx_cap;
-  DevCounters *ctr;      // this level's counters
-  DevGlobal *gctr;
-  // FP64 entries without an FP64 matrix: dot products of the standardised columns
-  const double *Z;       // n_z x p column-major (each variable contiguous) or null
-  int64_t n_z;
-  double denom;          // n - 1 (the Gram's divisor)
-  RetestItem *rq;        // deferred FP64 re-tests (tensor-core mode)
+  DevCounters *ctr;       // [HPC_MAX_LEVEL + 1]
+  DevGlobal *g;
+};
+
+// One level's launch over all instances, passed by value.
+struct Launch {
+  const Inst *inst;
+  int count;
+  int level;
+  const long long *word_prefix;     // adjacency words  sum p * W   (count + 1)
+  const long long *tile_prefix;     // 32x32 bit tiles  sum W(W+1)/2 (count + 1)
+  const long long *row_prefix;      // rows             sum p       (count + 1)
+  unsigned long long *work_prefix;  // CI tests of this level       (count + 1), written by the scan
+  LaunchCounters *lc;               // this level's
+  RetestItem *rq;                   // deferred FP64 re-tests
   long long rq_cap;
 };
 
+__device__ __forceinline__ int find_inst(const long long *prefix, int count, long long t) {
+  int lo = 0, hi = count;  // largest b with prefix[b] <= t
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int find_inst_u(const unsigned long long *prefix, int count, unsigned long long t) {
+  int lo = 0, hi = count;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // ---------------------------------------------------------------------------
-// kernels' host launchers (defined in the .cu files)
-hpc_status launch_standardise_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z,
-                                  cudaStream_t s);
-hpc_status launch_standardise_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z,
-                                  cudaStream_t s);
-hpc_status launch_gram_f64(const double *Z, int64_t n, int64_t p, double inv_denom, double *C,
-                           cudaStream_t s);
+// host launchers (defined in the .cu files)
+struct StdArgs {                    // grouped standardisation
+  int count;
+  const long long *row_prefix;      // variables (count + 1)
+  const long long *x_off;           // element offset of each instance's observations
+  const long long *z_off;           // element offset of each instance's Z
+  const long long *n;               // samples per instance
+  const long long *tc_off;          // element offset of each instance's split operands (or null)
+  const long long *n_pad;           // padded samples per instance (tensor-core layout)
+  const long long *kdim;            // K' per instance (tensor-core layout)
+  int ref_compat;
+};
+hpc_status launch_standardise(const void *X, bool f32, const StdArgs &a, long long total_rows, double *Z,
+                              __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
+struct GramArgs {                   // grouped FP64 Gram
+  int count;
+  const long long *tile_prefix;     // 64 x 64 upper-triangle tiles (count + 1)
+  const long long *z_off, *c_off, *n, *p;
+  const double *denom;
+};
+hpc_status launch_gram_f64(const double *Z, double *C, const GramArgs &a, long long total_tiles, cudaStream_t s);
+long long gram_f64_tiles(int64_t p);
 hpc_status launch_to_f32(const double *C, int64_t count, float *C32, cudaStream_t s);
 int64_t tc_n_pad(int64_t n);
 int64_t tc_p_pad(int64_t p);
 int64_t tc_k(int64_t n);
-hpc_status launch_standardise_split_f64(const double *X, int64_t n, int64_t p, int ref_compat, double *Z64,
-                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
-hpc_status launch_standardise_split_f32(const float *X, int64_t n, int64_t p, int ref_compat, double *Z64,
-                                        __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
-hpc_status launch_gram_tc(const __nv_bfloat16 *P, const __nv_bfloat16 *Q, int64_t n, int64_t p, float *C, int *err,
-                          cudaStream_t s);
-hpc_status launch_level0(const LevelArgs &a, double r_lo, double r_hi, cudaStream_t s);
-hpc_status launch_degrees(const LevelArgs &a, int *deg, cudaStream_t s);
-hpc_status launch_scan(int64_t p, int level, const int *deg, int *rowptr, unsigned long long *row_work,
-                       DevCounters *ctr, DevGlobal *g, cudaStream_t s);
-hpc_status launch_fill_csr(const LevelArgs &a, int *colidx, cudaStream_t s);
+long long gram_tc_tiles(int64_t p);
+hpc_status tc_make_maps(CUtensorMap *mp, CUtensorMap *mq, const __nv_bfloat16 *P, const __nv_bfloat16 *Q,
+                        int64_t p, int64_t n);
+struct TcArgs {                     // grouped tensor-core Gram
+  int count;
+  const long long *tile_prefix;     // 128 x 128 upper-triangle tiles (count + 1)
+  const CUtensorMap *maps;          // 2 per instance (P, Q), 64-byte aligned, device
+  const long long *c_off, *p, *n;
+  int *err;
+};
+hpc_status launch_gram_tc(float *C, const TcArgs &a, long long total_tiles, cudaStream_t s);
+
+hpc_status launch_level0(const Launch &L, long long total_words, cudaStream_t s);
+hpc_status launch_mirror(const Launch &L, long long total_tiles, cudaStream_t s);
+hpc_status launch_degrees(const Launch &L, long long total_rows, cudaStream_t s);
+hpc_status launch_scan(const Launch &L, cudaStream_t s);
+hpc_status launch_fill_csr(const Launch &L, long long total_rows, cudaStream_t s);
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
-hpc_status launch_citest(const LevelArgs &a, int precision, int grid, cudaStream_t s);
-hpc_status launch_finalize_records(const LevelArgs &a, cudaStream_t s);
-hpc_status launch_retest(const LevelArgs &a, int sms, cudaStream_t s);
-hpc_status launch_level0_f32(const LevelArgs &a, float lo, float hi, cudaStream_t s);
-hpc_status launch_mirror(const LevelArgs &a, cudaStream_t s);
+hpc_status launch_citest(const Launch &L, int precision, int grid, cudaStream_t s);
+hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
+hpc_status launch_finalize_records(const Launch &L, cudaStream_t s);
 int citest_grid(int precision, int level, int device);
+
+// per-instance host bookkeeping
+struct InstHost {
+  int64_t p = 0, n = 0;
+  double alpha = 0.05, zc = 0.0, r_crit = 0.0;
+  int W = 0;
+  long long cor_off = 0, z_off = 0, x_off = 0, adj_off = 0, row_off = 0, tc_off = 0;
+  long long colidx_off = 0, colidx_cap = 0, rec_off = 0, rec_cap = 0;
+  int64_t edges = 0;
+};
 
 }  // namespace hpc
 
 // ---------------------------------------------------------------------------
-// The context (opaque to callers).
+// The context (opaque to callers): `count` instances.
 struct hpc_ctx {
-  int64_t p = 0, n = 0;
+  int count = 1;
+  std::vector<hpc::InstHost> ih;
+  int64_t p = 0, n = 0;           // instance 0 (the single-instance API)
   hpc_opts opts{};
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
-  int W = 0;
-  double *cor64 = nullptr;
-  float *cor32 = nullptr;
-  double *Z = nullptr;          // standardised data (n x p)
-  int64_t Z_elems = 0;
-  __nv_bfloat16 *tcP = nullptr, *tcQ = nullptr;  // split-BF16 operands of the tensor-core Gram
-  int64_t tc_elems = 0;
-  void *X_stage = nullptr;      // device copy of host observations
+  cudaStream_t own_stream = nullptr;  // the context's stream; `stream` may be a caller's
+  // packed device buffers
+  double *cor64 = nullptr;        // sum p^2 (absent in tensor-core mode unless loaded)
+  float *cor32 = nullptr;         // sum p^2 (mixed modes)
+  double *Z = nullptr;            // sum n * p
+  __nv_bfloat16 *tcP = nullptr, *tcQ = nullptr;  // split-BF16 operands, sum p_pad * K'
+  CUtensorMap *tc_maps = nullptr;  // device, 2 per instance
+  void *X_stage = nullptr;        // device copy of host observations
   int64_t X_stage_bytes = 0;
-  uint32_t *adj = nullptr;
-  uint8_t *adj_bytes = nullptr;  // p x p expansion for hpc_get_adjacency
-  hpc::RetestItem *rq = nullptr;  // deferred FP64 re-tests (tensor-core mode)
-  int64_t rq_cap = 0;
-  bool cor64_valid = false;       // cor64 holds the current FP64 matrix
-  int *deg = nullptr;
-  int *rowptr = nullptr;
-  int *colidx = nullptr;
-  int64_t colidx_cap = 0;
-  unsigned long long *row_work = nullptr;
-  hpc_sepset_record *recs = nullptr;
-  int64_t rec_cap = 0;
-  hpc::DevCounters *ctr = nullptr;      // device, one slot per level (HPC_MAX_LEVEL + 1)
-  hpc::DevCounters *ctr_host = nullptr; // pinned mirror
-  hpc::DevGlobal *gctr = nullptr;       // device
-  hpc::DevGlobal *gctr_host = nullptr;  // pinned mirror
-  cudaStream_t own_stream = nullptr; // the context's stream; `stream` may be a caller's
-  cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
-  cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
-  // CUDA graph of the whole level sequence 0..graph_top, replayed while the
-  // buffers it was captured with stay in place
+  uint32_t *adj = nullptr;        // sum p * W
+  uint8_t *adj_bytes = nullptr;   // p x p expansion for hpc_get_adjacency (largest p)
+  int *deg = nullptr;             // sum p
+  int *rowptr = nullptr;          // sum (p + 1)
+  unsigned long long *row_work = nullptr;  // sum (p + 1)
+  int *colidx = nullptr;          // sum colidx_cap
+  long long colidx_total = 0;
+  hpc_sepset_record *recs = nullptr;  // sum rec_cap
+  long long rec_total = 0;
+  hpc::RetestItem *rq = nullptr;
+  long long rq_cap = 0;
+  hpc::DevCounters *ctr = nullptr;       // count x (HPC_MAX_LEVEL + 1)
+  hpc::DevCounters *ctr_host = nullptr;  // pinned mirror
+  hpc::DevGlobal *gctr = nullptr;        // count
+  hpc::DevGlobal *gctr_host = nullptr;
+  hpc::LaunchCounters *lc = nullptr;     // HPC_MAX_LEVEL + 1
+  hpc::Inst *inst = nullptr;             // device table (count)
+  std::vector<hpc::Inst> inst_host;      // the table last written
+  long long *prefixes = nullptr;         // device: word, tile, row prefixes (3 x (count + 1))
+  unsigned long long *work_prefix = nullptr;  // device: (HPC_MAX_LEVEL + 1) x (count + 1)
+  long long *meta = nullptr;             // device: correlation metadata arrays
+  double *meta_denom = nullptr;
+  long long total_words = 0, total_tiles = 0, total_rows = 0;
+  long long tiles64 = 0, tiles_tc = 0;
+  bool cor64_valid = false;       // cor64 holds the current FP64 matrices
+  bool cor32_rounded = true;      // cor32 is the FP32 rounding of cor64 (else the tensor-core Gram)
+  long long inst_version = 0;     // bumped whenever the device instance table changes
+  // CUDA graph of the whole level sequence 0..graph_top
   cudaGraphExec_t graph = nullptr;
   int graph_top = -1;
   cudaStream_t graph_stream = nullptr;
-  int64_t graph_colidx_cap = 0, graph_rec_cap = 0;
+  long long graph_version = -1;
   int64_t graph_launches = 0;
-  bool graph_cor64_valid = false;
   bool graphs_enabled = true;
   bool last_run_graph = false;
-  cudaEvent_t evr[2] = {nullptr, nullptr};  // whole skeleton run
-  int citest_grid[HPC_MAX_LEVEL + 1] = {};  // persistent grid size per level
+  int citest_grid[HPC_MAX_LEVEL + 1] = {};
+  cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
+  cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
+  cudaEvent_t evr[2] = {nullptr, nullptr};      // whole skeleton run
   bool cor_timed = false;
   hpc_timings timings{};
   bool have_cor = false;
-  bool cor32_rounded = true;   // cor32 is the FP32 rounding of cor64 (else the tensor-core Gram)
   int next_level = 0;
-  int64_t edges = 0;           // undirected edges after the last level
-  double zc = 0.0;             // z_crit (FP64)
-  double r_crit = 0.0;         // |r| at which p == alpha
 };

@@ -23,6 +23,9 @@
 //    n_obs * p values the Gram then reads. Calls whose work overlaps on the GPU
 //    (different streams, or different host threads) race on the array; order
 //    them on one stream or serialise them.
+//  * The shapes the grouped kernels read (offsets, sizes, tile counts) also live in
+//    a file-scope __device__ struct, written with cudaMemcpyToSymbolAsync on the
+//    caller's stream, and are shared between calls the same way.
 //  * No cudaMalloc, cudaFree or allocating library routine is called.
 #include <cuda_runtime.h>
 
@@ -37,10 +40,20 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_corr_scratch[HPC_NOALLOC_MAX_ELEMS];
 
+// Shape metadata of one instance in the layout the grouped standardisation and Gram
+// kernels read (StdArgs / GramArgs with count = 1).
+struct NoallocMeta {
+  long long row_prefix[2], x_off, z_off, n, tc_off, n_pad, kdim;
+  long long tile_prefix[2], c_off, p;
+  double denom;
+};
+static __device__ NoallocMeta g_meta;
+
 std::mutex g_scratch_mu;
 double *g_scratch_addr[kMaxDevices] = {};
+NoallocMeta *g_meta_addr[kMaxDevices] = {};
 
-hpc_status scratch_for_current_device(double **out) {
+hpc_status scratch_for_current_device(double **out, NoallocMeta **meta) {
   int dev = -1;
   HPC_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) {
@@ -58,8 +71,19 @@ hpc_status scratch_for_current_device(double **out) {
       return HPC_ERR_CUDA;
     }
     g_scratch_addr[dev] = (double *)ptr;
+    void *mp = nullptr;
+    e = cudaGetSymbolAddress(&mp, g_meta);
+    if (e != cudaSuccess || !mp) {
+      cudaGetLastError();
+      set_error("cudaGetSymbolAddress of the correlation metadata failed on device %d: %s", dev,
+                cudaGetErrorString(e));
+      g_scratch_addr[dev] = nullptr;
+      return HPC_ERR_CUDA;
+    }
+    g_meta_addr[dev] = (NoallocMeta *)mp;
   }
   *out = g_scratch_addr[dev];
+  *meta = g_meta_addr[dev];
   return HPC_OK;
 }
 
@@ -83,10 +107,38 @@ extern "C" hpc_status hpc_correlation_noalloc_f64(const double *X_dev, int64_t n
     return HPC_ERR_CAPACITY;
   }
   double *Z = nullptr;
-  hpc_status s = scratch_for_current_device(&Z);
+  NoallocMeta *md = nullptr;
+  hpc_status s = scratch_for_current_device(&Z, &md);
   if (s != HPC_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
-  if ((s = launch_standardise_f64(X_dev, n_obs, p, ref_compat_sd, Z, st)) != HPC_OK) return s;
-  const double denom = ref_compat_sd ? (double)((float)n_obs - 1.f) : (double)(n_obs - 1);
-  return launch_gram_f64(Z, n_obs, p, denom, C_dev, st);
+  NoallocMeta m{};
+  m.row_prefix[0] = 0;
+  m.row_prefix[1] = p;
+  m.n = n_obs;
+  m.tile_prefix[0] = 0;
+  m.tile_prefix[1] = gram_f64_tiles(p);
+  m.p = p;
+  m.denom = ref_compat_sd ? (double)((float)n_obs - 1.f) : (double)(n_obs - 1);
+  // pageable source: the copy has read `m` when the call returns
+  HPC_CUDA(cudaMemcpyToSymbolAsync(g_meta, &m, sizeof(m), 0, cudaMemcpyHostToDevice, st));
+  StdArgs sa{};
+  sa.count = 1;
+  sa.row_prefix = md->row_prefix;
+  sa.x_off = &md->x_off;
+  sa.z_off = &md->z_off;
+  sa.n = &md->n;
+  sa.tc_off = &md->tc_off;
+  sa.n_pad = &md->n_pad;
+  sa.kdim = &md->kdim;
+  sa.ref_compat = ref_compat_sd;
+  if ((s = launch_standardise(X_dev, false, sa, p, Z, nullptr, nullptr, st)) != HPC_OK) return s;
+  GramArgs ga{};
+  ga.count = 1;
+  ga.tile_prefix = md->tile_prefix;
+  ga.z_off = &md->z_off;
+  ga.c_off = &md->c_off;
+  ga.n = &md->n;
+  ga.p = &md->p;
+  ga.denom = &md->denom;
+  return launch_gram_f64(Z, C_dev, ga, gram_f64_tiles(p), st);
 }

@@ -98,6 +98,14 @@ _SIGS = {
     "hpc_pval_ln": (C.c_double, [C.c_void_p, C.c_int, C.c_int]),
     "hpc_z_crit": (C.c_double, [C.c_double]),
     "hpc_sem_generate": (C.c_int, [C.POINTER(SemParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hpc_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.POINTER(Opts)]),
+    "hpc_batch_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "hpc_batch_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hpc_batch_level_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LevelStats), C.c_int, C.POINTER(C.c_int)]),
+    "hpc_batch_get_adjacency": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "hpc_batch_edge_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]),
+    "hpc_batch_get_sepset_records": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
 }
 
 
@@ -303,4 +311,108 @@ class SkeletonCalculator:
         _check(lib().hpc_get_sepset_records(self._h, None, 0, C.byref(n)))
         recs = (SepsetRecord * max(1, n.value))()
         _check(lib().hpc_get_sepset_records(self._h, recs, n.value, C.byref(n)))
+        return [(r.i, r.j, r.level, tuple(r.ids[:r.level]), r.pmax) for r in recs[:n.value]]
+
+
+class SkeletonBatch:
+    """Many independent skeleton problems in one context: every level kernel runs
+    once for all of them (hpc_batch_* in include/heterogpc.h)."""
+
+    def __init__(self, ps, ns, alphas=None, max_level=4, precision=PREC_MIXED_TC, device=0, retest_margin=1e-3,
+                 verbose=False):
+        self.ps = np.ascontiguousarray(ps, dtype=np.int64)
+        self.ns = np.ascontiguousarray(ns, dtype=np.int64)
+        self.count = len(self.ps)
+        o = Opts()
+        lib().hpc_opts_default(C.byref(o))
+        o.device, o.max_level, o.precision, o.retest_margin, o.verbose = device, max_level, precision, \
+            retest_margin, int(verbose)
+        self.alphas = None if alphas is None else np.ascontiguousarray(alphas, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().hpc_batch_create(C.byref(h), self.count, _ptr(self.ps), _ptr(self.ns),
+                                      _ptr(self.alphas) if self.alphas is not None else None, C.byref(o)))
+        self._h = h
+        self.obs_off = np.empty(self.count + 1, np.int64)
+        self.cor_off = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_offsets(self._h, _ptr(self.obs_off), _ptr(self.cor_off)))
+        self.level_stats = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hpc_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pack(self, Xs, dtype=np.float32):
+        """Packed observations from per-instance arrays of shape (p_b, n_b)."""
+        out = np.empty(int(self.obs_off[-1]), dtype)
+        for b, X in enumerate(Xs):
+            out[self.obs_off[b]:self.obs_off[b + 1]] = np.asarray(X, dtype).reshape(-1)
+        return out
+
+    def add_observations(self, packed):
+        packed = np.ascontiguousarray(packed)
+        fn = lib().hpc_correlation_f32 if packed.dtype == np.float32 else lib().hpc_correlation_f64
+        _check(fn(self._h, _ptr(packed)))
+
+    def add_observations_device(self, ptr, dtype):
+        fn = lib().hpc_correlation_device_f32 if dtype == np.float32 else lib().hpc_correlation_device_f64
+        _check(fn(self._h, C.c_void_p(ptr)))
+
+    def add_correlation_matrices(self, mats):
+        packed = np.empty(int(self.cor_off[-1]), np.float64)
+        for b, M in enumerate(mats):
+            packed[self.cor_off[b]:self.cor_off[b + 1]] = np.asarray(M, np.float64).reshape(-1)
+        _check(lib().hpc_load_correlation(self._h, _ptr(packed)))
+
+    def set_stream(self, stream_handle):
+        _check(lib().hpc_ctx_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None))
+
+    def set_graphs(self, enable):
+        _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
+
+    def reset(self):
+        _check(lib().hpc_ctx_reset(self._h))
+
+    def run(self):
+        cap = HPC_MAX_LEVEL + 1
+        arr = (LevelStats * cap)()
+        ran = C.c_int(0)
+        _check(lib().hpc_run_skeleton(self._h, arr, cap, C.byref(ran)))
+        self.level_stats = [arr[i].as_dict() for i in range(ran.value)]
+        return self.level_stats
+
+    def timings(self):
+        t = Timings()
+        _check(lib().hpc_get_timings(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def adjacency(self, idx):
+        p = int(self.ps[idx])
+        out = np.empty((p, p), np.uint8)
+        _check(lib().hpc_batch_get_adjacency(self._h, idx, _ptr(out)))
+        return out
+
+    def edge_count(self, idx):
+        e = C.c_int64(0)
+        _check(lib().hpc_batch_edge_count(self._h, idx, C.byref(e)))
+        return e.value
+
+    def instance_levels(self, idx):
+        cap = HPC_MAX_LEVEL + 1
+        arr = (LevelStats * cap)()
+        k = C.c_int(0)
+        _check(lib().hpc_batch_level_stats(self._h, idx, arr, cap, C.byref(k)))
+        return [arr[i].as_dict() for i in range(k.value)]
+
+    def sepset_records(self, idx):
+        n = C.c_int64(0)
+        _check(lib().hpc_batch_get_sepset_records(self._h, idx, None, 0, C.byref(n)))
+        recs = (SepsetRecord * max(1, n.value))()
+        _check(lib().hpc_batch_get_sepset_records(self._h, idx, recs, n.value, C.byref(n)))
         return [(r.i, r.j, r.level, tuple(r.ids[:r.level]), r.pmax) for r in recs[:n.value]]
