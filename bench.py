@@ -39,7 +39,96 @@ import numpy as np  # noqa: E402
 WORKLOADS = {
     "c2": dict(p=2000, n=5000, graph=0, degree=4.0, pa_parents=2, w_lo=0.1, w_hi=1.0, seed=2, alpha=0.01,
                max_level=6, dtype="f32"),
+    # 512 instances, p ~ U[20, 800], n ~ U[200, 8000], ER degree ~ U[1, 5], alpha 0.01 / 0.05
+    # alternating, FP32 data, levels until exhausted; all instances in one context
+    "c4": dict(count=512, p=(20, 800), n=(200, 8000), degree=(1.0, 5.0), w_lo=0.1, w_hi=1.0, seed=4,
+               alphas=(0.01, 0.05), max_level=-1),
 }
+
+
+def c4_instances(wl, count=None):
+    rng = np.random.default_rng(wl["seed"])
+    k = wl["count"] if count is None else count
+    ps = rng.integers(wl["p"][0], wl["p"][1] + 1, wl["count"])[:k]
+    ns = rng.integers(wl["n"][0], wl["n"][1] + 1, wl["count"])[:k]
+    degs = rng.uniform(wl["degree"][0], wl["degree"][1], wl["count"])[:k]
+    alphas = np.array([wl["alphas"][b % 2] for b in range(k)])
+    return ps, ns, degs, alphas
+
+
+def run_c4(args, wl):
+    """Batched skeletons: one context, every level kernel launched once for all 512
+    instances; a step is correlation (split-BF16 tensor-core Gram) + all levels of
+    every instance from observations resident in HBM. Compared with the plain
+    single-instance FP64 path (FP64 Gram, FP64 tests) run instance by instance."""
+    import torch
+
+    import heterogpc as hg
+    import hpc_build
+    if not os.path.exists(hg.LIB_PATH):
+        hpc_build.build_library()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ps, ns, degs, alphas = c4_instances(wl, args.count)
+    bt = hg.SkeletonBatch(ps, ns, alphas, max_level=wl["max_level"], precision=hg.PREC_MIXED_TC)
+    bt.set_stream(stream.cuda_stream)
+    packed = np.empty(int(bt.obs_off[-1]), np.float32)
+    for b in range(bt.count):
+        X = hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, float(degs[b]), 2, wl["w_lo"], wl["w_hi"],
+                            wl["seed"] * 100000 + b, dtype=np.float32)
+        packed[bt.obs_off[b]:bt.obs_off[b + 1]] = X.reshape(-1)
+    Xd = torch.from_numpy(packed).to(dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def step():
+        bt.add_observations_device(Xd.data_ptr(), np.float32)
+        return bt.run()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ms, tests = [], 0
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        a, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st = step()
+        b_.record(stream)
+        b_.synchronize()
+        ms.append(a.elapsed_time(b_))
+        tests = sum(s_["executed_tests"] for s_ in st)
+    clk = clocks.stop()
+    t_cor = bt.timings()
+    value = bt.count * args.steps / (sum(ms) / 1e3)
+    # plain single-instance FP64 path, instance by instance (a bounded sample)
+    k_plain = min(bt.count, args.plain_sample)
+    t0 = time.perf_counter()
+    for b in range(k_plain):
+        sk = hg.SkeletonCalculator(int(ps[b]), int(ns[b]), alpha=float(alphas[b]), max_level=wl["max_level"],
+                                   precision=hg.PREC_FP64)
+        sk.add_observations_device(Xd.data_ptr() + int(bt.obs_off[b]) * 4, np.float32)
+        sk.run()
+        sk.close()
+    torch.cuda.synchronize()
+    plain = k_plain / (time.perf_counter() - t0)
+    line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sum(ms) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x4/f32/f64",
+            "data": "synthetic (seeded linear-Gaussian SEM)",
+            "config": {"workload": "c4", "instances": bt.count, "p": list(wl["p"]), "n": list(wl["n"]),
+                       "degree": list(wl["degree"]), "alphas": list(wl["alphas"]), "max_level": wl["max_level"],
+                       "precision": "tensor-core split-BF16 Gram, FP32 tests, FP64 re-tests",
+                       "l2": "flushed before every step"},
+            "ci_tests_per_step": tests, "correlation_ms": t_cor["standardise_ms"] + t_cor["gram_ms"],
+            "skeleton_ms": t_cor["skeleton_ms"],
+            "plain_gpu_path": {"skeletons_per_sec": plain, "sample": "%d instances, one context each" % k_plain,
+                               "precision": "fp64"},
+            "speedup_vs_plain": value / plain, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
 
 
 def load_peaks():
@@ -174,6 +263,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--count", type=int, default=None, help="c4: number of instances (default 512)")
+    ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -184,6 +275,10 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, wl, rank, world)
+        return
+    if args.workload == "c4":
+        if rank == 0:
+            run_c4(args, wl)
         return
 
     import torch
