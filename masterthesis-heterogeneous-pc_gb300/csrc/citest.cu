@@ -332,12 +332,14 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(Launch L) {
 // below alpha is counted as a band violation: the FP32 error bound did not hold),
 // else the FP64 formula on the stored FP32 |r|.
 __global__ void finalize_records_kernel(Launch L) {
-  for (int b = blockIdx.x; b < L.count; b += gridDim.x) {
+  const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  const unsigned long long nthreads = (unsigned long long)gridDim.x * blockDim.x;
+  for (int b = 0; b < L.count; ++b) {
     const Inst &I = L.inst[b];
     const unsigned long long begin = I.ctr[L.level].rec_begin;
     unsigned long long end = I.g->rec_count;
     if (end > (unsigned long long)I.rec_cap) end = (unsigned long long)I.rec_cap;
-    for (unsigned long long r = begin + threadIdx.x; r < end; r += blockDim.x) {
+    for (unsigned long long r = begin + tid; r < end; r += nthreads) {
       hpc_sepset_record *rec = I.recs + r;
       if (!(rec->pmax < 0.0)) continue;
       if (!I.cor64) {
@@ -439,8 +441,7 @@ hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
 }
 
 hpc_status launch_finalize_records(const Launch &L, cudaStream_t s) {
-  const int blocks = L.count < 304 ? L.count : 304;
-  finalize_records_kernel<<<blocks, 128, 0, s>>>(L);
+  finalize_records_kernel<<<152 * 2, 128, 0, s>>>(L);
   HPC_LAUNCH_CHECK("finalize_records_kernel");
   return HPC_OK;
 }
