@@ -209,6 +209,46 @@ hpc_status hpc_batch_edge_count(hpc_ctx *ctx, int idx, int64_t *edges);
 hpc_status hpc_batch_get_sepset_records(hpc_ctx *ctx, int idx, hpc_sepset_record *out, int64_t cap,
                                         int64_t *count);
 
+/* ---- serving ----------------------------------------------------------------
+ * Continuous batching of skeleton requests (no reference counterpart). A
+ * scheduler thread admits the requests that have arrived, in arrival order, as one
+ * batch (a context whose level kernels run once for all its instances) while the
+ * device bytes in flight (hpc_ctx_footprint per request) stay within budget_bytes
+ * and fewer than max_inflight batches run; every batch runs on its own worker
+ * thread and CUDA stream, so batches admitted while others are on the GPU overlap
+ * with them. Each request's data stay resident on the device until its batch is
+ * done. */
+typedef struct hpc_server hpc_server;
+typedef struct hpc_server_opts {
+  int device;
+  int precision;          /* default HPC_PREC_MIXED_TC */
+  int max_level;          /* default 4 */
+  int64_t budget_bytes;   /* device bytes admitted at once (default 150 GB) */
+  int max_batch;          /* requests per batch (default 64) */
+  int max_inflight;       /* batches on the device at once (default 4) */
+} hpc_server_opts;
+typedef struct hpc_served {
+  int64_t id;
+  int32_t status;         /* hpc_status of the request */
+  int32_t levels;         /* levels run */
+  int64_t edges;          /* undirected edges of its skeleton */
+  double queue_ms;        /* submit -> its batch started */
+  double run_ms;          /* batch start -> results copied */
+  double latency_ms;      /* submit -> results copied */
+  int32_t batch_size;
+  int32_t pad;
+} hpc_served;
+hpc_status hpc_server_opts_default(hpc_server_opts *opts);
+hpc_status hpc_server_create(hpc_server **out, const hpc_server_opts *opts);
+/* X: host FP32, column-major n_obs x p; X and adj_out (optional, p x p bytes) must
+ * stay valid until the request is returned by hpc_server_poll. */
+hpc_status hpc_server_submit(hpc_server *sv, const float *X, int64_t p, int64_t n_obs, double alpha, uint8_t *adj_out,
+                             int64_t *id);
+/* completed requests since the last poll, at most cap */
+hpc_status hpc_server_poll(hpc_server *sv, hpc_served *out, int cap, int *count);
+hpc_status hpc_server_drain(hpc_server *sv);
+hpc_status hpc_server_destroy(hpc_server *sv);
+
 /* ---- independence statistics (FP64) -------------------------------------
  * Same semantics as CPU::calcPValue / CPU::pValL1 / CPU::pValLN
  * (src/executor/independence/cpuInd.hpp:3-10, cpuInd.cpp:8-38). M is the

@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -65,10 +66,35 @@ double r_crit_of(double alpha, int n) {
 // times the model, which bounds the measured errors of tests/test_gpu_tensorcore.py.
 double tc_entry_err(int64_t n) { return 4.0 * (1.6e-5 / std::sqrt((double)n) + 1e-7); }
 
+// Device memory comes from the stream-ordered allocator on one non-blocking stream
+// per device: unlike cudaFree, returning memory does not synchronise the device, so
+// contexts created and destroyed while others run (the serving loop) do not stall
+// them. Freed memory stays in the device's default pool for the next context.
+cudaStream_t alloc_stream() {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> g(mu);
+  if (!streams[dev]) {
+    cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
+  return streams[dev];
+}
+
 template <typename T>
 hpc_status dev_alloc(T **ptr, int64_t count, const char *what) {
   if (count <= 0) count = 1;
-  const cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (size_t)count);
+  cudaStream_t as = alloc_stream();
+  cudaError_t e = cudaMallocAsync((void **)ptr, sizeof(T) * (size_t)count, as);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(as);
   if (e != cudaSuccess) {
     *ptr = nullptr;
     cudaGetLastError();
@@ -79,9 +105,10 @@ hpc_status dev_alloc(T **ptr, int64_t count, const char *what) {
   return HPC_OK;
 }
 
+// Only after the context's own work that used ptr has completed.
 template <typename T>
 void dev_free(T *&ptr) {
-  if (ptr) cudaFree(ptr);
+  if (ptr) cudaFreeAsync((void *)ptr, alloc_stream());
   ptr = nullptr;
 }
 
@@ -558,7 +585,9 @@ hpc_status correlation_host(hpc_ctx *c, const void *X, bool f32) {
   for (const auto &h : c->ih) elems += h.n * h.p;
   const int64_t bytes = elems * (f32 ? 4 : 8);
   if (c->X_stage_bytes < bytes) {
-    if (c->X_stage) cudaFree(c->X_stage);
+    HPC_CUDA(cudaStreamSynchronize(c->stream));
+    uint8_t *old = (uint8_t *)c->X_stage;
+    dev_free(old);
     c->X_stage = nullptr;
     c->X_stage_bytes = 0;
     uint8_t *buf = nullptr;
@@ -683,7 +712,11 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->tcP);
   dev_free(c->tcQ);
   dev_free(c->tc_maps);
-  if (c->X_stage) cudaFree(c->X_stage);
+  {
+    uint8_t *xs = (uint8_t *)c->X_stage;
+    dev_free(xs);
+    c->X_stage = nullptr;
+  }
   dev_free(c->adj);
   dev_free(c->adj_bytes);
   dev_free(c->deg);
@@ -700,8 +733,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->work_prefix);
   dev_free(c->meta);
   dev_free(c->meta_denom);
-  if (c->ctr_host) cudaFreeHost(c->ctr_host);
-  if (c->gctr_host) cudaFreeHost(c->gctr_host);
+  delete[] c->ctr_host;
+  delete[] c->gctr_host;
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (auto &e : c->evc)
     if (e) cudaEventDestroy(e);
@@ -1180,12 +1213,8 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   if ((s = dev_alloc(&c->inst, count, "instance table")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->prefixes, (int64_t)pre.size(), "prefixes")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->work_prefix, (int64_t)kLevels * (count + 1), "work prefixes")) != HPC_OK) return fail(s);
-  if (cudaMallocHost((void **)&c->ctr_host, sizeof(DevCounters) * (size_t)count * kLevels) != cudaSuccess ||
-      cudaMallocHost((void **)&c->gctr_host, sizeof(DevGlobal) * (size_t)count) != cudaSuccess) {
-    cudaGetLastError();
-    set_error("pinned counter allocation failed");
-    return fail(HPC_ERR_OOM);
-  }
+  c->ctr_host = new DevCounters[(size_t)count * kLevels];
+  c->gctr_host = new DevGlobal[(size_t)count];
   if (cudaMemcpyAsync(c->prefixes, pre.data(), sizeof(long long) * pre.size(), cudaMemcpyHostToDevice, c->stream) !=
           cudaSuccess ||
       cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)count * kLevels, c->stream) != cudaSuccess ||

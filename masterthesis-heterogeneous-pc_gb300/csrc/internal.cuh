@@ -228,7 +228,7 @@ struct hpc_ctx {
   hpc::RetestItem *rq = nullptr;
   long long rq_cap = 0;
   hpc::DevCounters *ctr = nullptr;       // count x (HPC_MAX_LEVEL + 1)
-  hpc::DevCounters *ctr_host = nullptr;  // pinned mirror
+  hpc::DevCounters *ctr_host = nullptr;  // host mirror
   hpc::DevGlobal *gctr = nullptr;        // count
   hpc::DevGlobal *gctr_host = nullptr;
   hpc::LaunchCounters *lc = nullptr;     // HPC_MAX_LEVEL + 1

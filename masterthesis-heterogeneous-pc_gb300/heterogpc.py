@@ -59,6 +59,17 @@ class Timings(C.Structure):
                 "launches": self.launches, "skeleton_ms": self.skeleton_ms}
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("max_level", C.c_int), ("budget_bytes", C.c_int64),
+                ("max_batch", C.c_int), ("max_inflight", C.c_int)]
+
+
+class Served(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("levels", C.c_int32), ("edges", C.c_int64),
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
+                ("batch_size", C.c_int32), ("pad", C.c_int32)]
+
+
 class SemParams(C.Structure):
     _fields_ = [("p", C.c_int64), ("n", C.c_int64), ("graph", C.c_int), ("degree", C.c_double),
                 ("pa_parents", C.c_int), ("w_lo", C.c_double), ("w_hi", C.c_double), ("seed", C.c_uint64)]
@@ -98,6 +109,13 @@ _SIGS = {
     "hpc_pval_ln": (C.c_double, [C.c_void_p, C.c_int, C.c_int]),
     "hpc_z_crit": (C.c_double, [C.c_double]),
     "hpc_sem_generate": (C.c_int, [C.POINTER(SemParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hpc_server_opts_default": (C.c_int, [C.POINTER(ServerOpts)]),
+    "hpc_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(ServerOpts)]),
+    "hpc_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p,
+                                    C.POINTER(C.c_int64)]),
+    "hpc_server_poll": (C.c_int, [C.c_void_p, C.POINTER(Served), C.c_int, C.POINTER(C.c_int)]),
+    "hpc_server_drain": (C.c_int, [C.c_void_p]),
+    "hpc_server_destroy": (C.c_int, [C.c_void_p]),
     "hpc_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.POINTER(Opts)]),
     "hpc_batch_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -416,3 +434,54 @@ class SkeletonBatch:
         recs = (SepsetRecord * max(1, n.value))()
         _check(lib().hpc_batch_get_sepset_records(self._h, idx, recs, n.value, C.byref(n)))
         return [(r.i, r.j, r.level, tuple(r.ids[:r.level]), r.pmax) for r in recs[:n.value]]
+
+
+class SkeletonServer:
+    """Continuous-batching skeleton server (hpc_server_* in include/heterogpc.h)."""
+
+    def __init__(self, precision=PREC_MIXED_TC, max_level=4, budget_bytes=150 * 10**9, max_batch=64,
+                 max_inflight=4, device=0):
+        o = ServerOpts()
+        lib().hpc_server_opts_default(C.byref(o))
+        o.device, o.precision, o.max_level = device, precision, max_level
+        o.budget_bytes, o.max_batch, o.max_inflight = budget_bytes, max_batch, max_inflight
+        h = C.c_void_p()
+        _check(lib().hpc_server_create(C.byref(h), C.byref(o)))
+        self._h = h
+        self._keep = {}
+
+    def submit(self, X, alpha, want_adjacency=False):
+        """X: float32 array (p, n), kept alive until the request completes."""
+        X = np.ascontiguousarray(X, np.float32)
+        p, n = X.shape
+        adj = np.empty((p, p), np.uint8) if want_adjacency else None
+        rid = C.c_int64(0)
+        _check(lib().hpc_server_submit(self._h, _ptr(X), p, n, float(alpha), _ptr(adj) if adj is not None else None,
+                                       C.byref(rid)))
+        self._keep[rid.value] = (X, adj)
+        return rid.value
+
+    def poll(self, cap=1024):
+        arr = (Served * cap)()
+        k = C.c_int(0)
+        _check(lib().hpc_server_poll(self._h, arr, cap, C.byref(k)))
+        out = []
+        for r in arr[:k.value]:
+            X, adj = self._keep.pop(r.id)
+            out.append(dict(id=r.id, status=r.status, levels=r.levels, edges=r.edges, queue_ms=r.queue_ms,
+                            run_ms=r.run_ms, latency_ms=r.latency_ms, batch_size=r.batch_size, adjacency=adj))
+        return out
+
+    def drain(self):
+        _check(lib().hpc_server_drain(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hpc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ctx.cu", "correlation.cu", "graph.cu", "citest.cu", "gram_tc.cu", "noalloc.cu"]
-HOST_SOURCES = ["semgen.cpp"]
+HOST_SOURCES = ["semgen.cpp", "serve.cpp"]
 
 
 def _run(cmd):
@@ -62,7 +62,8 @@ def _compile_host(src, extra=()):
     out = os.path.join(OBJ, os.path.basename(src) + ".o")
     if _newer(out, [src] + _headers()):
         return out
-    _run(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, *extra, "-c", src, "-o", out])
+    _run(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, "-I",
+          os.path.join(CUDA_HOME, "include"), *extra, "-c", src, "-o", out])
     return out
 
 
