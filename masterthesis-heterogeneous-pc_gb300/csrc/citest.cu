@@ -327,19 +327,126 @@ __global__ void __launch_bounds__(kThreads) citest_kernel(Launch L) {
   }
 }
 
-// p-values of the removals a level decided in FP32 (records [rec_begin, rec_count) of
-// each instance): FP64 re-evaluation where the instance has an FP64 matrix (a result
-// below alpha is counted as a band violation: the FP32 error bound did not hold),
-// else the FP64 formula on the stored FP32 |r|.
-__global__ void finalize_records_kernel(Launch L) {
+// Level 1, lane-interleaved: lane q of a warp takes tests t0 + q, t0 + q + 32, ... of
+// its tile, so the 32 lanes work on consecutive conditioning variables of the same
+// edge (i, j): their reads of the neighbour list and of row i of cor32 fall into few
+// cache lines and stay in L1 across the edges of row i, and only the reads of row j
+// are scattered. Decisions as test_f32 with l = 1 (the closed form of cpuInd.cpp:16-27
+// in FP32), FP64 re-tests as in citest_kernel.
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) citest_l1_kernel(Launch L) {
+  const int level = 1;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long total = L.work_prefix[L.count];
+  if (total == 0) return;
+  const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
+  const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
+  const unsigned long long per_tile = 32ull * (unsigned long long)m;
+  for (;;) {
+    unsigned long long tile = 0;
+    if (lane == 0) tile = atomicAdd(&L.lc->tile_next, 1ull);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    const unsigned long long t0 = tile * per_tile;
+    if (t0 >= total) break;
+    const unsigned long long tend = min(t0 + per_tile, total);
+    unsigned long long t = t0 + lane;
+    unsigned executed = 0, retests = 0;
+    int b_last = -1;
+    if (t < tend) {
+      int b = find_inst_u(L.work_prefix, L.count, t);
+      const Inst *I = L.inst + b;
+      unsigned long long base_t = L.work_prefix[b];
+      int64_t i = find_row(I->row_work, I->p, t - base_t);
+      int d = I->deg[i];
+      int c = d - 1;  // tests per edge at level 1
+      unsigned long long off = t - base_t - I->row_work[i];
+      int s = (int)(off / (unsigned long long)c);
+      int rank = (int)(off - (unsigned long long)s * c);
+      int base = I->rowptr[i];
+      int64_t j = I->colidx[base + s];
+      float rij = MIXED ? __ldg(I->cor32 + i * I->p + j) : 0.f;
+      for (;;) {
+        // the neighbour id and the live bit are loaded together (latency overlap)
+        const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
+        if (live_bit(I->adj, I->W, i, j)) {
+          int res = 2;
+          float rr = 0.f;
+          if (MIXED) {
+            const float x2 = __ldg(I->cor32 + i * I->p + k), x3 = __ldg(I->cor32 + j * I->p + k);
+            const float ax = 1.0f - x2 * x2, ay = 1.0f - x3 * x3;
+            const float cond = fminf(ax, ay);
+            if (cond > 1e-3f) {
+              rr = fabsf(rij - x2 * x3) * rsqrtf(ax * ay);
+              const float dist = rr - I->r_c;
+              const float band = I->margin_r + 8.0f * __fdividef(I->ke_a + 3.0f * I->ke_b, cond);
+              if (fabsf(dist) > band) res = dist < 0.0f ? 1 : 0;
+            }
+          }
+          ++executed;
+          if (res == 1) {
+            record_removal(*I, level, i, j, &k, 1, -1.0 - (double)rr);
+          } else if (res == 2) {
+            if (MIXED) ++retests;
+            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, &k, 1))) {
+              const double pv = exact_pvalue<1>(*I, i, j, &k, 1);
+              if (pv >= I->alpha) record_removal(*I, level, i, j, &k, 1, pv);
+            }
+          }
+        }
+        t += 32;
+        if (t >= tend) break;
+        rank += 32;
+        bool moved = false;
+        while (rank >= c) {  // next edge (and row, and instance) along the flattened order
+          rank -= c;
+          moved = true;
+          if (++s == d) {
+            if (t >= L.work_prefix[b + 1]) {
+              b = find_inst_u(L.work_prefix, L.count, t);
+              I = L.inst + b;
+              base_t = L.work_prefix[b];
+            }
+            i = find_row(I->row_work, I->p, t - base_t);
+            d = I->deg[i];
+            c = d - 1;
+            base = I->rowptr[i];
+            s = 0;
+            off = t - base_t - I->row_work[i];
+            s = (int)(off / (unsigned long long)c);
+            rank = (int)(off - (unsigned long long)s * c);
+            break;
+          }
+        }
+        if (moved) {
+          j = I->colidx[base + s];
+          if (MIXED) rij = __ldg(I->cor32 + i * I->p + j);
+        }
+      }
+      b_last = b;
+    }
+    const unsigned grp = __match_any_sync(0xffffffffu, b_last);
+    const unsigned ex = __reduce_add_sync(grp, executed);
+    const unsigned rt = __reduce_add_sync(grp, retests);
+    if (b_last >= 0 && lane == __ffs(grp) - 1) {
+      atomicAdd(&L.inst[b_last].ctr[level].tests, (unsigned long long)ex);
+      if (rt) atomicAdd(&L.inst[b_last].ctr[level].retests, (unsigned long long)rt);
+    }
+  }
+}
+
+// p-values of the removals decided in FP32 (negative pmax), for every instance's
+// records: FP64 re-evaluation where the instance has an FP64 matrix -- a result below
+// alpha flags kErrBandViolation (the FP32 error bound did not hold) -- else the FP64
+// formula on the stored FP32 |r|. Run when the records are first read, not inside the
+// level loop.
+__global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count) {
   const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
   const unsigned long long nthreads = (unsigned long long)gridDim.x * blockDim.x;
-  for (int b = 0; b < L.count; ++b) {
-    const Inst &I = L.inst[b];
-    const unsigned long long begin = I.ctr[L.level].rec_begin;
+  for (int b = 0; b < count; ++b) {
+    const Inst &I = inst[b];
     unsigned long long end = I.g->rec_count;
     if (end > (unsigned long long)I.rec_cap) end = (unsigned long long)I.rec_cap;
-    for (unsigned long long r = begin + tid; r < end; r += nthreads) {
+    for (unsigned long long r = tid; r < end; r += nthreads) {
       hpc_sepset_record *rec = I.recs + r;
       if (!(rec->pmax < 0.0)) continue;
       if (!I.cor64) {
@@ -348,7 +455,7 @@ __global__ void finalize_records_kernel(Launch L) {
       }
       const double pv = exact_pvalue<HPC_MAX_LEVEL>(I, rec->i, rec->j, rec->ids, rec->level);
       rec->pmax = pv;
-      if (!(pv >= I.alpha)) atomicAdd(&I.ctr[L.level].band_violations, 1ull);
+      if (!(pv >= I.alpha)) atomicOr(&I.g->err, kErrBandViolation);
     }
   }
 }
@@ -411,7 +518,7 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
 template <bool MIXED>
 void *kernel_for(int level) {
   switch (level) {
-    case 1: return (void *)citest_kernel<1, MIXED>;
+    case 1: return (void *)citest_l1_kernel<MIXED>;
     case 2: return (void *)citest_kernel<2, MIXED>;
     case 3: return (void *)citest_kernel<3, MIXED>;
     case 4: return (void *)citest_kernel<4, MIXED>;
@@ -440,8 +547,8 @@ hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
   return HPC_OK;
 }
 
-hpc_status launch_finalize_records(const Launch &L, cudaStream_t s) {
-  finalize_records_kernel<<<152 * 2, 128, 0, s>>>(L);
+hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s) {
+  finalize_records_kernel<<<152 * 2, 128, 0, s>>>(inst, count);
   HPC_LAUNCH_CHECK("finalize_records_kernel");
   return HPC_OK;
 }

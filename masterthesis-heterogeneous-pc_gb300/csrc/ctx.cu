@@ -233,10 +233,7 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += queue ? 5 : 4;
-  if (c->opts.precision != HPC_PREC_FP64) {
-    if ((s = launch_finalize_records(L, c->stream)) != HPC_OK) return s;
-    c->timings.launches += 1;
-  }
+  c->records_final = false;
   return HPC_OK;
 }
 
@@ -1020,6 +1017,24 @@ hpc_status hpc_batch_edge_count(hpc_ctx *c, int idx, int64_t *edges) {
 
 hpc_status hpc_edge_count(hpc_ctx *c, int64_t *edges) { return hpc_batch_edge_count(c, 0, edges); }
 
+// FP64 p-values of the FP32-decided removals of every instance, once per run.
+static hpc_status finalize_records(hpc_ctx *c) {
+  if (c->records_final || !c->recs) return HPC_OK;
+  hpc_status s;
+  if ((s = launch_finalize_records(c->inst, c->count, c->stream)) != HPC_OK) return s;
+  c->timings.launches += 1;
+  HPC_CUDA(cudaMemcpyAsync(c->gctr_host, c->gctr, sizeof(DevGlobal) * (size_t)c->count, cudaMemcpyDeviceToHost,
+                           c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  c->records_final = true;
+  for (int b = 0; b < c->count; ++b)
+    if (c->gctr_host[b].err & kErrBandViolation) {
+      set_error("instance %d: an FP32 removal was not confirmed in FP64 (error bound violated)", b);
+      return HPC_ERR_NUMERIC;
+    }
+  return HPC_OK;
+}
+
 hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *out, int64_t cap, int64_t *count) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
@@ -1028,6 +1043,7 @@ hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *
     set_error("null count pointer");
     return HPC_ERR_INVALID_ARG;
   }
+  if ((s = finalize_records(c)) != HPC_OK) return s;
   DevGlobal g{};
   HPC_CUDA(cudaMemcpyAsync(&g, c->gctr + idx, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));

@@ -68,6 +68,7 @@ constexpr int kErrRecOverflow = 1;
 constexpr int kErrWorkOverflow = 2;
 constexpr int kErrCsrOverflow = 4;
 constexpr int kErrTimeout = 8;
+constexpr int kErrBandViolation = 16;
 
 // One deferred FP64 re-test: edge (i, j) of instance `inst` given ids[0..level),
 // or a level-0 pair (i > j).
@@ -182,7 +183,7 @@ hpc_status launch_fill_csr(const Launch &L, long long total_rows, cudaStream_t s
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
 hpc_status launch_citest(const Launch &L, int precision, int grid, cudaStream_t s);
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
-hpc_status launch_finalize_records(const Launch &L, cudaStream_t s);
+hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
 int citest_grid(int precision, int level, int device);
 
 // per-instance host bookkeeping
@@ -259,4 +260,5 @@ struct hpc_ctx {
   hpc_timings timings{};
   bool have_cor = false;
   int next_level = 0;
+  bool records_final = true;     // the records' FP32 p-values have been evaluated in FP64
 };
