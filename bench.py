@@ -254,18 +254,23 @@ class ClockSampler:
 
 
 def citest_bytes(adjs, levels_stats, lane_bytes=4):
-    """Algorithmic bytes of the CI-test kernel per level: l(l+3)/2 correlation entries
-    per executed test, plus (2 + d_i) words per directed edge that has tests."""
+    """Algorithmic bytes of the level kernel per level: the snapshot rebuild (the p x W
+    adjacency words read; neighbour ids, degrees written; degrees read back and the
+    (p + 1) 8-byte row test counts written by the scan) plus, for the CI tests,
+    l(l+3)/2 correlation entries per executed test and (2 + d_i) words per directed
+    edge that has tests."""
     out = []
     for st, adj in zip(levels_stats, adjs):
         l = st["level"]
         if l == 0 or adj is None:
             out.append(0)
             continue
+        p = adj.shape[0]
         d = adj.sum(1).astype(np.int64)
         has = d - 1 >= l
         edge_bytes = int((d[has] * (2 + d[has])).sum()) * 4
-        out.append(st["executed_tests"] * lane_bytes * l * (l + 3) // 2 + edge_bytes)
+        rebuild = (p * ((p + 31) // 32) + int(d.sum()) + 2 * p) * 4 + (p + 1) * 8
+        out.append(st["executed_tests"] * lane_bytes * l * (l + 3) // 2 + edge_bytes + rebuild)
     return out
 
 
@@ -498,10 +503,10 @@ def main():
     l1_ms = float(test_ms[1])
     achieved_gbs = (bytes_l[1] / 1e9) / (l1_ms / 1e3) if l1_ms > 0 else 0.0
     tests_per_step = sum(s_["executed_tests"] for s_ in stats)
-    roofline = {"kernel": "citest_l1_kernel (level 1, mixed)", "bound": "hbm",
+    roofline = {"kernel": "level_kernel<1> (level 1: rebuild, scan, CI tests; mixed)", "bound": "hbm",
                 "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (hbm_gbs)",
-                "traffic": traffic_from_profile("citest_l1_kernel"),
+                "traffic": traffic_from_profile("level_kernel_l1"),
                 "algorithmic_bytes_per_launch": int(bytes_l[1]), "launch_ms": l1_ms,
                 "all_levels": {"algorithmic_bytes": int(sum(bytes_l)), "kernel_ms": float(sum(test_ms[1:len(lst)]))}}
     gram_flops = n * p * (p + 1)  # FP64 Gram, upper triangle incl. diagonal

@@ -193,6 +193,8 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.lc = c->lc + level;
   L.rq = c->rq;
   L.rq_cap = c->rq_cap;
+  L.seg_prefix = c->prefixes + 3 * (c->count + 1);
+  L.seg = c->seg + (size_t)level * c->total_segs;
   return L;
 }
 
@@ -225,14 +227,12 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
     c->timings.launches += queue ? 5 : 4;
     return HPC_OK;
   }
-  if ((s = launch_degrees(L, c->total_rows, c->stream)) != HPC_OK) return s;
-  if ((s = launch_scan(L, c->stream)) != HPC_OK) return s;
-  if ((s = launch_fill_csr(L, c->total_rows, c->stream)) != HPC_OK) return s;
+  // snapshot rebuild, test-count scan and CI tests in one launch
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  if ((s = launch_citest(L, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
+  if ((s = launch_level(L, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
-  c->timings.launches += queue ? 5 : 4;
+  c->timings.launches += queue ? 2 : 1;
   c->records_final = false;
   return HPC_OK;
 }
@@ -373,6 +373,8 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
   hpc_status s;
   auto enqueue_all = [&](bool timed) -> hpc_status {
     HPC_CUDA(cudaMemsetAsync(c->lc + first, 0, sizeof(LaunchCounters) * (size_t)(last - first + 1), c->stream));
+    HPC_CUDA(cudaMemsetAsync(c->seg + (size_t)first * c->total_segs, 0,
+                             sizeof(SegAgg) * (size_t)c->total_segs * (size_t)(last - first + 1), c->stream));
     for (int l = first; l <= last; ++l)
       if ((s = enqueue_level(c, l, timed)) != HPC_OK) return s;
     return HPC_OK;
@@ -670,6 +672,7 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   b += n * p * 4;                                                  // observation staging
   b += p * W * 4 + p * p;                                          // adjacency bits + bytes
   b += (p + 1) * (4 + 4 + 8);                                      // deg, rowptr, row_work
+  b += (int64_t)(HPC_MAX_LEVEL + 1) * ((p + kSegRows - 1) / kSegRows) * (int64_t)sizeof(SegAgg);  // scan sums
   // neighbour lists and records are sized after level 0; budget an average degree of 64
   const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
   b += 2 * e * 4 + e * (int64_t)sizeof(hpc_sepset_record);
@@ -728,6 +731,7 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->inst);
   dev_free(c->prefixes);
   dev_free(c->work_prefix);
+  dev_free(c->seg);
   dev_free(c->meta);
   dev_free(c->meta_denom);
   delete[] c->ctr_host;
@@ -1158,7 +1162,8 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   c->device = o.device;
   c->ih.resize((size_t)count);
   long long cor = 0, z = 0, adj = 0, rows = 0, tc = 0, words = 0, tiles = 0, nrows = 0;
-  std::vector<long long> pre((size_t)(3 * (count + 1)), 0);
+  std::vector<long long> pre((size_t)(4 * (count + 1)), 0);
+  long long segs = 0;
   for (int b = 0; b < count; ++b) {
     InstHost &h = c->ih[b];
     h.p = p[b];
@@ -1184,10 +1189,14 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
     tiles += (long long)h.W * (h.W + 1) / 2;
     pre[2 * (count + 1) + b] = nrows;
     nrows += h.p;
+    pre[3 * (count + 1) + b] = segs;
+    segs += (h.p + kSegRows - 1) / kSegRows;
   }
   pre[count] = words;
   pre[(count + 1) + count] = tiles;
   pre[2 * (count + 1) + count] = nrows;
+  pre[3 * (count + 1) + count] = segs;
+  c->total_segs = segs;
   c->total_words = words;
   c->total_tiles = tiles;
   c->total_rows = nrows;
@@ -1229,6 +1238,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   if ((s = dev_alloc(&c->inst, count, "instance table")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->prefixes, (int64_t)pre.size(), "prefixes")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->work_prefix, (int64_t)kLevels * (count + 1), "work prefixes")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->seg, (int64_t)kLevels * segs, "segment sums")) != HPC_OK) return fail(s);
   c->ctr_host = new DevCounters[(size_t)count * kLevels];
   c->gctr_host = new DevGlobal[(size_t)count];
   if (cudaMemcpyAsync(c->prefixes, pre.data(), sizeof(long long) * pre.size(), cudaMemcpyHostToDevice, c->stream) !=

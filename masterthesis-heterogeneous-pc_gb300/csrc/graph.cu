@@ -9,12 +9,11 @@
 // kept bits are written for the lower triangle and then mirrored by 32 x 32
 // bit-tile transposes.
 //
-// degrees + scan + fill_csr replace compactCUTiled (src/independence/compact.cu:4-89):
-// per-row popcounts; one block per instance scans its rows for the CSR offsets and
-// for the number of CI tests each row contributes at the level (d_i * C(d_i - 1, l));
-// the last scan block to finish forms the prefix of the instances' test counts that
-// the CI-test kernel flattens over; a warp per row then writes the ascending
-// neighbour ids.
+// degrees + scan after level 0: per-row popcounts, then one block per instance scans
+// the degrees into the offsets of each row's slot in the neighbour-list buffer. The
+// slots keep these sizes for the rest of the skeleton (degrees only fall); the level
+// kernels of levels >= 1 refill them and count their CI tests themselves
+// (rebuild.cuh).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -243,36 +242,6 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(Launch L) {
   }
 }
 
-__global__ void fill_csr_kernel(Launch L, long long total) {
-  const int lane = threadIdx.x & 31;
-  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long t = warp; t < total; t += nwarps) {
-    const int b = find_inst(L.row_prefix, L.count, t);
-    const Inst &I = L.inst[b];
-    if ((long long)I.ctr[L.level].edges2 > I.colidx_cap) continue;  // flagged by the scan
-    const int64_t i = t - L.row_prefix[b];
-    int base = I.rowptr[i];
-    for (int w0 = 0; w0 < I.W; w0 += 32) {
-      const int w = w0 + lane;
-      uint32_t word = w < I.W ? I.adj[i * I.W + w] : 0u;
-      const int c = __popc(word);
-      int incl = c;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-      }
-      int pos = base + incl - c;
-      while (word) {
-        const int bit = __ffs(word) - 1;
-        I.colidx[pos++] = w * 32 + bit;
-        word &= word - 1;
-      }
-      base += __shfl_sync(0xffffffffu, incl, 31);
-    }
-  }
-}
-
 // p x p bytes (1 = edge) from the bitmask, 4 bytes per thread
 __global__ void expand_adjacency_kernel(const uint32_t *__restrict__ adj, int64_t p, int W, uint8_t *__restrict__ out) {
   const int64_t total = p * p;
@@ -316,12 +285,6 @@ hpc_status launch_degrees(const Launch &L, long long total, cudaStream_t s) {
 hpc_status launch_scan(const Launch &L, cudaStream_t s) {
   scan_kernel<<<L.count, kScanThreads, 0, s>>>(L);
   HPC_LAUNCH_CHECK("scan_kernel");
-  return HPC_OK;
-}
-
-hpc_status launch_fill_csr(const Launch &L, long long total, cudaStream_t s) {
-  fill_csr_kernel<<<blocks_for(total, 8), 256, 0, s>>>(L, total);
-  HPC_LAUNCH_CHECK("fill_csr_kernel");
   return HPC_OK;
 }
 

@@ -62,6 +62,17 @@ struct LaunchCounters {
   unsigned long long tile_next;    // CI-test work-queue head
   unsigned long long rq_count;     // FP64 re-tests queued
   unsigned int scan_done;          // scan blocks finished (the last one forms the prefix)
+  unsigned int bar;                // grid-barrier arrivals of the level kernel
+};
+// Rows per segment of the level kernel's test-count scan, and the per-segment sums
+// the rebuild phase accumulates (one slice of segments per level).
+constexpr int kSegRows = 256;
+struct SegAgg {
+  unsigned long long deg;   // sum of degrees
+  unsigned long long work;  // sum of tests per row
+  int max_deg;
+  int rows;                 // rows with tests
+  int over;                 // a row's test count does not fit
   int pad;
 };
 constexpr int kErrRecOverflow = 1;
@@ -117,6 +128,8 @@ struct Launch {
   LaunchCounters *lc;               // this level's
   RetestItem *rq;                   // deferred FP64 re-tests
   long long rq_cap;
+  const long long *seg_prefix;      // scan segments  sum ceil(p / kSegRows) (count + 1)
+  SegAgg *seg;                      // this level's segment sums (zeroed before the level)
 };
 
 __device__ __forceinline__ int find_inst(const long long *prefix, int count, long long t) {
@@ -179,9 +192,9 @@ hpc_status launch_level0(const Launch &L, long long total_words, cudaStream_t s)
 hpc_status launch_mirror(const Launch &L, long long total_tiles, cudaStream_t s);
 hpc_status launch_degrees(const Launch &L, long long total_rows, cudaStream_t s);
 hpc_status launch_scan(const Launch &L, cudaStream_t s);
-hpc_status launch_fill_csr(const Launch &L, long long total_rows, cudaStream_t s);
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
-hpc_status launch_citest(const Launch &L, int precision, int grid, cudaStream_t s);
+// Level l >= 1 in one cooperative launch: snapshot rebuild, test-count scan, CI tests.
+hpc_status launch_level(const Launch &L, int precision, int grid, cudaStream_t s);
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
 int citest_grid(int precision, int level, int device);
@@ -235,7 +248,9 @@ struct hpc_ctx {
   hpc::LaunchCounters *lc = nullptr;     // HPC_MAX_LEVEL + 1
   hpc::Inst *inst = nullptr;             // device table (count)
   std::vector<hpc::Inst> inst_host;      // the table last written
-  long long *prefixes = nullptr;         // device: word, tile, row prefixes (3 x (count + 1))
+  long long *prefixes = nullptr;         // device: word, tile, row, segment prefixes (4 x (count + 1))
+  hpc::SegAgg *seg = nullptr;            // device: (HPC_MAX_LEVEL + 1) x total_segs
+  long long total_segs = 0;
   unsigned long long *work_prefix = nullptr;  // device: (HPC_MAX_LEVEL + 1) x (count + 1)
   long long *meta = nullptr;             // device: correlation metadata arrays
   double *meta_denom = nullptr;

@@ -1,0 +1,277 @@
+// The first two phases of a level kernel (levels >= 1), separated by grid barriers of
+// a cooperative launch:
+//
+//   rebuild  every warp takes a contiguous run of rows (flattened over the instances),
+//            counts each row's live bits (the snapshot degree d_i) and writes its
+//            neighbour ids, ascending, into the row's fixed slot of the neighbour-list
+//            buffer -- slots are sized by the degrees after level 0 (degrees only
+//            fall), so no per-level offsets are needed for the lists; the per-segment
+//            sums of d_i and of the row test counts d_i * C(d_i - 1, l) go to SegAgg.
+//   scan     one block per segment of kSegRows rows: the exclusive prefix of the row
+//            test counts (the CI-test phase's flattened index), each instance's level
+//            summary, and (one block) the prefix of the instances' test counts.
+//
+// Together they replace compactCUTiled (src/independence/compact.cu:4-89), which
+// rebuilds the reference's dense adj_compact rows with one thread block per row.
+#pragma once
+#include "internal.cuh"
+#include "stats.cuh"
+
+namespace hpc {
+
+constexpr int kLevelThreads = 256;
+static_assert(kLevelThreads == kSegRows, "one scan thread per segment row");
+// a row contributing more CI tests than this is reported as a work overflow
+constexpr unsigned long long kRowWorkLimit = 1ull << 40;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier of a cooperative launch (all blocks co-resident). `epoch` counts
+// the barriers this block has passed. The wait is bounded (2 s of %globaltimer): on
+// expiry the kernel's error flag is set and false is returned; the caller returns.
+__device__ __forceinline__ bool grid_barrier(const Launch &L, unsigned int &epoch) {
+  __shared__ int s_ok;
+  __syncthreads();
+  ++epoch;
+  if (threadIdx.x == 0) {
+    const unsigned int target = epoch * gridDim.x;
+    __threadfence();
+    atomicAdd(&L.lc->bar, 1u);
+    int ok = 1;
+    const unsigned long long t0 = globaltimer_ns();
+    while (ld_acquire_u32(&L.lc->bar) < target) {
+      if (globaltimer_ns() - t0 > 2000000000ull) {
+        ok = 0;
+        atomicOr(&L.inst[0].g->err, kErrTimeout);
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// tests a row of degree d contributes at level l; sets *over when beyond the limit
+__device__ __forceinline__ unsigned long long row_tests(int d, int level, int *over) {
+  if (d - 1 < level) return 0ull;
+  const unsigned long long c = binom_sat(d - 1, level);
+  if (c >= kRowWorkLimit || (unsigned long long)d * c >= kRowWorkLimit) {
+    *over = 1;
+    return 0ull;
+  }
+  return (unsigned long long)d * c;
+}
+
+__device__ __forceinline__ bool csr_overflow(const Inst &I) { return (long long)I.rowptr[I.p] > I.colidx_cap; }
+
+__device__ __forceinline__ void rebuild_phase(const Launch &L) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long R = L.row_prefix[L.count];
+  const long long per = (R + nw - 1) / nw;
+  long long t = gw * per;
+  const long long tend = t + per < R ? t + per : R;
+  const int level = L.level;
+  long long cur = -1;
+  unsigned long long a_deg = 0, a_work = 0;
+  int a_max = 0, a_rows = 0, a_over = 0;
+  auto flush = [&]() {
+    if (cur >= 0 && lane == 0) {
+      SegAgg &S = L.seg[cur];
+      if (a_deg) atomicAdd(&S.deg, a_deg);
+      if (a_work) atomicAdd(&S.work, a_work);
+      if (a_max) atomicMax(&S.max_deg, a_max);
+      if (a_rows) atomicAdd(&S.rows, a_rows);
+      if (a_over) atomicOr(&S.over, 1);
+    }
+    a_deg = a_work = 0;
+    a_max = a_rows = a_over = 0;
+  };
+  int b = -1;
+  const Inst *I = nullptr;
+  bool skip = false;
+  for (; t < tend; ++t) {
+    if (b < 0 || t >= L.row_prefix[b + 1]) {
+      b = find_inst(L.row_prefix, L.count, t);
+      I = L.inst + b;
+      skip = csr_overflow(*I);  // flagged by the scan phase; the host resizes and reruns
+    }
+    const int64_t i = t - L.row_prefix[b];
+    const long long g = L.seg_prefix[b] + i / kSegRows;
+    if (g != cur) {
+      flush();
+      cur = g;
+    }
+    if (skip) continue;
+    const uint32_t *words = I->adj + i * I->W;
+    int *out = I->colidx + I->rowptr[i];
+    int cnt = 0;
+    for (int w0 = 0; w0 < I->W; w0 += 32) {
+      const int w = w0 + lane;
+      uint32_t word = w < I->W ? words[w] : 0u;
+      const int c = __popc(word);
+      int incl = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      int pos = cnt + incl - c;
+      while (word) {
+        const int bit = __ffs(word) - 1;
+        out[pos++] = w * 32 + bit;
+        word &= word - 1;
+      }
+      cnt += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) I->deg[i] = cnt;
+    a_deg += (unsigned long long)cnt;
+    a_max = max(a_max, cnt);
+    const unsigned long long w = row_tests(cnt, level, &a_over);
+    a_work += w;
+    a_rows += w ? 1 : 0;
+  }
+  flush();
+}
+
+// block-wide exclusive scan of one value per thread; *total receives the sum
+__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long *total) {
+  __shared__ unsigned long long s_warp[kLevelThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += x;
+  }
+  if (lane == 31) s_warp[wid] = incl;
+  __syncthreads();
+  unsigned long long before = 0, all = 0;
+#pragma unroll
+  for (int q = 0; q < kLevelThreads / 32; ++q) {
+    const unsigned long long x = s_warp[q];
+    if (q < wid) before += x;
+    all += x;
+  }
+  __syncthreads();
+  *total = all;
+  return before + incl - v;
+}
+
+struct InstSums {
+  unsigned long long deg, work, base;
+  int max_deg, rows, over;
+};
+
+// sums over the segments of instance b (one warp); base = work of segments before g
+__device__ __forceinline__ InstSums warp_inst_sums(const Launch &L, int b, long long g) {
+  const int lane = threadIdx.x & 31;
+  InstSums r{0, 0, 0, 0, 0, 0};
+  for (long long q = L.seg_prefix[b] + lane; q < L.seg_prefix[b + 1]; q += 32) {
+    const SegAgg *S = L.seg + q;
+    const unsigned long long wk = __ldcg(&S->work);
+    r.deg += __ldcg(&S->deg);
+    r.work += wk;
+    if (q < g) r.base += wk;
+    r.max_deg = max(r.max_deg, __ldcg(&S->max_deg));
+    r.rows += __ldcg(&S->rows);
+    r.over |= __ldcg(&S->over);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    r.deg += __shfl_xor_sync(0xffffffffu, r.deg, o);
+    r.work += __shfl_xor_sync(0xffffffffu, r.work, o);
+    r.base += __shfl_xor_sync(0xffffffffu, r.base, o);
+    r.max_deg = max(r.max_deg, __shfl_xor_sync(0xffffffffu, r.max_deg, o));
+    r.rows += __shfl_xor_sync(0xffffffffu, r.rows, o);
+    r.over |= __shfl_xor_sync(0xffffffffu, r.over, o);
+  }
+  return r;
+}
+
+__device__ __forceinline__ void scan_phase(const Launch &L) {
+  __shared__ InstSums s_sum;
+  __shared__ int s_bad;
+  const int level = L.level;
+  const long long G = L.seg_prefix[L.count];
+  // the prefix of the instances' test counts, by the last block (the first blocks
+  // take the segments)
+  if (blockIdx.x == gridDim.x - 1) {
+    __shared__ unsigned long long s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < L.count; c0 += kLevelThreads) {
+      const int b = c0 + (int)threadIdx.x;
+      unsigned long long tot = 0;
+      if (b < L.count) {
+        int over = 0;
+        for (long long q = L.seg_prefix[b]; q < L.seg_prefix[b + 1]; ++q) {
+          tot += __ldcg(&L.seg[q].work);
+          over |= __ldcg(&L.seg[q].over);
+        }
+        if (over || csr_overflow(L.inst[b])) tot = 0;
+      }
+      unsigned long long all;
+      const unsigned long long ex = block_exclusive_scan(tot, &all);
+      if (b < L.count) L.work_prefix[b] = s_carry + ex;
+      __syncthreads();
+      if (threadIdx.x == 0) s_carry += all;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) L.work_prefix[L.count] = s_carry;
+  }
+  for (long long g = blockIdx.x; g < G; g += gridDim.x) {
+    const int b = find_inst(L.seg_prefix, L.count, g);
+    const Inst &I = L.inst[b];
+    if (threadIdx.x < 32) {
+      const InstSums r = warp_inst_sums(L, b, g);
+      if (threadIdx.x == 0) {
+        s_sum = r;
+        s_bad = (r.over || csr_overflow(I)) ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    const bool bad = s_bad != 0;
+    const int64_t r = (g - L.seg_prefix[b]) * kSegRows + threadIdx.x;
+    const bool valid = r < I.p;
+    int over = 0;
+    const int d = valid && !bad ? __ldcg(I.deg + r) : 0;
+    const unsigned long long w = row_tests(d, level, &over);
+    unsigned long long all;
+    const unsigned long long ex = block_exclusive_scan(w, &all);
+    if (valid && !bad) I.row_work[r] = s_sum.base + ex;
+    if (threadIdx.x == 0 && g == L.seg_prefix[b + 1] - 1) {
+      // last segment of the instance: its level summary
+      DevCounters &C = I.ctr[level];
+      if (!bad) I.row_work[I.p] = s_sum.work;
+      if (s_sum.over) atomicOr(&I.g->err, kErrWorkOverflow);
+      if (csr_overflow(I)) atomicOr(&I.g->err, kErrCsrOverflow);
+      C.edges2 = s_sum.deg;
+      C.work_total = bad ? 0ull : s_sum.work;
+      C.max_deg = s_sum.max_deg;
+      C.rows = s_sum.rows;
+      C.tests = 0;
+      C.retests = 0;
+      C.deleted = 0;
+      C.band_violations = 0;
+      C.rec_begin = *(volatile unsigned long long *)&I.g->rec_count;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace hpc
