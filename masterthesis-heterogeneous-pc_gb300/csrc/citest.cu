@@ -188,59 +188,79 @@ __device__ __noinline__ bool exact_remove(const Inst &I, int64_t i, int64_t j, c
   return decide_of_r(I, r, nan_p, pv);
 }
 
-// FP32 test. Returns 1 = remove, 0 = keep, 2 = undecided (re-test in FP64); *rr_out
-// receives |r|.
+// exact_remove from the FP64 matrix with the factorisation in registers: every entry
+// gathered in one round of loads, rsqrt in place of divisions and square roots (a
+// few ulps, far inside decide_of_r's guard band). Tests the Cholesky path does not
+// accept (an ill-conditioned block) and instances without an FP64 matrix go to
+// exact_remove.
 template <int LA>
-__device__ __forceinline__ int test_f32(const Inst &I, int64_t i, int64_t j, const int *ids, int l, float *rr_out) {
-  const float *__restrict__ C = I.cor32;
+__device__ __noinline__ bool exact_remove_fast(const Inst &I, int64_t i, int64_t j, const int *ids, int l, double *pv) {
+  const double *C = I.cor64;
+  if (!C) return exact_remove<LA>(I, i, j, ids, l, pv);
   const int64_t p = I.p;
-  const float rij = __ldg(C + i * p + j);
-  float Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1];
-  float invd[LA], wx[LA], wy[LA];
-  float dmin = 1.0f;
-  float sx = 0.f, sy = 0.f, sxy = 0.f;
+  const double rij = C[i * p + j];
+  double gx[LA], gy[LA], gs[LA * (LA - 1) / 2 > 0 ? LA * (LA - 1) / 2 : 1];
 #pragma unroll
-  for (int r = 0; r < LA; ++r) {
+  for (int r = 0; r < LA; ++r)
     if (r < l) {
-      const int idr = ids[r];
-      float vx = __ldg(C + i * p + idr);
-      float vy = __ldg(C + j * p + idr);
-      float d = 1.0f;
+      const int64_t idr = ids[r];
+      gx[r] = C[i * p + idr];
+      gy[r] = C[j * p + idr];
 #pragma unroll
-      for (int c = 0; c < LA; ++c) {
+      for (int c = 0; c < LA; ++c)
+        if (c < r) gs[r * (r - 1) / 2 + c] = C[(int64_t)ids[c] * p + idr];
+    }
+  if (l == 1) {  // the closed form, as pval_l1_64
+    const double x1 = rij, x2 = gx[0], x3 = gy[0];
+    if (isnan(x1) || isnan(x2) || isnan(x3)) return decide_of_r(I, 0.0, true, pv);
+    return decide_of_r(I, (x1 - x2 * x3) / sqrt((1.0 - x3 * x3) * (1.0 - x2 * x2)), false, pv);
+  }
+  bool nan_in = isnan(rij);
+#pragma unroll
+  for (int r = 0; r < LA; ++r)
+    if (r < l) {
+      nan_in |= isnan(gx[r]) || isnan(gy[r]);
+#pragma unroll
+      for (int c = 0; c < LA; ++c)
+        if (c < r) nan_in |= isnan(gs[r * (r - 1) / 2 + c]);
+    }
+  if (nan_in) return decide_of_r(I, 0.0, true, pv);
+  double Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1], inv[LA], wx[LA], wy[LA];
+  bool ok = true;
+#pragma unroll
+  for (int r = 0; r < LA; ++r)
+    if (r < l) {
+      double vx = gx[r], vy = gy[r], d = 1.0;
+#pragma unroll
+      for (int c = 0; c < LA; ++c)
         if (c < r) {
-          float v = __ldg(C + (int64_t)ids[c] * p + idr);
+          double v = gs[r * (r - 1) / 2 + c];
 #pragma unroll
           for (int q = 0; q < LA; ++q)
             if (q < c) v -= Lm[r * (r + 1) / 2 + q] * Lm[c * (c + 1) / 2 + q];
-          v *= invd[c];
+          v *= inv[c];
           Lm[r * (r + 1) / 2 + c] = v;
           d -= v * v;
           vx -= v * wx[c];
           vy -= v * wy[c];
         }
-      }
-      dmin = fminf(dmin, d);
-      const float id = rsqrtf(fmaxf(d, 1e-30f));
-      invd[r] = id;
-      wx[r] = vx * id;
-      wy[r] = vy * id;
-      sx += wx[r] * wx[r];
-      sy += wy[r] * wy[r];
-      sxy += wx[r] * wy[r];
+      ok = ok && d > 1e-10;
+      inv[r] = rsqrt(fmax(d, 1e-300));
+      wx[r] = vx * inv[r];
+      wy[r] = vy * inv[r];
     }
+  if (ok) {
+    double ax = 1.0, ay = 1.0, b = rij;
+#pragma unroll
+    for (int q = 0; q < LA; ++q)
+      if (q < l) {
+        ax -= wx[q] * wx[q];
+        ay -= wy[q] * wy[q];
+        b -= wx[q] * wy[q];
+      }
+    if (ax > 1e-10 && ay > 1e-10) return decide_of_r(I, b * rsqrt(ax * ay), false, pv);
   }
-  const float ax = 1.0f - sx, ay = 1.0f - sy;
-  const float cond = fminf(dmin, fminf(ax, ay));
-  if (!(cond > 1e-3f)) return 2;
-  // |r| = |b| / sqrt(ax * ay) against r_c: no transcendental on this path
-  const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
-  *rr_out = rr;
-  const float dist = rr - I.r_c;
-  const float ke = I.ke_a + (float)(l + 2) * I.ke_b;
-  const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
-  if (!(fabsf(dist) > band)) return 2;  // inside the band, or NaN
-  return dist < 0.0f ? 1 : 0;
+  return exact_remove<LA>(I, i, j, ids, l, pv);  // pinv semantics
 }
 
 // Running FP32 factorisation of the conditioning block of one lane's current test,
@@ -252,24 +272,43 @@ struct Fact {
   float invd[LA], piv[LA], wx[LA], wy[LA];
 };
 
-// FP32 test refactoring rows ci..l-1 only (rows below ci are still valid for the
-// current i, j and the unchanged first ci positions of S). Same decision as test_f32.
+// FP32 test of (i, j | ids). The partial correlation comes from a Cholesky
+// factorisation of the S block and forward solves for r_iS and r_jS:
+//   r = (r_ij - w_i . w_j) / sqrt((1 - |w_i|^2)(1 - |w_j|^2)),  w = L_S^-1 r_S;
+// only rows ci..l-1 are refactored (rows below ci are still valid for the current
+// i, j and the unchanged first ci members of S). Returns 1 = remove, 0 = keep,
+// 2 = undecided (re-test in FP64): |r| is compared with r_c outside a band of
+// margin_r + 8 * ke(l) / smallest pivot. *rr_out receives |r|.
 template <int LA>
 __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j, const int *ids, int l, int ci,
                                             Fact<LA> &F, float *rr_out) {
   const float *__restrict__ C = I.cor32;
   const int64_t p = I.p;
+  // all entries the changed rows need, gathered before any arithmetic (one round of
+  // independent loads instead of one per factor row)
+  float gx[LA], gy[LA], gs[LA * (LA - 1) / 2 > 0 ? LA * (LA - 1) / 2 : 1];
 #pragma unroll
   for (int r = 0; r < LA; ++r) {
     if (r >= ci && r < l) {
       const int idr = ids[r];
-      float vx = __ldg(C + i * p + idr);
-      float vy = __ldg(C + j * p + idr);
+      gx[r] = __ldg(C + i * p + idr);
+      gy[r] = __ldg(C + j * p + idr);
+#pragma unroll
+      for (int c = 0; c < LA; ++c)
+        if (c < r) gs[r * (r - 1) / 2 + c] = __ldg(C + (int64_t)ids[c] * p + idr);
+    }
+  }
+  const float rij = __ldg(C + i * p + j);
+#pragma unroll
+  for (int r = 0; r < LA; ++r) {
+    if (r >= ci && r < l) {
+      float vx = gx[r];
+      float vy = gy[r];
       float d = 1.0f;
 #pragma unroll
       for (int c = 0; c < LA; ++c) {
         if (c < r) {
-          float v = __ldg(C + (int64_t)ids[c] * p + idr);
+          float v = gs[r * (r - 1) / 2 + c];
 #pragma unroll
           for (int q = 0; q < LA; ++q)
             if (q < c) v -= F.Lm[r * (r + 1) / 2 + q] * F.Lm[c * (c + 1) / 2 + q];
@@ -287,7 +326,8 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
       F.wy[r] = vy * id;
     }
   }
-  // the sums in test_f32's order, so that both give the same decision
+  // the sums in row order, whatever ci was, so that the decision does not depend on
+  // the walk
   float sx = 0.f, sy = 0.f, sxy = 0.f, dmin = 1.f;
 #pragma unroll
   for (int r = 0; r < LA; ++r)
@@ -297,7 +337,6 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
       sy += F.wy[r] * F.wy[r];
       sxy += F.wx[r] * F.wy[r];
     }
-  const float rij = __ldg(C + i * p + j);
   const float ax = 1.0f - sx, ay = 1.0f - sy;
   const float cond = fminf(dmin, fminf(ax, ay));
   if (!(cond > 1e-3f)) return 2;
@@ -318,6 +357,19 @@ __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, 
     if (row_work[mid] <= t) lo = mid; else hi = mid;
   }
   return lo;
+}
+
+// The row offsets of a single-instance level copied into shared memory by the whole
+// block (one round of coalesced loads), so that every row search of the CI tests
+// stays on the SM; null when they do not fit (or for several instances).
+constexpr int kRowCache = 5120;
+__device__ __forceinline__ const unsigned long long *cache_row_work(const Launch &L, unsigned long long *smem) {
+  if (!smem || L.count != 1) return nullptr;
+  const Inst &I = L.inst[0];
+  if (I.p + 1 > kRowCache) return nullptr;
+  for (int64_t r = threadIdx.x; r <= I.p; r += blockDim.x) smem[r] = __ldcg(I.row_work + r);
+  __syncthreads();
+  return smem;
 }
 
 // Row of a warp-uniform position t: a 32-ary search (coalesced probes, two or three
@@ -474,7 +526,7 @@ __device__ __forceinline__ bool push_retest(const Launch &L, int b, int64_t i, i
 }
 
 template <int LT, bool MIXED>
-__device__ __forceinline__ void tests_generic(const Launch &L) {
+__device__ __forceinline__ void tests_generic(const Launch &L, unsigned long long *rw_smem) {
   constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
   const int l = LT > 0 ? LT : L.level;
   const int level = L.level;
@@ -487,6 +539,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L) {
   __syncwarp();
   const unsigned long long total = L.work_prefix[L.count];
   if (total == 0) return;
+  const unsigned long long *rw_c = cache_row_work(L, rw_smem);
   // tests per lane per tile: about four tiles per lane of the grid, 1..64
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
   const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
@@ -506,24 +559,24 @@ __device__ __forceinline__ void tests_generic(const Launch &L) {
     int b = find_inst_u(L.work_prefix, L.count, t0);
     const Inst *I = L.inst + b;
     unsigned long long base_t = L.work_prefix[b];
-    const int64_t i0 = warp_find_row(I->row_work, I->p, t0 - base_t);
+    const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
     const bool active = t < tend;
     const bool same = t < L.work_prefix[b + 1];
-    int64_t i = lane_find_row(I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
+    int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
     if (active && !same) {  // the tile runs into the next instance
       b = find_inst_u(L.work_prefix, L.count, t);
       I = L.inst + b;
       base_t = L.work_prefix[b];
-      i = find_row(I->row_work, I->p, t - base_t);
+      i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
     }
     if (active) {
       int d = I->deg[i];
-      unsigned long long c = binom_sat(d - 1, l);
-      const unsigned long long off = t - base_t - I->row_work[i];
+      unsigned long long c = binom_fast(d - 1, l);
+      const unsigned long long off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
       int s = (int)(off / c);
       unsigned long long rank = off - (unsigned long long)s * c;
       int base = I->rowptr[i];
-      unrank_lex(rank, l, d - 1, pos);
+      unrank_lex_fast(rank, l, d - 1, pos);
       int64_t j = I->colidx[base + s];
       bool alive = live_bit(I->adj, I->W, i, j);
       unsigned tested_edge = 0;
@@ -549,7 +602,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L) {
             pv = -1.0 - (double)rr;
           } else if (res == 2) {
             if (MIXED) ++retests;
-            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, ids, l))) rm = exact_remove<LA>(*I, i, j, ids, l, &pv);
+            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, ids, l))) rm = exact_remove_fast<LA>(*I, i, j, ids, l, &pv);
           }
           if (rm) {
             if (claim_edge(*I, i, j)) push_pending<LA>(pend, np, *I, b, level, i, j, ids, l, pv);
@@ -566,9 +619,9 @@ __device__ __forceinline__ void tests_generic(const Launch &L) {
               I = L.inst + b;
               base_t = L.work_prefix[b];
             }
-            i = find_row(I->row_work, I->p, t - base_t);
+            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
             d = I->deg[i];
-            c = binom_sat(d - 1, l);
+            c = binom_fast(d - 1, l);
             base = I->rowptr[i];
             s = 0;
           }
@@ -605,10 +658,10 @@ __device__ __forceinline__ void tests_generic(const Launch &L) {
 // its tile, so the 32 lanes work on consecutive conditioning variables of the same
 // edge (i, j): their reads of the neighbour list and of row i of cor32 fall into few
 // cache lines and stay in L1 across the edges of row i, and only the reads of row j
-// are scattered. Decisions as test_f32 with l = 1 (the closed form of cpuInd.cpp:16-27
+// are scattered. Decisions as test_f32_inc with l = 1 (the closed form of cpuInd.cpp:16-27
 // in FP32), FP64 re-tests as in citest_kernel.
 template <bool MIXED>
-__device__ __forceinline__ void tests_l1(const Launch &L) {
+__device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw_smem) {
   const int level = 1;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   __shared__ PendRem<1> s_pend[kThreads / 32][kPend];
@@ -619,6 +672,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L) {
   __syncwarp();
   const unsigned long long total = L.work_prefix[L.count];
   if (total == 0) return;
+  const unsigned long long *rw_c = cache_row_work(L, rw_smem);
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
   const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
@@ -636,29 +690,31 @@ __device__ __forceinline__ void tests_l1(const Launch &L) {
     int b = find_inst_u(L.work_prefix, L.count, t0);
     const Inst *I = L.inst + b;
     unsigned long long base_t = L.work_prefix[b];
-    const int64_t i0 = warp_find_row(I->row_work, I->p, t0 - base_t);
+    const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
     const bool active = t < tend;
     const bool same = t < L.work_prefix[b + 1];
-    int64_t i = lane_find_row(I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
+    int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
     if (active && !same) {  // the tile runs into the next instance
       b = find_inst_u(L.work_prefix, L.count, t);
       I = L.inst + b;
       base_t = L.work_prefix[b];
-      i = find_row(I->row_work, I->p, t - base_t);
+      i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
     }
     if (active) {
       int d = I->deg[i];
       int c = d - 1;  // tests per edge at level 1
-      unsigned long long off = t - base_t - I->row_work[i];
+      unsigned long long off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
       int s = (int)(off / (unsigned long long)c);
       int rank = (int)(off - (unsigned long long)s * c);
       int base = I->rowptr[i];
       int64_t j = I->colidx[base + s];
       float rij = MIXED ? __ldg(I->cor32 + i * I->p + j) : 0.f;
+      // the live bit is read when the lane enters an edge and every fourth step on it
+      // (removals by this warp reach its lanes through the step's ballot)
+      bool live = live_bit(I->adj, I->W, i, j);
+      unsigned steps_on_edge = 0;
       for (;;) {
-        // the neighbour id and the live bit are loaded together (latency overlap)
         const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
-        bool live = live_bit(I->adj, I->W, i, j);
         bool rm = false;
         double pv_rm = 0.0;
         if (live) {
@@ -683,7 +739,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L) {
           } else if (res == 2) {
             if (MIXED) ++retests;
             if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, &k, 1)))
-              rm = exact_remove<1>(*I, i, j, &k, 1, &pv_rm);
+              rm = exact_remove_fast<1>(*I, i, j, &k, 1, &pv_rm);
           }
         }
         {
@@ -714,11 +770,11 @@ __device__ __forceinline__ void tests_l1(const Launch &L) {
               I = L.inst + b;
               base_t = L.work_prefix[b];
             }
-            i = find_row(I->row_work, I->p, t - base_t);
+            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
             d = I->deg[i];
             c = d - 1;
             base = I->rowptr[i];
-            off = t - base_t - I->row_work[i];
+            off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
             s = (int)(off / (unsigned long long)c);
             rank = (int)(off - (unsigned long long)s * c);
             break;
@@ -727,6 +783,10 @@ __device__ __forceinline__ void tests_l1(const Launch &L) {
         if (moved) {
           j = I->colidx[base + s];
           if (MIXED) rij = __ldg(I->cor32 + i * I->p + j);
+          live = live_bit(I->adj, I->W, i, j);
+          steps_on_edge = 0;
+        } else if (live && (++steps_on_edge & 3u) == 0) {
+          live = live_bit(I->adj, I->W, i, j);
         }
       }
       b_last = b;
@@ -831,15 +891,16 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
 // is the lane-interleaved level-1 body, 2..8 the unrolled bodies, 0 any level.
 template <int LT, bool MIXED>
 __global__ void __launch_bounds__(kThreads, LT == 1 ? 4 : 2) level_kernel(Launch L) {
+  extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
   rebuild_phase(L);
   if (!grid_barrier(L, epoch)) return;
   scan_phase(L);
   if (!grid_barrier(L, epoch)) return;
   if (LT == 1)
-    tests_l1<MIXED>(L);
+    tests_l1<MIXED>(L, nullptr);  // level 1 keeps the SM's on-chip memory for L1 cache
   else
-    tests_generic<LT, MIXED>(L);
+    tests_generic<LT, MIXED>(L, rw_smem);
 }
 
 template <bool MIXED>
@@ -861,8 +922,11 @@ void *kernel_for(int level) {
 
 int citest_grid(int precision, int level, int device) {
   void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(level) : kernel_for<true>(level);
+  const int smem = level == 1 ? 0 : kRowCache * (int)sizeof(unsigned long long);
+  // the row-offset cache is beyond the default 48 KB of dynamic shared memory
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) cudaGetLastError();
   int per_sm = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) sms = 1;
   return per_sm * sms;
@@ -891,7 +955,7 @@ hpc_status launch_level(const Launch &L, int precision, int grid, cudaStream_t s
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = L.level == 1 ? 0 : kRowCache * sizeof(unsigned long long);
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;

@@ -55,7 +55,7 @@ __device__ __forceinline__ bool grid_barrier(const Launch &L, unsigned int &epoc
         atomicOr(&L.inst[0].g->err, kErrTimeout);
         break;
       }
-      __nanosleep(64);
+      __nanosleep(20);
     }
     __threadfence();
     s_ok = ok;
@@ -67,7 +67,7 @@ __device__ __forceinline__ bool grid_barrier(const Launch &L, unsigned int &epoc
 // tests a row of degree d contributes at level l; sets *over when beyond the limit
 __device__ __forceinline__ unsigned long long row_tests(int d, int level, int *over) {
   if (d - 1 < level) return 0ull;
-  const unsigned long long c = binom_sat(d - 1, level);
+  const unsigned long long c = binom_fast(d - 1, level);
   if (c >= kRowWorkLimit || (unsigned long long)d * c >= kRowWorkLimit) {
     *over = 1;
     return 0ull;
@@ -118,11 +118,14 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
     }
     if (skip) continue;
     const uint32_t *words = I->adj + i * I->W;
+    const int W = I->W;
+    // the first 128 words of the row are loaded at once (one round trip for p <= 4096)
+    uint32_t pre[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) pre[q] = q * 32 + lane < W ? words[q * 32 + lane] : 0u;
     int *out = I->colidx + I->rowptr[i];
     int cnt = 0;
-    for (int w0 = 0; w0 < I->W; w0 += 32) {
-      const int w = w0 + lane;
-      uint32_t word = w < I->W ? words[w] : 0u;
+    auto emit = [&](uint32_t word, int w) {
       const int c = __popc(word);
       int incl = c;
 #pragma unroll
@@ -137,7 +140,11 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
         word &= word - 1;
       }
       cnt += __shfl_sync(0xffffffffu, incl, 31);
-    }
+    };
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (q * 32 < W) emit(pre[q], q * 32 + lane);
+    for (int w0 = 128; w0 < W; w0 += 32) emit(w0 + lane < W ? words[w0 + lane] : 0u, w0 + lane);
     if (lane == 0) I->deg[i] = cnt;
     a_deg += (unsigned long long)cnt;
     a_max = max(a_max, cnt);

@@ -10,6 +10,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "../../include/heterogpc.h"
+
 #define HPC_HD __host__ __device__ __forceinline__
 
 namespace hpc {
@@ -101,6 +103,46 @@ HPC_HD unsigned long long binom_sat(int n, int k) {
   }
   return res;
 }
+
+#ifdef __CUDACC__
+// C(n, k) for n < 64 and k <= HPC_MAX_LEVEL (Pascal's triangle at compile time; the
+// largest entry, C(63, 16), fits 64 bits). Device lookups replace binom_sat's
+// 64-bit divisions on the CI-test path.
+struct BinomTable {
+  unsigned long long v[64][HPC_MAX_LEVEL + 1];
+  constexpr BinomTable() : v() {
+    v[0][0] = 1ull;
+    for (int n = 1; n < 64; ++n) {
+      v[n][0] = 1ull;
+      for (int k = 1; k <= HPC_MAX_LEVEL; ++k) v[n][k] = v[n - 1][k - 1] + v[n - 1][k];
+    }
+  }
+};
+static __device__ const BinomTable kBinomTab = BinomTable();
+
+__device__ __forceinline__ unsigned long long binom_fast(int n, int k) {
+  if (k < 0 || n < k) return 0ull;
+  if (n < 64 && k <= HPC_MAX_LEVEL) return __ldg(&kBinomTab.v[n][k]);
+  return binom_sat(n, k);
+}
+
+// unrank_lex (below) with table lookups
+__device__ __forceinline__ void unrank_lex_fast(unsigned long long rank, int l, int m, int *pos) {
+  int x = 0;
+  for (int i = 0; i < l; ++i) {
+    for (;;) {
+      const unsigned long long cnt = binom_fast(m - x - 1, l - i - 1);
+      if (rank < cnt) {
+        pos[i] = x;
+        ++x;
+        break;
+      }
+      rank -= cnt;
+      ++x;
+    }
+  }
+}
+#endif
 
 // Lexicographic unranking of an l-subset of {0, .., m-1}: rank -> ascending
 // positions. The same order as ithCombination (src/util/cuda_util.cu:34-50),
