@@ -51,6 +51,22 @@ WORKLOADS = {
 }
 
 
+class L2Flush:
+    """Evicts the step's data from L2 between timed steps: a 256 MB write (twice the
+    129 MB L2), then a 256 MB read of a second buffer, so that the lines the write
+    left dirty are written back here and not inside the next timed step."""
+
+    def __init__(self, torch, dev):
+        self.w = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+        self.r = torch.ones(64 * 1024 * 1024, dtype=torch.int32, device=dev)
+
+    def __call__(self):
+        self.w.fill_(1)
+        self.sink = self.r.sum()
+
+    desc = "flushed before every step (256 MB write, then 256 MB read)"
+
+
 def c4_instances(wl, count=None):
     rng = np.random.default_rng(wl["seed"])
     k = wl["count"] if count is None else count
@@ -139,7 +155,7 @@ def run_c4(args, wl):
                             wl["seed"] * 100000 + b, dtype=np.float32)
         packed[bt.obs_off[b]:bt.obs_off[b + 1]] = X.reshape(-1)
     Xd = torch.from_numpy(packed).to(dev)
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    flush = L2Flush(torch, dev)
 
     def step():
         bt.add_observations_device(Xd.data_ptr(), np.float32)
@@ -152,7 +168,7 @@ def run_c4(args, wl):
     clocks = ClockSampler(0)
     clocks.start()
     for _ in range(args.steps):
-        flush.fill_(1)
+        flush()
         a, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         st = step()
@@ -181,12 +197,17 @@ def run_c4(args, wl):
             "config": {"workload": "c4", "instances": bt.count, "p": list(wl["p"]), "n": list(wl["n"]),
                        "degree": list(wl["degree"]), "alphas": list(wl["alphas"]), "max_level": wl["max_level"],
                        "precision": "tensor-core split-BF16 Gram, FP32 tests, FP64 re-tests",
-                       "l2": "flushed before every step"},
+                       "l2": L2Flush.desc},
             "ci_tests_per_step": tests, "correlation_ms": t_cor["standardise_ms"] + t_cor["gram_ms"],
             "skeleton_ms": t_cor["skeleton_ms"],
             "plain_gpu_path": {"skeletons_per_sec": plain, "sample": "%d instances, one context each" % k_plain,
                                "precision": "fp64"},
-            "speedup_vs_plain": value / plain, "clocks": clk}
+            "speedup_vs_plain": value / plain, "clocks": clk,
+            "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
+                        "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
+                        "retests": s_["retests"], "edges_after": s_["edges_after"],
+                        "test_ms": t_cor["test_ms"][s_["level"]] if s_["level"] < len(t_cor["test_ms"]) else None}
+                       for s_ in st]}
     print(json.dumps(line), flush=True)
 
 
@@ -397,13 +418,13 @@ def main():
     sk_plain.add_observations_device(Xd.data_ptr(), np.float32)
     torch.cuda.synchronize()
 
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    flush = L2Flush(torch, dev)
 
     def timed_steps(s, k):
         ms, stats = [], None
         launches0 = s.timings()["launches"]
         for _ in range(k):
-            flush.fill_(1)
+            flush()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             s.reset()
@@ -421,7 +442,7 @@ def main():
         s.set_graphs(False)
         acc = np.zeros(hg.HPC_MAX_LEVEL + 1)
         for _ in range(k):
-            flush.fill_(1)
+            flush()
             s.reset()
             s.run()
             acc += np.array(s.timings()["test_ms"])
@@ -516,7 +537,7 @@ def main():
             "data": "synthetic (seeded linear-Gaussian SEM)",
             "config": dict(workload=args.workload, p=p, n=n, degree=wl["degree"], alpha=wl["alpha"],
                            max_level=wl["max_level"], precision="mixed (FP32 tests, FP64 re-tests)",
-                           l2="flushed before every step (256 MB write)", parallelism="replicas"),
+                           l2=L2Flush.desc, parallelism="replicas"),
             "ci_tests_per_step": tests_per_step, "ci_tests_per_sec": tests_per_step * args.steps * world / (total_ms / 1e3),
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "levels": [{k: s_[k] for k in ("level", "max_degree", "potential_tests", "executed_tests", "retests",

@@ -1,807 +1,10 @@
-// Level-l conditional-independence tests (l >= 1) on a persistent grid, over all
-// instances of a context in one launch.
-//
-// Replaces testRowL1 / testRowLN<l+2,l> (src/executor/testing/gpuRowTests.cu:29-205),
-// their workstealing twins (src/executor/testing/gpuWorkstealingTests.cu) and the
-// CPU/GPU balancer (src/loadbalance/balancer.cpp): the reference launches one
-// 64-thread block per (row, neighbour slot) with grid y = the maximum degree and has
-// each thread unrank a subset and run a 30-iteration FP64 SVD in local memory.
-//
-// Here every test of the level is one index of a flattened space
-//   t in [0, sum_b T_l(b)),  T_l(b) = sum_i d_i * C(d_i - 1, l)
-// ordered by (instance b, row i, neighbour slot s, lexicographic subset rank). Warps
-// claim tiles of 32 * m consecutive tests with one atomicAdd on a device-wide counter;
-// each lane takes m consecutive tests, finds its instance and row by binary search,
-// unranks its first subset once (the order of ithCombination,
-// src/util/cuda_util.cu:34-50) and then steps to the lexicographic successor. Lanes
-// stop testing an edge as soon as its live bit is cleared (the reference's
-// `adj == 0` early exit, gpuRowTests.cu:166-168).
-//
-// The partial correlation of (i, j) given S comes from a Cholesky factorisation of
-// the S block and forward solves for r_iS and r_jS:
-//   r = (r_ij - w_i . w_j) / sqrt((1 - |w_i|^2)(1 - |w_j|^2)),  w = L_S^-1 r_S.
-// In mixed precision this runs in FP32 on cor32; a test is decided in FP32 only when
-// |r| is outside the re-test band around r_crit (the configured relative |z| margin
-// plus an error bound from the smallest pivot); every other test is re-evaluated in
-// FP64 with the reference's formula (closed form at l = 1 as cpuInd.cpp:16-27; pinv
-// semantics at l >= 2 as cpuInd.cpp:29-38: Cholesky when well conditioned, Jacobi
-// pseudoinverse with arma::pinv's tolerance otherwise). The decision is p >= alpha in
-// FP64. With an FP64 matrix the re-test runs inline; without one (tensor-core mode)
-// it is queued for retest_kernel, which forms the FP64 entries as warp-cooperative
-// dot products of the standardised data.
-//
-// Removal (src/executor/testing/cpuUtil.cpp:23-48, gpuRowTests.cu:172-201): the lane
-// clearing the (min, max) bit with atomicAnd owns the edge, clears the mirror bit and
-// appends one separation-set record.
-//
-// A level is one cooperative launch (level_kernel): snapshot rebuild and test-count
-// scan (rebuild.cuh), each followed by a grid barrier, then the CI tests.
-#include <cuda_runtime.h>
-
-#include "internal.cuh"
-#include "rebuild.cuh"
-#include "stats.cuh"
+// Level-l CI tests (l >= 1): the re-test and record kernels, the level-kernel
+// instantiations of levels 1-8 and the launchers (the level kernels' device code is in
+// citest.cuh).
+#include "citest.cuh"
 
 namespace hpc {
 namespace {
-
-constexpr int kThreads = kLevelThreads;
-
-__device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, int64_t j) {
-  const volatile uint32_t *w = adj + i * W + (j >> 5);
-  return (*w >> (j & 31)) & 1u;
-}
-
-// FP64 correlation entries of one instance: read from its FP64 matrix when there is
-// one, else the dot product of its FP64-standardised columns. Index order as the
-// reference reads cor[row * p + col].
-__device__ __forceinline__ double exact_entry(const Inst &I, int64_t x, int64_t y) {
-  if (I.cor64) return I.cor64[x * I.p + y];
-  const double *a = I.Z + x * I.n_z, *b = I.Z + y * I.n_z;
-  double s = 0.0;
-  for (int64_t k = 0; k < I.n_z; ++k) s = fma(a[k], b[k], s);
-  return s / I.denom;
-}
-
-// FP64 partial correlation of a k x k submatrix M (row-major, ordered i, j, S;
-// overwritten): the value the reference's p-value formula is applied to. *nan_p is
-// set where the reference's p-value is NaN (a NaN entry, cpuInd.cpp:31-33 and the
-// closed form at l = 1): the edge is kept.
-template <int LA>
-__device__ __noinline__ double partial_r_of_matrix(double *M, int l, bool *nan_p) {
-  const int k = l + 2;
-  *nan_p = false;
-  if (l == 1) {  // closed form (cpuInd.cpp:16-27), as pval_l1_64
-    const double x1 = M[1], x2 = M[2], x3 = M[k + 2];
-    if (isnan(x1) || isnan(x2) || isnan(x3)) {
-      *nan_p = true;
-      return 0.0;
-    }
-    return (x1 - x2 * x3) / sqrt((1.0 - x3 * x3) * (1.0 - x2 * x2));
-  }
-  for (int q = 0; q < k * k; ++q)
-    if (isnan(M[q])) {
-      *nan_p = true;
-      return 0.0;
-    }
-  double Lm[LA * (LA + 1) / 2], wx[LA], wy[LA];
-  double dmin = 1.0;
-  for (int r = 0; r < l; ++r) {
-    for (int c = 0; c < r; ++c) {
-      double v = M[(c + 2) * k + (r + 2)];
-      for (int q = 0; q < c; ++q) v -= Lm[r * (r + 1) / 2 + q] * Lm[c * (c + 1) / 2 + q];
-      Lm[r * (r + 1) / 2 + c] = v / Lm[c * (c + 1) / 2 + c];
-    }
-    double d = 1.0;
-    for (int q = 0; q < r; ++q) d -= Lm[r * (r + 1) / 2 + q] * Lm[r * (r + 1) / 2 + q];
-    dmin = fmin(dmin, d);
-    if (!(d > 1e-10)) break;
-    const double lrr = sqrt(d);
-    Lm[r * (r + 1) / 2 + r] = lrr;
-    double vx = M[r + 2], vy = M[k + r + 2];
-    for (int q = 0; q < r; ++q) {
-      vx -= Lm[r * (r + 1) / 2 + q] * wx[q];
-      vy -= Lm[r * (r + 1) / 2 + q] * wy[q];
-    }
-    wx[r] = vx / lrr;
-    wy[r] = vy / lrr;
-  }
-  if (dmin > 1e-10) {
-    double ax = 1.0, ay = 1.0, b = M[1];
-    for (int q = 0; q < l; ++q) {
-      ax -= wx[q] * wx[q];
-      ay -= wy[q] * wy[q];
-      b -= wx[q] * wy[q];
-    }
-    if (ax > 1e-10 && ay > 1e-10) return b / sqrt(ax * ay);
-  }
-  double V[(LA + 2) * (LA + 2)];
-  double p00, p01, p11;
-  pinv_sym64_corner(M, k, V, &p00, &p01, &p11);
-  return -p01 / sqrt(p00 * p11);
-}
-
-// FP64 p-value of a k x k submatrix M with the reference's semantics.
-template <int LA>
-__device__ __forceinline__ double pvalue_of_matrix(double *M, int l, int n_obs) {
-  bool nan_p;
-  const double r = partial_r_of_matrix<LA>(M, l, &nan_p);
-  return nan_p ? nan("") : calc_pvalue64(r, n_obs);
-}
-
-// The reference's decision p >= alpha from the FP64 partial correlation r: the
-// p-value is monotone in |r|, so outside [r_lo, r_hi] (|r_crit| -+ 1e-7 relative,
-// far beyond the formula's rounding) |r| decides; inside, the formula itself. *pv
-// receives the p-value where it was evaluated, else -1 - |r| (evaluated later, when
-// the records are read; calc_pvalue64 clamps |r| the same way).
-__device__ __forceinline__ bool decide_of_r(const Inst &I, double r, bool nan_p, double *pv) {
-  if (nan_p) {
-    *pv = nan("");
-    return false;
-  }
-  const double ar = isnan(r) ? 0.0 : fmin(kCutThr, fabs(r));
-  if (ar < I.r_lo) {
-    *pv = isnan(r) ? 1.0 : -1.0 - ar;
-    return true;
-  }
-  if (ar > I.r_hi) {
-    *pv = -1.0 - ar;
-    return false;
-  }
-  *pv = calc_pvalue64(r, I.n_obs);
-  return *pv >= I.alpha;
-}
-
-// FP64 p-value of the test (i, j | ids) of instance I.
-template <int LA>
-__device__ __noinline__ double exact_pvalue(const Inst &I, int64_t i, int64_t j, const int *ids, int l) {
-  const int k = l + 2;
-  double M[(LA + 2) * (LA + 2)];
-  for (int q = 0; q < k * k; ++q) M[q] = 0.0;
-  for (int q = 0; q < k; ++q) M[q * k + q] = 1.0;
-  M[1] = M[k] = exact_entry(I, i, j);
-  for (int q = 2; q < k; ++q) {
-    M[q] = M[q * k] = exact_entry(I, i, ids[q - 2]);
-    M[k + q] = M[q * k + 1] = exact_entry(I, j, ids[q - 2]);
-  }
-  for (int r = 2; r < k; ++r)
-    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = exact_entry(I, ids[r - 2], ids[c - 2]);
-  return pvalue_of_matrix<LA>(M, l, I.n_obs);
-}
-
-// The reference's decision for the test (i, j | ids) in FP64 (see decide_of_r).
-template <int LA>
-__device__ __noinline__ bool exact_remove(const Inst &I, int64_t i, int64_t j, const int *ids, int l, double *pv) {
-  const int k = l + 2;
-  double M[(LA + 2) * (LA + 2)];
-  for (int q = 0; q < k * k; ++q) M[q] = 0.0;
-  for (int q = 0; q < k; ++q) M[q * k + q] = 1.0;
-  M[1] = M[k] = exact_entry(I, i, j);
-  for (int q = 2; q < k; ++q) {
-    M[q] = M[q * k] = exact_entry(I, i, ids[q - 2]);
-    M[k + q] = M[q * k + 1] = exact_entry(I, j, ids[q - 2]);
-  }
-  for (int r = 2; r < k; ++r)
-    for (int c = r + 1; c < k; ++c) M[r * k + c] = M[c * k + r] = exact_entry(I, ids[r - 2], ids[c - 2]);
-  bool nan_p;
-  const double r = partial_r_of_matrix<LA>(M, l, &nan_p);
-  return decide_of_r(I, r, nan_p, pv);
-}
-
-// exact_remove from the FP64 matrix with the factorisation in registers: every entry
-// gathered in one round of loads, rsqrt in place of divisions and square roots (a
-// few ulps, far inside decide_of_r's guard band). Tests the Cholesky path does not
-// accept (an ill-conditioned block) and instances without an FP64 matrix go to
-// exact_remove.
-template <int LA>
-__device__ __noinline__ bool exact_remove_fast(const Inst &I, int64_t i, int64_t j, const int *ids, int l, double *pv) {
-  const double *C = I.cor64;
-  if (!C) return exact_remove<LA>(I, i, j, ids, l, pv);
-  const int64_t p = I.p;
-  const double rij = C[i * p + j];
-  double gx[LA], gy[LA], gs[LA * (LA - 1) / 2 > 0 ? LA * (LA - 1) / 2 : 1];
-#pragma unroll
-  for (int r = 0; r < LA; ++r)
-    if (r < l) {
-      const int64_t idr = ids[r];
-      gx[r] = C[i * p + idr];
-      gy[r] = C[j * p + idr];
-#pragma unroll
-      for (int c = 0; c < LA; ++c)
-        if (c < r) gs[r * (r - 1) / 2 + c] = C[(int64_t)ids[c] * p + idr];
-    }
-  if (l == 1) {  // the closed form, as pval_l1_64
-    const double x1 = rij, x2 = gx[0], x3 = gy[0];
-    if (isnan(x1) || isnan(x2) || isnan(x3)) return decide_of_r(I, 0.0, true, pv);
-    return decide_of_r(I, (x1 - x2 * x3) / sqrt((1.0 - x3 * x3) * (1.0 - x2 * x2)), false, pv);
-  }
-  bool nan_in = isnan(rij);
-#pragma unroll
-  for (int r = 0; r < LA; ++r)
-    if (r < l) {
-      nan_in |= isnan(gx[r]) || isnan(gy[r]);
-#pragma unroll
-      for (int c = 0; c < LA; ++c)
-        if (c < r) nan_in |= isnan(gs[r * (r - 1) / 2 + c]);
-    }
-  if (nan_in) return decide_of_r(I, 0.0, true, pv);
-  double Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1], inv[LA], wx[LA], wy[LA];
-  bool ok = true;
-#pragma unroll
-  for (int r = 0; r < LA; ++r)
-    if (r < l) {
-      double vx = gx[r], vy = gy[r], d = 1.0;
-#pragma unroll
-      for (int c = 0; c < LA; ++c)
-        if (c < r) {
-          double v = gs[r * (r - 1) / 2 + c];
-#pragma unroll
-          for (int q = 0; q < LA; ++q)
-            if (q < c) v -= Lm[r * (r + 1) / 2 + q] * Lm[c * (c + 1) / 2 + q];
-          v *= inv[c];
-          Lm[r * (r + 1) / 2 + c] = v;
-          d -= v * v;
-          vx -= v * wx[c];
-          vy -= v * wy[c];
-        }
-      ok = ok && d > 1e-10;
-      inv[r] = rsqrt(fmax(d, 1e-300));
-      wx[r] = vx * inv[r];
-      wy[r] = vy * inv[r];
-    }
-  if (ok) {
-    double ax = 1.0, ay = 1.0, b = rij;
-#pragma unroll
-    for (int q = 0; q < LA; ++q)
-      if (q < l) {
-        ax -= wx[q] * wx[q];
-        ay -= wy[q] * wy[q];
-        b -= wx[q] * wy[q];
-      }
-    if (ax > 1e-10 && ay > 1e-10) return decide_of_r(I, b * rsqrt(ax * ay), false, pv);
-  }
-  return exact_remove<LA>(I, i, j, ids, l, pv);  // pinv semantics
-}
-
-// Running FP32 factorisation of the conditioning block of one lane's current test,
-// kept across the lexicographic walk: the Cholesky factor of S (rows, inverse
-// diagonal, pivots) and the forward solves w_i, w_j.
-template <int LA>
-struct Fact {
-  float Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1];
-  float invd[LA], piv[LA], wx[LA], wy[LA];
-};
-
-// FP32 test of (i, j | ids). The partial correlation comes from a Cholesky
-// factorisation of the S block and forward solves for r_iS and r_jS:
-//   r = (r_ij - w_i . w_j) / sqrt((1 - |w_i|^2)(1 - |w_j|^2)),  w = L_S^-1 r_S;
-// only rows ci..l-1 are refactored (rows below ci are still valid for the current
-// i, j and the unchanged first ci members of S). Returns 1 = remove, 0 = keep,
-// 2 = undecided (re-test in FP64): |r| is compared with r_c outside a band of
-// margin_r + 8 * ke(l) / smallest pivot. *rr_out receives |r|.
-template <int LA>
-__device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j, const int *ids, int l, int ci,
-                                            Fact<LA> &F, float *rr_out) {
-  const float *__restrict__ C = I.cor32;
-  const int64_t p = I.p;
-  // all entries the changed rows need, gathered before any arithmetic (one round of
-  // independent loads instead of one per factor row)
-  float gx[LA], gy[LA], gs[LA * (LA - 1) / 2 > 0 ? LA * (LA - 1) / 2 : 1];
-#pragma unroll
-  for (int r = 0; r < LA; ++r) {
-    if (r >= ci && r < l) {
-      const int idr = ids[r];
-      gx[r] = __ldg(C + i * p + idr);
-      gy[r] = __ldg(C + j * p + idr);
-#pragma unroll
-      for (int c = 0; c < LA; ++c)
-        if (c < r) gs[r * (r - 1) / 2 + c] = __ldg(C + (int64_t)ids[c] * p + idr);
-    }
-  }
-  const float rij = __ldg(C + i * p + j);
-#pragma unroll
-  for (int r = 0; r < LA; ++r) {
-    if (r >= ci && r < l) {
-      float vx = gx[r];
-      float vy = gy[r];
-      float d = 1.0f;
-#pragma unroll
-      for (int c = 0; c < LA; ++c) {
-        if (c < r) {
-          float v = gs[r * (r - 1) / 2 + c];
-#pragma unroll
-          for (int q = 0; q < LA; ++q)
-            if (q < c) v -= F.Lm[r * (r + 1) / 2 + q] * F.Lm[c * (c + 1) / 2 + q];
-          v *= F.invd[c];
-          F.Lm[r * (r + 1) / 2 + c] = v;
-          d -= v * v;
-          vx -= v * F.wx[c];
-          vy -= v * F.wy[c];
-        }
-      }
-      const float id = rsqrtf(fmaxf(d, 1e-30f));
-      F.piv[r] = d;
-      F.invd[r] = id;
-      F.wx[r] = vx * id;
-      F.wy[r] = vy * id;
-    }
-  }
-  // the sums in row order, whatever ci was, so that the decision does not depend on
-  // the walk
-  float sx = 0.f, sy = 0.f, sxy = 0.f, dmin = 1.f;
-#pragma unroll
-  for (int r = 0; r < LA; ++r)
-    if (r < l) {
-      dmin = fminf(dmin, F.piv[r]);
-      sx += F.wx[r] * F.wx[r];
-      sy += F.wy[r] * F.wy[r];
-      sxy += F.wx[r] * F.wy[r];
-    }
-  const float ax = 1.0f - sx, ay = 1.0f - sy;
-  const float cond = fminf(dmin, fminf(ax, ay));
-  if (!(cond > 1e-3f)) return 2;
-  const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
-  *rr_out = rr;
-  const float dist = rr - I.r_c;
-  const float ke = I.ke_a + (float)(l + 2) * I.ke_b;
-  const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
-  if (!(fabsf(dist) > band)) return 2;
-  return dist < 0.0f ? 1 : 0;
-}
-
-__device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, int64_t p, unsigned long long t) {
-  // largest i with row_work[i] <= t (row_work is non-decreasing, row_work[p] > t)
-  int64_t lo = 0, hi = p;
-  while (hi - lo > 1) {
-    const int64_t mid = (lo + hi) >> 1;
-    if (row_work[mid] <= t) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
-// The row offsets of a single-instance level copied into shared memory by the whole
-// block (one round of coalesced loads), so that every row search of the CI tests
-// stays on the SM; null when they do not fit (or for several instances).
-constexpr int kRowCache = 5120;
-__device__ __forceinline__ const unsigned long long *cache_row_work(const Launch &L, unsigned long long *smem) {
-  if (!smem || L.count != 1) return nullptr;
-  const Inst &I = L.inst[0];
-  if (I.p + 1 > kRowCache) return nullptr;
-  for (int64_t r = threadIdx.x; r <= I.p; r += blockDim.x) smem[r] = __ldcg(I.row_work + r);
-  __syncthreads();
-  return smem;
-}
-
-// Row of a warp-uniform position t: a 32-ary search (coalesced probes, two or three
-// rounds for thousands of rows) instead of log2(p) dependent loads. Whole warp.
-__device__ __forceinline__ int64_t warp_find_row(const unsigned long long *rw, int64_t p, unsigned long long t) {
-  const int lane = threadIdx.x & 31;
-  int64_t lo = 0, hi = p;  // rw[lo] <= t < rw[hi]
-  while (hi - lo > 32) {
-    const int64_t step = (hi - lo + 31) >> 5;
-    const int64_t probe = lo + (int64_t)(lane + 1) * step;
-    const bool le = probe < hi && rw[probe] <= t;
-    lo += (int64_t)__popc(__ballot_sync(0xffffffffu, le)) * step;
-    hi = min(hi, lo + step);
-  }
-  const int64_t probe = lo + 1 + lane;
-  const bool le = probe < hi && rw[probe] <= t;
-  return lo + __popc(__ballot_sync(0xffffffffu, le));
-}
-
-// Row of each lane's position t >= t0, given i0 = the row of t0 (same instance): the
-// next 32 row offsets in one coalesced load and a shuffle search; a lane further on
-// (rows without tests in between) searches alone. Whole warp; `valid` lanes only use
-// the result.
-__device__ __forceinline__ int64_t lane_find_row(const unsigned long long *rw, int64_t p, int64_t i0,
-                                                 unsigned long long t, bool valid) {
-  const int lane = threadIdx.x & 31;
-  const int64_t r = i0 + 1 + lane;
-  const unsigned long long v = r <= p ? rw[r] : ~0ull;
-  int pos = 0;  // number of the 32 offsets <= t (up to 31 here)
-#pragma unroll
-  for (int sh = 16; sh >= 1; sh >>= 1) {
-    const unsigned long long vv = __shfl_sync(0xffffffffu, v, pos + sh - 1);
-    if (vv <= t) pos += sh;
-  }
-  const unsigned long long v31 = __shfl_sync(0xffffffffu, v, 31);
-  if (valid && v31 <= t) return find_row(rw, p, t);
-  return i0 + pos;
-}
-
-// Removals: the lane whose atomicAnd clears the (min, max) bit owns the edge and clears
-// the mirror bit at once (other tests see the edge gone); its separation-set record
-// waits in the warp's shared-memory list until the tile is done, so that one
-// record-counter atomic per instance and flush replaces one per removal.
-constexpr int kPend = 32;
-template <int LA>
-struct PendRem {
-  int32_t lo, hi, b, pad;
-  double pv;
-  int32_t ids[LA > 0 ? LA : 1];
-};
-
-__device__ __forceinline__ bool claim_edge(const Inst &I, int64_t i, int64_t j) {
-  const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
-  const uint32_t bit = 1u << (hi & 31);
-  const uint32_t old = atomicAnd(I.adj + lo * I.W + (hi >> 5), ~bit);
-  if (!(old & bit)) return false;  // another test removed it first
-  atomicAnd(I.adj + hi * I.W + (lo >> 5), ~(1u << (lo & 31)));
-  return true;
-}
-
-// the record of a removal this lane owns (claim_edge returned true)
-__device__ __forceinline__ void write_record(const Inst &I, int level, int64_t i, int64_t j, const int *ids, int l,
-                                             double pv) {
-  atomicAdd(&I.ctr[level].deleted, 1ull);
-  const unsigned long long slot = atomicAdd(&I.g->rec_count, 1ull);
-  if ((long long)slot >= I.rec_cap) {
-    atomicOr(&I.g->err, kErrRecOverflow);
-    return;
-  }
-  hpc_sepset_record *rec = I.recs + slot;
-  rec->i = (int32_t)(i < j ? i : j);
-  rec->j = (int32_t)(i < j ? j : i);
-  rec->level = l;
-  rec->pad = 0;
-  rec->pmax = pv;
-  for (int q = 0; q < HPC_MAX_LEVEL; ++q) rec->ids[q] = q < l ? ids[q] : -1;
-}
-
-template <int LA>
-__device__ __forceinline__ void push_pending(PendRem<LA> *list, int *np, const Inst &I, int b, int level, int64_t i,
-                                             int64_t j, const int *ids, int l, double pv) {
-  const int slot = atomicAdd(np, 1);
-  if (slot >= kPend) {  // list full: record at once
-    write_record(I, level, i, j, ids, l, pv);
-    return;
-  }
-  PendRem<LA> &e = list[slot];
-  e.lo = (int32_t)(i < j ? i : j);
-  e.hi = (int32_t)(i < j ? j : i);
-  e.b = b;
-  e.pad = 0;
-  e.pv = pv;
-#pragma unroll
-  for (int q = 0; q < (LA > 0 ? LA : 1); ++q) e.ids[q] = q < l ? ids[q] : -1;
-}
-
-// Apply a warp's pending removals (whole warp, converged).
-template <int LA>
-__device__ __forceinline__ void flush_pending(const Launch &L, int level, PendRem<LA> *list, int *np) {
-  const int lane = threadIdx.x & 31;
-  __syncwarp();
-  const int n = min(*np, kPend);
-  for (int q0 = 0; q0 < n; q0 += 32) {
-    const int q = q0 + lane;
-    const bool won = q < n;
-    const Inst *I = nullptr;
-    int b = -1;
-    if (won) {
-      b = list[q].b;
-      I = L.inst + b;
-    }
-    const unsigned wm = __ballot_sync(0xffffffffu, won);
-    if (won) {
-      const unsigned g = __match_any_sync(wm, b);
-      const int leader = __ffs(g) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) {
-        base = atomicAdd(&I->g->rec_count, (unsigned long long)__popc(g));
-        atomicAdd(&I->ctr[level].deleted, (unsigned long long)__popc(g));
-      }
-      base = __shfl_sync(g, base, leader);
-      const unsigned long long slot = base + (unsigned long long)__popc(g & ((1u << lane) - 1u));
-      if ((long long)slot >= I->rec_cap) {
-        atomicOr(&I->g->err, kErrRecOverflow);
-      } else {
-        const PendRem<LA> &e = list[q];
-        hpc_sepset_record *rec = I->recs + slot;
-        rec->i = e.lo;
-        rec->j = e.hi;
-        rec->level = level;
-        rec->pad = 0;
-        rec->pmax = e.pv;
-#pragma unroll
-        for (int t = 0; t < HPC_MAX_LEVEL; ++t) rec->ids[t] = t < (LA > 0 ? LA : 1) ? e.ids[t < (LA > 0 ? LA : 1) ? t : 0] : -1;
-      }
-    }
-  }
-  __syncwarp();
-  if (lane == 0) *np = 0;
-  __syncwarp();
-}
-
-// Defer an undecided test to the FP64 re-test kernel; false when the queue is full.
-__device__ __forceinline__ bool push_retest(const Launch &L, int b, int64_t i, int64_t j, const int *ids, int l) {
-  const unsigned long long slot = atomicAdd(&L.lc->rq_count, 1ull);
-  if ((long long)slot >= L.rq_cap) return false;
-  RetestItem *it = L.rq + slot;
-  it->i = (int32_t)i;
-  it->j = (int32_t)j;
-  it->level = l;
-  it->inst = b;
-  for (int q = 0; q < HPC_MAX_LEVEL; ++q) it->ids[q] = q < l ? ids[q] : -1;
-  return true;
-}
-
-template <int LT, bool MIXED>
-__device__ __forceinline__ void tests_generic(const Launch &L, unsigned long long *rw_smem) {
-  constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
-  const int l = LT > 0 ? LT : L.level;
-  const int level = L.level;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  __shared__ PendRem<LA> s_pend[kThreads / 32][kPend];
-  __shared__ int s_np[kThreads / 32];
-  PendRem<LA> *pend = s_pend[wib];
-  int *np = s_np + wib;
-  if (lane == 0) *np = 0;
-  __syncwarp();
-  const unsigned long long total = L.work_prefix[L.count];
-  if (total == 0) return;
-  const unsigned long long *rw_c = cache_row_work(L, rw_smem);
-  // tests per lane per tile: about four tiles per lane of the grid, 1..64
-  const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
-  const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
-  const unsigned long long per_tile = 32ull * (unsigned long long)m;
-  int pos[LA], ids[LA];
-  for (;;) {
-    unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(&L.lc->tile_next, 1ull);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
-    const unsigned long long t0 = tile * per_tile;
-    if (t0 >= total) break;
-    unsigned long long t = t0 + (unsigned long long)lane * m;
-    const unsigned long long tend = min(t + (unsigned long long)m, total);
-    unsigned executed = 0, retests = 0;
-    int b_last = -1;
-    // instance and row of the tile start (whole warp), then each lane's row
-    int b = find_inst_u(L.work_prefix, L.count, t0);
-    const Inst *I = L.inst + b;
-    unsigned long long base_t = L.work_prefix[b];
-    const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
-    const bool active = t < tend;
-    const bool same = t < L.work_prefix[b + 1];
-    int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
-    if (active && !same) {  // the tile runs into the next instance
-      b = find_inst_u(L.work_prefix, L.count, t);
-      I = L.inst + b;
-      base_t = L.work_prefix[b];
-      i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
-    }
-    if (active) {
-      int d = I->deg[i];
-      unsigned long long c = binom_fast(d - 1, l);
-      const unsigned long long off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
-      int s = (int)(off / c);
-      unsigned long long rank = off - (unsigned long long)s * c;
-      int base = I->rowptr[i];
-      unrank_lex_fast(rank, l, d - 1, pos);
-      int64_t j = I->colidx[base + s];
-      bool alive = live_bit(I->adj, I->W, i, j);
-      unsigned tested_edge = 0;
-      int ci = 0;  // lowest position changed since the last test (rows below are valid)
-      Fact<LA> F;
-      for (;;) {
-        if (alive) {
-#pragma unroll
-          for (int q = 0; q < LA; ++q)
-            if (q < l && q >= ci) ids[q] = I->colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
-          int res = 2;
-          float rr = 0.f;
-          if (MIXED) res = test_f32_inc<LA>(*I, i, j, ids, l, ci, F, &rr);
-          ci = l;
-          ++executed;
-          ++tested_edge;
-          bool rm = false;
-          double pv = 0.0;
-          if (res == 1) {
-            // decided in FP32; the p-value is evaluated when the records are read
-            // (the negative value carries |r| for instances without an FP64 matrix)
-            rm = true;
-            pv = -1.0 - (double)rr;
-          } else if (res == 2) {
-            if (MIXED) ++retests;
-            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, ids, l))) rm = exact_remove_fast<LA>(*I, i, j, ids, l, &pv);
-          }
-          if (rm) {
-            if (claim_edge(*I, i, j)) push_pending<LA>(pend, np, *I, b, level, i, j, ids, l, pv);
-            alive = false;
-          }
-        }
-        if (++t >= tend) break;
-        if (++rank == c) {
-          rank = 0;
-          if (++s == d) {
-            // next row with tests, possibly of the next instance
-            if (t >= L.work_prefix[b + 1]) {
-              b = find_inst_u(L.work_prefix, L.count, t);
-              I = L.inst + b;
-              base_t = L.work_prefix[b];
-            }
-            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
-            d = I->deg[i];
-            c = binom_fast(d - 1, l);
-            base = I->rowptr[i];
-            s = 0;
-          }
-#pragma unroll
-          for (int q = 0; q < LA; ++q)
-            if (q < l) pos[q] = q;
-          j = I->colidx[base + s];
-          alive = live_bit(I->adj, I->W, i, j);
-          tested_edge = 0;
-          ci = 0;
-        } else {
-          const int changed = next_lex(l, d - 1, pos);
-          ci = min(ci, changed);
-          if (alive && (tested_edge & 3u) == 0) alive = live_bit(I->adj, I->W, i, j);
-        }
-      }
-      b_last = b;
-    }
-    __syncwarp();
-    flush_pending<LA>(L, level, pend, np);
-    // per-instance test counts, one atomic per instance present in the warp (a
-    // lane's range rarely crosses instances: its counts go to its last instance)
-    const unsigned grp = __match_any_sync(0xffffffffu, b_last);
-    const unsigned ex = __reduce_add_sync(grp, executed);
-    const unsigned rt = __reduce_add_sync(grp, retests);
-    if (b_last >= 0 && lane == __ffs(grp) - 1) {
-      atomicAdd(&L.inst[b_last].ctr[level].tests, (unsigned long long)ex);
-      if (rt) atomicAdd(&L.inst[b_last].ctr[level].retests, (unsigned long long)rt);
-    }
-  }
-}
-
-// Level 1, lane-interleaved: lane q of a warp takes tests t0 + q, t0 + q + 32, ... of
-// its tile, so the 32 lanes work on consecutive conditioning variables of the same
-// edge (i, j): their reads of the neighbour list and of row i of cor32 fall into few
-// cache lines and stay in L1 across the edges of row i, and only the reads of row j
-// are scattered. Decisions as test_f32_inc with l = 1 (the closed form of cpuInd.cpp:16-27
-// in FP32), FP64 re-tests as in citest_kernel.
-template <bool MIXED>
-__device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw_smem) {
-  const int level = 1;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  __shared__ PendRem<1> s_pend[kThreads / 32][kPend];
-  __shared__ int s_np[kThreads / 32];
-  PendRem<1> *pend = s_pend[wib];
-  int *np = s_np + wib;
-  if (lane == 0) *np = 0;
-  __syncwarp();
-  const unsigned long long total = L.work_prefix[L.count];
-  if (total == 0) return;
-  const unsigned long long *rw_c = cache_row_work(L, rw_smem);
-  const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
-  const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
-  const unsigned long long per_tile = 32ull * (unsigned long long)m;
-  for (;;) {
-    unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(&L.lc->tile_next, 1ull);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
-    const unsigned long long t0 = tile * per_tile;
-    if (t0 >= total) break;
-    const unsigned long long tend = min(t0 + per_tile, total);
-    unsigned long long t = t0 + lane;
-    unsigned executed = 0, retests = 0;
-    int b_last = -1;
-    // instance and row of the tile start (whole warp), then each lane's row
-    int b = find_inst_u(L.work_prefix, L.count, t0);
-    const Inst *I = L.inst + b;
-    unsigned long long base_t = L.work_prefix[b];
-    const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
-    const bool active = t < tend;
-    const bool same = t < L.work_prefix[b + 1];
-    int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
-    if (active && !same) {  // the tile runs into the next instance
-      b = find_inst_u(L.work_prefix, L.count, t);
-      I = L.inst + b;
-      base_t = L.work_prefix[b];
-      i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
-    }
-    if (active) {
-      int d = I->deg[i];
-      int c = d - 1;  // tests per edge at level 1
-      unsigned long long off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
-      int s = (int)(off / (unsigned long long)c);
-      int rank = (int)(off - (unsigned long long)s * c);
-      int base = I->rowptr[i];
-      int64_t j = I->colidx[base + s];
-      float rij = MIXED ? __ldg(I->cor32 + i * I->p + j) : 0.f;
-      // the live bit is read when the lane enters an edge and every fourth step on it
-      // (removals by this warp reach its lanes through the step's ballot)
-      bool live = live_bit(I->adj, I->W, i, j);
-      unsigned steps_on_edge = 0;
-      for (;;) {
-        const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
-        bool rm = false;
-        double pv_rm = 0.0;
-        if (live) {
-          int res = 2;
-          float rr = 0.f;
-          if (MIXED) {
-            const float x2 = __ldg(I->cor32 + i * I->p + k), x3 = __ldg(I->cor32 + j * I->p + k);
-            const float ax = 1.0f - x2 * x2, ay = 1.0f - x3 * x3;
-            const float cond = fminf(ax, ay);
-            if (cond > 1e-3f) {
-              rr = fabsf(rij - x2 * x3) * rsqrtf(ax * ay);
-              const float dist = rr - I->r_c;
-              const float band = I->margin_r + 8.0f * __fdividef(I->ke_a + 3.0f * I->ke_b, cond);
-              if (fabsf(dist) > band) res = dist < 0.0f ? 1 : 0;
-            }
-          }
-          ++executed;
-          if (res == 1) {
-            // decided in FP32; the p-value is evaluated when the records are read
-            rm = true;
-            pv_rm = -1.0 - (double)rr;
-          } else if (res == 2) {
-            if (MIXED) ++retests;
-            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, &k, 1)))
-              rm = exact_remove_fast<1>(*I, i, j, &k, 1, &pv_rm);
-          }
-        }
-        {
-          // lanes on the same edge learn of its removal in this step; one of them
-          // claims the edge and keeps its record for the flush
-          const unsigned act = __activemask();
-          const unsigned grp = __match_any_sync(act, (unsigned)(t - (unsigned long long)rank));
-          const unsigned rmask = __ballot_sync(act, rm) & grp;
-          if (rmask) {
-            if (lane == __ffs(rmask) - 1 && claim_edge(*I, i, j))
-              push_pending<1>(pend, np, *I, b, level, i, j, &k, 1, pv_rm);
-            live = false;
-          }
-        }
-        // a removed edge is left at once: the lane moves to its first position of
-        // the next edge (its positions are 32 apart)
-        const int steps = live ? 1 : (c - rank + 31) >> 5;
-        t += 32ull * (unsigned long long)steps;
-        if (t >= tend) break;
-        rank += 32 * steps;
-        bool moved = false;
-        while (rank >= c) {  // next edge (and row, and instance) along the flattened order
-          rank -= c;
-          moved = true;
-          if (++s == d) {
-            if (t >= L.work_prefix[b + 1]) {
-              b = find_inst_u(L.work_prefix, L.count, t);
-              I = L.inst + b;
-              base_t = L.work_prefix[b];
-            }
-            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
-            d = I->deg[i];
-            c = d - 1;
-            base = I->rowptr[i];
-            off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
-            s = (int)(off / (unsigned long long)c);
-            rank = (int)(off - (unsigned long long)s * c);
-            break;
-          }
-        }
-        if (moved) {
-          j = I->colidx[base + s];
-          if (MIXED) rij = __ldg(I->cor32 + i * I->p + j);
-          live = live_bit(I->adj, I->W, i, j);
-          steps_on_edge = 0;
-        } else if (live && (++steps_on_edge & 3u) == 0) {
-          live = live_bit(I->adj, I->W, i, j);
-        }
-      }
-      b_last = b;
-    }
-    __syncwarp();
-    flush_pending<1>(L, level, pend, np);
-    const unsigned grp = __match_any_sync(0xffffffffu, b_last);
-    const unsigned ex = __reduce_add_sync(grp, executed);
-    const unsigned rt = __reduce_add_sync(grp, retests);
-    if (b_last >= 0 && lane == __ffs(grp) - 1) {
-      atomicAdd(&L.inst[b_last].ctr[level].tests, (unsigned long long)ex);
-      if (rt) atomicAdd(&L.inst[b_last].ctr[level].retests, (unsigned long long)rt);
-    }
-  }
-}
 
 // p-values of the removals decided in FP32 (negative pmax), for every instance's
 // records: FP64 re-evaluation where the instance has an FP64 matrix -- a result below
@@ -841,7 +44,7 @@ __device__ __forceinline__ double warp_dot(const double *__restrict__ x, const d
 // FP64 re-tests deferred by the level kernels (instances without an FP64 matrix):
 // one warp per queued test forms the FP64 correlation entries it needs as dot
 // products of the FP64-standardised columns, lane 0 evaluates the reference formula.
-// Level-0 items set the kept lower-triangle bit; level >= 1 items remove the edge.
+// Level-0 items set the kept bits of both triangles; level >= 1 items remove the edge.
 constexpr int kRetestWarps = 8;
 __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
   __shared__ double Ms[kRetestWarps][(HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2)];
@@ -859,8 +62,10 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
     if (l == 0) {
       const double r = warp_dot(I.Z + i * n, I.Z + j * n, n) / I.denom;
       double pv;
-      if (lane == 0 && !decide_of_r(I, r, false, &pv))
-        atomicOr(I.adj + i * I.W + (j >> 5), 1u << (j & 31));  // kept: lower-triangle bit (i > j)
+      if (lane == 0 && !decide_of_r(I, r, false, &pv)) {  // kept: both triangles' bits
+        atomicOr(I.adj + i * I.W + (j >> 5), 1u << (j & 31));
+        atomicOr(I.adj + j * I.W + (i >> 5), 1u << (i & 31));
+      }
       continue;
     }
     if (!live_bit(I.adj, I.W, i, j)) continue;  // removed by another test meanwhile
@@ -887,22 +92,6 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
   }
 }
 
-// One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
-// is the lane-interleaved level-1 body, 2..8 the unrolled bodies, 0 any level.
-template <int LT, bool MIXED>
-__global__ void __launch_bounds__(kThreads, LT == 1 ? 4 : 2) level_kernel(Launch L) {
-  extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
-  unsigned int epoch = 0;
-  rebuild_phase(L);
-  if (!grid_barrier(L, epoch)) return;
-  scan_phase(L);
-  if (!grid_barrier(L, epoch)) return;
-  if (LT == 1)
-    tests_l1<MIXED>(L, nullptr);  // level 1 keeps the SM's on-chip memory for L1 cache
-  else
-    tests_generic<LT, MIXED>(L, rw_smem);
-}
-
 template <bool MIXED>
 void *kernel_for(int level) {
   switch (level) {
@@ -914,7 +103,7 @@ void *kernel_for(int level) {
     case 6: return (void *)level_kernel<6, MIXED>;
     case 7: return (void *)level_kernel<7, MIXED>;
     case 8: return (void *)level_kernel<8, MIXED>;
-    default: return (void *)level_kernel<0, MIXED>;
+    default: return level <= 12 ? level_kernel_9_12(level, MIXED) : level_kernel_13_16(level, MIXED);
   }
 }
 
@@ -955,7 +144,7 @@ hpc_status launch_level(const Launch &L, int precision, int grid, cudaStream_t s
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = L.level == 1 ? 0 : kRowCache * sizeof(unsigned long long);
+  cfg.dynamicSmemBytes = L.level == 1 || !L.row_cache ? 0 : kRowCache * sizeof(unsigned long long);
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;

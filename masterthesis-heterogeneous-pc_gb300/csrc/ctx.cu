@@ -195,6 +195,7 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.rq_cap = c->rq_cap;
   L.seg_prefix = c->prefixes + 3 * (c->count + 1);
   L.seg = c->seg + (size_t)level * c->total_segs;
+  L.row_cache = c->count == 1 && c->ih[0].p + 1 <= kRowCache;
   return L;
 }
 
@@ -218,13 +219,12 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   if (timed) HPC_CUDA(cudaEventRecord(ev[0], c->stream));
   if (level == 0) {
     if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-    if ((s = launch_level0(L, c->total_words, c->stream)) != HPC_OK) return s;
+    if ((s = launch_level0(L, c->total_tiles, c->stream)) != HPC_OK) return s;
     if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
-    if ((s = launch_mirror(L, c->total_tiles, c->stream)) != HPC_OK) return s;
     if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
     if ((s = launch_degrees(L, c->total_rows, c->stream)) != HPC_OK) return s;
     if ((s = launch_scan(L, c->stream)) != HPC_OK) return s;
-    c->timings.launches += queue ? 5 : 4;
+    c->timings.launches += queue ? 4 : 3;
     return HPC_OK;
   }
   // snapshot rebuild, test-count scan and CI tests in one launch

@@ -3,11 +3,10 @@
 // The live adjacency of an instance is a symmetric bitmask, p rows of W = ceil(p/32)
 // words (the reference keeps an int32 p x p matrix, src/util/state.cu:21-29).
 //
-// level0 + mirror replace testRowL0 (src/executor/testing/gpuRowTests.cu:4-27) /
+// level0 replaces testRowL0 (src/executor/testing/gpuRowTests.cu:4-27) /
 // testRowL0Triangluar (src/executor/testing/cpuRowTests.cpp:5-21): every pair i > j
-// is tested once on cor[i][j] (the lower-triangle entry the reference reads), the
-// kept bits are written for the lower triangle and then mirrored by 32 x 32
-// bit-tile transposes.
+// is tested once on cor[i][j] (the lower-triangle entry the reference reads), a warp
+// per 32 x 32 bit tile, which writes the tile and its transpose.
 //
 // degrees + scan after level 0: per-row popcounts, then one block per instance scans
 // the degrees into the offsets of each row's slot in the neighbour-list buffer. The
@@ -24,94 +23,90 @@
 namespace hpc {
 namespace {
 
-// one thread per (instance, row, word): 32 decisions for j < i
-__global__ void level0_kernel(Launch L, long long total) {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int b = find_inst(L.word_prefix, L.count, t);
-    const Inst &I = L.inst[b];
-    const long long lt = t - L.word_prefix[b];
-    const int64_t i = lt / I.W;
-    const int w = (int)(lt % I.W);
-    const int64_t j0 = (int64_t)w * 32;
-    uint32_t bits = 0;
-    if (j0 < i) {
-      const int jend = (i - j0) < 32 ? (int)(i - j0) : 32;
-      if (I.cor64) {
-        // FP64 entries: the exact formula only inside [r_lo, r_hi]
-        const double *row = I.cor64 + i * I.p;
-        for (int q = 0; q < jend; ++q) {
-          const double v = row[j0 + q];
-          const double av = fabs(v);
-          bool remove;
-          if (isnan(v) || av < I.r_lo)
-            remove = true;  // p certainly >= alpha (NaN r is treated as 0)
-          else if (av > I.r_hi)
-            remove = false;
-          else
-            remove = calc_pvalue64(v, I.n_obs) >= I.alpha;
-          if (!remove) bits |= 1u << q;
-        }
-      } else {
-        // FP32 tensor-core entries: pairs inside the band (or NaN) are queued for
-        // the FP64 re-test kernel, which sets their kept bits
-        const float *row = I.cor32 + i * I.p;
-        for (int q = 0; q < jend; ++q) {
-          const float av = fabsf(row[j0 + q]);
-          if (av < I.lo32) continue;
-          if (av > I.hi32) {
-            bits |= 1u << q;
-            continue;
-          }
-          const int64_t j = j0 + q;
-          const unsigned long long slot = atomicAdd(&L.lc->rq_count, 1ull);
-          if ((long long)slot < L.rq_cap) {
-            RetestItem *it = L.rq + slot;
-            it->i = (int32_t)i;
-            it->j = (int32_t)j;
-            it->level = 0;
-            it->inst = b;
-          } else {  // queue full: serial FP64 dot product here
-            const double *x = I.Z + i * I.n_z, *y = I.Z + j * I.n_z;
-            double s = 0.0;
-            for (int64_t k = 0; k < I.n_z; ++k) s = fma(x[k], y[k], s);
-            if (!(calc_pvalue64(s / I.denom, I.n_obs) >= I.alpha)) bits |= 1u << q;
-          }
-        }
-      }
-    }
-    I.adj[lt] = bits;
+// One warp per 32 x 32 bit tile (I, w), w <= I, of the lower triangle: lane q decides
+// the pairs (i, 32w + q) with j < i of the tile's 32 rows from the entries it reads
+// (32 consecutive entries per row: coalesced; eight rows' loads in flight), each
+// row's ballot is its word, and 32 more ballots transpose the tile, so that both
+// triangles are written here (the diagonal tile as the union of the two).
+__device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int b, int64_t i, int64_t j, double v64,
+                                            float v32) {
+  if (I.cor64) {
+    // FP64 entries: the exact formula only inside [r_lo, r_hi]
+    const double av = fabs(v64);
+    if (isnan(v64) || av < I.r_lo) return false;  // p certainly >= alpha (NaN r is treated as 0)
+    if (av > I.r_hi) return true;
+    return !(calc_pvalue64(v64, I.n_obs) >= I.alpha);
   }
+  // FP32 tensor-core entries: pairs inside the band (or NaN) are queued for the FP64
+  // re-test kernel, which sets their kept bits
+  const float av = fabsf(v32);
+  if (av > I.hi32) return true;
+  if (av < I.lo32) return false;
+  const unsigned long long slot = atomicAdd(&L.lc->rq_count, 1ull);
+  if ((long long)slot < L.rq_cap) {
+    RetestItem *it = L.rq + slot;
+    it->i = (int32_t)i;
+    it->j = (int32_t)j;
+    it->level = 0;
+    it->inst = b;
+    return false;
+  }
+  // queue full: serial FP64 dot product here
+  const double *x = I.Z + i * I.n_z, *y = I.Z + j * I.n_z;
+  double sum = 0.0;
+  for (int64_t k = 0; k < I.n_z; ++k) sum = fma(x[k], y[k], sum);
+  return !(calc_pvalue64(sum / I.denom, I.n_obs) >= I.alpha);
 }
 
-// Mirror the lower triangle into the upper: warp per 32x32 bit tile (I, w), w <= I.
-__global__ void mirror_bits_kernel(Launch L, long long total) {
+__global__ void level0_kernel(Launch L, long long total) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long t = warp; t < total; t += nwarps) {
     const int b = find_inst(L.tile_prefix, L.count, t);
-    const Inst &In = L.inst[b];
+    const Inst &I = L.inst[b];
     const long long lt = t - L.tile_prefix[b];
-    // lt -> (I, w), w <= I, row-major over the lower triangle of tiles
-    int64_t I = (int64_t)((sqrt(8.0 * (double)lt + 1.0) - 1.0) * 0.5);
-    while (I * (I + 1) / 2 > lt) --I;
-    while ((I + 1) * (I + 2) / 2 <= lt) ++I;
-    const int64_t w = lt - I * (I + 1) / 2;
-    const int64_t row = I * 32 + lane;
-    const int W = In.W;
-    uint32_t word = row < In.p ? In.adj[row * W + w] : 0u;
-    // transposed (lane c) = bits of column 32w + c over rows 32I .. 32I+31
-    uint32_t tr = 0;
+    // lt -> (TI, w), w <= TI, row-major over the lower triangle of tiles
+    int64_t TI = (int64_t)((sqrt(8.0 * (double)lt + 1.0) - 1.0) * 0.5);
+    while (TI * (TI + 1) / 2 > lt) --TI;
+    while ((TI + 1) * (TI + 2) / 2 <= lt) ++TI;
+    const int64_t w = lt - TI * (TI + 1) / 2;
+    const int64_t j = w * 32 + lane;
+    uint32_t word = 0;  // lane r: the word of row 32 TI + r
+#pragma unroll
+    for (int r0 = 0; r0 < 32; r0 += 8) {
+      double v64[8];
+      float v32[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int64_t i = TI * 32 + r0 + k;
+        v64[k] = 0.0;
+        v32[k] = 0.f;
+        if (i < I.p && j < i) {
+          if (I.cor64) v64[k] = I.cor64[i * I.p + j];
+          else v32[k] = I.cor32[i * I.p + j];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int64_t i = TI * 32 + r0 + k;
+        const bool keep = i < I.p && j < i && level0_keep(L, I, b, i, j, v64[k], v32[k]);
+        const uint32_t bits = __ballot_sync(0xffffffffu, keep);
+        if (lane == r0 + k) word = bits;
+      }
+    }
+    uint32_t tr = 0;  // lane c: the bits of column 32 w + c over the tile's rows
     for (int c = 0; c < 32; ++c) {
-      uint32_t bb = __ballot_sync(0xffffffffu, (word >> c) & 1u);
+      const uint32_t bb = __ballot_sync(0xffffffffu, (word >> c) & 1u);
       if (lane == c) tr = bb;
     }
-    const int64_t trow = w * 32 + lane;
-    if (I == w) {
-      if (row < In.p) In.adj[row * W + w] = word | tr;  // diagonal tile: symmetric union
-    } else if (trow < In.p) {
-      In.adj[trow * W + I] = tr;
+    const int W = I.W;
+    const int64_t row = TI * 32 + lane, trow = w * 32 + lane;
+    if (TI == w) {
+      if (row < I.p) I.adj[row * W + w] = word | tr;
+    } else {
+      if (row < I.p) I.adj[row * W + w] = word;
+      if (trow < I.p) I.adj[trow * W + TI] = tr;
     }
   }
 }
@@ -264,15 +259,9 @@ int blocks_for(long long items, int per_block) {
 
 }  // namespace
 
-hpc_status launch_level0(const Launch &L, long long total, cudaStream_t s) {
-  level0_kernel<<<blocks_for(total, 256), 256, 0, s>>>(L, total);
+hpc_status launch_level0(const Launch &L, long long total_tiles, cudaStream_t s) {
+  level0_kernel<<<blocks_for(total_tiles, 8), 256, 0, s>>>(L, total_tiles);
   HPC_LAUNCH_CHECK("level0_kernel");
-  return HPC_OK;
-}
-
-hpc_status launch_mirror(const Launch &L, long long total, cudaStream_t s) {
-  mirror_bits_kernel<<<blocks_for(total, 8), 256, 0, s>>>(L, total);
-  HPC_LAUNCH_CHECK("mirror_bits_kernel");
   return HPC_OK;
 }
 

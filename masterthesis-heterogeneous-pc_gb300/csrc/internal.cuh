@@ -130,7 +130,10 @@ struct Launch {
   long long rq_cap;
   const long long *seg_prefix;      // scan segments  sum ceil(p / kSegRows) (count + 1)
   SegAgg *seg;                      // this level's segment sums (zeroed before the level)
+  int row_cache;                    // the CI tests keep the row offsets in shared memory
 };
+// row offsets a level kernel of levels >= 2 caches in shared memory (one instance)
+constexpr int kRowCache = 5120;
 
 __device__ __forceinline__ int find_inst(const long long *prefix, int count, long long t) {
   int lo = 0, hi = count;  // largest b with prefix[b] <= t
@@ -188,8 +191,7 @@ struct TcArgs {                     // grouped tensor-core Gram
 };
 hpc_status launch_gram_tc(float *C, const TcArgs &a, long long total_tiles, cudaStream_t s);
 
-hpc_status launch_level0(const Launch &L, long long total_words, cudaStream_t s);
-hpc_status launch_mirror(const Launch &L, long long total_tiles, cudaStream_t s);
+hpc_status launch_level0(const Launch &L, long long total_tiles, cudaStream_t s);
 hpc_status launch_degrees(const Launch &L, long long total_rows, cudaStream_t s);
 hpc_status launch_scan(const Launch &L, cudaStream_t s);
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);

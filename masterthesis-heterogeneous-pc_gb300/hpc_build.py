@@ -21,7 +21,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ctx.cu", "correlation.cu", "graph.cu", "citest.cu", "gram_tc.cu", "noalloc.cu"]
+CU_SOURCES = ["citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
+              "noalloc.cu"]
 HOST_SOURCES = ["semgen.cpp", "serve.cpp"]
 
 
