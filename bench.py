@@ -48,7 +48,109 @@ WORKLOADS = {
                w_hi=1.0, alpha=0.01, seed=5, budget=150 * 10**9, max_level=4),
     "c4": dict(count=512, p=(20, 800), n=(200, 8000), degree=(1.0, 5.0), w_lo=0.1, w_hi=1.0, seed=4,
                alphas=(0.01, 0.05), max_level=-1),
+    # wide, hub-heavy: preferential attachment (2 parents per new node), p=15000, n=3000,
+    # weights +-[0.2, 1.0], alpha 0.05, FP32 data, split-BF16 tensor-core Gram. Run to a
+    # level cap: at level 4 the hubs alone would need ~1e10 tests each (reported).
+    "c3": dict(p=15000, n=3000, graph=1, degree=4.0, pa_parents=2, w_lo=0.2, w_hi=1.0, seed=3, alpha=0.05,
+               max_level=3),
 }
+
+
+def correlation_error(hg, c32, p, n, Xd, stream):
+    """max |rho| and max Fisher-|z| error of an FP32 correlation against the FP64 Gram of
+    the same observations (device-resident FP32 data at Xd)."""
+    ref = hg.SkeletonCalculator(p, n, max_level=0, precision=hg.PREC_FP64)
+    ref.set_stream(stream.cuda_stream)
+    ref.add_observations_device(Xd.data_ptr(), np.float32)
+    c64 = ref.correlation()
+    ref.close()
+    off = ~np.eye(p, dtype=bool)
+    a, b = c32.astype(np.float64)[off], c64[off]
+    drho = float(np.max(np.abs(a - b)))
+    clip = lambda x: np.clip(np.abs(x), 0.0, 0.9999999)  # noqa: E731
+    dz = float(np.max(np.abs(np.arctanh(clip(a)) - np.arctanh(clip(b))))) * float(np.sqrt(n - 3.0))
+    return {"max_abs_rho_err": drho, "max_abs_z_err": dz, "against": "FP64 Gram of the same data"}
+
+
+def run_c3(args, wl):
+    """Wide hub-heavy single instance: a step is the tensor-core correlation of the
+    step's observations (resident in HBM) plus levels 0..max_level. Reports the Gram's
+    tensor throughput and each level's tests."""
+    import torch
+
+    import heterogpc as hg
+    import hpc_build
+    if not os.path.exists(hg.LIB_PATH):
+        hpc_build.build_library()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    p, n = wl["p"], wl["n"]
+    max_level = wl["max_level"] if args.max_level is None else args.max_level
+    X = hg.sem_generate(p, n, wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"], wl["seed"],
+                        dtype=np.float32)
+    Xd = torch.from_numpy(X).to(dev)
+    sk = hg.SkeletonCalculator(p, n, alpha=wl["alpha"], max_level=max_level, precision=hg.PREC_MIXED_TC)
+    sk.set_stream(stream.cuda_stream)
+    flush = L2Flush(torch, dev)
+
+    def step():
+        sk.add_observations_device(Xd.data_ptr(), np.float32)
+        sk.reset()
+        return sk.run()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ms, cor_ms, gram_ms, skel_ms = [], [], [], []
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.steps):
+        flush()
+        a, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st = step()
+        b_.record(stream)
+        b_.synchronize()
+        ms.append(a.elapsed_time(b_))
+        t = sk.timings()
+        cor_ms.append(t["standardise_ms"] + t["gram_ms"])
+        gram_ms.append(t["gram_ms"])
+        skel_ms.append(t["skeleton_ms"])
+    clk = clocks.stop()
+    peaks = load_peaks()
+    n_pad = (n + 63) // 64 * 64
+    nb = (p + 127) // 128
+    gram_issued = nb * (nb + 1) / 2 * 2.0 * 128 * 128 * 4 * n_pad  # 128x128 upper tiles, four BF16 products
+    gram_alg = 3.0 * n * p * (p + 1)                  # three products, the survey's count
+    g_ms = float(np.median(gram_ms))
+    adj = sk.adjacency()
+    d = adj.sum(1).astype(np.int64)
+    from math import comb
+    next_level = len(st)
+    t_next = int(sum(int(x) * comb(int(x) - 1, next_level) for x in d if x - 1 >= next_level))
+    tests = sum(s_["executed_tests"] for s_ in st)
+    step_ms = float(np.median(ms))
+    # accuracy of the tensor-core correlation against an FP64 Gram of the same data
+    acc = correlation_error(hg, sk.correlation_f32(), p, n, Xd, stream)
+    line = {"metric": "skeletons/sec", "value": 1e3 / step_ms, "unit": "skeletons/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x4/f32/f64",
+            "data": "synthetic (seeded linear-Gaussian SEM)",
+            "config": {"workload": "c3", "p": p, "n": n, "graph": "preferential attachment, 2 parents",
+                       "alpha": wl["alpha"], "max_level": max_level, "precision": "tensor-core split-BF16 Gram, "
+                       "FP32 tests, FP64 re-tests within 1e-3 relative |z| of the threshold", "l2": L2Flush.desc},
+            "correlation_ms": float(np.median(cor_ms)), "skeleton_ms": float(np.median(skel_ms)),
+            "ci_tests_per_step": tests, "ci_tests_per_sec": tests / (float(np.median(skel_ms)) / 1e3),
+            "gram": {"ms": g_ms, "issued_tflops": gram_issued / g_ms / 1e9,
+                     "algorithmic_tflops": gram_alg / g_ms / 1e9, "peak_tflops": peaks["bf16_tflops"],
+                     "frac_issued": gram_issued / g_ms / 1e9 / peaks["bf16_tflops"],
+                     "peak_source": peaks["source"] + " (bf16_tflops, burst)"},
+            "levels": [{k: s_[k] for k in ("level", "max_degree", "potential_tests", "executed_tests", "retests",
+                                           "edges_after")} for s_ in st],
+            "next_level": {"level": next_level, "potential_tests": t_next, "max_degree": int(d.max())},
+            "accuracy": acc, "clocks": clk}
+    print(json.dumps(line), flush=True)
 
 
 class L2Flush:
@@ -351,6 +453,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=None, help="c4: number of instances (default 512)")
     ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
+    ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -369,6 +472,10 @@ def main():
     if args.workload == "c5":
         if rank == 0:
             run_c5(args, wl)
+        return
+    if args.workload == "c3":
+        if rank == 0:
+            run_c3(args, wl)
         return
 
     import torch
