@@ -46,7 +46,7 @@ __device__ __forceinline__ double warp_dot(const double *__restrict__ x, const d
 // products of the FP64-standardised columns, lane 0 evaluates the reference formula.
 // Level-0 items set the kept bits of both triangles; level >= 1 items remove the edge.
 constexpr int kRetestWarps = 8;
-__global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
+__global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_constant__ Launch L) {
   __shared__ double Ms[kRetestWarps][(HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2)];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   double *M = Ms[wib];
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(Launch L) {
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   for (unsigned long long q = warp; q < count; q += nwarps) {
     const RetestItem it = L.rq[q];
-    const Inst &I = L.inst[it.inst];
+    const Inst &I = *inst_of(L, it.inst);
     const int64_t i = it.i, j = it.j, n = I.n_z;
     const int l = it.level;
     if (l == 0) {

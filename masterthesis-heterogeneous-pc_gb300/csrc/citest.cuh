@@ -388,7 +388,7 @@ __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, 
 // kRowCache - 1 rows: the shared memory is then left to the L1 cache).
 __device__ __forceinline__ const unsigned long long *cache_row_work(const Launch &L, unsigned long long *smem) {
   if (!smem || !L.row_cache) return nullptr;
-  const Inst &I = L.inst[0];
+  const Inst &I = *inst_of(L, 0);
   for (int64_t r = threadIdx.x; r <= I.p; r += blockDim.x) smem[r] = __ldcg(I.row_work + r);
   __syncthreads();
   return smem;
@@ -501,7 +501,7 @@ __device__ __forceinline__ void flush_pending(const Launch &L, int level, PendRe
     int b = -1;
     if (won) {
       b = list[q].b;
-      I = L.inst + b;
+      I = inst_of(L, b);
     }
     const unsigned wm = __ballot_sync(0xffffffffu, won);
     if (won) {
@@ -579,7 +579,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
     int b_last = -1;
     // instance and row of the tile start (whole warp), then each lane's row
     int b = find_inst_u(L.work_prefix, L.count, t0);
-    const Inst *I = L.inst + b;
+    const Inst *I = inst_of(L, b);
     unsigned long long base_t = L.work_prefix[b];
     const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
     const bool active = t < tend;
@@ -587,7 +587,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
     int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
     if (active && !same) {  // the tile runs into the next instance
       b = find_inst_u(L.work_prefix, L.count, t);
-      I = L.inst + b;
+      I = inst_of(L, b);
       base_t = L.work_prefix[b];
       i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
     }
@@ -638,7 +638,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
             // next row with tests, possibly of the next instance
             if (t >= L.work_prefix[b + 1]) {
               b = find_inst_u(L.work_prefix, L.count, t);
-              I = L.inst + b;
+              I = inst_of(L, b);
               base_t = L.work_prefix[b];
             }
             i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
@@ -670,8 +670,8 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
     const unsigned ex = __reduce_add_sync(grp, executed);
     const unsigned rt = __reduce_add_sync(grp, retests);
     if (b_last >= 0 && lane == __ffs(grp) - 1) {
-      atomicAdd(&L.inst[b_last].ctr[level].tests, (unsigned long long)ex);
-      if (rt) atomicAdd(&L.inst[b_last].ctr[level].retests, (unsigned long long)rt);
+      atomicAdd(&inst_of(L, b_last)->ctr[level].tests, (unsigned long long)ex);
+      if (rt) atomicAdd(&inst_of(L, b_last)->ctr[level].retests, (unsigned long long)rt);
     }
   }
 }
@@ -710,7 +710,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
     int b_last = -1;
     // instance and row of the tile start (whole warp), then each lane's row
     int b = find_inst_u(L.work_prefix, L.count, t0);
-    const Inst *I = L.inst + b;
+    const Inst *I = inst_of(L, b);
     unsigned long long base_t = L.work_prefix[b];
     const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
     const bool active = t < tend;
@@ -718,7 +718,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
     int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
     if (active && !same) {  // the tile runs into the next instance
       b = find_inst_u(L.work_prefix, L.count, t);
-      I = L.inst + b;
+      I = inst_of(L, b);
       base_t = L.work_prefix[b];
       i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
     }
@@ -789,7 +789,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
           if (++s == d) {
             if (t >= L.work_prefix[b + 1]) {
               b = find_inst_u(L.work_prefix, L.count, t);
-              I = L.inst + b;
+              I = inst_of(L, b);
               base_t = L.work_prefix[b];
             }
             i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
@@ -819,8 +819,8 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
     const unsigned ex = __reduce_add_sync(grp, executed);
     const unsigned rt = __reduce_add_sync(grp, retests);
     if (b_last >= 0 && lane == __ffs(grp) - 1) {
-      atomicAdd(&L.inst[b_last].ctr[level].tests, (unsigned long long)ex);
-      if (rt) atomicAdd(&L.inst[b_last].ctr[level].retests, (unsigned long long)rt);
+      atomicAdd(&inst_of(L, b_last)->ctr[level].tests, (unsigned long long)ex);
+      if (rt) atomicAdd(&inst_of(L, b_last)->ctr[level].retests, (unsigned long long)rt);
     }
   }
 }
@@ -828,7 +828,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 // One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
 // is the lane-interleaved level-1 body, LT = 2..16 the bodies unrolled for l = LT.
 template <int LT, bool MIXED>
-__global__ void __launch_bounds__(kThreads, LT == 1 ? 4 : 2) level_kernel(Launch L) {
+__global__ void __launch_bounds__(kThreads, LT == 1 ? 4 : 2) level_kernel(const __grid_constant__ Launch L) {
   extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
   rebuild_phase(L);

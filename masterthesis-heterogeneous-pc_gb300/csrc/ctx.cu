@@ -196,6 +196,9 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.seg_prefix = c->prefixes + 3 * (c->count + 1);
   L.seg = c->seg + (size_t)level * c->total_segs;
   L.row_cache = c->count == 1 && c->ih[0].p + 1 <= kRowCache;
+  L.total_rows = c->total_rows;
+  L.total_segs = c->total_segs;
+  L.inst0 = c->inst_host[0];
   return L;
 }
 

@@ -58,13 +58,13 @@ __device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int 
   return !(calc_pvalue64(sum / I.denom, I.n_obs) >= I.alpha);
 }
 
-__global__ void level0_kernel(Launch L, long long total) {
+__global__ void level0_kernel(const __grid_constant__ Launch L, long long total) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long t = warp; t < total; t += nwarps) {
     const int b = find_inst(L.tile_prefix, L.count, t);
-    const Inst &I = L.inst[b];
+    const Inst &I = *inst_of(L, b);
     const long long lt = t - L.tile_prefix[b];
     // lt -> (TI, w), w <= TI, row-major over the lower triangle of tiles
     int64_t TI = (int64_t)((sqrt(8.0 * (double)lt + 1.0) - 1.0) * 0.5);
@@ -111,13 +111,13 @@ __global__ void level0_kernel(Launch L, long long total) {
   }
 }
 
-__global__ void degrees_kernel(Launch L, long long total) {
+__global__ void degrees_kernel(const __grid_constant__ Launch L, long long total) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long t = warp; t < total; t += nwarps) {
     const int b = find_inst(L.row_prefix, L.count, t);
-    const Inst &I = L.inst[b];
+    const Inst &I = *inst_of(L, b);
     const int64_t i = t - L.row_prefix[b];
     int c = 0;
     for (int w = lane; w < I.W; w += 32) c += __popc(I.adj[i * I.W + w]);
@@ -131,7 +131,7 @@ constexpr int kScanThreads = 512;
 // One block per instance: exclusive prefixes of degrees (CSR offsets) and of per-row
 // test counts, the instance's level summary; the last block to finish forms the
 // prefix of test counts over instances (work_prefix) for the CI-test kernel.
-__global__ void __launch_bounds__(kScanThreads) scan_kernel(Launch L) {
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(const __grid_constant__ Launch L) {
   __shared__ unsigned long long s_deg[kScanThreads];
   __shared__ unsigned long long s_work[kScanThreads];
   __shared__ int s_max[kScanThreads / 32];
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(Launch L) {
   __shared__ int s_over;
   __shared__ bool s_last;
   const int b = blockIdx.x;
-  const Inst &I = L.inst[b];
+  const Inst &I = *inst_of(L, b);
   const int level = L.level;
   const int tid = threadIdx.x;
   const int64_t p = I.p;
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(Launch L) {
     unsigned long long acc = 0;
     for (int q = 0; q < L.count; ++q) {
       L.work_prefix[q] = acc;
-      acc += *(volatile unsigned long long *)&L.inst[q].ctr[level].work_total;
+      acc += *(volatile unsigned long long *)&inst_of(L, q)->ctr[level].work_total;
     }
     L.work_prefix[L.count] = acc;
   }

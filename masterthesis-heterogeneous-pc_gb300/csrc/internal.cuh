@@ -131,7 +131,25 @@ struct Launch {
   const long long *seg_prefix;      // scan segments  sum ceil(p / kSegRows) (count + 1)
   SegAgg *seg;                      // this level's segment sums (zeroed before the level)
   int row_cache;                    // the CI tests keep the row offsets in shared memory
+  long long total_rows, total_segs; // row_prefix[count], seg_prefix[count]
+  Inst inst0;                       // inst[0] by value: read from the parameter bank when count == 1
 };
+
+// Instance b's descriptor: the launch's parameter copy for a single instance (no
+// memory round trip; kernels take the Launch as a __grid_constant__ parameter), else
+// the device table.
+__device__ __forceinline__ const Inst *inst_of(const Launch &L, int b) {
+  return L.count == 1 ? &L.inst0 : L.inst + b;
+}
+// first and end rows / scan segments of instance b in the flattened spaces
+__device__ __forceinline__ long long row_begin(const Launch &L, int b) { return L.count == 1 ? 0 : L.row_prefix[b]; }
+__device__ __forceinline__ long long row_end(const Launch &L, int b) {
+  return L.count == 1 ? L.total_rows : L.row_prefix[b + 1];
+}
+__device__ __forceinline__ long long seg_begin(const Launch &L, int b) { return L.count == 1 ? 0 : L.seg_prefix[b]; }
+__device__ __forceinline__ long long seg_end(const Launch &L, int b) {
+  return L.count == 1 ? L.total_segs : L.seg_prefix[b + 1];
+}
 // row offsets a level kernel of levels >= 2 caches in shared memory (one instance)
 constexpr int kRowCache = 5120;
 

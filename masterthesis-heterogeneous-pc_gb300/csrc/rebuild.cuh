@@ -52,7 +52,7 @@ __device__ __forceinline__ bool grid_barrier(const Launch &L, unsigned int &epoc
     while (ld_acquire_u32(&L.lc->bar) < target) {
       if (globaltimer_ns() - t0 > 2000000000ull) {
         ok = 0;
-        atomicOr(&L.inst[0].g->err, kErrTimeout);
+        atomicOr(&inst_of(L, 0)->g->err, kErrTimeout);
         break;
       }
       __nanosleep(20);
@@ -81,7 +81,7 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
   const int lane = threadIdx.x & 31;
   const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long R = L.row_prefix[L.count];
+  const long long R = L.total_rows;
   const long long per = (R + nw - 1) / nw;
   long long t = gw * per;
   const long long tend = t + per < R ? t + per : R;
@@ -103,27 +103,32 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
   };
   int b = -1;
   const Inst *I = nullptr;
+  long long r0 = 0, r1 = 0, g0 = 0;
   bool skip = false;
   for (; t < tend; ++t) {
-    if (b < 0 || t >= L.row_prefix[b + 1]) {
-      b = find_inst(L.row_prefix, L.count, t);
-      I = L.inst + b;
+    if (b < 0 || t >= r1) {
+      b = L.count == 1 ? 0 : find_inst(L.row_prefix, L.count, t);
+      I = inst_of(L, b);
+      r0 = row_begin(L, b);
+      r1 = row_end(L, b);
+      g0 = seg_begin(L, b);
       skip = csr_overflow(*I);  // flagged by the scan phase; the host resizes and reruns
     }
-    const int64_t i = t - L.row_prefix[b];
-    const long long g = L.seg_prefix[b] + i / kSegRows;
+    const int64_t i = t - r0;
+    const long long g = g0 + i / kSegRows;
     if (g != cur) {
       flush();
       cur = g;
     }
-    if (skip) continue;
+    // the row's first 128 words, its slot offset and the overflow flag in one round trip
     const uint32_t *words = I->adj + i * I->W;
     const int W = I->W;
-    // the first 128 words of the row are loaded at once (one round trip for p <= 4096)
     uint32_t pre[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) pre[q] = q * 32 + lane < W ? words[q * 32 + lane] : 0u;
-    int *out = I->colidx + I->rowptr[i];
+    const int slot = I->rowptr[i];
+    if (skip) continue;
+    int *out = I->colidx + slot;
     int cnt = 0;
     auto emit = [&](uint32_t word, int w) {
       const int c = __popc(word);
@@ -188,7 +193,7 @@ struct InstSums {
 __device__ __forceinline__ InstSums warp_inst_sums(const Launch &L, int b, long long g) {
   const int lane = threadIdx.x & 31;
   InstSums r{0, 0, 0, 0, 0, 0};
-  for (long long q = L.seg_prefix[b] + lane; q < L.seg_prefix[b + 1]; q += 32) {
+  for (long long q = seg_begin(L, b) + lane; q < seg_end(L, b); q += 32) {
     const SegAgg *S = L.seg + q;
     const unsigned long long wk = __ldcg(&S->work);
     r.deg += __ldcg(&S->deg);
@@ -214,7 +219,7 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
   __shared__ InstSums s_sum;
   __shared__ int s_bad;
   const int level = L.level;
-  const long long G = L.seg_prefix[L.count];
+  const long long G = L.total_segs;
   // the prefix of the instances' test counts, by the last block (the first blocks
   // take the segments)
   if (blockIdx.x == gridDim.x - 1) {
@@ -226,11 +231,11 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
       unsigned long long tot = 0;
       if (b < L.count) {
         int over = 0;
-        for (long long q = L.seg_prefix[b]; q < L.seg_prefix[b + 1]; ++q) {
+        for (long long q = seg_begin(L, b); q < seg_end(L, b); ++q) {
           tot += __ldcg(&L.seg[q].work);
           over |= __ldcg(&L.seg[q].over);
         }
-        if (over || csr_overflow(L.inst[b])) tot = 0;
+        if (over || csr_overflow(*inst_of(L, b))) tot = 0;
       }
       unsigned long long all;
       const unsigned long long ex = block_exclusive_scan(tot, &all);
@@ -242,8 +247,8 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
     if (threadIdx.x == 0) L.work_prefix[L.count] = s_carry;
   }
   for (long long g = blockIdx.x; g < G; g += gridDim.x) {
-    const int b = find_inst(L.seg_prefix, L.count, g);
-    const Inst &I = L.inst[b];
+    const int b = L.count == 1 ? 0 : find_inst(L.seg_prefix, L.count, g);
+    const Inst &I = *inst_of(L, b);
     if (threadIdx.x < 32) {
       const InstSums r = warp_inst_sums(L, b, g);
       if (threadIdx.x == 0) {
@@ -253,7 +258,7 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
     }
     __syncthreads();
     const bool bad = s_bad != 0;
-    const int64_t r = (g - L.seg_prefix[b]) * kSegRows + threadIdx.x;
+    const int64_t r = (g - seg_begin(L, b)) * kSegRows + threadIdx.x;
     const bool valid = r < I.p;
     int over = 0;
     const int d = valid && !bad ? __ldcg(I.deg + r) : 0;
@@ -261,7 +266,7 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
     unsigned long long all;
     const unsigned long long ex = block_exclusive_scan(w, &all);
     if (valid && !bad) I.row_work[r] = s_sum.base + ex;
-    if (threadIdx.x == 0 && g == L.seg_prefix[b + 1] - 1) {
+    if (threadIdx.x == 0 && g == seg_end(L, b) - 1) {
       // last segment of the instance: its level summary
       DevCounters &C = I.ctr[level];
       if (!bad) I.row_work[I.p] = s_sum.work;
