@@ -528,18 +528,21 @@ def main():
     flush = L2Flush(torch, dev)
 
     def timed_steps(s, k):
-        ms, stats = [], None
+        # every step queued behind the previous one (flush, start event, whole
+        # skeleton, end event) and collected once: the events time the skeleton's GPU
+        # work, not the host's launch and synchronisation
+        evs = []
         launches0 = s.timings()["launches"]
         for _ in range(k):
             flush()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            s.reset()
-            s.run()
+            s.run_async()
             b.record(stream)
-            b.synchronize()
-            ms.append(a.elapsed_time(b))
-            stats = s.level_stats
+            evs.append((a, b))
+        stats = s.wait()
+        torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in evs]
         launches = s.timings()["launches"] - launches0
         return ms, stats, launches
 

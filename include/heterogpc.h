@@ -174,6 +174,16 @@ hpc_status hpc_run_level(hpc_ctx *ctx, int level, hpc_level_stats *stats);
  * levels 0..max_level (opts.max_level, -1 = until exhausted), stopping early once a
  * level has no tests. `stats` receives up to `cap` per-level records. */
 hpc_status hpc_run_skeleton(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_run);
+/* hpc_run_skeleton from a fresh start (as after hpc_ctx_reset) without waiting: the
+ * counter reset and the captured level sequence are queued on the context's stream
+ * and the call returns; hpc_wait synchronises and returns what hpc_run_skeleton
+ * would have. Runs of the same context queue behind each other, so a caller can keep
+ * the GPU busy across skeletons. Needs a known opts.max_level; the first run of a
+ * context (which sizes the neighbour lists) and runs that cannot be captured (legacy
+ * default stream, graphs disabled) are run synchronously inside the call. No
+ * counterpart in the reference, which runs one skeleton per process. */
+hpc_status hpc_run_skeleton_async(hpc_ctx *ctx);
+hpc_status hpc_wait(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_run);
 
 /* ---- results ------------------------------------------------------------ */
 /* adj (row-major p x p, 1 = edge kept), the reference's state.adj. */

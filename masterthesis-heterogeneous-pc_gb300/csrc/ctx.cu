@@ -372,9 +372,13 @@ bool capturable(cudaStream_t s) { return s != nullptr && s != cudaStreamLegacy &
 
 // Run levels first..last with one host sync at the end; the whole sequence 0..last
 // is captured once into a CUDA graph and replayed while the buffers stay in place.
-hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
+hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait = true) {
   hpc_status s;
   auto enqueue_all = [&](bool timed) -> hpc_status {
+    if (first == 0) {  // a skeleton from the start: its counters and records begin at zero
+      HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)c->count * kLevels, c->stream));
+      HPC_CUDA(cudaMemsetAsync(c->gctr, 0, sizeof(DevGlobal) * (size_t)c->count, c->stream));
+    }
     HPC_CUDA(cudaMemsetAsync(c->lc + first, 0, sizeof(LaunchCounters) * (size_t)(last - first + 1), c->stream));
     HPC_CUDA(cudaMemsetAsync(c->seg + (size_t)first * c->total_segs, 0,
                              sizeof(SegAgg) * (size_t)c->total_segs * (size_t)(last - first + 1), c->stream));
@@ -416,7 +420,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph) {
     if ((s = enqueue_all(true)) != HPC_OK) return s;
     c->last_run_graph = false;
   }
-  return pull_counters(c);
+  return wait ? pull_counters(c) : HPC_OK;
 }
 
 // ---- correlation ----------------------------------------------------------
@@ -859,9 +863,13 @@ hpc_status hpc_get_correlation_f32(hpc_ctx *c, float *C) {
   return HPC_OK;
 }
 
+// results and further runs first collect a pending asynchronous run
+hpc_status settle(hpc_ctx *c) { return c->async_pending ? hpc_wait(c, nullptr, 0, nullptr) : HPC_OK; }
+
 hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   if (!c->have_cor) {
     set_error("run before a correlation matrix was computed or loaded");
     return HPC_ERR_STATE;
@@ -891,6 +899,7 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
 hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   if (!c->have_cor) {
     set_error("run before a correlation matrix was computed or loaded");
     return HPC_ERR_STATE;
@@ -970,9 +979,70 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
   return HPC_ERR_CAPACITY;
 }
 
+hpc_status hpc_run_skeleton_async(hpc_ctx *c) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (!c->have_cor) {
+    set_error("run before a correlation matrix was computed or loaded");
+    return HPC_ERR_STATE;
+  }
+  if (c->opts.max_level < 0) {
+    set_error("an asynchronous run needs a known max_level");
+    return HPC_ERR_INVALID_ARG;
+  }
+  const int top = c->opts.max_level;
+  if (!(c->colidx && c->recs) || !c->graphs_enabled || !capturable(c->stream)) {
+    // the first run sizes the neighbour lists; uncapturable streams run eagerly
+    c->async_pending = false;
+    if ((s = hpc_ctx_reset(c)) != HPC_OK) return s;
+    return hpc_run_skeleton(c, nullptr, 0, nullptr);
+  }
+  for (auto &h : c->ih) h.edges = h.p * (h.p - 1) / 2;
+  HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
+  if ((s = run_levels(c, 0, top, true, false)) != HPC_OK) return s;
+  HPC_CUDA(cudaEventRecord(c->evr[1], c->stream));
+  c->async_pending = true;
+  c->async_top = top;
+  c->records_final = false;
+  c->next_level = 0;
+  return HPC_OK;
+}
+
+hpc_status hpc_wait(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  int ran = 0;
+  if (c->async_pending) {
+    c->async_pending = false;
+    if ((s = pull_counters(c)) != HPC_OK) return s;
+    if (any_csr_overflow(c)) {
+      // the data changed since the neighbour lists were sized: resize and rerun
+      bool changed;
+      if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
+      if ((s = hpc_ctx_reset(c)) != HPC_OK) return s;
+      return hpc_run_skeleton(c, stats, cap, levels_run);
+    }
+    if ((s = global_errors(c)) != HPC_OK) return s;
+    c->next_level = c->async_top + 1;
+    float tr = 0.f;
+    HPC_CUDA(cudaEventElapsedTime(&tr, c->evr[0], c->evr[1]));
+    c->timings.skeleton_ms = tr;
+  }
+  for (int l = 0; l < c->next_level; ++l) {
+    hpc_level_stats st{};
+    if ((s = collect_level(c, l, &st)) != HPC_OK) return s;
+    if (stats && ran < cap) stats[ran] = st;
+    ++ran;
+    if (l >= 1 && !any_work(c, l)) break;
+  }
+  if (levels_run) *levels_run = ran;
+  return HPC_OK;
+}
+
 hpc_status hpc_batch_level_stats(hpc_ctx *c, int idx, hpc_level_stats *out, int cap, int *levels) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   if ((s = check_index(c, idx)) != HPC_OK) return s;
   int k = 0;
   for (int l = 0; l < c->next_level && l <= HPC_MAX_LEVEL; ++l) {
@@ -986,6 +1056,7 @@ hpc_status hpc_batch_level_stats(hpc_ctx *c, int idx, hpc_level_stats *out, int 
 hpc_status hpc_batch_get_adjacency(hpc_ctx *c, int idx, uint8_t *out) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   if ((s = check_index(c, idx)) != HPC_OK) return s;
   if (!out) {
     set_error("null output pointer");
@@ -1018,6 +1089,7 @@ hpc_status hpc_batch_edge_count(hpc_ctx *c, int idx, int64_t *edges) {
   }
   hpc_status s = check_index(c, idx);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   *edges = c->ih[idx].edges;
   return HPC_OK;
 }
@@ -1045,6 +1117,7 @@ static hpc_status finalize_records(hpc_ctx *c) {
 hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *out, int64_t cap, int64_t *count) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   if ((s = check_index(c, idx)) != HPC_OK) return s;
   if (!count) {
     set_error("null count pointer");
@@ -1073,6 +1146,7 @@ hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t ca
 hpc_status hpc_get_sepsets(hpc_ctx *c, int32_t *out, int max_cond) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
   if (!out || max_cond < 1) {
     set_error("null output or max_cond < 1");
     return HPC_ERR_INVALID_ARG;

@@ -23,25 +23,11 @@
 namespace hpc {
 namespace {
 
-// One warp per 32 x 32 bit tile (I, w), w <= I, of the lower triangle: lane q decides
-// the pairs (i, 32w + q) with j < i of the tile's 32 rows from the entries it reads
-// (32 consecutive entries per row: coalesced; eight rows' loads in flight), each
-// row's ballot is its word, and 32 more ballots transpose the tile, so that both
-// triangles are written here (the diagonal tile as the union of the two).
-__device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int b, int64_t i, int64_t j, double v64,
-                                            float v32) {
-  if (I.cor64) {
-    // FP64 entries: the exact formula only inside [r_lo, r_hi]
-    const double av = fabs(v64);
-    if (isnan(v64) || av < I.r_lo) return false;  // p certainly >= alpha (NaN r is treated as 0)
-    if (av > I.r_hi) return true;
-    return !(calc_pvalue64(v64, I.n_obs) >= I.alpha);
-  }
-  // FP32 tensor-core entries: pairs inside the band (or NaN) are queued for the FP64
-  // re-test kernel, which sets their kept bits
-  const float av = fabsf(v32);
-  if (av > I.hi32) return true;
-  if (av < I.lo32) return false;
+// the rare cases of a level-0 decision (FP64 entry inside the guard band, FP32 entry
+// inside the tensor-core band): out of line, so that the 32 unrolled decisions of a
+// tile stay small
+__device__ __noinline__ bool level0_keep_slow(const Launch &L, const Inst &I, int b, int64_t i, int64_t j, double v64) {
+  if (I.cor64) return !(calc_pvalue64(v64, I.n_obs) >= I.alpha);
   const unsigned long long slot = atomicAdd(&L.lc->rq_count, 1ull);
   if ((long long)slot < L.rq_cap) {
     RetestItem *it = L.rq + slot;
@@ -49,7 +35,7 @@ __device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int 
     it->j = (int32_t)j;
     it->level = 0;
     it->inst = b;
-    return false;
+    return false;  // the FP64 re-test kernel sets the kept bits
   }
   // queue full: serial FP64 dot product here
   const double *x = I.Z + i * I.n_z, *y = I.Z + j * I.n_z;
@@ -58,56 +44,79 @@ __device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int 
   return !(calc_pvalue64(sum / I.denom, I.n_obs) >= I.alpha);
 }
 
-__global__ void level0_kernel(const __grid_constant__ Launch L, long long total) {
-  const int lane = threadIdx.x & 31;
-  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long t = warp; t < total; t += nwarps) {
-    const int b = find_inst(L.tile_prefix, L.count, t);
+__device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int b, int64_t i, int64_t j, double v64,
+                                            float v32) {
+  if (I.cor64) {
+    // FP64 entries: the exact formula only inside [r_lo, r_hi]
+    const double av = fabs(v64);
+    if (isnan(v64) || av < I.r_lo) return false;  // p certainly >= alpha (NaN r is treated as 0)
+    if (av > I.r_hi) return true;
+    return level0_keep_slow(L, I, b, i, j, v64);
+  }
+  // FP32 tensor-core entries: pairs inside the band (or NaN) are re-tested in FP64
+  const float av = fabsf(v32);
+  if (av > I.hi32) return true;
+  if (av < I.lo32) return false;
+  return level0_keep_slow(L, I, b, i, j, 0.0);
+}
+
+// One 4-warp block per 32 x 32 bit tile (TI, w), w <= TI, of the lower triangle: warp
+// q decides rows 8q..8q+7 of the tile -- lane c the pairs (i, 32w + c) with j < i, from
+// the entries it reads (32 consecutive entries per row: coalesced; the eight rows'
+// loads issued together) -- and each row's ballot is its word; warp 0 then transposes
+// the tile with 32 more ballots and writes both triangles (the diagonal tile as the
+// union of the two).
+constexpr int kL0Threads = 128;
+__global__ void __launch_bounds__(kL0Threads) level0_kernel(const __grid_constant__ Launch L, long long total) {
+  __shared__ uint32_t s_word[32];
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    const int b = L.count == 1 ? 0 : find_inst(L.tile_prefix, L.count, t);
     const Inst &I = *inst_of(L, b);
-    const long long lt = t - L.tile_prefix[b];
+    const long long lt = t - (L.count == 1 ? 0 : L.tile_prefix[b]);
     // lt -> (TI, w), w <= TI, row-major over the lower triangle of tiles
     int64_t TI = (int64_t)((sqrt(8.0 * (double)lt + 1.0) - 1.0) * 0.5);
     while (TI * (TI + 1) / 2 > lt) --TI;
     while ((TI + 1) * (TI + 2) / 2 <= lt) ++TI;
     const int64_t w = lt - TI * (TI + 1) / 2;
     const int64_t j = w * 32 + lane;
-    uint32_t word = 0;  // lane r: the word of row 32 TI + r
+    double v64[8];
+    float v32[8];
 #pragma unroll
-    for (int r0 = 0; r0 < 32; r0 += 8) {
-      double v64[8];
-      float v32[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int64_t i = TI * 32 + r0 + k;
-        v64[k] = 0.0;
-        v32[k] = 0.f;
-        if (i < I.p && j < i) {
-          if (I.cor64) v64[k] = I.cor64[i * I.p + j];
-          else v32[k] = I.cor32[i * I.p + j];
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int64_t i = TI * 32 + r0 + k;
-        const bool keep = i < I.p && j < i && level0_keep(L, I, b, i, j, v64[k], v32[k]);
-        const uint32_t bits = __ballot_sync(0xffffffffu, keep);
-        if (lane == r0 + k) word = bits;
+    for (int k = 0; k < 8; ++k) {
+      const int64_t i = TI * 32 + wq * 8 + k;
+      v64[k] = 0.0;
+      v32[k] = 0.f;
+      if (i < I.p && j < i) {
+        if (I.cor64) v64[k] = I.cor64[i * I.p + j];
+        else v32[k] = I.cor32[i * I.p + j];
       }
     }
-    uint32_t tr = 0;  // lane c: the bits of column 32 w + c over the tile's rows
-    for (int c = 0; c < 32; ++c) {
-      const uint32_t bb = __ballot_sync(0xffffffffu, (word >> c) & 1u);
-      if (lane == c) tr = bb;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int64_t i = TI * 32 + wq * 8 + k;
+      const bool keep = i < I.p && j < i && level0_keep(L, I, b, i, j, v64[k], v32[k]);
+      const uint32_t bits = __ballot_sync(0xffffffffu, keep);
+      if (lane == 0) s_word[wq * 8 + k] = bits;
     }
-    const int W = I.W;
-    const int64_t row = TI * 32 + lane, trow = w * 32 + lane;
-    if (TI == w) {
-      if (row < I.p) I.adj[row * W + w] = word | tr;
-    } else {
-      if (row < I.p) I.adj[row * W + w] = word;
-      if (trow < I.p) I.adj[trow * W + TI] = tr;
+    __syncthreads();
+    if (wq == 0) {
+      const uint32_t word = s_word[lane];  // the word of row 32 TI + lane
+      uint32_t tr = 0;                     // lane c: the bits of column 32 w + c
+      for (int c = 0; c < 32; ++c) {
+        const uint32_t bb = __ballot_sync(0xffffffffu, (word >> c) & 1u);
+        if (lane == c) tr = bb;
+      }
+      const int W = I.W;
+      const int64_t row = TI * 32 + lane, trow = w * 32 + lane;
+      if (TI == w) {
+        if (row < I.p) I.adj[row * W + w] = word | tr;
+      } else {
+        if (row < I.p) I.adj[row * W + w] = word;
+        if (trow < I.p) I.adj[trow * W + TI] = tr;
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -126,114 +135,72 @@ __global__ void degrees_kernel(const __grid_constant__ Launch L, long long total
   }
 }
 
-constexpr int kScanThreads = 512;
+constexpr int kScanThreads = 1024;
 
-// One block per instance: exclusive prefixes of degrees (CSR offsets) and of per-row
-// test counts, the instance's level summary; the last block to finish forms the
-// prefix of test counts over instances (work_prefix) for the CI-test kernel.
+// After level 0, one block per instance: the exclusive prefix of the degrees, i.e. the
+// offset of each row's slot in the neighbour-list buffer (kept for the rest of the
+// skeleton), and the instance's level-0 summary. Warp-shuffle scan; level 0 has no CI
+// tests, so the test counts and their prefix are zero.
 __global__ void __launch_bounds__(kScanThreads) scan_kernel(const __grid_constant__ Launch L) {
-  __shared__ unsigned long long s_deg[kScanThreads];
-  __shared__ unsigned long long s_work[kScanThreads];
+  __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ int s_max[kScanThreads / 32];
-  __shared__ int s_rows[kScanThreads / 32];
-  __shared__ int s_over;
-  __shared__ bool s_last;
   const int b = blockIdx.x;
   const Inst &I = *inst_of(L, b);
-  const int level = L.level;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int64_t p = I.p;
   const int64_t per = (p + kScanThreads - 1) / kScanThreads;
   const int64_t lo = tid * per, hi = (lo + per) < p ? (lo + per) : p;
-  if (tid == 0) s_over = 0;
-  __syncthreads();
-  unsigned long long sd = 0, sw = 0;
-  int mx = 0, rows = 0;
-  bool over = false;
+  unsigned long long sd = 0;
+  int mx = 0;
   for (int64_t i = lo; i < hi; ++i) {
     const int d = I.deg[i];
     sd += (unsigned long long)d;
     mx = max(mx, d);
-    if (level >= 1 && d - 1 >= level) {
-      const unsigned long long c = binom_sat(d - 1, level);
-      const unsigned long long w = (unsigned long long)d * c;
-      if (c == 0xFFFFFFFFFFFFFFFFull || w / (unsigned long long)d != c || sw + w < sw) over = true;
-      sw += w;
-      ++rows;
+  }
+  unsigned long long incl = sd;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += x;
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if (lane == 31) s_warp[wid] = incl;
+  if (lane == 0) s_max[wid] = mx;
+  __syncthreads();
+  if (wid == 0) {  // scan of the warp totals
+    unsigned long long v = s_warp[lane], iv = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long x = __shfl_up_sync(0xffffffffu, iv, o);
+      if (lane >= o) iv += x;
+    }
+    s_warp[lane] = iv - v;  // exclusive
+    const int m = __reduce_max_sync(0xffffffffu, s_max[lane]);
+    if (lane == 31) {
+      // level-0 summary of the instance
+      DevCounters &C = I.ctr[0];
+      const unsigned long long e2 = iv;
+      I.rowptr[p] = (int)e2;
+      I.row_work[p] = 0;
+      C.edges2 = e2;
+      C.work_total = 0;
+      C.max_deg = m;
+      C.rows = 0;
+      C.tests = 0;
+      C.retests = 0;
+      C.deleted = 0;
+      C.band_violations = 0;
+      C.rec_begin = I.g->rec_count;
+      L.work_prefix[b] = 0;
+      if (b == L.count - 1) L.work_prefix[L.count] = 0;
     }
   }
-  s_deg[tid] = sd;
-  s_work[tid] = sw;
-  for (int o = 16; o > 0; o >>= 1) {
-    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    rows += __shfl_xor_sync(0xffffffffu, rows, o);
-  }
-  if ((tid & 31) == 0) {
-    s_max[tid >> 5] = mx;
-    s_rows[tid >> 5] = rows;
-  }
-  if (over) atomicOr(&s_over, 1);
   __syncthreads();
-  for (int off = 1; off < kScanThreads; off <<= 1) {  // Hillis-Steele inclusive scan
-    const unsigned long long x = tid >= off ? s_deg[tid - off] : 0ull;
-    const unsigned long long y = tid >= off ? s_work[tid - off] : 0ull;
-    __syncthreads();
-    s_deg[tid] += x;
-    s_work[tid] += y;
-    __syncthreads();
-  }
-  unsigned long long bd = tid > 0 ? s_deg[tid - 1] : 0ull;
-  unsigned long long bw = tid > 0 ? s_work[tid - 1] : 0ull;
+  unsigned long long bd = s_warp[wid] + incl - sd;
   for (int64_t i = lo; i < hi; ++i) {
     I.rowptr[i] = (int)bd;
-    I.row_work[i] = bw;
-    const int d = I.deg[i];
-    bd += (unsigned long long)d;
-    if (level >= 1 && d - 1 >= level) bw += (unsigned long long)d * binom_sat(d - 1, level);
-  }
-  if (tid == 0) {
-    DevCounters &C = I.ctr[level];
-    const unsigned long long e2 = s_deg[kScanThreads - 1];
-    unsigned long long work = s_work[kScanThreads - 1];
-    I.rowptr[p] = (int)e2;
-    I.row_work[p] = work;
-    int m = 0, r = 0;
-    for (int w = 0; w < kScanThreads / 32; ++w) {
-      m = max(m, s_max[w]);
-      r += s_rows[w];
-    }
-    if (s_over) {
-      atomicOr(&I.g->err, kErrWorkOverflow);
-      work = 0;  // nothing of this level runs for the instance
-    }
-    if (level >= 1 && (long long)e2 > I.colidx_cap) {
-      atomicOr(&I.g->err, kErrCsrOverflow);  // neighbour lists do not fit: resized by the host
-      work = 0;
-    }
-    C.edges2 = e2;
-    C.work_total = work;
-    C.max_deg = m;
-    C.rows = r;
-    C.tests = 0;
-    C.retests = 0;
-    C.deleted = 0;
-    C.band_violations = 0;
-    C.rec_begin = I.g->rec_count;
-    __threadfence();
-    const unsigned int done = atomicAdd(&L.lc->scan_done, 1u);
-    s_last = done == (unsigned int)L.count - 1;
-  }
-  __syncthreads();
-  if (s_last && tid == 0) {
-    // last block: the prefix of the instances' test counts (the other blocks'
-    // counters are visible after their fence and this block's atomic)
-    __threadfence();
-    unsigned long long acc = 0;
-    for (int q = 0; q < L.count; ++q) {
-      L.work_prefix[q] = acc;
-      acc += *(volatile unsigned long long *)&inst_of(L, q)->ctr[level].work_total;
-    }
-    L.work_prefix[L.count] = acc;
+    I.row_work[i] = 0;
+    bd += (unsigned long long)I.deg[i];
   }
 }
 
@@ -260,7 +227,8 @@ int blocks_for(long long items, int per_block) {
 }  // namespace
 
 hpc_status launch_level0(const Launch &L, long long total_tiles, cudaStream_t s) {
-  level0_kernel<<<blocks_for(total_tiles, 8), 256, 0, s>>>(L, total_tiles);
+  const int blocks = (int)std::max<long long>(1, std::min<long long>(total_tiles, 152LL * 16 * 8));
+  level0_kernel<<<blocks, kL0Threads, 0, s>>>(L, total_tiles);
   HPC_LAUNCH_CHECK("level0_kernel");
   return HPC_OK;
 }

@@ -296,4 +296,6 @@ struct hpc_ctx {
   bool have_cor = false;
   int next_level = 0;
   bool records_final = true;     // the records' FP32 p-values have been evaluated in FP64
+  bool async_pending = false;    // an hpc_run_skeleton_async run not yet collected by hpc_wait
+  int async_top = -1;
 };

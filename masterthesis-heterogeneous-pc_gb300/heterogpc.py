@@ -100,6 +100,8 @@ _SIGS = {
     "hpc_correlation_noalloc_f64": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
     "hpc_run_level": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LevelStats)]),
     "hpc_run_skeleton": (C.c_int, [C.c_void_p, C.POINTER(LevelStats), C.c_int, C.POINTER(C.c_int)]),
+    "hpc_run_skeleton_async": (C.c_int, [C.c_void_p]),
+    "hpc_wait": (C.c_int, [C.c_void_p, C.POINTER(LevelStats), C.c_int, C.POINTER(C.c_int)]),
     "hpc_get_adjacency": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hpc_edge_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "hpc_get_sepsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
@@ -266,6 +268,19 @@ class SkeletonCalculator:
         ran = C.c_int(0)
         _check(lib().hpc_run_skeleton(self._h, arr, cap, C.byref(ran)))
         self.level_stats.extend(arr[i].as_dict() for i in range(ran.value))
+        return self.level_stats
+
+    def run_async(self):
+        """Queue a whole skeleton (from level 0) on the context's stream and return;
+        wait() collects it (hpc_run_skeleton_async / hpc_wait)."""
+        _check(lib().hpc_run_skeleton_async(self._h))
+
+    def wait(self):
+        cap = HPC_MAX_LEVEL + 1
+        arr = (LevelStats * cap)()
+        ran = C.c_int(0)
+        _check(lib().hpc_wait(self._h, arr, cap, C.byref(ran)))
+        self.level_stats = [arr[i].as_dict() for i in range(ran.value)]
         return self.level_stats
 
     def set_stream(self, stream_handle):
