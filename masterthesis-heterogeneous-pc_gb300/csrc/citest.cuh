@@ -567,10 +567,17 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
   const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
   int pos[LA], ids[LA];
+  // the first tile of every warp is its global index, later tiles come from the
+  // device-wide counter (one atomic round trip fewer per warp)
+  const unsigned long long nwarps = lanes >> 5;
+  bool first_tile = true;
   for (;;) {
-    unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(&L.lc->tile_next, 1ull);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
+    unsigned long long tile = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    if (!first_tile) {
+      if (lane == 0) tile = nwarps + atomicAdd(&L.lc->tile_next, 1ull);
+      tile = __shfl_sync(0xffffffffu, tile, 0);
+    }
+    first_tile = false;
     const unsigned long long t0 = tile * per_tile;
     if (t0 >= total) break;
     unsigned long long t = t0 + (unsigned long long)lane * m;
@@ -698,10 +705,17 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
   const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
+  // the first tile of every warp is its global index, later tiles come from the
+  // device-wide counter (one atomic round trip fewer per warp)
+  const unsigned long long nwarps = lanes >> 5;
+  bool first_tile = true;
   for (;;) {
-    unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(&L.lc->tile_next, 1ull);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
+    unsigned long long tile = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    if (!first_tile) {
+      if (lane == 0) tile = nwarps + atomicAdd(&L.lc->tile_next, 1ull);
+      tile = __shfl_sync(0xffffffffu, tile, 0);
+    }
+    first_tile = false;
     const unsigned long long t0 = tile * per_tile;
     if (t0 >= total) break;
     const unsigned long long tend = min(t0 + per_tile, total);
@@ -737,13 +751,19 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
       unsigned steps_on_edge = 0;
       for (;;) {
         const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
+        // the entries are loaded before the live bit is known (in bounds either way):
+        // the two round trips overlap instead of following each other
+        float x2 = 0.f, x3 = 0.f;
+        if (MIXED) {
+          x2 = __ldg(I->cor32 + i * I->p + k);
+          x3 = __ldg(I->cor32 + j * I->p + k);
+        }
         bool rm = false;
         double pv_rm = 0.0;
         if (live) {
           int res = 2;
           float rr = 0.f;
           if (MIXED) {
-            const float x2 = __ldg(I->cor32 + i * I->p + k), x3 = __ldg(I->cor32 + j * I->p + k);
             const float ax = 1.0f - x2 * x2, ay = 1.0f - x3 * x3;
             const float cond = fminf(ax, ay);
             if (cond > 1e-3f) {
