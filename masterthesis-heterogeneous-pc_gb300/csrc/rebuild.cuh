@@ -157,7 +157,45 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
     a_work += w;
     a_rows += w ? 1 : 0;
   }
-  flush();
+  // the warps' last segment sums are merged per block first (the warps of a block
+  // take neighbouring rows): one set of global atomics per block and segment
+  __shared__ long long s_seg[kLevelThreads / 32];
+  __shared__ unsigned long long s_v[kLevelThreads / 32][2];
+  __shared__ int s_i[kLevelThreads / 32][3];
+  const int wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_seg[wid] = cur;
+    s_v[wid][0] = a_deg;
+    s_v[wid][1] = a_work;
+    s_i[wid][0] = a_max;
+    s_i[wid][1] = a_rows;
+    s_i[wid][2] = a_over;
+  }
+  __syncthreads();
+  if (threadIdx.x < kLevelThreads / 32) {
+    const int q = threadIdx.x;
+    const long long g = s_seg[q];
+    bool leader = g >= 0;
+    for (int r = 0; r < q && leader; ++r) leader = s_seg[r] != g;
+    if (leader) {
+      unsigned long long v0 = 0, v1 = 0;
+      int i0 = 0, i1 = 0, i2 = 0;
+      for (int r = q; r < kLevelThreads / 32; ++r)
+        if (s_seg[r] == g) {
+          v0 += s_v[r][0];
+          v1 += s_v[r][1];
+          i0 = max(i0, s_i[r][0]);
+          i1 += s_i[r][1];
+          i2 |= s_i[r][2];
+        }
+      SegAgg &S = L.seg[g];
+      if (v0) atomicAdd(&S.deg, v0);
+      if (v1) atomicAdd(&S.work, v1);
+      if (i0) atomicMax(&S.max_deg, i0);
+      if (i1) atomicAdd(&S.rows, i1);
+      if (i2) atomicOr(&S.over, 1);
+    }
+  }
 }
 
 // block-wide exclusive scan of one value per thread; *total receives the sum
@@ -249,19 +287,21 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
   for (long long g = blockIdx.x; g < G; g += gridDim.x) {
     const int b = L.count == 1 ? 0 : find_inst(L.seg_prefix, L.count, g);
     const Inst &I = *inst_of(L, b);
+    // the row's degree is read before the segment sums (one round trip for both)
+    const int64_t r = (g - seg_begin(L, b)) * kSegRows + threadIdx.x;
+    const bool valid = r < I.p;
+    const int d_row = valid ? __ldcg(I.deg + r) : 0;
     if (threadIdx.x < 32) {
-      const InstSums r = warp_inst_sums(L, b, g);
+      const InstSums rs = warp_inst_sums(L, b, g);
       if (threadIdx.x == 0) {
-        s_sum = r;
-        s_bad = (r.over || csr_overflow(I)) ? 1 : 0;
+        s_sum = rs;
+        s_bad = (rs.over || csr_overflow(I)) ? 1 : 0;
       }
     }
     __syncthreads();
     const bool bad = s_bad != 0;
-    const int64_t r = (g - seg_begin(L, b)) * kSegRows + threadIdx.x;
-    const bool valid = r < I.p;
     int over = 0;
-    const int d = valid && !bad ? __ldcg(I.deg + r) : 0;
+    const int d = bad ? 0 : d_row;
     const unsigned long long w = row_tests(d, level, &over);
     unsigned long long all;
     const unsigned long long ex = block_exclusive_scan(w, &all);

@@ -126,7 +126,8 @@ __device__ __forceinline__ unsigned long long binom_fast(int n, int k) {
   return binom_sat(n, k);
 }
 
-// unrank_lex (below) with table lookups
+// unrank_lex (below) with table lookups (the member x only moves forward, so one
+// unranking costs about m lookups)
 __device__ __forceinline__ void unrank_lex_fast(unsigned long long rank, int l, int m, int *pos) {
   int x = 0;
   for (int i = 0; i < l; ++i) {
