@@ -15,9 +15,11 @@
 // Here every test of the level is one index of a flattened space
 //   t in [0, sum_b T_l(b)),  T_l(b) = sum_i d_i * C(d_i - 1, l)
 // ordered by (instance b, row i, neighbour slot s, lexicographic subset rank). Warps
-// claim tiles of 32 * m consecutive tests with one atomicAdd on a device-wide counter;
-// each lane takes m consecutive tests, finds its instance and row by binary search,
-// unranks its first subset once (the order of ithCombination,
+// take tiles of 32 * m consecutive tests (the first by their index, later ones with
+// one atomicAdd on a device-wide counter); the warp finds the row of its tile start by
+// a 32-ary search, each lane its own row from the next 32 row offsets. At level 1 the
+// lanes are interleaved over the tile (tests_l1); at levels >= 2 each lane takes m
+// consecutive tests, unranks its first subset once (the order of ithCombination,
 // src/util/cuda_util.cu:34-50) and then steps to the lexicographic successor. Lanes
 // stop testing an edge as soon as its live bit is cleared (the reference's
 // `adj == 0` early exit, gpuRowTests.cu:166-168).
@@ -36,8 +38,8 @@
 // dot products of the standardised data.
 //
 // Removal (src/executor/testing/cpuUtil.cpp:23-48, gpuRowTests.cu:172-201): the lane
-// clearing the (min, max) bit with atomicAnd owns the edge, clears the mirror bit and
-// appends one separation-set record.
+// clearing the (min, max) bit with atomicAnd owns the edge and clears the mirror bit;
+// its separation-set record is appended when the warp's tile is done.
 //
 // A level is one cooperative launch (level_kernel): snapshot rebuild and test-count
 // scan (rebuild.cuh), each followed by a grid barrier, then the CI tests.
@@ -564,7 +566,11 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
   const unsigned long long *rw_c = cache_row_work(L, rw_smem);
   // tests per lane per tile: about four tiles per lane of the grid, 1..64
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
-  const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
+  // a level with at most four tests per lane of the grid runs in one round of tiles
+  // (one set-up per warp; the lane's further tests are successor steps), a larger one
+  // in about four tiles per lane for balance
+  const int m = total <= lanes * 4ull ? (int)((total + lanes - 1) / lanes)
+                                      : (int)max(1ull, min(64ull, total / (lanes * 4ull)));
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
   int pos[LA], ids[LA];
   // the first tile of every warp is its global index, later tiles come from the
