@@ -120,8 +120,10 @@ def run_c3(args, wl):
     clk = clocks.stop()
     peaks = load_peaks()
     n_pad = (n + 63) // 64 * 64
-    nb = (p + 127) // 128
-    gram_issued = nb * (nb + 1) / 2 * 2.0 * 128 * 128 * 4 * n_pad  # 128x128 upper tiles, four BF16 products
+    p_pad = (p + 255) // 256 * 256
+    nb, nbc = p_pad // 128, p_pad // 256
+    tiles = sum(nbc - bi // 2 for bi in range(nb))  # 128 x 256 tiles reaching the upper triangle
+    gram_issued = tiles * 2.0 * 128 * 256 * 4 * n_pad  # four BF16 products
     gram_alg = 3.0 * n * p * (p + 1)                  # three products, the survey's count
     g_ms = float(np.median(gram_ms))
     adj = sk.adjacency()

@@ -12,9 +12,11 @@
 // so one BF16 GEMM with K' = 4n gives the products of the split. With lo.lo the
 // product of the two 16-bit representations is complete and what is left is the
 // rounding of lo (2^-17 relative per value), which averages out over n samples;
-// without it a systematic error of about 2^-18 |r| remains. Only
-// upper-triangle 128 x 128 tiles are computed; each is written twice (direct and
-// mirrored), diagonal tiles from their upper half only, so C is exactly symmetric.
+// without it a systematic error of about 2^-18 |r| remains. Tiles are 128 rows x 256
+// columns (one N = 256 MMA per K-step: 48 KB of operands per 2 x 128 x 256 x 64 flops,
+// a third more work per byte of L2 traffic than square 128-tiles), over the column
+// blocks that reach the upper triangle; each entry with col >= row is written twice
+// (direct and mirrored), so C is exactly symmetric.
 //
 // The tensor core rounds its FP32 accumulator once per MMA; along K = 3n that is
 // thousands of roundings with a systematic bias (measured about 3e-5 on sums of
@@ -22,17 +24,18 @@
 // TMEM buffers while the epilogue warps drain the other into FP32 registers
 // (round-to-nearest adds): about 3n/256 register additions per output instead.
 //
-// Kernel structure (one CTA of 6 warps per tile, 6-stage shared-memory ring):
-//   warp 0 lane 0   TMA producer: cp.async.bulk.tensor of the A (rows of P) and B
-//                   (rows of Q) 128 x 64 tiles, 128-byte swizzle, into stage s,
+// Kernel structure (one CTA of 10 warps per tile, 4-stage shared-memory ring):
+//   warp 0 lane 0   TMA producer: cp.async.bulk.tensor of the A (128 rows of P) and B
+//                   (256 rows of Q) x 64 K tiles, 128-byte swizzle, into stage s,
 //                   completion counted on full[s] (expect_tx)
-//   warp 1 lane 0   MMA issuer: 4 x tcgen05.mma.kind::f16 (M=128, N=128, K=16) per
-//                   stage into TMEM buffer g % 2 (128 columns each), tcgen05.commit
+//   warp 1 lane 0   MMA issuer: 4 x tcgen05.mma.kind::f16 (M=128, N=256, K=16) per
+//                   stage into TMEM buffer g % 2 (256 columns each), tcgen05.commit
 //                   to empty[s] (frees the stage) and, after each group of kGroup
 //                   stages, to acc_full[g % 2]
-//   warps 2-5       accumulate: tcgen05.ld 32x32b of their TMEM lane quadrant
-//                   (warp % 4), add into 128 registers per thread, arrive on
-//                   acc_empty[g % 2]; finally write the tile
+//   warps 2-9       accumulate: tcgen05.ld 32x32b of their TMEM lane quadrant
+//                   (warp % 4) and column half ((warp - 2) / 4), add into 128
+//                   registers per thread, arrive on acc_empty[g % 2]; finally write
+//                   the tile
 // Every mbarrier wait is bounded by a %globaltimer deadline; on time-out the CTA
 // records kErrTimeout, stops issuing, waits (bounded) for what it already issued,
 // frees its TMEM and returns.
@@ -45,15 +48,16 @@
 namespace hpc {
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 64;  // tile: 128 x 128 outputs, 64 bf16 (128 B) of K per stage
-constexpr int kStages = 6;
+constexpr int TM = 128, TN = 256, TK = 64;  // tile: 128 x 256 outputs, 64 bf16 (128 B) of K per stage
+constexpr int kStages = 4;
 constexpr int kSlices = 4;       // K' = kSlices * n_pad: hi.hi, hi.lo, lo.hi, lo.lo
 constexpr int kStageBytesA = TM * TK * 2;   // 16 KB
-constexpr int kStageBytesB = TN * TK * 2;   // 16 KB
+constexpr int kStageBytesB = TN * TK * 2;   // 32 KB
 constexpr int kStageBytes = kStageBytesA + kStageBytesB;
-constexpr int kTmemCols = 256;   // two 128-column accumulators
+constexpr int kTmemCols = 512;   // two 256-column accumulators
 constexpr int kGroup = 4;        // k-blocks (16 MMAs) per accumulation group
-constexpr int kThreadsTc = 192;  // producer warp, MMA warp, 4 accumulator warps
+constexpr int kAccWarps = 8;     // two per TMEM lane quadrant, 128 columns each
+constexpr int kThreadsTc = 64 + 32 * kAccWarps;  // producer warp, MMA warp, accumulator warps
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -114,7 +118,7 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
 }
 
 // Instruction descriptor of tcgen05.mma.kind::f16: D = F32, A = B = BF16, both
-// K-major, N = 128, M = 128.
+// K-major, N = 256, M = 128.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
                             ((uint32_t)(TM >> 4) << 24);
 
@@ -151,7 +155,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__host__ __device__ __forceinline__ int64_t tc_p_pad_dev(int64_t p) { return (p + TM - 1) / TM * TM; }
+// operand rows padded to the column-block size, so that every TMA box lies inside
+__host__ __device__ __forceinline__ int64_t tc_p_pad_dev(int64_t p) { return (p + TN - 1) / TN * TN; }
+
+// the tiles of one instance: 128-row blocks bi, and for each the 256-column blocks
+// bj >= bi / 2 (those holding entries with col >= row)
+__host__ __device__ __forceinline__ int tc_col_blocks(int64_t p) { return (int)((tc_p_pad_dev(p) + TN - 1) / TN); }
 
 struct alignas(1024) TcSmem {
   uint8_t stage[kStages][kStageBytes];
@@ -181,17 +190,17 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   const int inst = find_inst(ta.tile_prefix, ta.count, tt);
   long long t = tt - ta.tile_prefix[inst];
   const int64_t p = ta.p[inst];
-  const int nb = (int)(tc_p_pad_dev(p) / TM);
+  const int nbc = tc_col_blocks(p);
   const int kblocks = (int)(kSlices * ((ta.n[inst] + TK - 1) / TK));
   const CUtensorMap *mapP = ta.maps + 2 * inst, *mapQ = ta.maps + 2 * inst + 1;
   float *__restrict__ C = Call + ta.c_off[inst];
   int *err = ta.err;
   int bi = 0;
-  while (t >= nb - bi) {
-    t -= nb - bi;
+  while (t >= nbc - bi / 2) {
+    t -= nbc - bi / 2;
     ++bi;
   }
-  const int bj = bi + (int)t;
+  const int bj = bi / 2 + (int)t;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -200,7 +209,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.acc_full[b], 1);
-      mbar_init(&sm.acc_empty[b], 4);  // one arrival per accumulator warp
+      mbar_init(&sm.acc_empty[b], kAccWarps);  // one arrival per accumulator warp
     }
     mbar_init(&sm.drain, 1);
     sm.abort = 0;
@@ -239,7 +248,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         fail(sm, err);
         break;
       }
-      const uint32_t dcol = tmem + (uint32_t)(b * 128);
+      const uint32_t dcol = tmem + (uint32_t)(b * TN);
       const int kb_end = min(kblocks, (g + 1) * kGroup);
       for (int kb = g * kGroup; kb < kb_end; ++kb) {
         const int s = kb % kStages;
@@ -263,11 +272,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     mma_commit(&sm.drain);
     if (!mbar_wait(&sm.drain, 0)) fail(sm, err);
   } else if (warp >= 2) {
-    // accumulator warps: TMEM lane quadrant warp % 4 = rows 32*(warp%4) .. +31
+    // accumulator warps: TMEM lane quadrant warp % 4 = rows 32*(warp%4) .. +31, and
+    // column half (warp - 2) / 4
     const int quad = warp & 3;
-    float acc[TN];
+    const int half = (warp - 2) >> 2;
+    constexpr int kCols = TN / 2;
+    float acc[kCols];
 #pragma unroll
-    for (int q = 0; q < TN; ++q) acc[q] = 0.f;
+    for (int q = 0; q < kCols; ++q) acc[q] = 0.f;
     const int groups = (kblocks + kGroup - 1) / kGroup;
     bool ok = true;
     for (int g = 0; g < groups; ++g) {
@@ -280,9 +292,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       __syncwarp();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-      for (int c0 = 0; c0 < TN; c0 += 32) {
+      for (int c0 = 0; c0 < kCols; c0 += 32) {
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * 128 + c0), v);
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TN + half * kCols + c0), v);
 #pragma unroll
         for (int q = 0; q < 32; ++q) acc[c0 + q] += v[q];
       }
@@ -291,16 +303,31 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       if (lane == 0) mbar_arrive(&sm.acc_empty[b]);
     }
     if (ok && !aborted(sm)) {
-      const int r = quad * 32 + lane;  // tile row
-      const int64_t row = (int64_t)bi * TM + r;
-      const bool diag = bi == bj;
+      const int64_t row = (int64_t)bi * TM + quad * 32 + lane;
+      const int64_t col0 = (int64_t)bj * TN + half * kCols;
+      // mirrored copy: for a fixed column the warp's lanes hold 32 consecutive rows,
+      // i.e. a contiguous run of C[col][...]: coalesced as it is
 #pragma unroll
-      for (int cc = 0; cc < TN; ++cc) {
-        const int64_t col = (int64_t)bj * TN + cc;
-        if (row < p && col < p && (!diag || cc >= r)) {
-          C[row * p + col] = acc[cc];
-          C[col * p + row] = acc[cc];
+      for (int cc = 0; cc < kCols; ++cc) {
+        const int64_t col = col0 + cc;
+        if (row < p && col < p && col >= row) C[col * p + row] = acc[cc];
+      }
+      // direct copy through the idle stage buffer (every MMA has completed): each
+      // warp transposes 32 x 32 blocks (33-float rows, no bank conflicts) so that its
+      // lanes write 32 consecutive columns of one row per store
+      float *tb = reinterpret_cast<float *>(sm.stage[0]) + (warp - 2) * 32 * 33;
+#pragma unroll
+      for (int c0 = 0; c0 < kCols; c0 += 32) {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) tb[lane * 33 + q] = acc[c0 + q];
+        __syncwarp();
+        const int64_t col = col0 + c0 + lane;
+#pragma unroll 4
+        for (int k = 0; k < 32; ++k) {
+          const int64_t rw = (int64_t)bi * TM + quad * 32 + k;
+          if (rw < p && col < p && col >= rw) C[rw * p + col] = tb[k * 33 + lane];
         }
+        __syncwarp();
       }
     }
   }
@@ -360,12 +387,14 @@ hpc_status make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int
 }  // namespace
 
 int64_t tc_n_pad(int64_t n) { return (n + TK - 1) / TK * TK; }
-int64_t tc_p_pad(int64_t p) { return (p + TM - 1) / TM * TM; }
+int64_t tc_p_pad(int64_t p) { return tc_p_pad_dev(p); }
 int64_t tc_k(int64_t n) { return kSlices * tc_n_pad(n); }
 
 long long gram_tc_tiles(int64_t p) {
-  const long long nb = tc_p_pad(p) / TM;
-  return nb * (nb + 1) / 2;
+  const long long nb = tc_p_pad(p) / TM, nbc = tc_col_blocks(p);
+  long long t = 0;
+  for (long long bi = 0; bi < nb; ++bi) t += nbc - bi / 2;
+  return t;
 }
 
 // Tensor maps of one instance's operands P and Q (tc_p_pad(p) rows of tc_k(n) bf16).
