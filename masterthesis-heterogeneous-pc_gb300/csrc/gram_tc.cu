@@ -57,6 +57,7 @@ constexpr int kStageBytes = kStageBytesA + kStageBytesB;
 constexpr int kTmemCols = 512;   // two 256-column accumulators
 constexpr int kGroup = 4;        // k-blocks (16 MMAs) per accumulation group
 constexpr int kAccWarps = 8;     // two per TMEM lane quadrant, 128 columns each
+constexpr int kBand = 16;        // row blocks per band of the tile order (even)
 constexpr int kThreadsTc = 64 + 32 * kAccWarps;  // producer warp, MMA warp, accumulator warps
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
@@ -195,12 +196,28 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   const CUtensorMap *mapP = ta.maps + 2 * inst, *mapQ = ta.maps + 2 * inst + 1;
   float *__restrict__ C = Call + ta.c_off[inst];
   int *err = ta.err;
-  int bi = 0;
-  while (t >= nbc - bi / 2) {
-    t -= nbc - bi / 2;
-    ++bi;
+  // tiles in bands of kBand row blocks, each band column block by column block, so
+  // that the CTAs running at one time share a few A and B blocks that stay in L2
+  const int nb = (int)(tc_p_pad_dev(p) / TM);
+  int b0 = 0;
+  for (;;) {
+    const int b1 = min(nb, b0 + kBand);
+    long long cnt = 0;
+    for (int r = b0; r < b1; ++r) cnt += nbc - r / 2;
+    if (t < cnt || b1 >= nb) break;
+    t -= cnt;
+    b0 = b1;
   }
-  const int bj = bi / 2 + (int)t;
+  int bi = b0, bj = b0 / 2;
+  for (;; ++bj) {
+    // rows of the band whose column blocks start at or before bj (bi / 2 <= bj)
+    const int rows = min(min(nb, b0 + kBand), 2 * bj + 2) - b0;
+    if (t < rows) {
+      bi = b0 + (int)t;
+      break;
+    }
+    t -= rows;
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
