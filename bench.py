@@ -236,6 +236,28 @@ def run_c5(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def c4_roofline(levels, timings):
+    """The survey's byte model for the CI tests (4 l(l+3)/2 bytes of FP32 gathers per
+    executed test; the per-edge bytes are left out) over the level kernels' CUDA-event
+    times: per level and for levels >= 1 together."""
+    peaks = load_peaks()
+    per, tot_b, tot_ms = [], 0, 0.0
+    for s_ in levels:
+        l = s_["level"]
+        ms = timings["test_ms"][l] if l < len(timings["test_ms"]) else 0.0
+        if l == 0 or ms <= 0:
+            continue
+        b = s_["executed_tests"] * 4 * l * (l + 3) // 2
+        per.append({"level": l, "achieved_gbs": b / 1e9 / (ms / 1e3), "ms": ms})
+        tot_b += b
+        tot_ms += ms
+    ach = tot_b / 1e9 / (tot_ms / 1e3) if tot_ms > 0 else 0.0
+    return {"kernel": "level kernels, levels >= 1, all 512 instances per launch", "bound": "hbm",
+            "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+            "peak_source": peaks["source"] + " (hbm_gbs)", "model": "4 l(l+3)/2 bytes per executed test",
+            "per_level": per}
+
+
 def run_c4(args, wl):
     """Batched skeletons: one context, every level kernel launched once for all 512
     instances; a step is correlation (split-BF16 tensor-core Gram) + all levels of
@@ -307,6 +329,7 @@ def run_c4(args, wl):
             "plain_gpu_path": {"skeletons_per_sec": plain, "sample": "%d instances, one context each" % k_plain,
                                "precision": "fp64"},
             "speedup_vs_plain": value / plain, "clocks": clk,
+            "roofline": c4_roofline(st, t_cor),
             "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
                         "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
                         "retests": s_["retests"], "edges_after": s_["edges_after"],
