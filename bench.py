@@ -72,6 +72,14 @@ def correlation_error(hg, c32, p, n, Xd, stream):
     return {"max_abs_rho_err": drho, "max_abs_z_err": dz, "against": "FP64 Gram of the same data"}
 
 
+# c3's candidates (each run of the wide workload takes seconds): tile caps from the
+# default to long chunks for the hub rows, both level-1 lane mappings
+C3_CANDIDATES = [{"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32},
+                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 32},
+                 {"tile_cap": 8192, "tiles_per_lane": 8, "l1_lanes": 32},
+                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 1}]
+
+
 def run_c3(args, wl):
     """Wide hub-heavy single instance: a step is the tensor-core correlation of the
     step's observations (resident in HBM) plus levels 0..max_level. Reports the Gram's
@@ -99,6 +107,8 @@ def run_c3(args, wl):
         sk.reset()
         return sk.run()
 
+    step()
+    tuned = autotune_setup(args, sk, C3_CANDIDATES, 1)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -118,6 +128,12 @@ def run_c3(args, wl):
         gram_ms.append(t["gram_ms"])
         skel_ms.append(t["skeleton_ms"])
     clk = clocks.stop()
+    # one more skeleton kernel by kernel (outside the timed steps): per-level device times
+    sk.set_graphs(False)
+    st_k = step()
+    torch.cuda.synchronize()
+    level_ms = [float(s_["ms"]) for s_ in st_k]
+    sk.set_graphs(True)
     peaks = load_peaks()
     n_pad = (n + 63) // 64 * 64
     p_pad = (p + 255) // 256 * 256
@@ -148,11 +164,27 @@ def run_c3(args, wl):
                      "algorithmic_tflops": gram_alg / g_ms / 1e9, "peak_tflops": peaks["bf16_tflops"],
                      "frac_issued": gram_issued / g_ms / 1e9 / peaks["bf16_tflops"],
                      "peak_source": peaks["source"] + " (bf16_tflops, burst)"},
-            "levels": [{k: s_[k] for k in ("level", "max_degree", "potential_tests", "executed_tests", "retests",
-                                           "edges_after")} for s_ in st],
+            "levels": [dict({k: s_[k] for k in ("level", "max_degree", "potential_tests", "executed_tests", "retests",
+                                                "edges_after")}, ms=level_ms[q] if q < len(level_ms) else None)
+                       for q, s_ in enumerate(st)],
+            "level_ms_note": "per-level device time from one more skeleton run kernel by kernel (not graph-replayed)",
             "next_level": {"level": next_level, "potential_tests": t_next, "max_degree": int(d.max())},
-            "accuracy": acc, "clocks": clk}
+            "accuracy": acc, "clocks": clk, "tile_policy": tuned}
     print(json.dumps(line), flush=True)
+
+
+def autotune_setup(args, ctx, candidates, reps):
+    """hpc_autotune on a warmed-up context (untimed): the fastest candidate tile policy
+    of every level goes into the process-wide table that the timed runs read."""
+    if args.no_autotune:
+        return {"autotuned": False}
+    import heterogpc as hg
+    hg.tune_clear()
+    t0 = time.perf_counter()
+    chosen, entries = ctx.autotune(candidates, reps=reps)
+    return {"autotuned": True, "candidates": "built-in grid (24)" if candidates is None else candidates,
+            "chosen": {str(k): v for k, v in chosen.items()}, "entries": entries,
+            "tuning_s": time.perf_counter() - t0}
 
 
 class L2Flush:
@@ -289,6 +321,8 @@ def run_c4(args, wl):
 
     for _ in range(args.warmup):
         step()
+    tuned = autotune_setup(args, bt, None, 1)
+    step()
     torch.cuda.synchronize()
     ms, tests = [], 0
     clocks = ClockSampler(0)
@@ -328,7 +362,7 @@ def run_c4(args, wl):
             "skeleton_ms": t_cor["skeleton_ms"],
             "plain_gpu_path": {"skeletons_per_sec": plain, "sample": "%d instances, one context each" % k_plain,
                                "precision": "fp64"},
-            "speedup_vs_plain": value / plain, "clocks": clk,
+            "speedup_vs_plain": value / plain, "clocks": clk, "tile_policy": tuned,
             "roofline": c4_roofline(st, t_cor),
             "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
                         "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
@@ -479,6 +513,7 @@ def main():
     ap.add_argument("--count", type=int, default=None, help="c4: number of instances (default 512)")
     ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
     ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile policy (no hpc_autotune)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -589,6 +624,12 @@ def main():
         sk.run()
         sk_plain.reset()
         sk_plain.run()
+    # tile policy: hpc_autotune (untimed set-up, like a library's heuristics query) over
+    # its built-in candidates, then one more warm-up run of each context with the table
+    tuned = autotune_setup(args, sk, None, 2)
+    for s_ in (sk, sk_plain):
+        s_.reset()
+        s_.run()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -681,7 +722,8 @@ def main():
                                "ms_per_step": sum(plain_ms) / args.steps, "precision": "fp64"},
             "correlation": {"ms": cor_ms, "gram_ms": cor_t["gram_ms"], "standardise_ms": cor_t["standardise_ms"],
                             "kernel": "gram_f64_kernel", "fp64_gflops": gram_flops / (cor_t["gram_ms"] / 1e3) / 1e9},
-            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+            "tile_policy": tuned}
     if not args.no_cpu_baseline:
         from oracle import oracle as orc
         hpc_build.build_oracle()

@@ -185,6 +185,46 @@ hpc_status hpc_run_skeleton(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *
 hpc_status hpc_run_skeleton_async(hpc_ctx *ctx);
 hpc_status hpc_wait(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_run);
 
+/* ---- tile policy and autotuner -------------------------------------------
+ * No counterpart in the reference, whose launch shapes are fixed
+ * (src/executor/gpuExecutor.cu:45-106). The CI tests of a level are a flattened
+ * space of (row, neighbour, subset) indices that warps claim in tiles; a tile policy
+ * sets how a launch cuts it:
+ *   tile_cap        largest run of consecutive tests (subset chunk) a lane takes per tile
+ *   tiles_per_lane  target number of tiles per lane of the grid (balance vs claim cost)
+ *   l1_lanes        level 1 only: 32 = a warp's lanes interleaved over one edge's tests,
+ *                   1 = each lane a chunk of consecutive tests
+ * Defaults: 64, 4, 32. A process-wide table holds policies keyed by buckets of
+ * (largest p of the launch, level, largest degree at the level start), buckets being
+ * bit lengths; every level kernel reads its entry on the device after its test-count
+ * scan, so the table also steers CUDA-graph replays. */
+typedef struct hpc_tune_params {
+  int tile_cap;        /* 1..65536 */
+  int tiles_per_lane;  /* 1..64 */
+  int l1_lanes;        /* 1 or 32 */
+} hpc_tune_params;
+/* Sets (prm != NULL) or erases (NULL) the table entry of the key's buckets. */
+hpc_status hpc_tune_set(int64_t p, int level, int max_degree, const hpc_tune_params *prm);
+/* The policy a launch with this key uses; *found (optional) = 0 when it is the default. */
+hpc_status hpc_tune_lookup(int64_t p, int level, int max_degree, hpc_tune_params *out, int *found);
+hpc_status hpc_tune_clear(void);
+/* The table as a text file (entries only), and back: loaded entries replace those of
+ * the same key. */
+hpc_status hpc_tune_save(const char *path);
+hpc_status hpc_tune_load(const char *path);
+/* Forces one policy on every level of the context's runs (NULL = the table again). */
+hpc_status hpc_ctx_set_tune(hpc_ctx *ctx, const hpc_tune_params *force);
+/* Autotuner: runs the context's skeleton (on its current correlation, kernel by
+ * kernel) once per candidate policy and repetition, times every level's CI-test
+ * kernel with CUDA events, and stores for each level the fastest candidate under the
+ * level's key. cands/ncands: the candidates (NULL = the built-in grid: tile_cap
+ * 16, 64, 256, 1024 x tiles_per_lane 2, 4, 8 x l1_lanes 32, 1). chosen (optional,
+ * HPC_MAX_LEVEL + 1 entries) receives each level's choice (zeros for levels not run);
+ * *entries (optional) the number of table entries written. Decisions, and so the
+ * skeleton, do not depend on the policy; the context is reset afterwards. */
+hpc_status hpc_autotune(hpc_ctx *ctx, const hpc_tune_params *cands, int ncands, int reps, hpc_tune_params *chosen,
+                        int *entries);
+
 /* ---- results ------------------------------------------------------------ */
 /* adj (row-major p x p, 1 = edge kept), the reference's state.adj. */
 hpc_status hpc_get_adjacency(hpc_ctx *ctx, uint8_t *adj_host);

@@ -549,8 +549,46 @@ __device__ __forceinline__ bool push_retest(const Launch &L, int b, int64_t i, i
   return true;
 }
 
+// The level's tile policy: the forced one, else the context's table entry for (largest
+// p, level, largest degree at the level start), else the defaults. Read after the
+// scan phase's grid barrier (the degree is formed there).
+__device__ __forceinline__ TuneEntry tile_policy(const Launch &L) {
+  TuneEntry te = L.force;
+  if (te.tile_cap <= 0 && L.tune) {
+    const int md = *(volatile const int *)&L.lc->max_deg;
+    te = L.tune[((size_t)L.p_bucket * (HPC_MAX_LEVEL + 1) + L.level) * kTuneDB + tune_bucket(md, kTuneDB)];
+  }
+  if (te.tile_cap <= 0) te = TuneEntry{kTuneDefaultCap, kTuneDefaultTpl, kTuneDefaultL1Lanes, 0};
+  te.tiles_per_lane = max(1, te.tiles_per_lane);
+  return te;
+}
+
+// tests per lane per tile: about te.tiles_per_lane tiles per lane of the grid, at most
+// te.tile_cap; a level with at most tiles_per_lane tests per lane runs in one round of
+// tiles (one set-up per warp; the lane's further tests are successor steps)
+__device__ __forceinline__ int tile_tests_per_lane(unsigned long long total, unsigned long long lanes,
+                                                   const TuneEntry &te, bool one_round) {
+  const unsigned long long tpl = (unsigned long long)te.tiles_per_lane;
+  if (one_round && total <= lanes * tpl) return (int)((total + lanes - 1) / lanes);
+  return (int)max(1ull, min((unsigned long long)te.tile_cap, total / (lanes * tpl)));
+}
+
+// Tiles are claimed in increasing order (tile = nwarps + counter), so once an edge is
+// removed, every tile lying wholly inside its remaining tests holds nothing to do:
+// raising the counter to the tile that holds the edge's end (which may hold tests of
+// the next edge, so it is still claimed) skips them all. edge_end and tile_end are
+// positions in the level's flattened test space; only tiles after the caller's own
+// are affected.
+__device__ __forceinline__ void skip_tiles_of_edge(const Launch &L, unsigned long long edge_end,
+                                                   unsigned long long tile_end, unsigned long long per_tile,
+                                                   unsigned long long nwarps) {
+  if (edge_end <= tile_end) return;
+  const unsigned long long target = edge_end / per_tile;
+  if (target > nwarps) atomicMax(&L.lc->tile_next, target - nwarps);
+}
+
 template <int LT, bool MIXED>
-__device__ __forceinline__ void tests_generic(const Launch &L, unsigned long long *rw_smem) {
+__device__ __forceinline__ void tests_generic(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te) {
   constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
   const int l = LT > 0 ? LT : L.level;
   const int level = L.level;
@@ -564,13 +602,8 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
   const unsigned long long total = L.work_prefix[L.count];
   if (total == 0) return;
   const unsigned long long *rw_c = cache_row_work(L, rw_smem);
-  // tests per lane per tile: about four tiles per lane of the grid, 1..64
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
-  // a level with at most four tests per lane of the grid runs in one round of tiles
-  // (one set-up per warp; the lane's further tests are successor steps), a larger one
-  // in about four tiles per lane for balance
-  const int m = total <= lanes * 4ull ? (int)((total + lanes - 1) / lanes)
-                                      : (int)max(1ull, min(64ull, total / (lanes * 4ull)));
+  const int m = tile_tests_per_lane(total, lanes, te, true);
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
   int pos[LA], ids[LA];
   // the first tile of every warp is its global index, later tiles come from the
@@ -611,9 +644,12 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
       int s = (int)(off / c);
       unsigned long long rank = off - (unsigned long long)s * c;
       int base = I->rowptr[i];
-      unrank_lex_fast(rank, l, d - 1, pos);
       int64_t j = I->colidx[base + s];
       bool alive = live_bit(I->adj, I->W, i, j);
+      // a removed edge needs no subset: its rest is skipped below, and when the whole
+      // tile lies inside it, so are the edge's further tiles
+      if (alive) unrank_lex_fast(rank, l, d - 1, pos);
+      else if (lane == 0) skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
       unsigned tested_edge = 0;
       int ci = 0;  // lowest position changed since the last test (rows below are valid)
       Fact<LA> F;
@@ -640,9 +676,16 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
             if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, ids, l))) rm = exact_remove_fast<LA>(*I, i, j, ids, l, &pv);
           }
           if (rm) {
-            if (claim_edge(*I, i, j)) push_pending<LA>(pend, np, *I, b, level, i, j, ids, l, pv);
+            if (claim_edge(*I, i, j)) {
+              push_pending<LA>(pend, np, *I, b, level, i, j, ids, l, pv);
+              skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
+            }
             alive = false;
           }
+        }
+        if (!alive) {  // the rest of a removed edge
+          t += c - 1ull - rank;
+          rank = c - 1ull;
         }
         if (++t >= tend) break;
         if (++rank == c) {
@@ -696,7 +739,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
 // are scattered. Decisions as test_f32_inc with l = 1 (the closed form of cpuInd.cpp:16-27
 // in FP32), FP64 re-tests as in citest_kernel.
 template <bool MIXED>
-__device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw_smem) {
+__device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te) {
   const int level = 1;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   __shared__ PendRem<1> s_pend[kThreads / 32][kPend];
@@ -709,7 +752,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
   if (total == 0) return;
   const unsigned long long *rw_c = cache_row_work(L, rw_smem);
   const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
-  const int m = (int)max(1ull, min(64ull, total / (lanes * 4ull)));
+  const int m = tile_tests_per_lane(total, lanes, te, false);
   const unsigned long long per_tile = 32ull * (unsigned long long)m;
   // the first tile of every warp is its global index, later tiles come from the
   // device-wide counter (one atomic round trip fewer per warp)
@@ -754,6 +797,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
       // the live bit is read when the lane enters an edge and every fourth step on it
       // (removals by this warp reach its lanes through the step's ballot)
       bool live = live_bit(I->adj, I->W, i, j);
+      if (!live && lane == 0) skip_tiles_of_edge(L, t - rank + c, tend, per_tile, nwarps);
       unsigned steps_on_edge = 0;
       for (;;) {
         const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
@@ -797,8 +841,10 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
           const unsigned grp = __match_any_sync(act, (unsigned)(t - (unsigned long long)rank));
           const unsigned rmask = __ballot_sync(act, rm) & grp;
           if (rmask) {
-            if (lane == __ffs(rmask) - 1 && claim_edge(*I, i, j))
+            if (lane == __ffs(rmask) - 1 && claim_edge(*I, i, j)) {
               push_pending<1>(pend, np, *I, b, level, i, j, &k, 1, pv_rm);
+              skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
+            }
             live = false;
           }
         }
@@ -852,19 +898,21 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 }
 
 // One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
-// is the lane-interleaved level-1 body, LT = 2..16 the bodies unrolled for l = LT.
-template <int LT, bool MIXED>
-__global__ void __launch_bounds__(kThreads, LT == 1 ? 4 : 2) level_kernel(const __grid_constant__ Launch L) {
+// is the lane-interleaved level-1 body (L1C: the chunked body of the higher levels,
+// picked by the tile policy's l1_lanes = 1), LT = 2..16 the bodies unrolled for l = LT.
+template <int LT, bool MIXED, bool L1C = false>
+__global__ void __launch_bounds__(kThreads, LT == 1 && !L1C ? 4 : 2) level_kernel(const __grid_constant__ Launch L) {
   extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
   rebuild_phase(L);
   if (!grid_barrier(L, epoch)) return;
   scan_phase(L);
   if (!grid_barrier(L, epoch)) return;
-  if (LT == 1)
-    tests_l1<MIXED>(L, nullptr);  // level 1 keeps the SM's on-chip memory for L1 cache
+  const TuneEntry te = tile_policy(L);
+  if (LT == 1 && !L1C)
+    tests_l1<MIXED>(L, nullptr, te);  // level 1 keeps the SM's on-chip memory for L1 cache
   else
-    tests_generic<LT, MIXED>(L, rw_smem);
+    tests_generic<LT, MIXED>(L, LT == 1 ? nullptr : rw_smem, te);
 }
 
 }  // namespace

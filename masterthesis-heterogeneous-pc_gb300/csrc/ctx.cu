@@ -198,6 +198,9 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.row_cache = c->count == 1 && c->ih[0].p + 1 <= kRowCache;
   L.total_rows = c->total_rows;
   L.total_segs = c->total_segs;
+  L.tune = c->tune_dev;
+  L.force = c->tune_force;
+  L.p_bucket = c->p_bucket;
   L.inst0 = c->inst_host[0];
   return L;
 }
@@ -232,7 +235,10 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   }
   // snapshot rebuild, test-count scan and CI tests in one launch
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  if ((s = launch_level(L, c->opts.precision, c->citest_grid[level], c->stream)) != HPC_OK) return s;
+  const bool l1c = level == 1 && c->l1c_now;
+  if ((s = launch_level(L, c->opts.precision, l1c ? c->citest_grid_l1c : c->citest_grid[level], l1c, c->stream)) !=
+      HPC_OK)
+    return s;
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += queue ? 2 : 1;
@@ -309,6 +315,7 @@ hpc_level_stats level_stats_of(hpc_ctx *c, int level, int only) {
 // Per-level statistics and timings after a level ran (counters pulled).
 hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
   hpc_level_stats st = level_stats_of(c, level, -1);
+  if (level == 1) c->l1_max_deg = st.max_degree;
   float t_all = 0.f, t_snap = 0.f, t_test = 0.f;
   if (!c->last_run_graph) {
     HPC_CUDA(cudaEventElapsedTime(&t_snap, c->evl[level][0], c->evl[level][1]));
@@ -370,10 +377,40 @@ bool any_work(hpc_ctx *c, int level) {
 
 bool capturable(cudaStream_t s) { return s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread; }
 
+// Level 1's kernel (the kernel is chosen on the host, the tile sizes on the device):
+// the forced policy's l1_lanes, else the table entry for the level-1 degree of the
+// context's last run (the default, interleaved, before any run).
+bool level1_chunked(hpc_ctx *c) {
+  if (c->tune_force.tile_cap > 0) return c->tune_force.l1_lanes == 1;
+  if (c->l1_max_deg < 0) return false;
+  const TuneEntry e = tune_get(c->p_bucket, 1, tune_bucket(c->l1_max_deg, kTuneDB));
+  return e.tile_cap > 0 && e.l1_lanes == 1;
+}
+
+// The context's device copy of the tile-policy table, refreshed when the table
+// changed (before any capture: graphs keep the pointer and read the current entries).
+hpc_status sync_tune(hpc_ctx *c) {
+  if (c->tune_dev && c->tune_version_dev == tune_version()) return HPC_OK;
+  std::vector<TuneEntry> t;
+  long long v = 0;
+  tune_snapshot(&t, &v);
+  hpc_status s;
+  if (!c->tune_dev) {
+    if ((s = dev_alloc(&c->tune_dev, (int64_t)t.size(), "tile-policy table")) != HPC_OK) return s;
+    ++c->inst_version;  // a graph captured before holds no table pointer
+  }
+  HPC_CUDA(cudaMemcpyAsync(c->tune_dev, t.data(), sizeof(TuneEntry) * t.size(), cudaMemcpyHostToDevice, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));  // t is released on return
+  c->tune_version_dev = v;
+  return HPC_OK;
+}
+
 // Run levels first..last with one host sync at the end; the whole sequence 0..last
 // is captured once into a CUDA graph and replayed while the buffers stay in place.
 hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait = true) {
   hpc_status s;
+  if ((s = sync_tune(c)) != HPC_OK) return s;
+  c->l1c_now = level1_chunked(c);
   auto enqueue_all = [&](bool timed) -> hpc_status {
     if (first == 0) {  // a skeleton from the start: its counters and records begin at zero
       HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)c->count * kLevels, c->stream));
@@ -388,7 +425,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
   };
   if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
-                       c->graph_version == c->inst_version;
+                       c->graph_version == c->inst_version && c->graph_l1c == c->l1c_now;
     if (!valid) {
       if (c->graph) cudaGraphExecDestroy(c->graph);
       c->graph = nullptr;
@@ -412,6 +449,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
       c->graph_top = last;
       c->graph_stream = c->stream;
       c->graph_version = c->inst_version;
+      c->graph_l1c = c->l1c_now;
     }
     HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
     c->timings.launches += c->graph_launches;
@@ -498,6 +536,12 @@ GramArgs gram_args(hpc_ctx *c) {
   return g;
 }
 
+// Entries of the deferred FP64 re-test queue (tensor-core mode): a test is queued when
+// its FP32 |r| lies within the band around r_crit, about 1e-4 of the tests of a wide
+// level 1 (18.7 M of 1.3e11 at p = 15000), so the queue grows with sum p^2 / 8, from 1 Mi
+// to 32 Mi entries (80 B each). Tests beyond it are re-tested in place.
+long long retest_queue_cap(long long sum_p2) { return std::min<long long>(32ll << 20, std::max<long long>(1ll << 20, sum_p2 / 8)); }
+
 hpc_status after_correlation(hpc_ctx *c) {
   c->have_cor = true;
   hpc_status s = write_inst_table(c);
@@ -540,7 +584,9 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
       HPC_CUDA(cudaStreamSynchronize(c->stream));
     }
     if (!c->rq) {
-      const long long cap = 1 << 20;
+      long long p2 = 0;
+      for (const auto &h : c->ih) p2 += h.p * h.p;
+      const long long cap = retest_queue_cap(p2);
       if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
       c->rq_cap = cap;
     }
@@ -683,6 +729,7 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   // neighbour lists and records are sized after level 0; budget an average degree of 64
   const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
   b += 2 * e * 4 + e * (int64_t)sizeof(hpc_sepset_record);
+  if (o->precision == HPC_PREC_MIXED_TC) b += retest_queue_cap(p * p) * (int64_t)sizeof(RetestItem);
   *bytes = b;
   return HPC_OK;
 }
@@ -741,6 +788,7 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->seg);
   dev_free(c->meta);
   dev_free(c->meta_denom);
+  dev_free(c->tune_dev);
   delete[] c->ctr_host;
   delete[] c->gctr_host;
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -779,6 +827,97 @@ hpc_status hpc_ctx_set_graphs(hpc_ctx *c, int enable) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
   c->graphs_enabled = enable != 0;
+  return HPC_OK;
+}
+
+hpc_status settle(hpc_ctx *c);
+
+hpc_status hpc_ctx_set_tune(hpc_ctx *c, const hpc_tune_params *force) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (force && !tune_params_valid(force)) {
+    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32", kTuneMaxCap);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if ((s = settle(c)) != HPC_OK) return s;
+  c->tune_force = force ? tune_entry_of(*force) : TuneEntry{0, 0, 0, 0};
+  ++c->inst_version;  // the policy is a launch parameter: graphs are captured anew
+  return HPC_OK;
+}
+
+hpc_status hpc_autotune(hpc_ctx *c, const hpc_tune_params *cands, int ncands, int reps, hpc_tune_params *chosen,
+                        int *entries) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
+  if (!c->have_cor) {
+    set_error("autotune before a correlation matrix was computed or loaded");
+    return HPC_ERR_STATE;
+  }
+  if (reps < 1 || (cands && ncands < 1)) {
+    set_error("autotune needs reps >= 1 and ncands >= 1");
+    return HPC_ERR_INVALID_ARG;
+  }
+  std::vector<hpc_tune_params> grid;
+  if (cands) {
+    for (int q = 0; q < ncands; ++q) {
+      if (!tune_params_valid(&cands[q])) {
+        set_error("autotune candidate %d is not a valid tile policy", q);
+        return HPC_ERR_INVALID_ARG;
+      }
+      grid.push_back(cands[q]);
+    }
+  } else {
+    for (int l1 : {32, 1})
+      for (int cap : {16, 64, 256, 1024})
+        for (int tpl : {2, 4, 8}) grid.push_back(hpc_tune_params{cap, tpl, l1});
+  }
+  const bool graphs = c->graphs_enabled;
+  const TuneEntry force0 = c->tune_force;
+  c->graphs_enabled = false;  // kernel by kernel: every level's kernels are timed
+  double best_ms[kLevels];
+  int best[kLevels], max_deg[kLevels];
+  for (int l = 0; l < kLevels; ++l) {
+    best_ms[l] = 1e300;
+    best[l] = -1;
+    max_deg[l] = -1;
+  }
+  hpc_level_stats st[kLevels];
+  for (size_t q = 0; q < grid.size() && s == HPC_OK; ++q) {
+    c->tune_force = tune_entry_of(grid[q]);
+    ++c->inst_version;
+    for (int r = 0; r < reps && s == HPC_OK; ++r) {
+      int ran = 0;
+      if ((s = hpc_ctx_reset(c)) != HPC_OK) break;
+      if ((s = hpc_run_skeleton(c, st, kLevels, &ran)) != HPC_OK) break;
+      for (int k = 0; k < ran; ++k) {
+        const int l = st[k].level;
+        if (l < 1 || st[k].potential_tests == 0) continue;
+        const double ms = c->timings.test_ms[l];
+        max_deg[l] = st[k].max_degree;
+        if (ms < best_ms[l]) {
+          best_ms[l] = ms;
+          best[l] = (int)q;
+        }
+      }
+    }
+  }
+  c->tune_force = force0;
+  c->graphs_enabled = graphs;
+  ++c->inst_version;
+  const hpc_status reset = hpc_ctx_reset(c);
+  if (s != HPC_OK) return s;
+  if (reset != HPC_OK) return reset;
+  int64_t pmax = 0;
+  for (const auto &h : c->ih) pmax = std::max<int64_t>(pmax, h.p);
+  int written = 0;
+  for (int l = 0; l < kLevels; ++l) {
+    if (chosen) chosen[l] = best[l] >= 0 ? grid[(size_t)best[l]] : hpc_tune_params{0, 0, 0};
+    if (best[l] < 0) continue;
+    tune_store(pmax, l, max_deg[l], tune_entry_of(grid[(size_t)best[l]]));
+    ++written;
+  }
+  if (entries) *entries = written;
   return HPC_OK;
 }
 
@@ -1279,6 +1418,11 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   c->total_rows = nrows;
   c->p = c->ih[0].p;
   c->n = c->ih[0].n;
+  {
+    int64_t pmax = 0;
+    for (const auto &h : c->ih) pmax = std::max<int64_t>(pmax, h.p);
+    c->p_bucket = tune_bucket(pmax, kTunePB);
+  }
   hpc_status s = HPC_OK;
   auto fail = [&](hpc_status st) {
     hpc_ctx_destroy(c);
@@ -1303,6 +1447,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   }
   c->stream = c->own_stream;
   for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
+  c->citest_grid_l1c = citest_grid(o.precision, 1, c->device, true);
   if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, cor, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, cor, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, adj, "adjacency")) != HPC_OK) return fail(s);

@@ -63,7 +63,29 @@ struct LaunchCounters {
   unsigned long long rq_count;     // FP64 re-tests queued
   unsigned int scan_done;          // scan blocks finished (the last one forms the prefix)
   unsigned int bar;                // grid-barrier arrivals of the level kernel
+  int max_deg;                     // largest degree at the level start over all instances
+  int pad;
 };
+
+// Tile policy of a level's CI tests (set by the autotuner, else the defaults):
+// tile_cap bounds the consecutive tests a lane takes per tile (the subset chunk),
+// tiles_per_lane is the target number of tiles per lane of the grid (balance), and
+// l1_lanes picks level 1's mapping: 32 = the warp's lanes interleaved over one edge's
+// tests, 1 = each lane a chunk of consecutive tests (the levels >= 2 mapping).
+struct TuneEntry {
+  int tile_cap, tiles_per_lane, l1_lanes, pad;
+};
+constexpr int kTuneDefaultCap = 64, kTuneDefaultTpl = 4, kTuneDefaultL1Lanes = 32, kTuneMaxCap = 65536;
+// table of a context: [p bucket][level][degree bucket]; bucket = bit length, capped
+constexpr int kTunePB = 32, kTuneDB = 18;
+__host__ __device__ __forceinline__ int tune_bucket(long long v, int cap) {
+  int b = 0;
+  while (v > 0 && b < cap - 1) {
+    ++b;
+    v >>= 1;
+  }
+  return b;
+}
 // Rows per segment of the level kernel's test-count scan, and the per-segment sums
 // the rebuild phase accumulates (one slice of segments per level).
 constexpr int kSegRows = 256;
@@ -132,6 +154,9 @@ struct Launch {
   SegAgg *seg;                      // this level's segment sums (zeroed before the level)
   int row_cache;                    // the CI tests keep the row offsets in shared memory
   long long total_rows, total_segs; // row_prefix[count], seg_prefix[count]
+  const TuneEntry *tune;            // the context's tile-policy table (kTunePB x kLevels x kTuneDB)
+  TuneEntry force;                  // tile_cap > 0: this policy for the level, whatever the table says
+  int p_bucket;                     // tune_bucket of the largest p of the launch
   Inst inst0;                       // inst[0] by value: read from the parameter bank when count == 1
 };
 
@@ -214,10 +239,19 @@ hpc_status launch_degrees(const Launch &L, long long total_rows, cudaStream_t s)
 hpc_status launch_scan(const Launch &L, cudaStream_t s);
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
 // Level l >= 1 in one cooperative launch: snapshot rebuild, test-count scan, CI tests.
-hpc_status launch_level(const Launch &L, int precision, int grid, cudaStream_t s);
+// l1_chunked: level 1 with the chunked body of the higher levels (tile policy l1_lanes = 1).
+hpc_status launch_level(const Launch &L, int precision, int grid, bool l1_chunked, cudaStream_t s);
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
-int citest_grid(int precision, int level, int device);
+int citest_grid(int precision, int level, int device, bool l1_chunked = false);
+
+// process-wide tile-policy table (tune.cu)
+TuneEntry tune_entry_of(const hpc_tune_params &p);
+bool tune_params_valid(const hpc_tune_params *p);
+void tune_snapshot(std::vector<TuneEntry> *out, long long *version);
+long long tune_version();
+void tune_store(int64_t p, int level, int max_degree, const TuneEntry &e);
+TuneEntry tune_get(int p_bucket, int level, int deg_bucket);  // by bucket indices
 
 // per-instance host bookkeeping
 struct InstHost {
@@ -288,6 +322,15 @@ struct hpc_ctx {
   bool graphs_enabled = true;
   bool last_run_graph = false;
   int citest_grid[HPC_MAX_LEVEL + 1] = {};
+  // tile policy: device copy of the process-wide table, its version, a forced policy
+  hpc::TuneEntry *tune_dev = nullptr;
+  long long tune_version_dev = -1;
+  hpc::TuneEntry tune_force{};
+  int p_bucket = 0;
+  int citest_grid_l1c = 0;        // grid of the chunked level-1 kernel
+  int l1_max_deg = -1;            // level-1 max degree of the last run (keys level 1's kernel choice)
+  bool l1c_now = false;           // the level-1 kernel of the runs being queued is the chunked one
+  bool graph_l1c = false;         // ... and of the captured graph
   cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
   cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
   cudaEvent_t evr[2] = {nullptr, nullptr};      // whole skeleton run

@@ -268,12 +268,14 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
       const int b = c0 + (int)threadIdx.x;
       unsigned long long tot = 0;
       if (b < L.count) {
-        int over = 0;
+        int over = 0, md = 0;
         for (long long q = seg_begin(L, b); q < seg_end(L, b); ++q) {
           tot += __ldcg(&L.seg[q].work);
           over |= __ldcg(&L.seg[q].over);
+          md = max(md, __ldcg(&L.seg[q].max_deg));
         }
         if (over || csr_overflow(*inst_of(L, b))) tot = 0;
+        if (md > 0) atomicMax(&L.lc->max_deg, md);  // the key of the level's tile policy
       }
       unsigned long long all;
       const unsigned long long ex = block_exclusive_scan(tot, &all);

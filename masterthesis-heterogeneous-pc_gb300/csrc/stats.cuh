@@ -119,28 +119,78 @@ struct BinomTable {
   }
 };
 static __device__ const BinomTable kBinomTab = BinomTable();
+static constexpr BinomTable kBinomHostTab = BinomTable();
 
-__device__ __forceinline__ unsigned long long binom_fast(int n, int k) {
-  if (k < 0 || n < k) return 0ull;
-  if (n < 64 && k <= HPC_MAX_LEVEL) return __ldg(&kBinomTab.v[n][k]);
-  return binom_sat(n, k);
+HPC_HD unsigned long long binom_table(int n, int k) {
+#ifdef __CUDA_ARCH__
+  return __ldg(&kBinomTab.v[n][k]);
+#else
+  return kBinomHostTab.v[n][k];
+#endif
 }
 
-// unrank_lex (below) with table lookups (the member x only moves forward, so one
-// unranking costs about m lookups)
-__device__ __forceinline__ void unrank_lex_fast(unsigned long long rank, int l, int m, int *pos) {
-  int x = 0;
-  for (int i = 0; i < l; ++i) {
-    for (;;) {
-      const unsigned long long cnt = binom_fast(m - x - 1, l - i - 1);
-      if (rank < cnt) {
-        pos[i] = x;
-        ++x;
-        break;
-      }
-      rank -= cnt;
-      ++x;
+HPC_HD unsigned long long umul64hi(unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// C(n, k) for k <= HPC_MAX_LEVEL: the table below n = 64, else the product
+// C(n, q + 1) = C(n, q) (n - q) / (q + 1) with the loop unrolled, so that every
+// division is by a constant (a multiply-high, not a 64-bit division routine).
+// Saturates at UINT64_MAX when a partial product overflows (the work of such a row
+// does not fit 64 bits either and is rejected by the test-count scan).
+HPC_HD unsigned long long binom_fast(int n, int k) {
+  if (k < 0 || n < k) return 0ull;
+  if (n < 64) return binom_table(n, k);
+  unsigned long long res = 1ull;
+#pragma unroll
+  for (int q = 0; q < HPC_MAX_LEVEL; ++q) {
+    if (q < k) {
+      const unsigned long long num = (unsigned long long)(n - q);
+      if (umul64hi(res, num) != 0ull) return 0xFFFFFFFFFFFFFFFFull;
+      res = res * num / (unsigned long long)(q + 1);
     }
+  }
+  return res;
+}
+
+// unrank_lex (below) in O(l log m) binomials: the subsets whose member i lies in
+// [a, x] number C(m - a, k + 1) - C(m - x - 1, k + 1) (k = l - i - 1, the hockey-stick
+// identity), so member i is the smallest x with C(m - x - 1, k + 1) < C(m - a, k + 1) -
+// rank, found by bisection (C(m - x - 1, k + 1) falls as x grows). Below m = 64 the
+// members are found by a forward scan of table lookups.
+HPC_HD void unrank_lex_fast(unsigned long long rank, int l, int m, int *pos) {
+  int x = 0;
+  if (m < 64) {
+    for (int i = 0; i < l; ++i) {
+      for (;;) {
+        const unsigned long long cnt = binom_fast(m - x - 1, l - i - 1);
+        if (rank < cnt) {
+          pos[i] = x;
+          ++x;
+          break;
+        }
+        rank -= cnt;
+        ++x;
+      }
+    }
+    return;
+  }
+  for (int i = 0; i < l; ++i) {
+    const int k1 = l - i;  // k + 1
+    const unsigned long long all = binom_fast(m - x, k1);
+    const unsigned long long R = all - rank;  // > 0: rank < C(m - x, l - i)
+    int lo = x, hi = m - k1;                  // C(m - hi - 1, k1) = C(k1 - 1, k1) = 0 < R
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (binom_fast(m - mid - 1, k1) < R) hi = mid; else lo = mid + 1;
+    }
+    pos[i] = lo;
+    rank -= all - binom_fast(m - lo, k1);  // subsets with member i in [x, lo)
+    x = lo + 1;
   }
 }
 #endif

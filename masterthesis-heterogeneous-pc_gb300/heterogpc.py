@@ -70,6 +70,13 @@ class Served(C.Structure):
                 ("batch_size", C.c_int32), ("pad", C.c_int32)]
 
 
+class TuneParams(C.Structure):
+    _fields_ = [("tile_cap", C.c_int), ("tiles_per_lane", C.c_int), ("l1_lanes", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class SemParams(C.Structure):
     _fields_ = [("p", C.c_int64), ("n", C.c_int64), ("graph", C.c_int), ("degree", C.c_double),
                 ("pa_parents", C.c_int), ("w_lo", C.c_double), ("w_hi", C.c_double), ("seed", C.c_uint64)]
@@ -126,7 +133,62 @@ _SIGS = {
     "hpc_batch_get_adjacency": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "hpc_batch_edge_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]),
     "hpc_batch_get_sepset_records": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "hpc_tune_set": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.POINTER(TuneParams)]),
+    "hpc_tune_lookup": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.POINTER(TuneParams), C.POINTER(C.c_int)]),
+    "hpc_tune_clear": (C.c_int, []),
+    "hpc_tune_save": (C.c_int, [C.c_char_p]),
+    "hpc_tune_load": (C.c_int, [C.c_char_p]),
+    "hpc_ctx_set_tune": (C.c_int, [C.c_void_p, C.POINTER(TuneParams)]),
+    "hpc_autotune": (C.c_int, [C.c_void_p, C.POINTER(TuneParams), C.c_int, C.c_int, C.POINTER(TuneParams),
+                               C.POINTER(C.c_int)]),
 }
+
+
+# ---- tile policy and autotuner (hpc_tune_* / hpc_autotune) ----------------------
+
+def tune_set(p, level, max_degree, tile_cap=None, tiles_per_lane=4, l1_lanes=32):
+    """Set (tile_cap given) or erase (None) the tile policy of a key's buckets."""
+    prm = None if tile_cap is None else C.byref(TuneParams(tile_cap, tiles_per_lane, l1_lanes))
+    _check(lib().hpc_tune_set(int(p), int(level), int(max_degree), prm))
+
+
+def tune_lookup(p, level, max_degree):
+    """(policy dict, found) of the key."""
+    t, f = TuneParams(), C.c_int(0)
+    _check(lib().hpc_tune_lookup(int(p), int(level), int(max_degree), C.byref(t), C.byref(f)))
+    return t.as_dict(), bool(f.value)
+
+
+def tune_clear():
+    _check(lib().hpc_tune_clear())
+
+
+def tune_save(path):
+    _check(lib().hpc_tune_save(os.fsencode(path)))
+
+
+def tune_load(path):
+    _check(lib().hpc_tune_load(os.fsencode(path)))
+
+
+def _set_tune(h, policy):
+    prm = None if policy is None else C.byref(TuneParams(policy["tile_cap"], policy.get("tiles_per_lane", 4),
+                                                         policy.get("l1_lanes", 32)))
+    _check(lib().hpc_ctx_set_tune(h, prm))
+
+
+def _autotune(h, candidates, reps):
+    """hpc_autotune on a context: {level: chosen policy}, entries written."""
+    cap = HPC_MAX_LEVEL + 1
+    chosen = (TuneParams * cap)()
+    n = C.c_int(0)
+    if candidates is None:
+        _check(lib().hpc_autotune(h, None, 0, int(reps), chosen, C.byref(n)))
+    else:
+        arr = (TuneParams * len(candidates))(*[TuneParams(c["tile_cap"], c.get("tiles_per_lane", 4),
+                                                          c.get("l1_lanes", 32)) for c in candidates])
+        _check(lib().hpc_autotune(h, arr, len(candidates), int(reps), chosen, C.byref(n)))
+    return {l: chosen[l].as_dict() for l in range(cap) if chosen[l].tile_cap > 0}, n.value
 
 
 def lib():
@@ -290,6 +352,14 @@ class SkeletonCalculator:
     def set_graphs(self, enable):
         _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
 
+    def set_tune(self, policy):
+        """Force a tile policy ({"tile_cap", "tiles_per_lane", "l1_lanes"}) on every level; None = the table."""
+        _set_tune(self._h, policy)
+
+    def autotune(self, candidates=None, reps=1):
+        """Time every candidate tile policy on this context's skeleton and store the fastest per level."""
+        return _autotune(self._h, candidates, reps)
+
     def timings(self):
         t = Timings()
         _check(lib().hpc_get_timings(self._h, C.byref(t)))
@@ -408,6 +478,14 @@ class SkeletonBatch:
 
     def set_graphs(self, enable):
         _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
+
+    def set_tune(self, policy):
+        """Force a tile policy ({"tile_cap", "tiles_per_lane", "l1_lanes"}) on every level; None = the table."""
+        _set_tune(self._h, policy)
+
+    def autotune(self, candidates=None, reps=1):
+        """Time every candidate tile policy on this context's skeleton and store the fastest per level."""
+        return _autotune(self._h, candidates, reps)
 
     def reset(self):
         _check(lib().hpc_ctx_reset(self._h))

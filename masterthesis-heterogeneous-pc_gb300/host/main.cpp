@@ -1,7 +1,8 @@
 // heterogpc command line (src/main.cpp:17-141): same flags, defaults, messages and
 // exit codes. Flags that steer the reference's CPU side (--cpu-only, -w, --row-mult*,
 // --power9-ats, -t) are accepted; every CI test here runs on the GPU work queue,
-// so they change nothing and a note says so. New: --precision fp64|mixed|mixed-tc.
+// so they change nothing and a note says so. New: --precision fp64|mixed|mixed-tc,
+// --autotune and --tune-file (the CI tests' tile policy, hpc_autotune / hpc_tune_*).
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -49,6 +50,8 @@ const std::vector<Opt> kOpts = {
     {"print-sepsets", 'p', false, false, "prints-sepsets", ""},
     {"verbose", 'v', false, false, "verbose output", ""},
     {"precision", 0, true, false, "CI-test precision: fp64, mixed (default) or mixed-tc", "mixed"},
+    {"autotune", 0, false, false, "time the tile-policy candidates on this input before the run", ""},
+    {"tune-file", 0, true, false, "tile-policy table: loaded before the run, written after --autotune", ""},
 };
 
 const Opt *find_long(const std::string &n) {
@@ -189,6 +192,12 @@ int main(int argc, char const *argv[]) {
   if (gpus.size() > 1) std::cerr << "note: one GPU per process; using device " << gpus.front() << "\n";
 
   try {
+    // the tile-policy table is read first (a bad file fails before any GPU work)
+    const std::string tuneFile = vm.count("tune-file") ? get("tune-file") : "";
+    if (!tuneFile.empty() && !vm.count("autotune")) {
+      const hpc_status st = hpc_tune_load(tuneFile.c_str());
+      if (st != HPC_OK) throw HpcException(st, hpc_last_error_string());
+    }
     SkeletonCalculator sk(maxLevel, alpha, workstealing, csvExportFile, numberOfThreads, verbose);
     if (vm.count("gpu-only")) sk.set_heterogeneity(Heterogeneity::GPUOnly);
     else if (vm.count("cpu-only")) sk.set_heterogeneity(Heterogeneity::CPUOnly);
@@ -206,6 +215,14 @@ int main(int argc, char const *argv[]) {
     }
     sk.initialize_balancer({(float)to_double("row-mult", get("row-mult")), (float)to_double("row-mult2", get("row-mult2")),
                             (float)to_double("row-mult3", get("row-mult3"))});
+    if (vm.count("autotune")) {
+      int entries = 0;
+      hpc_status st = hpc_autotune(sk.context(), nullptr, 0, 1, nullptr, &entries);
+      if (st != HPC_OK) throw HpcException(st, hpc_last_error_string());
+      std::cerr << "autotune: " << entries << " tile-policy entries" << std::endl;
+      if (!tuneFile.empty() && (st = hpc_tune_save(tuneFile.c_str())) != HPC_OK)
+        throw HpcException(st, hpc_last_error_string());
+    }
     sk.run(print_sepsets);
   } catch (const HpcException &e) {
     std::cerr << "Error: " << e.what() << "\n";

@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
-              "noalloc.cu"]
+              "noalloc.cu", "tune.cu"]
 HOST_SOURCES = ["semgen.cpp", "serve.cpp"]
 
 

@@ -96,3 +96,34 @@ def test_correlation_csv_skeleton(tmp_path):
     edges, _ = parse_output(r.stdout)
     assert edges == want.edges()
     assert "no effect" in r.stderr
+
+
+@pytest.mark.gpu
+def test_autotune_and_tune_file(tmp_path):
+    """--autotune times the tile-policy candidates on the input and writes the table to
+    --tune-file; a later run loads it. Both print the oracle's skeleton."""
+    X = gen(dict(p=120, n=1500, graph=hg.GRAPH_PA, pa_parents=2, w_lo=0.2, seed=19))
+    Cm = orc.correlation(X)
+    path = tmp_path / "cor.csv"
+    write_csv(path, Cm)
+    want = orc.run(Cm, 1500, 0.05, 3)
+    table = tmp_path / "policy.txt"
+    r = run("--corr", "-o", "1500", "-i", str(path), "-a", "0.05", "-m", "3", "--autotune", "--tune-file", str(table))
+    assert r.returncode == 0, r.stderr
+    assert parse_output(r.stdout)[0] == want.edges()
+    assert "tile-policy entries" in r.stderr
+    lines = open(table).read().splitlines()
+    assert lines[0].startswith("heterogpc-tile-policy") and len(lines) > 1
+    r = run("--corr", "-o", "1500", "-i", str(path), "-a", "0.05", "-m", "3", "--tune-file", str(table))
+    assert r.returncode == 0, r.stderr
+    assert parse_output(r.stdout)[0] == want.edges()
+
+
+def test_bad_tune_file_is_an_error(tmp_path):
+    bad = tmp_path / "bad.txt"
+    bad.write_text("nonsense\n")
+    X = gen(dict(p=10, n=100, graph=hg.GRAPH_ER, degree=2.0, seed=20))
+    path = tmp_path / "cor.csv"
+    write_csv(path, orc.correlation(X))
+    r = run("--corr", "-o", "100", "-i", str(path), "--tune-file", str(bad))
+    assert r.returncode == 2 and "not a tile-policy file" in r.stderr
