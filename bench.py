@@ -37,6 +37,11 @@ for _d in (PKG, ROOT):
 import numpy as np  # noqa: E402
 
 WORKLOADS = {
+    # plain single instance: ER p=50, degree 2, n=1000 FP64 samples, alpha 0.01, levels until
+    # no edge has enough neighbours (level 16 is the kernels' limit; the run stops at the
+    # first level without tests)
+    "c1": dict(p=50, n=1000, graph=0, degree=2.0, pa_parents=2, w_lo=0.1, w_hi=1.0, seed=1, alpha=0.01,
+               max_level=16, dtype="f64"),
     "c2": dict(p=2000, n=5000, graph=0, degree=4.0, pa_parents=2, w_lo=0.1, w_hi=1.0, seed=2, alpha=0.01,
                max_level=6, dtype="f32"),
     # 512 instances, p ~ U[20, 800], n ~ U[200, 8000], ER degree ~ U[1, 5], alpha 0.01 / 0.05
@@ -179,9 +184,15 @@ def autotune_setup(args, ctx, candidates, reps):
     if args.no_autotune:
         return {"autotuned": False}
     import heterogpc as hg
+    if args.tune_file and os.path.exists(args.tune_file):
+        hg.tune_clear()
+        hg.tune_load(args.tune_file)
+        return {"autotuned": False, "loaded": args.tune_file}
     hg.tune_clear()
     t0 = time.perf_counter()
     chosen, entries = ctx.autotune(candidates, reps=reps)
+    if args.tune_file:
+        hg.tune_save(args.tune_file)
     return {"autotuned": True, "candidates": "built-in grid (24)" if candidates is None else candidates,
             "chosen": {str(k): v for k, v in chosen.items()}, "entries": entries,
             "tuning_s": time.perf_counter() - t0}
@@ -290,6 +301,20 @@ def c4_roofline(levels, timings):
             "per_level": per}
 
 
+def c4_cpu_baseline(args, wl, bt):
+    if args.no_cpu_baseline:
+        return None
+    import hpc_build
+    hpc_build.build_oracle()
+    k = min(bt.count, C4_CPU_SAMPLE)
+    value, dt, tests, edges, cores = c4_cpu_sample(wl, k)
+    same = all(np.array_equal(edges[b], bt.adjacency(b)) for b in range(k))
+    return {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
+            "sample": "the first %d of the 512 instances, one after another (%.1f s); later instances cost far "
+                      "more on the CPU (instance 5, p=782, runs for minutes), so this rate flatters the CPU" % (k, dt),
+            "ci_tests_per_sec": tests / dt, "same_skeletons_as_gpu": bool(same)}
+
+
 def run_c4(args, wl):
     """Batched skeletons: one context, every level kernel launched once for all 512
     instances; a step is correlation (split-BF16 tensor-core Gram) + all levels of
@@ -363,6 +388,7 @@ def run_c4(args, wl):
             "plain_gpu_path": {"skeletons_per_sec": plain, "sample": "%d instances, one context each" % k_plain,
                                "precision": "fp64"},
             "speedup_vs_plain": value / plain, "clocks": clk, "tile_policy": tuned,
+            "cpu_baseline": c4_cpu_baseline(args, wl, bt),
             "roofline": c4_roofline(st, t_cor),
             "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
                         "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
@@ -466,6 +492,52 @@ def traffic_from_profile(kernel):
     return ent.get("dram_bytes_per_launch") if ent else None
 
 
+# CPU-baseline sample of c4: the oracle's cost per instance ranges from 0.1 s to minutes
+# (levels up to 16 on some instances); the first five instances take about 2 s
+C4_CPU_SAMPLE = 5
+
+
+def c4_cpu_sample(wl, k):
+    """The oracle (the reference's CPU path restated, all host cores) on the first k
+    instances of the c4 batch, one after another: (skeletons/s, seconds, tests, edges
+    per instance). The bounded sample keeps the run to seconds."""
+    import heterogpc as hg
+    from oracle import oracle as orc
+    ps, ns, degs, alphas = c4_instances(wl)
+    cores = os.cpu_count()
+    tot, tests, edges = 0.0, 0, []
+    for b in range(k):
+        X = hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, float(degs[b]), 2, wl["w_lo"], wl["w_hi"],
+                            wl["seed"] * 100000 + b, dtype=np.float32)
+        Cm = orc.correlation(X.astype(np.float64))
+        t0 = time.perf_counter()
+        res = orc.run(Cm, int(ns[b]), float(alphas[b]), wl["max_level"], threads=cores)
+        tot += time.perf_counter() - t0
+        tests += sum(l["executed_tests"] for l in res.levels)
+        edges.append(res.adj)
+    return k / tot, tot, tests, edges, cores
+
+
+def run_reference_c4(args, wl):
+    k = min(wl["count"], C4_CPU_SAMPLE)
+    times, tests = [], 0
+    for _ in range(args.steps):
+        v, dt, tests, _, cores = c4_cpu_sample(wl, k)
+        times.append(dt)
+    value = k * args.steps / sum(times)
+    line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded linear-Gaussian SEM)", "impl": "reference",
+            "config": {"workload": "c4", "instances": wl["count"], "p": list(wl["p"]), "n": list(wl["n"])},
+            "ci_tests_per_step": tests, "ci_tests_per_sec": tests * args.steps / sum(times),
+            "cpu_baseline": {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
+                             "sample": "the first %d of the 512 instances, one after another, per step (later "
+                                       "instances cost far more on the CPU)" % k},
+            "e2e": {"value": value, "unit": "skeletons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, wl, rank, world):
     if rank != 0:
         return
@@ -474,8 +546,17 @@ def run_reference(args, wl, rank, world):
 
     import hpc_build
     hpc_build.build_oracle()
+    if args.workload == "c4":
+        run_reference_c4(args, wl)
+        return
+    if args.workload in ("c3", "c5"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the CPU restatement needs hours per %s step (C3's level 1 alone executes 1.1e11 tests at "
+                          "about 5e6 tests/s on 16 cores)" % args.workload}), flush=True)
+        return
+    xdt = np.float64 if wl.get("dtype") == "f64" else np.float32
     X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
-                        wl["seed"], dtype=np.float32)
+                        wl["seed"], dtype=xdt)
     Cm = orc.correlation(X.astype(np.float64))
     cores = os.cpu_count()
     for _ in range(args.warmup):
@@ -514,6 +595,8 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
     ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile policy (no hpc_autotune)")
+    ap.add_argument("--tune-file", default=None,
+                    help="tile-policy table: loaded instead of autotuning when it exists, else written after it")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -557,8 +640,9 @@ def main():
     torch.cuda.set_stream(stream)
 
     # data: generated on the host, then resident in HBM
+    xdt = np.float64 if wl.get("dtype") == "f64" else np.float32
     X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
-                        wl["seed"] + 1000 * rank * 0, dtype=np.float32)
+                        wl["seed"] + 1000 * rank * 0, dtype=xdt)
     Xd = torch.from_numpy(X).to(dev)
     p, n = wl["p"], wl["n"]
 
@@ -571,18 +655,18 @@ def main():
     sk = make(hg.PREC_MIXED)
     # correlation once (FP64-accurate), timed separately
     for _ in range(2):
-        sk.add_observations_device(Xd.data_ptr(), np.float32)
+        sk.add_observations_device(Xd.data_ptr(), xdt)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    sk.add_observations_device(Xd.data_ptr(), np.float32)
+    sk.add_observations_device(Xd.data_ptr(), xdt)
     e1.record(stream)
     torch.cuda.synchronize()
     cor_ms = e0.elapsed_time(e1)
     cor_t = sk.timings()
     Cdev = torch.empty((p, p), dtype=torch.float64, device=dev)
     sk_plain = make(hg.PREC_FP64)
-    sk_plain.add_observations_device(Xd.data_ptr(), np.float32)
+    sk_plain.add_observations_device(Xd.data_ptr(), xdt)
     torch.cuda.synchronize()
 
     flush = L2Flush(torch, dev)
@@ -710,7 +794,7 @@ def main():
     line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded linear-Gaussian SEM)",
+            "data": "synthetic (seeded linear-Gaussian SEM, %s samples)" % ("FP64" if xdt == np.float64 else "FP32"),
             "config": dict(workload=args.workload, p=p, n=n, degree=wl["degree"], alpha=wl["alpha"],
                            max_level=wl["max_level"], precision="mixed (FP32 tests, FP64 re-tests)",
                            l2=L2Flush.desc, parallelism="replicas"),

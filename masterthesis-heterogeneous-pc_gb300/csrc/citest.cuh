@@ -384,6 +384,25 @@ __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, 
   return lo;
 }
 
+// find_row for a position at or after the start of row i0 (t >= row_work[i0]): the
+// lanes walk forward through the flattened space, so the row is usually i0 + 1 or a
+// few rows on; a galloping probe finds it in O(log distance) loads instead of the
+// log2(p) of a search over all rows.
+__device__ __forceinline__ int64_t find_row_from(const unsigned long long *row_work, int64_t p, int64_t i0,
+                                                 unsigned long long t) {
+  int64_t lo = i0, step = 1;  // row_work[lo] <= t
+  while (lo + step < p && row_work[lo + step] <= t) {
+    lo += step;
+    step <<= 1;
+  }
+  int64_t hi = min(lo + step, p);  // row_work[hi] > t (row_work[p] > t)
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (row_work[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // The row offsets of a single-instance level copied into shared memory by the whole
 // block (one round of coalesced loads), so that every row search of the CI tests
 // stays on the SM; null when the launch has no cache (several instances, or more than
@@ -696,8 +715,10 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
               b = find_inst_u(L.work_prefix, L.count, t);
               I = inst_of(L, b);
               base_t = L.work_prefix[b];
+              i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
+            } else {
+              i = find_row_from(rw_c ? rw_c : I->row_work, I->p, i, t - base_t);
             }
-            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
             d = I->deg[i];
             c = binom_fast(d - 1, l);
             base = I->rowptr[i];
@@ -792,21 +813,28 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
       int s = (int)(off / (unsigned long long)c);
       int rank = (int)(off - (unsigned long long)s * c);
       int base = I->rowptr[i];
-      int64_t j = I->colidx[base + s];
-      float rij = MIXED ? __ldg(I->cor32 + i * I->p + j) : 0.f;
+      // the instance's fields a step needs, in registers (the descriptor is reached
+      // through a generic pointer, which the compiler would reload every step)
+      const int *nbr = I->colidx + base;  // row i's neighbour list
+      const float *cor32 = I->cor32;
+      int64_t p_i = I->p;
+      float r_c = I->r_c, band_a = I->margin_r, band_b = 8.0f * (I->ke_a + 3.0f * I->ke_b);
+      int64_t j = nbr[s];
+      const float *row_i = cor32 + i * p_i, *row_j = cor32 + j * p_i;
+      float rij = MIXED ? __ldg(row_i + j) : 0.f;
       // the live bit is read when the lane enters an edge and every fourth step on it
       // (removals by this warp reach its lanes through the step's ballot)
       bool live = live_bit(I->adj, I->W, i, j);
       if (!live && lane == 0) skip_tiles_of_edge(L, t - rank + c, tend, per_tile, nwarps);
       unsigned steps_on_edge = 0;
       for (;;) {
-        const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
+        const int k = nbr[rank + (rank >= s ? 1 : 0)];
         // the entries are loaded before the live bit is known (in bounds either way):
         // the two round trips overlap instead of following each other
         float x2 = 0.f, x3 = 0.f;
         if (MIXED) {
-          x2 = __ldg(I->cor32 + i * I->p + k);
-          x3 = __ldg(I->cor32 + j * I->p + k);
+          x2 = __ldg(row_i + k);
+          x3 = __ldg(row_j + k);
         }
         bool rm = false;
         double pv_rm = 0.0;
@@ -818,8 +846,8 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
             const float cond = fminf(ax, ay);
             if (cond > 1e-3f) {
               rr = fabsf(rij - x2 * x3) * rsqrtf(ax * ay);
-              const float dist = rr - I->r_c;
-              const float band = I->margin_r + 8.0f * __fdividef(I->ke_a + 3.0f * I->ke_b, cond);
+              const float dist = rr - r_c;
+              const float band = band_a + __fdividef(band_b, cond);
               if (fabsf(dist) > band) res = dist < 0.0f ? 1 : 0;
             }
           }
@@ -863,11 +891,20 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
               b = find_inst_u(L.work_prefix, L.count, t);
               I = inst_of(L, b);
               base_t = L.work_prefix[b];
+              cor32 = I->cor32;
+              p_i = I->p;
+              r_c = I->r_c;
+              band_a = I->margin_r;
+              band_b = 8.0f * (I->ke_a + 3.0f * I->ke_b);
+              i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
+            } else {
+              i = find_row_from(rw_c ? rw_c : I->row_work, I->p, i, t - base_t);
             }
-            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
             d = I->deg[i];
             c = d - 1;
             base = I->rowptr[i];
+            nbr = I->colidx + base;
+            row_i = cor32 + i * p_i;
             off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
             s = (int)(off / (unsigned long long)c);
             rank = (int)(off - (unsigned long long)s * c);
@@ -875,8 +912,9 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
           }
         }
         if (moved) {
-          j = I->colidx[base + s];
-          if (MIXED) rij = __ldg(I->cor32 + i * I->p + j);
+          j = nbr[s];
+          row_j = cor32 + j * p_i;
+          if (MIXED) rij = __ldg(row_i + j);
           live = live_bit(I->adj, I->W, i, j);
           steps_on_edge = 0;
         } else if (live && (++steps_on_edge & 3u) == 0) {

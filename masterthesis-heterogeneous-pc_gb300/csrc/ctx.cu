@@ -201,6 +201,8 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.tune = c->tune_dev;
   L.force = c->tune_force;
   L.p_bucket = c->p_bucket;
+  L.row_work_limit = std::min<unsigned long long>(1ull << 56, 0x7FFFFFFFFFFFFFFFull /
+                                                                  (unsigned long long)std::max<long long>(1, c->total_rows));
   L.inst0 = c->inst_host[0];
   return L;
 }
@@ -348,7 +350,8 @@ hpc_status global_errors(hpc_ctx *c) {
   for (int b = 0; b < c->count; ++b) {
     const int err = c->gctr_host[b].err;
     if (err & kErrWorkOverflow) {
-      set_error("instance %d: the number of CI tests of a level overflows 64 bits", b);
+      set_error("instance %d: a row's CI tests at this level exceed the limit of 2^63 / (rows of the context); "
+                "run fewer levels (max_level)", b);
       return HPC_ERR_CAPACITY;
     }
     if (err & kErrRecOverflow) {

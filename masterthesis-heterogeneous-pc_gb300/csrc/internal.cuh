@@ -157,6 +157,8 @@ struct Launch {
   const TuneEntry *tune;            // the context's tile-policy table (kTunePB x kLevels x kTuneDB)
   TuneEntry force;                  // tile_cap > 0: this policy for the level, whatever the table says
   int p_bucket;                     // tune_bucket of the largest p of the launch
+  unsigned long long row_work_limit;  // a row with this many CI tests or more is a work overflow
+                                      // (rows x limit < 2^63: the level's total fits)
   Inst inst0;                       // inst[0] by value: read from the parameter bank when count == 1
 };
 

@@ -21,8 +21,6 @@ namespace hpc {
 
 constexpr int kLevelThreads = 256;
 static_assert(kLevelThreads == kSegRows, "one scan thread per segment row");
-// a row contributing more CI tests than this is reported as a work overflow
-constexpr unsigned long long kRowWorkLimit = 1ull << 40;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
@@ -65,10 +63,11 @@ __device__ __forceinline__ bool grid_barrier(const Launch &L, unsigned int &epoc
 }
 
 // tests a row of degree d contributes at level l; sets *over when beyond the limit
-__device__ __forceinline__ unsigned long long row_tests(int d, int level, int *over) {
+// (limit: the launch's row_work_limit, so that the level's total fits 63 bits)
+__device__ __forceinline__ unsigned long long row_tests(int d, int level, unsigned long long limit, int *over) {
   if (d - 1 < level) return 0ull;
   const unsigned long long c = binom_fast(d - 1, level);
-  if (c >= kRowWorkLimit || (unsigned long long)d * c >= kRowWorkLimit) {
+  if (c >= limit || (unsigned long long)d * c >= limit || umul64hi((unsigned long long)d, c) != 0ull) {
     *over = 1;
     return 0ull;
   }
@@ -153,7 +152,7 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
     if (lane == 0) I->deg[i] = cnt;
     a_deg += (unsigned long long)cnt;
     a_max = max(a_max, cnt);
-    const unsigned long long w = row_tests(cnt, level, &a_over);
+    const unsigned long long w = row_tests(cnt, level, L.row_work_limit, &a_over);
     a_work += w;
     a_rows += w ? 1 : 0;
   }
@@ -304,7 +303,7 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
     const bool bad = s_bad != 0;
     int over = 0;
     const int d = bad ? 0 : d_row;
-    const unsigned long long w = row_tests(d, level, &over);
+    const unsigned long long w = row_tests(d, level, L.row_work_limit, &over);
     unsigned long long all;
     const unsigned long long ex = block_exclusive_scan(w, &all);
     if (valid && !bad) I.row_work[r] = s_sum.base + ex;

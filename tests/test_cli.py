@@ -108,13 +108,14 @@ def test_autotune_and_tune_file(tmp_path):
     write_csv(path, Cm)
     want = orc.run(Cm, 1500, 0.05, 3)
     table = tmp_path / "policy.txt"
-    r = run("--corr", "-o", "1500", "-i", str(path), "-a", "0.05", "-m", "3", "--autotune", "--tune-file", str(table))
+    r = run("--corr", "-o", "1500", "-i", str(path), "-a", "0.05", "-m", "3", "-v", "--autotune", "--tune-file",
+            str(table))
     assert r.returncode == 0, r.stderr
     assert parse_output(r.stdout)[0] == want.edges()
     assert "tile-policy entries" in r.stderr
     lines = open(table).read().splitlines()
     assert lines[0].startswith("heterogpc-tile-policy") and len(lines) > 1
-    r = run("--corr", "-o", "1500", "-i", str(path), "-a", "0.05", "-m", "3", "--tune-file", str(table))
+    r = run("--corr", "-o", "1500", "-i", str(path), "-a", "0.05", "-m", "3", "-v", "--tune-file", str(table))
     assert r.returncode == 0, r.stderr
     assert parse_output(r.stdout)[0] == want.edges()
 
