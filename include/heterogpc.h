@@ -23,8 +23,10 @@ extern "C" {
 #endif
 
 #define HPC_ABI_VERSION 1
-/* Highest conditioning-set size the kernels accept. */
-#define HPC_MAX_LEVEL 16
+/* Highest conditioning-set size the kernels accept (levels 1-16 run unrolled kernels,
+ * 17-32 one kernel with the level read at run time). A skeleton run "until exhausted"
+ * (max_level = -1) stops after this level. */
+#define HPC_MAX_LEVEL 32
 
 typedef enum hpc_status {
   HPC_OK = 0,

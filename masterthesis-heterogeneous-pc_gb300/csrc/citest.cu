@@ -45,7 +45,7 @@ __device__ __forceinline__ double warp_dot(const double *__restrict__ x, const d
 // one warp per queued test forms the FP64 correlation entries it needs as dot
 // products of the FP64-standardised columns, lane 0 evaluates the reference formula.
 // Level-0 items set the kept bits of both triangles; level >= 1 items remove the edge.
-constexpr int kRetestWarps = 8;
+constexpr int kRetestWarps = 4;  // a (HPC_MAX_LEVEL + 2)^2 FP64 matrix per warp: 37 KB of shared memory
 __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_constant__ Launch L) {
   __shared__ double Ms[kRetestWarps][(HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2)];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -103,7 +103,9 @@ void *kernel_for(int level, bool l1_chunked) {
     case 6: return (void *)level_kernel<6, MIXED>;
     case 7: return (void *)level_kernel<7, MIXED>;
     case 8: return (void *)level_kernel<8, MIXED>;
-    default: return level <= 12 ? level_kernel_9_12(level, MIXED) : level_kernel_13_16(level, MIXED);
+    default:
+      return level <= 12 ? level_kernel_9_12(level, MIXED)
+                         : level <= 16 ? level_kernel_13_16(level, MIXED) : level_kernel_17_up(level, MIXED);
   }
 }
 
@@ -122,7 +124,7 @@ int citest_grid(int precision, int level, int device, bool l1_chunked) {
 }
 
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
-  retest_kernel<<<sms * 4, kRetestWarps * 32, 0, s>>>(L);
+  retest_kernel<<<sms * 8, kRetestWarps * 32, 0, s>>>(L);
   HPC_LAUNCH_CHECK("retest_kernel");
   return HPC_OK;
 }

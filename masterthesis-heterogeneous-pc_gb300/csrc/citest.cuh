@@ -1,7 +1,7 @@
 // Device code of the level kernels (levels >= 1), shared by the translation units
 // that instantiate them: citest.cu (levels 1-8, the re-test and record kernels and the
-// launchers) and citest_l9.cu / citest_l13.cu (levels 9-12 and 13-16, compiled in
-// parallel).
+// launchers) and citest_l9.cu / citest_l13.cu / citest_l17.cu (levels 9-12, 13-16 and
+// the runtime-level kernel of levels 17-32, compiled in parallel).
 //
 // Level-l conditional-independence tests (l >= 1) on a persistent grid, over all
 // instances of a context in one launch.
@@ -54,6 +54,12 @@ namespace hpc {
 namespace {
 
 constexpr int kThreads = kLevelThreads;
+
+// Loops over a level's conditioning-set members are unrolled in the kernels of levels
+// 1-16 (LA = the level); the runtime-level kernel of levels 17-32 (LA = HPC_MAX_LEVEL)
+// keeps them rolled, which bounds its code size and compile time.
+template <int LA>
+constexpr int kUnr = LA <= 16 ? (LA > 0 ? LA : 1) : 1;
 
 __device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, int64_t j) {
   const volatile uint32_t *w = adj + i * W + (j >> 5);
@@ -208,13 +214,13 @@ __device__ __noinline__ bool exact_remove_fast(const Inst &I, int64_t i, int64_t
   const int64_t p = I.p;
   const double rij = C[i * p + j];
   double gx[LA], gy[LA], gs[LA * (LA - 1) / 2 > 0 ? LA * (LA - 1) / 2 : 1];
-#pragma unroll
+#pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r)
     if (r < l) {
       const int64_t idr = ids[r];
       gx[r] = C[i * p + idr];
       gy[r] = C[j * p + idr];
-#pragma unroll
+#pragma unroll (kUnr<LA>)
       for (int c = 0; c < LA; ++c)
         if (c < r) gs[r * (r - 1) / 2 + c] = C[(int64_t)ids[c] * p + idr];
     }
@@ -224,26 +230,26 @@ __device__ __noinline__ bool exact_remove_fast(const Inst &I, int64_t i, int64_t
     return decide_of_r(I, (x1 - x2 * x3) / sqrt((1.0 - x3 * x3) * (1.0 - x2 * x2)), false, pv);
   }
   bool nan_in = isnan(rij);
-#pragma unroll
+#pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r)
     if (r < l) {
       nan_in |= isnan(gx[r]) || isnan(gy[r]);
-#pragma unroll
+#pragma unroll (kUnr<LA>)
       for (int c = 0; c < LA; ++c)
         if (c < r) nan_in |= isnan(gs[r * (r - 1) / 2 + c]);
     }
   if (nan_in) return decide_of_r(I, 0.0, true, pv);
   double Lm[LA * (LA + 1) / 2 > 0 ? LA * (LA + 1) / 2 : 1], inv[LA], wx[LA], wy[LA];
   bool ok = true;
-#pragma unroll
+#pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r)
     if (r < l) {
       double vx = gx[r], vy = gy[r], d = 1.0;
-#pragma unroll
+#pragma unroll (kUnr<LA>)
       for (int c = 0; c < LA; ++c)
         if (c < r) {
           double v = gs[r * (r - 1) / 2 + c];
-#pragma unroll
+#pragma unroll (kUnr<LA>)
           for (int q = 0; q < LA; ++q)
             if (q < c) v -= Lm[r * (r + 1) / 2 + q] * Lm[c * (c + 1) / 2 + q];
           v *= inv[c];
@@ -259,7 +265,7 @@ __device__ __noinline__ bool exact_remove_fast(const Inst &I, int64_t i, int64_t
     }
   if (ok) {
     double ax = 1.0, ay = 1.0, b = rij;
-#pragma unroll
+#pragma unroll (kUnr<LA>)
     for (int q = 0; q < LA; ++q)
       if (q < l) {
         ax -= wx[q] * wx[q];
@@ -300,20 +306,20 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
   constexpr int kG = kGather ? LA : 1;
   float gx[kG], gy[kG], gs[kG * (kG - 1) / 2 > 0 ? kG * (kG - 1) / 2 : 1];
   if constexpr (kGather) {
-#pragma unroll
+#pragma unroll (kUnr<LA>)
     for (int r = 0; r < LA; ++r) {
       if (r >= ci && r < l) {
         const int idr = ids[r];
         gx[r] = __ldg(C + i * p + idr);
         gy[r] = __ldg(C + j * p + idr);
-#pragma unroll
+#pragma unroll (kUnr<LA>)
         for (int c = 0; c < LA; ++c)
           if (c < r) gs[r * (r - 1) / 2 + c] = __ldg(C + (int64_t)ids[c] * p + idr);
       }
     }
   }
   const float rij = __ldg(C + i * p + j);
-#pragma unroll
+#pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r) {
     if (r >= ci && r < l) {
       const int idr = ids[r];
@@ -326,7 +332,7 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
         vy = __ldg(C + j * p + idr);
       }
       float d = 1.0f;
-#pragma unroll
+#pragma unroll (kUnr<LA>)
       for (int c = 0; c < LA; ++c) {
         if (c < r) {
           float v;
@@ -334,7 +340,7 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
             v = gs[r * (r - 1) / 2 + c];
           else
             v = __ldg(C + (int64_t)ids[c] * p + idr);
-#pragma unroll
+#pragma unroll (kUnr<LA>)
           for (int q = 0; q < LA; ++q)
             if (q < c) v -= F.Lm[r * (r + 1) / 2 + q] * F.Lm[c * (c + 1) / 2 + q];
           v *= F.invd[c];
@@ -354,7 +360,7 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
   // the sums in row order, whatever ci was, so that the decision does not depend on
   // the walk
   float sx = 0.f, sy = 0.f, sxy = 0.f, dmin = 1.f;
-#pragma unroll
+#pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r)
     if (r < l) {
       dmin = fminf(dmin, F.piv[r]);
@@ -505,7 +511,7 @@ __device__ __forceinline__ void push_pending(PendRem<LA> *list, int *np, const I
   e.b = b;
   e.pad = 0;
   e.pv = pv;
-#pragma unroll
+#pragma unroll (kUnr<LA>)
   for (int q = 0; q < (LA > 0 ? LA : 1); ++q) e.ids[q] = q < l ? ids[q] : -1;
 }
 
@@ -674,7 +680,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
       Fact<LA> F;
       for (;;) {
         if (alive) {
-#pragma unroll
+#pragma unroll (kUnr<LA>)
           for (int q = 0; q < LA; ++q)
             if (q < l && q >= ci) ids[q] = I->colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
           int res = 2;
@@ -724,7 +730,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
             base = I->rowptr[i];
             s = 0;
           }
-#pragma unroll
+#pragma unroll (kUnr<LA>)
           for (int q = 0; q < LA; ++q)
             if (q < l) pos[q] = q;
           j = I->colidx[base + s];
@@ -813,28 +819,21 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
       int s = (int)(off / (unsigned long long)c);
       int rank = (int)(off - (unsigned long long)s * c);
       int base = I->rowptr[i];
-      // the instance's fields a step needs, in registers (the descriptor is reached
-      // through a generic pointer, which the compiler would reload every step)
-      const int *nbr = I->colidx + base;  // row i's neighbour list
-      const float *cor32 = I->cor32;
-      int64_t p_i = I->p;
-      float r_c = I->r_c, band_a = I->margin_r, band_b = 8.0f * (I->ke_a + 3.0f * I->ke_b);
-      int64_t j = nbr[s];
-      const float *row_i = cor32 + i * p_i, *row_j = cor32 + j * p_i;
-      float rij = MIXED ? __ldg(row_i + j) : 0.f;
+      int64_t j = I->colidx[base + s];
+      float rij = MIXED ? __ldg(I->cor32 + i * I->p + j) : 0.f;
       // the live bit is read when the lane enters an edge and every fourth step on it
       // (removals by this warp reach its lanes through the step's ballot)
       bool live = live_bit(I->adj, I->W, i, j);
       if (!live && lane == 0) skip_tiles_of_edge(L, t - rank + c, tend, per_tile, nwarps);
       unsigned steps_on_edge = 0;
       for (;;) {
-        const int k = nbr[rank + (rank >= s ? 1 : 0)];
+        const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
         // the entries are loaded before the live bit is known (in bounds either way):
         // the two round trips overlap instead of following each other
         float x2 = 0.f, x3 = 0.f;
         if (MIXED) {
-          x2 = __ldg(row_i + k);
-          x3 = __ldg(row_j + k);
+          x2 = __ldg(I->cor32 + i * I->p + k);
+          x3 = __ldg(I->cor32 + j * I->p + k);
         }
         bool rm = false;
         double pv_rm = 0.0;
@@ -846,8 +845,8 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
             const float cond = fminf(ax, ay);
             if (cond > 1e-3f) {
               rr = fabsf(rij - x2 * x3) * rsqrtf(ax * ay);
-              const float dist = rr - r_c;
-              const float band = band_a + __fdividef(band_b, cond);
+              const float dist = rr - I->r_c;
+              const float band = I->margin_r + 8.0f * __fdividef(I->ke_a + 3.0f * I->ke_b, cond);
               if (fabsf(dist) > band) res = dist < 0.0f ? 1 : 0;
             }
           }
@@ -891,11 +890,6 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
               b = find_inst_u(L.work_prefix, L.count, t);
               I = inst_of(L, b);
               base_t = L.work_prefix[b];
-              cor32 = I->cor32;
-              p_i = I->p;
-              r_c = I->r_c;
-              band_a = I->margin_r;
-              band_b = 8.0f * (I->ke_a + 3.0f * I->ke_b);
               i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
             } else {
               i = find_row_from(rw_c ? rw_c : I->row_work, I->p, i, t - base_t);
@@ -903,8 +897,6 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
             d = I->deg[i];
             c = d - 1;
             base = I->rowptr[i];
-            nbr = I->colidx + base;
-            row_i = cor32 + i * p_i;
             off = t - base_t - (rw_c ? rw_c : I->row_work)[i];
             s = (int)(off / (unsigned long long)c);
             rank = (int)(off - (unsigned long long)s * c);
@@ -912,9 +904,8 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
           }
         }
         if (moved) {
-          j = nbr[s];
-          row_j = cor32 + j * p_i;
-          if (MIXED) rij = __ldg(row_i + j);
+          j = I->colidx[base + s];
+          if (MIXED) rij = __ldg(I->cor32 + i * I->p + j);
           live = live_bit(I->adj, I->W, i, j);
           steps_on_edge = 0;
         } else if (live && (++steps_on_edge & 3u) == 0) {
@@ -955,8 +946,9 @@ __global__ void __launch_bounds__(kThreads, LT == 1 && !L1C ? 4 : 2) level_kerne
 
 }  // namespace
 
-// level kernels of levels 9-16 (citest_l9.cu, citest_l13.cu)
+// level kernels of levels 9-32 (citest_l9.cu, citest_l13.cu, citest_l17.cu)
 void *level_kernel_9_12(int level, bool mixed);
 void *level_kernel_13_16(int level, bool mixed);
+void *level_kernel_17_up(int level, bool mixed);
 
 }  // namespace hpc

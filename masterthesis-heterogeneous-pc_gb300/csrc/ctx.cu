@@ -540,10 +540,12 @@ GramArgs gram_args(hpc_ctx *c) {
 }
 
 // Entries of the deferred FP64 re-test queue (tensor-core mode): a test is queued when
-// its FP32 |r| lies within the band around r_crit, about 1e-4 of the tests of a wide
-// level 1 (18.7 M of 1.3e11 at p = 15000), so the queue grows with sum p^2 / 8, from 1 Mi
-// to 32 Mi entries (80 B each). Tests beyond it are re-tested in place.
-long long retest_queue_cap(long long sum_p2) { return std::min<long long>(32ll << 20, std::max<long long>(1ll << 20, sum_p2 / 8)); }
+// its FP32 |r| lies within the band around r_crit, about 4e-5 of the tests of a wide
+// level 1 (4.7 M of 1.1e11 at p = 15000), so the queue grows with sum p^2 / 16, from 1 Mi
+// to 16 Mi entries (144 B each). Tests beyond it are re-tested in place.
+long long retest_queue_cap(long long sum_p2) {
+  return std::min<long long>(16ll << 20, std::max<long long>(1ll << 20, sum_p2 / 16));
+}
 
 hpc_status after_correlation(hpc_ctx *c) {
   c->have_cor = true;

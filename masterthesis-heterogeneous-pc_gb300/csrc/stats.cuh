@@ -106,7 +106,7 @@ HPC_HD unsigned long long binom_sat(int n, int k) {
 
 #ifdef __CUDACC__
 // C(n, k) for n < 64 and k <= HPC_MAX_LEVEL (Pascal's triangle at compile time; the
-// largest entry, C(63, 16), fits 64 bits). Device lookups replace binom_sat's
+// largest entry, C(63, 32) = 9.2e17, fits 64 bits). Lookups replace binom_sat's
 // 64-bit divisions on the CI-test path.
 struct BinomTable {
   unsigned long long v[64][HPC_MAX_LEVEL + 1];

@@ -14,7 +14,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libheterogpc.so")
 
-HPC_MAX_LEVEL = 16
+HPC_MAX_LEVEL = 32
 PREC_FP64, PREC_MIXED, PREC_MIXED_TC = 0, 1, 2
 GRAPH_ER, GRAPH_PA = 0, 1
 

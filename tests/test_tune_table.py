@@ -45,16 +45,16 @@ def test_file_round_trip(tmp_path):
 
 @pytest.mark.parametrize("args", [(2000, 1, 10, 0, 4, 32), (2000, 1, 10, 65537, 4, 32), (2000, 1, 10, 64, 0, 32),
                                   (2000, 1, 10, 64, 65, 32), (2000, 1, 10, 64, 4, 8), (1, 1, 10, 64, 4, 32),
-                                  (2000, 0, 10, 64, 4, 32), (2000, 17, 10, 64, 4, 32), (2000, 1, -1, 64, 4, 32)])
+                                  (2000, 0, 10, 64, 4, 32), (2000, hg.HPC_MAX_LEVEL + 1, 10, 64, 4, 32), (2000, 1, -1, 64, 4, 32)])
 def test_rejects_bad_policies_and_keys(args):
     with pytest.raises(hg.HpcError) as e:
         hg.tune_set(*args)
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("text", ["not a policy file\n", "heterogpc-tile-policy 1 32 17 18\n1 0 3 64 4 32\n",
-                                  "heterogpc-tile-policy 1 32 17 18\n1 2 3 64 4\n",
-                                  "heterogpc-tile-policy 2 32 17 18\n", "heterogpc-tile-policy 1 32 17 18\n1 2 3 0 4 32\n"])
+@pytest.mark.parametrize("text", ["not a policy file\n", "heterogpc-tile-policy 1 32 33 18\n1 0 3 64 4 32\n",
+                                  "heterogpc-tile-policy 1 32 33 18\n1 2 3 64 4\n",
+                                  "heterogpc-tile-policy 2 32 33 18\n", "heterogpc-tile-policy 1 32 33 18\n1 2 3 0 4 32\n"])
 def test_rejects_bad_files(tmp_path, text):
     path = tmp_path / "bad.txt"
     path.write_text(text)
