@@ -79,10 +79,11 @@ def correlation_error(hg, c32, p, n, Xd, stream):
 
 # c3's candidates (each run of the wide workload takes seconds): tile caps from the
 # default to long chunks for the hub rows, both level-1 lane mappings
-C3_CANDIDATES = [{"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32},
-                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 32},
-                 {"tile_cap": 8192, "tiles_per_lane": 8, "l1_lanes": 32},
-                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 1}]
+C3_CANDIDATES = [{"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 0},
+                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 1},
+                 {"tile_cap": 8192, "tiles_per_lane": 8, "l1_lanes": 32, "l1_prefetch": 0},
+                 {"tile_cap": 8192, "tiles_per_lane": 8, "l1_lanes": 32, "l1_prefetch": 1},
+                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 1, "l1_prefetch": 0}]
 
 
 def run_c3(args, wl):
@@ -193,7 +194,7 @@ def autotune_setup(args, ctx, candidates, reps):
     chosen, entries = ctx.autotune(candidates, reps=reps)
     if args.tune_file:
         hg.tune_save(args.tune_file)
-    return {"autotuned": True, "candidates": "built-in grid (24)" if candidates is None else candidates,
+    return {"autotuned": True, "candidates": "built-in grid (36)" if candidates is None else candidates,
             "chosen": {str(k): v for k, v in chosen.items()}, "entries": entries,
             "tuning_s": time.perf_counter() - t0}
 
@@ -346,7 +347,7 @@ def run_c4(args, wl):
 
     for _ in range(args.warmup):
         step()
-    tuned = autotune_setup(args, bt, None, 1)
+    tuned = autotune_setup(args, bt, None, 2)
     step()
     torch.cuda.synchronize()
     ms, tests = [], 0
@@ -710,7 +711,7 @@ def main():
         sk_plain.run()
     # tile policy: hpc_autotune (untimed set-up, like a library's heuristics query) over
     # its built-in candidates, then one more warm-up run of each context with the table
-    tuned = autotune_setup(args, sk, None, 2)
+    tuned = autotune_setup(args, sk, None, 3)
     for s_ in (sk, sk_plain):
         s_.reset()
         s_.run()

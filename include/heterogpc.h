@@ -196,7 +196,9 @@ hpc_status hpc_wait(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_r
  *   tiles_per_lane  target number of tiles per lane of the grid (balance vs claim cost)
  *   l1_lanes        level 1 only: 32 = a warp's lanes interleaved over one edge's tests,
  *                   1 = each lane a chunk of consecutive tests
- * Defaults: 64, 4, 32. A process-wide table holds policies keyed by buckets of
+ *   l1_prefetch     level 1 with l1_lanes 32 only: 1 = the next step's entries are loaded
+ *                   one step ahead (pays off on long neighbour lists)
+ * Defaults: 64, 4, 32, 0. A process-wide table holds policies keyed by buckets of
  * (largest p of the launch, level, largest degree at the level start), buckets being
  * bit lengths; every level kernel reads its entry on the device after its test-count
  * scan, so the table also steers CUDA-graph replays. */
@@ -204,6 +206,7 @@ typedef struct hpc_tune_params {
   int tile_cap;        /* 1..65536 */
   int tiles_per_lane;  /* 1..64 */
   int l1_lanes;        /* 1 or 32 */
+  int l1_prefetch;     /* 0 or 1 */
 } hpc_tune_params;
 /* Sets (prm != NULL) or erases (NULL) the table entry of the key's buckets. */
 hpc_status hpc_tune_set(int64_t p, int level, int max_degree, const hpc_tune_params *prm);
@@ -220,7 +223,8 @@ hpc_status hpc_ctx_set_tune(hpc_ctx *ctx, const hpc_tune_params *force);
  * kernel) once per candidate policy and repetition, times every level's CI-test
  * kernel with CUDA events, and stores for each level the fastest candidate under the
  * level's key. cands/ncands: the candidates (NULL = the built-in grid: tile_cap
- * 16, 64, 256, 1024 x tiles_per_lane 2, 4, 8 x l1_lanes 32, 1). chosen (optional,
+ * 16, 64, 256, 1024 x tiles_per_lane 2, 4, 8 x level-1 kernel interleaved,
+ * interleaved with prefetch, chunked). chosen (optional,
  * HPC_MAX_LEVEL + 1 entries) receives each level's choice (zeros for levels not run);
  * *entries (optional) the number of table entries written. Decisions, and so the
  * skeleton, do not depend on the policy; the context is reset afterwards. */

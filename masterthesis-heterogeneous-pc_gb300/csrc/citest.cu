@@ -93,9 +93,12 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_
 }
 
 template <bool MIXED>
-void *kernel_for(int level, bool l1_chunked) {
+void *kernel_for(int level, int l1_variant) {
   switch (level) {
-    case 1: return l1_chunked ? (void *)level_kernel<1, MIXED, true> : (void *)level_kernel<1, MIXED>;
+    case 1:
+      return l1_variant == kL1Chunked    ? (void *)level_kernel<1, MIXED, kL1Chunked>
+             : l1_variant == kL1Prefetch ? (void *)level_kernel<1, MIXED, kL1Prefetch>
+                                         : (void *)level_kernel<1, MIXED>;
     case 2: return (void *)level_kernel<2, MIXED>;
     case 3: return (void *)level_kernel<3, MIXED>;
     case 4: return (void *)level_kernel<4, MIXED>;
@@ -111,8 +114,8 @@ void *kernel_for(int level, bool l1_chunked) {
 
 }  // namespace
 
-int citest_grid(int precision, int level, int device, bool l1_chunked) {
-  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(level, l1_chunked) : kernel_for<true>(level, l1_chunked);
+int citest_grid(int precision, int level, int device, int l1_variant) {
+  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(level, l1_variant) : kernel_for<true>(level, l1_variant);
   const int smem = level == 1 ? 0 : kRowCache * (int)sizeof(unsigned long long);
   // the row-offset cache is beyond the default 48 KB of dynamic shared memory
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) cudaGetLastError();
@@ -135,9 +138,9 @@ hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s) 
   return HPC_OK;
 }
 
-hpc_status launch_level(const Launch &L, int precision, int grid, bool l1_chunked, cudaStream_t s) {
-  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(L.level, l1_chunked)
-                                       : kernel_for<true>(L.level, l1_chunked);
+hpc_status launch_level(const Launch &L, int precision, int grid, int l1_variant, cudaStream_t s) {
+  void *k = precision == HPC_PREC_FP64 ? kernel_for<false>(L.level, l1_variant)
+                                       : kernel_for<true>(L.level, l1_variant);
   Launch args = L;
   void *params[] = {&args};
   // cooperative: every block co-resident, as the grid barriers require

@@ -765,7 +765,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
 // cache lines and stay in L1 across the edges of row i, and only the reads of row j
 // are scattered. Decisions as test_f32_inc with l = 1 (the closed form of cpuInd.cpp:16-27
 // in FP32), FP64 re-tests as in citest_kernel.
-template <bool MIXED>
+template <bool MIXED, bool PF>
 __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te) {
   const int level = 1;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -826,14 +826,33 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
       bool live = live_bit(I->adj, I->W, i, j);
       if (!live && lane == 0) skip_tiles_of_edge(L, t - rank + c, tend, per_tile, nwarps);
       unsigned steps_on_edge = 0;
-      for (;;) {
-        const int k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
-        // the entries are loaded before the live bit is known (in bounds either way):
-        // the two round trips overlap instead of following each other
-        float x2 = 0.f, x3 = 0.f;
+      // The entries are loaded before the live bit is known (in bounds either way): the
+      // two round trips overlap instead of following each other. With PF (the prefetch
+      // variant, for long edges) the entries of the next position on the same edge are
+      // also loaded one step ahead -- its neighbour id before the test, its entries
+      // before the step's ballots -- so that their round trip overlaps this step.
+      int k = 0;
+      float x2 = 0.f, x3 = 0.f;
+      if (PF) {
+        k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
         if (MIXED) {
           x2 = __ldg(I->cor32 + i * I->p + k);
           x3 = __ldg(I->cor32 + j * I->p + k);
+        }
+      }
+      for (;;) {
+        int kn = 0;
+        bool ahead = false;
+        if (PF) {
+          const int rn = rank + 32;
+          ahead = rn < c;
+          if (ahead) kn = I->colidx[base + rn + (rn >= s ? 1 : 0)];
+        } else {
+          k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
+          if (MIXED) {
+            x2 = __ldg(I->cor32 + i * I->p + k);
+            x3 = __ldg(I->cor32 + j * I->p + k);
+          }
         }
         bool rm = false;
         double pv_rm = 0.0;
@@ -860,6 +879,11 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
             if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, &k, 1)))
               rm = exact_remove_fast<1>(*I, i, j, &k, 1, &pv_rm);
           }
+        }
+        float x2n = 0.f, x3n = 0.f;
+        if (PF && MIXED && ahead) {
+          x2n = __ldg(I->cor32 + i * I->p + kn);
+          x3n = __ldg(I->cor32 + j * I->p + kn);
         }
         {
           // lanes on the same edge learn of its removal in this step; one of them
@@ -908,8 +932,20 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
           if (MIXED) rij = __ldg(I->cor32 + i * I->p + j);
           live = live_bit(I->adj, I->W, i, j);
           steps_on_edge = 0;
-        } else if (live && (++steps_on_edge & 3u) == 0) {
-          live = live_bit(I->adj, I->W, i, j);
+          if (PF) {
+            k = I->colidx[base + rank + (rank >= s ? 1 : 0)];
+            if (MIXED) {
+              x2 = __ldg(I->cor32 + i * I->p + k);
+              x3 = __ldg(I->cor32 + j * I->p + k);
+            }
+          }
+        } else {
+          if (PF) {  // one step on the same edge: the position loaded ahead
+            k = kn;
+            x2 = x2n;
+            x3 = x3n;
+          }
+          if (live && (++steps_on_edge & 3u) == 0) live = live_bit(I->adj, I->W, i, j);
         }
       }
       b_last = b;
@@ -927,10 +963,12 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 }
 
 // One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
-// is the lane-interleaved level-1 body (L1C: the chunked body of the higher levels,
-// picked by the tile policy's l1_lanes = 1), LT = 2..16 the bodies unrolled for l = LT.
-template <int LT, bool MIXED, bool L1C = false>
-__global__ void __launch_bounds__(kThreads, LT == 1 && !L1C ? 4 : 2) level_kernel(const __grid_constant__ Launch L) {
+// is the lane-interleaved level-1 body (L1V: kL1Prefetch loads one step ahead,
+// kL1Chunked runs the chunked body of the higher levels; picked by the tile policy),
+// LT = 2..16 the bodies unrolled for l = LT, LT = 0 the runtime-level body.
+template <int LT, bool MIXED, int L1V = kL1Interleaved>
+__global__ void __launch_bounds__(kThreads, LT == 1 && L1V != kL1Chunked ? 4 : 2)
+    level_kernel(const __grid_constant__ Launch L) {
   extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
   rebuild_phase(L);
@@ -938,8 +976,8 @@ __global__ void __launch_bounds__(kThreads, LT == 1 && !L1C ? 4 : 2) level_kerne
   scan_phase(L);
   if (!grid_barrier(L, epoch)) return;
   const TuneEntry te = tile_policy(L);
-  if (LT == 1 && !L1C)
-    tests_l1<MIXED>(L, nullptr, te);  // level 1 keeps the SM's on-chip memory for L1 cache
+  if (LT == 1 && L1V != kL1Chunked)  // level 1 keeps the SM's on-chip memory for L1 cache
+    tests_l1<MIXED, L1V == kL1Prefetch>(L, nullptr, te);
   else
     tests_generic<LT, MIXED>(L, LT == 1 ? nullptr : rw_smem, te);
 }

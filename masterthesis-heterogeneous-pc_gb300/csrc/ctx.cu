@@ -237,9 +237,9 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   }
   // snapshot rebuild, test-count scan and CI tests in one launch
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  const bool l1c = level == 1 && c->l1c_now;
-  if ((s = launch_level(L, c->opts.precision, l1c ? c->citest_grid_l1c : c->citest_grid[level], l1c, c->stream)) !=
-      HPC_OK)
+  const int l1v = level == 1 ? c->l1v_now : kL1Interleaved;
+  if ((s = launch_level(L, c->opts.precision, level == 1 ? c->citest_grid_l1[l1v] : c->citest_grid[level], l1v,
+                        c->stream)) != HPC_OK)
     return s;
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
@@ -380,14 +380,19 @@ bool any_work(hpc_ctx *c, int level) {
 
 bool capturable(cudaStream_t s) { return s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread; }
 
-// Level 1's kernel (the kernel is chosen on the host, the tile sizes on the device):
-// the forced policy's l1_lanes, else the table entry for the level-1 degree of the
-// context's last run (the default, interleaved, before any run).
-bool level1_chunked(hpc_ctx *c) {
-  if (c->tune_force.tile_cap > 0) return c->tune_force.l1_lanes == 1;
-  if (c->l1_max_deg < 0) return false;
-  const TuneEntry e = tune_get(c->p_bucket, 1, tune_bucket(c->l1_max_deg, kTuneDB));
-  return e.tile_cap > 0 && e.l1_lanes == 1;
+// Level 1's kernel variant (kL1*; the kernel is chosen on the host, the tile sizes on
+// the device): from the forced policy, else from the table entry for the level-1
+// degree of the context's last run (the default, interleaved, before any run).
+int l1_variant_of(const TuneEntry &e) {
+  if (e.tile_cap <= 0) return kL1Interleaved;
+  if (e.l1_lanes == 1) return kL1Chunked;
+  return e.l1_prefetch ? kL1Prefetch : kL1Interleaved;
+}
+
+int level1_variant(hpc_ctx *c) {
+  if (c->tune_force.tile_cap > 0) return l1_variant_of(c->tune_force);
+  if (c->l1_max_deg < 0) return kL1Interleaved;
+  return l1_variant_of(tune_get(c->p_bucket, 1, tune_bucket(c->l1_max_deg, kTuneDB)));
 }
 
 // The context's device copy of the tile-policy table, refreshed when the table
@@ -413,7 +418,7 @@ hpc_status sync_tune(hpc_ctx *c) {
 hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait = true) {
   hpc_status s;
   if ((s = sync_tune(c)) != HPC_OK) return s;
-  c->l1c_now = level1_chunked(c);
+  c->l1v_now = level1_variant(c);
   auto enqueue_all = [&](bool timed) -> hpc_status {
     if (first == 0) {  // a skeleton from the start: its counters and records begin at zero
       HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)c->count * kLevels, c->stream));
@@ -428,7 +433,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
   };
   if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
-                       c->graph_version == c->inst_version && c->graph_l1c == c->l1c_now;
+                       c->graph_version == c->inst_version && c->graph_l1v == c->l1v_now;
     if (!valid) {
       if (c->graph) cudaGraphExecDestroy(c->graph);
       c->graph = nullptr;
@@ -452,7 +457,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
       c->graph_top = last;
       c->graph_stream = c->stream;
       c->graph_version = c->inst_version;
-      c->graph_l1c = c->l1c_now;
+      c->graph_l1v = c->l1v_now;
     }
     HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
     c->timings.launches += c->graph_launches;
@@ -841,7 +846,8 @@ hpc_status hpc_ctx_set_tune(hpc_ctx *c, const hpc_tune_params *force) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
   if (force && !tune_params_valid(force)) {
-    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32", kTuneMaxCap);
+    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32, l1_prefetch 0 or 1",
+              kTuneMaxCap);
     return HPC_ERR_INVALID_ARG;
   }
   if ((s = settle(c)) != HPC_OK) return s;
@@ -873,9 +879,9 @@ hpc_status hpc_autotune(hpc_ctx *c, const hpc_tune_params *cands, int ncands, in
       grid.push_back(cands[q]);
     }
   } else {
-    for (int l1 : {32, 1})
+    for (int v = 0; v < 3; ++v)  // level-1 variants: interleaved, interleaved with prefetch, chunked
       for (int cap : {16, 64, 256, 1024})
-        for (int tpl : {2, 4, 8}) grid.push_back(hpc_tune_params{cap, tpl, l1});
+        for (int tpl : {2, 4, 8}) grid.push_back(hpc_tune_params{cap, tpl, v == 2 ? 1 : 32, v == 1 ? 1 : 0});
   }
   const bool graphs = c->graphs_enabled;
   const TuneEntry force0 = c->tune_force;
@@ -917,7 +923,7 @@ hpc_status hpc_autotune(hpc_ctx *c, const hpc_tune_params *cands, int ncands, in
   for (const auto &h : c->ih) pmax = std::max<int64_t>(pmax, h.p);
   int written = 0;
   for (int l = 0; l < kLevels; ++l) {
-    if (chosen) chosen[l] = best[l] >= 0 ? grid[(size_t)best[l]] : hpc_tune_params{0, 0, 0};
+    if (chosen) chosen[l] = best[l] >= 0 ? grid[(size_t)best[l]] : hpc_tune_params{0, 0, 0, 0};
     if (best[l] < 0) continue;
     tune_store(pmax, l, max_deg[l], tune_entry_of(grid[(size_t)best[l]]));
     ++written;
@@ -1452,7 +1458,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   }
   c->stream = c->own_stream;
   for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
-  c->citest_grid_l1c = citest_grid(o.precision, 1, c->device, true);
+  for (int v = 0; v < 3; ++v) c->citest_grid_l1[v] = citest_grid(o.precision, 1, c->device, v);
   if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, cor, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, cor, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, adj, "adjacency")) != HPC_OK) return fail(s);

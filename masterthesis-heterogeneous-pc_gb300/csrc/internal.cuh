@@ -73,8 +73,11 @@ struct LaunchCounters {
 // l1_lanes picks level 1's mapping: 32 = the warp's lanes interleaved over one edge's
 // tests, 1 = each lane a chunk of consecutive tests (the levels >= 2 mapping).
 struct TuneEntry {
-  int tile_cap, tiles_per_lane, l1_lanes, pad;
+  int tile_cap, tiles_per_lane, l1_lanes, l1_prefetch;
 };
+// level-1 kernel variants: lanes interleaved over an edge, the same with the next
+// position's entries loaded a step ahead, each lane a chunk of consecutive tests
+constexpr int kL1Interleaved = 0, kL1Prefetch = 1, kL1Chunked = 2;
 constexpr int kTuneDefaultCap = 64, kTuneDefaultTpl = 4, kTuneDefaultL1Lanes = 32, kTuneMaxCap = 65536;
 // table of a context: [p bucket][level][degree bucket]; bucket = bit length, capped
 constexpr int kTunePB = 32, kTuneDB = 18;
@@ -241,11 +244,11 @@ hpc_status launch_degrees(const Launch &L, long long total_rows, cudaStream_t s)
 hpc_status launch_scan(const Launch &L, cudaStream_t s);
 hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_t *out, cudaStream_t s);
 // Level l >= 1 in one cooperative launch: snapshot rebuild, test-count scan, CI tests.
-// l1_chunked: level 1 with the chunked body of the higher levels (tile policy l1_lanes = 1).
-hpc_status launch_level(const Launch &L, int precision, int grid, bool l1_chunked, cudaStream_t s);
+// l1_variant: level 1's kernel (kL1Interleaved, kL1Prefetch or kL1Chunked, from the tile policy).
+hpc_status launch_level(const Launch &L, int precision, int grid, int l1_variant, cudaStream_t s);
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
-int citest_grid(int precision, int level, int device, bool l1_chunked = false);
+int citest_grid(int precision, int level, int device, int l1_variant = kL1Interleaved);
 
 // process-wide tile-policy table (tune.cu)
 TuneEntry tune_entry_of(const hpc_tune_params &p);
@@ -329,10 +332,10 @@ struct hpc_ctx {
   long long tune_version_dev = -1;
   hpc::TuneEntry tune_force{};
   int p_bucket = 0;
-  int citest_grid_l1c = 0;        // grid of the chunked level-1 kernel
+  int citest_grid_l1[3] = {};     // grids of the level-1 kernel variants (kL1*)
   int l1_max_deg = -1;            // level-1 max degree of the last run (keys level 1's kernel choice)
-  bool l1c_now = false;           // the level-1 kernel of the runs being queued is the chunked one
-  bool graph_l1c = false;         // ... and of the captured graph
+  int l1v_now = 0;                // the level-1 kernel variant of the runs being queued
+  int graph_l1v = 0;              // ... and of the captured graph
   cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
   cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
   cudaEvent_t evr[2] = {nullptr, nullptr};      // whole skeleton run

@@ -23,7 +23,7 @@ size_t index_of(int pb, int level, int db) { return ((size_t)pb * kLv + level) *
 
 bool valid_params(const hpc_tune_params &p) {
   return p.tile_cap >= 1 && p.tile_cap <= kTuneMaxCap && p.tiles_per_lane >= 1 && p.tiles_per_lane <= 64 &&
-         (p.l1_lanes == 1 || p.l1_lanes == 32);
+         (p.l1_lanes == 1 || p.l1_lanes == 32) && (p.l1_prefetch == 0 || p.l1_prefetch == 1);
 }
 
 hpc_status check_key(int64_t p, int level, int max_degree) {
@@ -36,7 +36,9 @@ hpc_status check_key(int64_t p, int level, int max_degree) {
 
 }  // namespace
 
-TuneEntry tune_entry_of(const hpc_tune_params &p) { return TuneEntry{p.tile_cap, p.tiles_per_lane, p.l1_lanes, 0}; }
+TuneEntry tune_entry_of(const hpc_tune_params &p) {
+  return TuneEntry{p.tile_cap, p.tiles_per_lane, p.l1_lanes, p.l1_prefetch};
+}
 
 bool tune_params_valid(const hpc_tune_params *p) { return p && valid_params(*p); }
 
@@ -72,7 +74,8 @@ hpc_status hpc_tune_set(int64_t p, int level, int max_degree, const hpc_tune_par
   hpc_status s = check_key(p, level, max_degree);
   if (s != HPC_OK) return s;
   if (prm && !valid_params(*prm)) {
-    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32", kTuneMaxCap);
+    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32, l1_prefetch 0 or 1",
+              kTuneMaxCap);
     return HPC_ERR_INVALID_ARG;
   }
   tune_store(p, level, max_degree, prm ? tune_entry_of(*prm) : TuneEntry{0, 0, 0, 0});
@@ -95,6 +98,7 @@ hpc_status hpc_tune_lookup(int64_t p, int level, int max_degree, hpc_tune_params
   out->tile_cap = have ? e.tile_cap : kTuneDefaultCap;
   out->tiles_per_lane = have ? e.tiles_per_lane : kTuneDefaultTpl;
   out->l1_lanes = have ? e.l1_lanes : kTuneDefaultL1Lanes;
+  out->l1_prefetch = have ? e.l1_prefetch : 0;
   if (found) *found = have ? 1 : 0;
   return HPC_OK;
 }
@@ -107,7 +111,7 @@ hpc_status hpc_tune_clear(void) {
 }
 
 // Text file: a header line, then one line per entry:
-//   p_bucket level degree_bucket tile_cap tiles_per_lane l1_lanes
+//   p_bucket level degree_bucket tile_cap tiles_per_lane l1_lanes l1_prefetch
 hpc_status hpc_tune_save(const char *path) {
   if (!path) {
     set_error("null path");
@@ -121,12 +125,13 @@ hpc_status hpc_tune_save(const char *path) {
     set_error("cannot write %s", path);
     return HPC_ERR_INVALID_ARG;
   }
-  std::fprintf(f, "heterogpc-tile-policy 1 %d %d %d\n", kTunePB, kLv, kTuneDB);
+  std::fprintf(f, "heterogpc-tile-policy 2 %d %d %d\n", kTunePB, kLv, kTuneDB);
   for (int pb = 0; pb < kTunePB; ++pb)
     for (int l = 0; l < kLv; ++l)
       for (int db = 0; db < kTuneDB; ++db) {
         const TuneEntry &e = t[index_of(pb, l, db)];
-        if (e.tile_cap > 0) std::fprintf(f, "%d %d %d %d %d %d\n", pb, l, db, e.tile_cap, e.tiles_per_lane, e.l1_lanes);
+        if (e.tile_cap > 0)
+          std::fprintf(f, "%d %d %d %d %d %d %d\n", pb, l, db, e.tile_cap, e.tiles_per_lane, e.l1_lanes, e.l1_prefetch);
       }
   const bool ok = std::fclose(f) == 0;
   if (!ok) {
@@ -148,20 +153,20 @@ hpc_status hpc_tune_load(const char *path) {
     return HPC_ERR_INVALID_ARG;
   }
   int ver = 0, npb = 0, nl = 0, ndb = 0;
-  if (std::fscanf(f, "heterogpc-tile-policy %d %d %d %d", &ver, &npb, &nl, &ndb) != 4 || ver != 1 ||
+  if (std::fscanf(f, "heterogpc-tile-policy %d %d %d %d", &ver, &npb, &nl, &ndb) != 4 || ver != 2 ||
       npb != kTunePB || nl != kLv || ndb != kTuneDB) {
     std::fclose(f);
     set_error("%s is not a tile-policy file of this library", path);
     return HPC_ERR_INVALID_ARG;
   }
   std::vector<std::pair<size_t, TuneEntry>> rows;
-  int pb, l, db, cap, tpl, l1;
+  int pb, l, db, cap, tpl, l1, pf;
   int r;
-  while ((r = std::fscanf(f, "%d %d %d %d %d %d", &pb, &l, &db, &cap, &tpl, &l1)) == 6) {
-    const hpc_tune_params prm{cap, tpl, l1};
+  while ((r = std::fscanf(f, "%d %d %d %d %d %d %d", &pb, &l, &db, &cap, &tpl, &l1, &pf)) == 7) {
+    const hpc_tune_params prm{cap, tpl, l1, pf};
     if (pb < 0 || pb >= kTunePB || l < 1 || l >= kLv || db < 0 || db >= kTuneDB || !valid_params(prm)) {
       std::fclose(f);
-      set_error("%s: bad entry %d %d %d %d %d %d", path, pb, l, db, cap, tpl, l1);
+      set_error("%s: bad entry %d %d %d %d %d %d %d", path, pb, l, db, cap, tpl, l1, pf);
       return HPC_ERR_INVALID_ARG;
     }
     rows.push_back({index_of(pb, l, db), tune_entry_of(prm)});

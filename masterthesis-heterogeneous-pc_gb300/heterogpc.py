@@ -71,7 +71,7 @@ class Served(C.Structure):
 
 
 class TuneParams(C.Structure):
-    _fields_ = [("tile_cap", C.c_int), ("tiles_per_lane", C.c_int), ("l1_lanes", C.c_int)]
+    _fields_ = [("tile_cap", C.c_int), ("tiles_per_lane", C.c_int), ("l1_lanes", C.c_int), ("l1_prefetch", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -146,9 +146,9 @@ _SIGS = {
 
 # ---- tile policy and autotuner (hpc_tune_* / hpc_autotune) ----------------------
 
-def tune_set(p, level, max_degree, tile_cap=None, tiles_per_lane=4, l1_lanes=32):
+def tune_set(p, level, max_degree, tile_cap=None, tiles_per_lane=4, l1_lanes=32, l1_prefetch=0):
     """Set (tile_cap given) or erase (None) the tile policy of a key's buckets."""
-    prm = None if tile_cap is None else C.byref(TuneParams(tile_cap, tiles_per_lane, l1_lanes))
+    prm = None if tile_cap is None else C.byref(TuneParams(tile_cap, tiles_per_lane, l1_lanes, l1_prefetch))
     _check(lib().hpc_tune_set(int(p), int(level), int(max_degree), prm))
 
 
@@ -171,9 +171,12 @@ def tune_load(path):
     _check(lib().hpc_tune_load(os.fsencode(path)))
 
 
+def _params(c):
+    return TuneParams(c["tile_cap"], c.get("tiles_per_lane", 4), c.get("l1_lanes", 32), c.get("l1_prefetch", 0))
+
+
 def _set_tune(h, policy):
-    prm = None if policy is None else C.byref(TuneParams(policy["tile_cap"], policy.get("tiles_per_lane", 4),
-                                                         policy.get("l1_lanes", 32)))
+    prm = None if policy is None else C.byref(_params(policy))
     _check(lib().hpc_ctx_set_tune(h, prm))
 
 
@@ -185,8 +188,7 @@ def _autotune(h, candidates, reps):
     if candidates is None:
         _check(lib().hpc_autotune(h, None, 0, int(reps), chosen, C.byref(n)))
     else:
-        arr = (TuneParams * len(candidates))(*[TuneParams(c["tile_cap"], c.get("tiles_per_lane", 4),
-                                                          c.get("l1_lanes", 32)) for c in candidates])
+        arr = (TuneParams * len(candidates))(*[_params(c) for c in candidates])
         _check(lib().hpc_autotune(h, arr, len(candidates), int(reps), chosen, C.byref(n)))
     return {l: chosen[l].as_dict() for l in range(cap) if chosen[l].tile_cap > 0}, n.value
 

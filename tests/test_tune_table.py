@@ -15,13 +15,14 @@ def _clean_table():
 
 def test_defaults_without_entries():
     pol, found = hg.tune_lookup(2000, 1, 237)
-    assert not found and pol == {"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32}
+    assert not found and pol == {"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 0}
 
 
 def test_buckets_and_erase():
     hg.tune_set(2000, 2, 100, 256, 8, 1)
     # same buckets: p in [1024, 2047], degree in [64, 127]
-    assert hg.tune_lookup(1024, 2, 64) == ({"tile_cap": 256, "tiles_per_lane": 8, "l1_lanes": 1}, True)
+    assert hg.tune_lookup(1024, 2, 64) == ({"tile_cap": 256, "tiles_per_lane": 8, "l1_lanes": 1, "l1_prefetch": 0},
+                                           True)
     assert hg.tune_lookup(2047, 2, 127)[1]
     # other buckets or levels
     assert not hg.tune_lookup(2048, 2, 100)[1]
@@ -32,29 +33,31 @@ def test_buckets_and_erase():
 
 
 def test_file_round_trip(tmp_path):
-    hg.tune_set(15000, 1, 13000, 1024, 2, 32)
+    hg.tune_set(15000, 1, 13000, 1024, 2, 32, 1)
     hg.tune_set(300, 7, 20, 16, 16, 1)
     path = str(tmp_path / "t.txt")
     hg.tune_save(path)
     hg.tune_clear()
     assert not hg.tune_lookup(300, 7, 20)[1]
     hg.tune_load(path)
-    assert hg.tune_lookup(15000, 1, 13000) == ({"tile_cap": 1024, "tiles_per_lane": 2, "l1_lanes": 32}, True)
-    assert hg.tune_lookup(300, 7, 20) == ({"tile_cap": 16, "tiles_per_lane": 16, "l1_lanes": 1}, True)
+    assert hg.tune_lookup(15000, 1, 13000) == ({"tile_cap": 1024, "tiles_per_lane": 2, "l1_lanes": 32, "l1_prefetch": 1},
+                                               True)
+    assert hg.tune_lookup(300, 7, 20) == ({"tile_cap": 16, "tiles_per_lane": 16, "l1_lanes": 1, "l1_prefetch": 0}, True)
 
 
 @pytest.mark.parametrize("args", [(2000, 1, 10, 0, 4, 32), (2000, 1, 10, 65537, 4, 32), (2000, 1, 10, 64, 0, 32),
                                   (2000, 1, 10, 64, 65, 32), (2000, 1, 10, 64, 4, 8), (1, 1, 10, 64, 4, 32),
-                                  (2000, 0, 10, 64, 4, 32), (2000, hg.HPC_MAX_LEVEL + 1, 10, 64, 4, 32), (2000, 1, -1, 64, 4, 32)])
+                                  (2000, 0, 10, 64, 4, 32), (2000, hg.HPC_MAX_LEVEL + 1, 10, 64, 4, 32),
+                                  (2000, 1, -1, 64, 4, 32), (2000, 1, 10, 64, 4, 32, 2)])
 def test_rejects_bad_policies_and_keys(args):
     with pytest.raises(hg.HpcError) as e:
         hg.tune_set(*args)
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("text", ["not a policy file\n", "heterogpc-tile-policy 1 32 33 18\n1 0 3 64 4 32\n",
-                                  "heterogpc-tile-policy 1 32 33 18\n1 2 3 64 4\n",
-                                  "heterogpc-tile-policy 2 32 33 18\n", "heterogpc-tile-policy 1 32 33 18\n1 2 3 0 4 32\n"])
+@pytest.mark.parametrize("text", ["not a policy file\n", "heterogpc-tile-policy 2 32 33 18\n1 0 3 64 4 32 0\n",
+                                  "heterogpc-tile-policy 2 32 33 18\n1 2 3 64 4 32\n",
+                                  "heterogpc-tile-policy 1 32 33 18\n", "heterogpc-tile-policy 2 32 33 18\n1 2 3 0 4 32 0\n"])
 def test_rejects_bad_files(tmp_path, text):
     path = tmp_path / "bad.txt"
     path.write_text(text)
