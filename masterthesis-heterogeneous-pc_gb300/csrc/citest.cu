@@ -19,14 +19,15 @@ __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count
     unsigned long long end = I.g->rec_count;
     if (end > (unsigned long long)I.rec_cap) end = (unsigned long long)I.rec_cap;
     for (unsigned long long r = tid; r < end; r += nthreads) {
-      hpc_sepset_record *rec = I.recs + r;
-      if (!(rec->pmax < 0.0)) continue;
+      int32_t *rec = I.recs + r * (unsigned long long)I.rec_stride;
+      RecHead *h = reinterpret_cast<RecHead *>(rec);
+      if (!(h->pmax < 0.0)) continue;
       if (!I.cor64) {
-        rec->pmax = calc_pvalue64(-1.0 - rec->pmax, I.n_obs);
+        h->pmax = calc_pvalue64(-1.0 - h->pmax, I.n_obs);
         continue;
       }
-      const double pv = exact_pvalue<HPC_MAX_LEVEL>(I, rec->i, rec->j, rec->ids, rec->level);
-      rec->pmax = pv;
+      const double pv = exact_pvalue<HPC_MAX_LEVEL>(I, h->i, h->j, rec + kRecHeadWords, h->level);
+      h->pmax = pv;
       if (!(pv >= I.alpha)) atomicOr(&I.g->err, kErrBandViolation);
     }
   }
@@ -45,11 +46,18 @@ __device__ __forceinline__ double warp_dot(const double *__restrict__ x, const d
 // one warp per queued test forms the FP64 correlation entries it needs as dot
 // products of the FP64-standardised columns, lane 0 evaluates the reference formula.
 // Level-0 items set the kept bits of both triangles; level >= 1 items remove the edge.
-constexpr int kRetestWarps = 4;  // a (HPC_MAX_LEVEL + 2)^2 FP64 matrix per warp: 37 KB of shared memory
+// The matrices live in dynamic shared memory sized by the launch's level ((l + 2)^2
+// doubles per warp: 2.6 KB at level 16, 9 KB at level 32), so the low levels, where
+// the re-tests are many, keep the SM's warps resident for the dot products.
+// KM: the highest level of the launch's items (16 for levels up to 16, HPC_MAX_LEVEL
+// above), which sizes the FP64 fallback's local arrays.
+constexpr int kRetestWarps = 8;
+template <int KM>
 __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_constant__ Launch L) {
-  __shared__ double Ms[kRetestWarps][(HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2)];
+  extern __shared__ double retest_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double *M = Ms[wib];
+  const int kmax = L.level + 2;
+  double *M = retest_smem + (size_t)wib * kmax * kmax;
   unsigned long long count = L.lc->rq_count;
   if (count > (unsigned long long)L.rq_cap) count = (unsigned long long)L.rq_cap;
   const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
@@ -84,7 +92,7 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_
     __syncwarp();
     if (lane == 0) {
       bool nan_p;
-      const double r = partial_r_of_matrix<HPC_MAX_LEVEL>(M, l, &nan_p);
+      const double r = partial_r_of_matrix<KM>(M, l, &nan_p);
       double pv;
       if (decide_of_r(I, r, nan_p, &pv) && claim_edge(I, i, j)) write_record(I, L.level, i, j, it.ids, l, pv);
     }
@@ -126,8 +134,22 @@ int citest_grid(int precision, int level, int device, int l1_variant) {
   return per_sm * sms;
 }
 
+// The re-test kernel's dynamic shared memory reaches 74 KB at level 32, above the default
+// 48 KB: allowed once per context creation (not at launch, which may be under capture).
+void retest_setup() {
+  const int most = (int)(sizeof(double) * kRetestWarps * (HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2));
+  if (cudaFuncSetAttribute((const void *)retest_kernel<HPC_MAX_LEVEL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           most) != cudaSuccess)
+    cudaGetLastError();
+}
+
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
-  retest_kernel<<<sms * 8, kRetestWarps * 32, 0, s>>>(L);
+  const int kmax = L.level + 2;
+  const size_t smem = sizeof(double) * (size_t)kRetestWarps * kmax * kmax;  // 20.7 KB at level 16
+  if (L.level <= 16)
+    retest_kernel<16><<<sms * 4, kRetestWarps * 32, smem, s>>>(L);
+  else
+    retest_kernel<HPC_MAX_LEVEL><<<sms * 4, kRetestWarps * 32, smem, s>>>(L);
   HPC_LAUNCH_CHECK("retest_kernel");
   return HPC_OK;
 }

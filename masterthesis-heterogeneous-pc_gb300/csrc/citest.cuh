@@ -488,13 +488,14 @@ __device__ __forceinline__ void write_record(const Inst &I, int level, int64_t i
     atomicOr(&I.g->err, kErrRecOverflow);
     return;
   }
-  hpc_sepset_record *rec = I.recs + slot;
-  rec->i = (int32_t)(i < j ? i : j);
-  rec->j = (int32_t)(i < j ? j : i);
-  rec->level = l;
-  rec->pad = 0;
-  rec->pmax = pv;
-  for (int q = 0; q < HPC_MAX_LEVEL; ++q) rec->ids[q] = q < l ? ids[q] : -1;
+  int32_t *rec = I.recs + slot * (unsigned long long)I.rec_stride;
+  RecHead *h = reinterpret_cast<RecHead *>(rec);
+  h->i = (int32_t)(i < j ? i : j);
+  h->j = (int32_t)(i < j ? j : i);
+  h->level = l;
+  h->pad = 0;
+  h->pmax = pv;
+  for (int q = 0; q < I.rec_ids; ++q) rec[kRecHeadWords + q] = q < l ? ids[q] : -1;
 }
 
 template <int LA>
@@ -545,14 +546,18 @@ __device__ __forceinline__ void flush_pending(const Launch &L, int level, PendRe
         atomicOr(&I->g->err, kErrRecOverflow);
       } else {
         const PendRem<LA> &e = list[q];
-        hpc_sepset_record *rec = I->recs + slot;
-        rec->i = e.lo;
-        rec->j = e.hi;
-        rec->level = level;
-        rec->pad = 0;
-        rec->pmax = e.pv;
-#pragma unroll
-        for (int t = 0; t < HPC_MAX_LEVEL; ++t) rec->ids[t] = t < (LA > 0 ? LA : 1) ? e.ids[t < (LA > 0 ? LA : 1) ? t : 0] : -1;
+        int32_t *rec = I->recs + slot * (unsigned long long)I->rec_stride;
+        RecHead *h = reinterpret_cast<RecHead *>(rec);
+        h->i = e.lo;
+        h->j = e.hi;
+        h->level = level;
+        h->pad = 0;
+        h->pmax = e.pv;
+        const int nid = I->rec_ids;
+#pragma unroll (kUnr<LA>)
+        for (int t = 0; t < (LA > 0 ? LA : 1); ++t)
+          if (t < nid) rec[kRecHeadWords + t] = e.ids[t];
+        for (int t = (LA > 0 ? LA : 1); t < nid; ++t) rec[kRecHeadWords + t] = -1;
       }
     }
   }

@@ -169,6 +169,8 @@ hpc_status write_inst_table(hpc_ctx *c) {
     I.colidx_cap = c->colidx ? h.colidx_cap : 0;
     I.recs = c->recs ? c->recs + h.rec_off : nullptr;
     I.rec_cap = c->recs ? h.rec_cap : 0;
+    I.rec_ids = c->rec_ids;
+    I.rec_stride = rec_stride_words(c->rec_ids);
     I.ctr = c->ctr + (size_t)b * kLevels;
     I.g = c->gctr + b;
   }
@@ -258,7 +260,8 @@ hpc_status ensure_capacity(hpc_ctx *c, bool *changed) {
     if (e2 > c->ih[b].colidx_cap || e2 / 2 > c->ih[b].rec_cap) grow = true;
   }
   if (!grow) return HPC_OK;
-  long long ct = 0, rt = 0;
+  long long ct = 0, rt = 0;  // neighbour ids, record words
+  const long long stride = rec_stride_words(c->rec_ids);
   for (int b = 0; b < c->count; ++b) {
     InstHost &h = c->ih[b];
     const long long e2 = (long long)c->ctr_host[(size_t)b * kLevels].edges2;
@@ -267,7 +270,7 @@ hpc_status ensure_capacity(hpc_ctx *c, bool *changed) {
     h.colidx_off = ct;
     h.rec_off = rt;
     ct += h.colidx_cap;
-    rt += h.rec_cap;
+    rt += h.rec_cap * stride;
   }
   hpc_status s;
   if (ct > c->colidx_total || !c->colidx) {
@@ -738,7 +741,8 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   b += (int64_t)(HPC_MAX_LEVEL + 1) * ((p + kSegRows - 1) / kSegRows) * (int64_t)sizeof(SegAgg);  // scan sums
   // neighbour lists and records are sized after level 0; budget an average degree of 64
   const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
-  b += 2 * e * 4 + e * (int64_t)sizeof(hpc_sepset_record);
+  const int rec_ids = o->max_level < 0 ? HPC_MAX_LEVEL : std::min(std::max(o->max_level, 1), HPC_MAX_LEVEL);
+  b += 2 * e * 4 + e * 4 * (int64_t)rec_stride_words(rec_ids);
   if (o->precision == HPC_PREC_MIXED_TC) b += retest_queue_cap(p * p) * (int64_t)sizeof(RetestItem);
   *bytes = b;
   return HPC_OK;
@@ -1032,6 +1036,10 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     set_error("level %d above HPC_MAX_LEVEL", level);
     return HPC_ERR_INVALID_ARG;
   }
+  if (level > c->rec_ids) {  // the records hold ids up to the context's max_level
+    set_error("level %d above the context's max_level %d", level, c->opts.max_level);
+    return HPC_ERR_INVALID_ARG;
+  }
   if (level == 1) {
     bool changed = false;
     if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
@@ -1282,9 +1290,23 @@ hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *
   *count = n;
   if (out && cap > 0 && n > 0) {
     const int64_t k = std::min<int64_t>(cap, n);
-    HPC_CUDA(cudaMemcpyAsync(out, c->recs + h.rec_off, sizeof(hpc_sepset_record) * (size_t)k, cudaMemcpyDeviceToHost,
+    const int stride = rec_stride_words(c->rec_ids);
+    std::vector<int32_t> raw((size_t)k * stride);
+    HPC_CUDA(cudaMemcpyAsync(raw.data(), c->recs + h.rec_off, sizeof(int32_t) * raw.size(), cudaMemcpyDeviceToHost,
                              c->stream));
     HPC_CUDA(cudaStreamSynchronize(c->stream));
+    for (int64_t r = 0; r < k; ++r) {  // packed records -> hpc_sepset_record
+      const int32_t *rec = raw.data() + (size_t)r * stride;
+      RecHead head;
+      std::memcpy(&head, rec, sizeof(head));
+      hpc_sepset_record &o = out[r];
+      o.i = head.i;
+      o.j = head.j;
+      o.level = head.level;
+      o.pad = 0;
+      o.pmax = head.pmax;
+      for (int q = 0; q < HPC_MAX_LEVEL; ++q) o.ids[q] = q < c->rec_ids ? rec[kRecHeadWords + q] : -1;
+    }
   }
   return HPC_OK;
 }
@@ -1386,6 +1408,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   hpc_ctx *c = new hpc_ctx();
   c->count = count;
   c->opts = o;
+  c->rec_ids = o.max_level < 0 ? HPC_MAX_LEVEL : std::min(std::max(o.max_level, 1), HPC_MAX_LEVEL);
   c->device = o.device;
   c->ih.resize((size_t)count);
   long long cor = 0, z = 0, adj = 0, rows = 0, tc = 0, words = 0, tiles = 0, nrows = 0;
@@ -1457,8 +1480,12 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
     return fail(HPC_ERR_CUDA);
   }
   c->stream = c->own_stream;
-  for (int l = 1; l <= HPC_MAX_LEVEL; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
+  // grids of the levels this context can run (up to its max_level): a context that stays
+  // at low levels never loads the level-17..32 kernel, whose local-memory stack frame
+  // (35 KB per thread) would otherwise be reserved for the whole device
+  for (int l = 1; l <= c->rec_ids; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
   for (int v = 0; v < 3; ++v) c->citest_grid_l1[v] = citest_grid(o.precision, 1, c->device, v);
+  retest_setup();
   if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, cor, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, cor, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, adj, "adjacency")) != HPC_OK) return fail(s);

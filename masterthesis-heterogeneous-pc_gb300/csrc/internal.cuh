@@ -106,6 +106,19 @@ constexpr int kErrCsrOverflow = 4;
 constexpr int kErrTimeout = 8;
 constexpr int kErrBandViolation = 16;
 
+// Separation-set records on the device, packed: a head (the removed edge i < j, the
+// level and the p-value) and then the context's `rec_ids` separating-variable slots,
+// at a stride of rec_stride_words(rec_ids) 32-bit words (even, so that every head's
+// double is 8-byte aligned). rec_ids is the highest level the context runs, so a
+// skeleton run to level 4 stores 40-byte records; they are expanded to
+// hpc_sepset_record when read.
+struct RecHead {
+  int32_t i, j, level, pad;
+  double pmax;
+};
+constexpr int kRecHeadWords = 6;
+__host__ __device__ __forceinline__ int rec_stride_words(int rec_ids) { return kRecHeadWords + ((rec_ids + 1) & ~1); }
+
 // One deferred FP64 re-test: edge (i, j) of instance `inst` given ids[0..level),
 // or a level-0 pair (i > j).
 struct RetestItem {
@@ -135,8 +148,9 @@ struct Inst {
   int *colidx;            // snapshot neighbour ids, ascending per row
   long long colidx_cap;
   unsigned long long *row_work;  // exclusive prefix of tests per row (p + 1)
-  hpc_sepset_record *recs;
-  long long rec_cap;
+  int32_t *recs;          // packed records (RecHead + rec_ids slots each)
+  long long rec_cap;      // records
+  int rec_ids, rec_stride;  // id slots per record, words per record
   DevCounters *ctr;       // [HPC_MAX_LEVEL + 1]
   DevGlobal *g;
 };
@@ -247,6 +261,7 @@ hpc_status launch_expand_adjacency(const uint32_t *adj, int64_t p, int W, uint8_
 // l1_variant: level 1's kernel (kL1Interleaved, kL1Prefetch or kL1Chunked, from the tile policy).
 hpc_status launch_level(const Launch &L, int precision, int grid, int l1_variant, cudaStream_t s);
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
+void retest_setup();  // once per context creation, before any launch_retest
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
 int citest_grid(int precision, int level, int device, int l1_variant = kL1Interleaved);
 
@@ -296,8 +311,9 @@ struct hpc_ctx {
   unsigned long long *row_work = nullptr;  // sum (p + 1)
   int *colidx = nullptr;          // sum colidx_cap
   long long colidx_total = 0;
-  hpc_sepset_record *recs = nullptr;  // sum rec_cap
-  long long rec_total = 0;
+  int32_t *recs = nullptr;       // packed records, sum rec_cap x rec_stride words
+  long long rec_total = 0;        // words
+  int rec_ids = HPC_MAX_LEVEL;    // id slots per record: the highest level the context runs
   hpc::RetestItem *rq = nullptr;
   long long rq_cap = 0;
   hpc::DevCounters *ctr = nullptr;       // count x (HPC_MAX_LEVEL + 1)

@@ -133,6 +133,15 @@ def test_call_order_errors():
     assert e.value.status == 6  # levels run in order
     sk.calc_level(0)
     assert sk.edge_count() == 0  # identity: every pair independent
+    # levels above the context's max_level are refused (its records hold that many ids)
+    X = gen(dict(p=30, n=500, graph=hg.GRAPH_ER, degree=3.0, seed=45))
+    sk = hg.SkeletonCalculator(30, 500, alpha=0.05, max_level=1)
+    sk.add_correlation_matrix(orc.correlation(X))
+    sk.calc_level(0)
+    sk.calc_level(1)
+    with pytest.raises(hg.HpcError) as e:
+        sk.calc_level(2)
+    assert e.value.status == 1  # HPC_ERR_INVALID_ARG
 
 
 @pytest.mark.parametrize("alpha,max_level", [(1.0, 3), (0.999, 2), (1e-300, 0), (1e-12, 3)])
