@@ -179,6 +179,23 @@ def run_c3(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over the process group's ranks (x itself without one): every rank
+    times its own replica, and the slowest sets the job's time."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world, steps, seconds):
+    """Whole-job skeletons/s of `world` replicas that each ran `steps` skeletons in at
+    most `seconds` (weak scaling: the work per GPU is fixed)."""
+    return world * steps / seconds
+
+
 def autotune_setup(args, ctx, candidates, reps):
     """hpc_autotune on a warmed-up context (untimed): the fastest candidate tile policy
     of every level goes into the process-wide table that the timed runs read."""
@@ -726,12 +743,8 @@ def main():
     clk = clocks.stop()
     test_ms = kernel_times(sk, args.steps)
     plain_ms, plain_stats, _ = timed_steps(sk_plain, args.steps)
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(step_ms), dist, dev)
+    value = replica_rate(world, args.steps, total_ms / 1e3)
 
     # e2e through the C ABI from pinned host memory
     Ch = torch.empty((p, p), dtype=torch.float64, pin_memory=True)
@@ -751,13 +764,9 @@ def main():
         sk.adjacency_into(adj_h.data_ptr())
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_t)
-    if dist:
-        t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = max_over_ranks(sum(e2e_t), dist, dev)
     W = (p + 31) // 32
-    e2e = {"value": world * args.steps / e2e_total, "unit": "skeletons/s", "h2d_bytes_per_step": p * p * 8,
+    e2e = {"value": replica_rate(world, args.steps, e2e_total), "unit": "skeletons/s", "h2d_bytes_per_step": p * p * 8,
            "d2h_bytes_per_step": p * p}
 
     if rank != 0:
