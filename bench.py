@@ -79,11 +79,12 @@ def correlation_error(hg, c32, p, n, Xd, stream):
 
 # c3's candidates (each run of the wide workload takes seconds): tile caps from the
 # default to long chunks for the hub rows, both level-1 lane mappings
-C3_CANDIDATES = [{"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 0},
-                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 1},
-                 {"tile_cap": 8192, "tiles_per_lane": 8, "l1_lanes": 32, "l1_prefetch": 0},
-                 {"tile_cap": 8192, "tiles_per_lane": 8, "l1_lanes": 32, "l1_prefetch": 1},
-                 {"tile_cap": 1024, "tiles_per_lane": 4, "l1_lanes": 1, "l1_prefetch": 0}]
+C3_CANDIDATES = [{"tile_cap": 64, "tiles_per_lane": 4, "edge_lanes": 32, "l1_prefetch": 0},
+                 {"tile_cap": 1024, "tiles_per_lane": 4, "edge_lanes": 32, "l1_prefetch": 1},
+                 {"tile_cap": 8192, "tiles_per_lane": 8, "edge_lanes": 32, "l1_prefetch": 0},
+                 {"tile_cap": 8192, "tiles_per_lane": 8, "edge_lanes": 32, "l1_prefetch": 1},
+                 {"tile_cap": 1024, "tiles_per_lane": 4, "edge_lanes": 1, "l1_prefetch": 0},
+                 {"tile_cap": 256, "tiles_per_lane": 4, "edge_lanes": 1, "l1_prefetch": 0}]
 
 
 def run_c3(args, wl):

@@ -194,9 +194,10 @@ hpc_status hpc_wait(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_r
  * sets how a launch cuts it:
  *   tile_cap        largest run of consecutive tests (subset chunk) a lane takes per tile
  *   tiles_per_lane  target number of tiles per lane of the grid (balance vs claim cost)
- *   l1_lanes        level 1 only: 32 = a warp's lanes interleaved over one edge's tests,
- *                   1 = each lane a chunk of consecutive tests
- *   l1_prefetch     level 1 with l1_lanes 32 only: 1 = the next step's entries are loaded
+ *   edge_lanes      level 1 only: 32 = a warp's lanes interleaved over one edge's tests
+ *                   (coalesced gathers), 1 = each lane a chunk of consecutive tests (the
+ *                   mapping of the higher levels)
+ *   l1_prefetch     level 1 with edge_lanes 32 only: 1 = the next step's entries are loaded
  *                   one step ahead (pays off on long neighbour lists)
  * Defaults: 64, 4, 32, 0. A process-wide table holds policies keyed by buckets of
  * (largest p of the launch, level, largest degree at the level start), buckets being
@@ -205,7 +206,7 @@ hpc_status hpc_wait(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_r
 typedef struct hpc_tune_params {
   int tile_cap;        /* 1..65536 */
   int tiles_per_lane;  /* 1..64 */
-  int l1_lanes;        /* 1 or 32 */
+  int edge_lanes;      /* 1 or 32 */
   int l1_prefetch;     /* 0 or 1 */
 } hpc_tune_params;
 /* Sets (prm != NULL) or erases (NULL) the table entry of the key's buckets. */

@@ -134,8 +134,9 @@ int citest_grid(int precision, int level, int device, int l1_variant) {
   return per_sm * sms;
 }
 
-// The re-test kernel's dynamic shared memory reaches 74 KB at level 32, above the default
-// 48 KB: allowed once per context creation (not at launch, which may be under capture).
+// The re-test kernel of levels 17-32 needs up to 74 KB of dynamic shared memory, above
+// the default 48 KB: allowed once per creation of a context that can reach those levels
+// (not at launch, which may be under capture; levels up to 16 stay below 48 KB).
 void retest_setup() {
   const int most = (int)(sizeof(double) * kRetestWarps * (HPC_MAX_LEVEL + 2) * (HPC_MAX_LEVEL + 2));
   if (cudaFuncSetAttribute((const void *)retest_kernel<HPC_MAX_LEVEL>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -588,7 +588,7 @@ __device__ __forceinline__ TuneEntry tile_policy(const Launch &L) {
     const int md = *(volatile const int *)&L.lc->max_deg;
     te = L.tune[((size_t)L.p_bucket * (HPC_MAX_LEVEL + 1) + L.level) * kTuneDB + tune_bucket(md, kTuneDB)];
   }
-  if (te.tile_cap <= 0) te = TuneEntry{kTuneDefaultCap, kTuneDefaultTpl, kTuneDefaultL1Lanes, 0};
+  if (te.tile_cap <= 0) te = TuneEntry{kTuneDefaultCap, kTuneDefaultTpl, kTuneDefaultEdgeLanes, 0};
   te.tiles_per_lane = max(1, te.tiles_per_lane);
   return te;
 }
@@ -968,11 +968,11 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 }
 
 // One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
-// is the lane-interleaved level-1 body (L1V: kL1Prefetch loads one step ahead,
+// is the lane-interleaved level-1 body (V: kL1Prefetch loads one step ahead,
 // kL1Chunked runs the chunked body of the higher levels; picked by the tile policy),
 // LT = 2..16 the bodies unrolled for l = LT, LT = 0 the runtime-level body.
-template <int LT, bool MIXED, int L1V = kL1Interleaved>
-__global__ void __launch_bounds__(kThreads, LT == 1 && L1V != kL1Chunked ? 4 : 2)
+template <int LT, bool MIXED, int V = kL1Interleaved>
+__global__ void __launch_bounds__(kThreads, LT == 1 && V != kL1Chunked ? 4 : 2)
     level_kernel(const __grid_constant__ Launch L) {
   extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
@@ -981,8 +981,8 @@ __global__ void __launch_bounds__(kThreads, LT == 1 && L1V != kL1Chunked ? 4 : 2
   scan_phase(L);
   if (!grid_barrier(L, epoch)) return;
   const TuneEntry te = tile_policy(L);
-  if (LT == 1 && L1V != kL1Chunked)  // level 1 keeps the SM's on-chip memory for L1 cache
-    tests_l1<MIXED, L1V == kL1Prefetch>(L, nullptr, te);
+  if (LT == 1 && V != kL1Chunked)  // level 1 keeps the SM's on-chip memory for L1 cache
+    tests_l1<MIXED, V == kL1Prefetch>(L, nullptr, te);
   else
     tests_generic<LT, MIXED>(L, LT == 1 ? nullptr : rw_smem, te);
 }

@@ -239,7 +239,7 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   }
   // snapshot rebuild, test-count scan and CI tests in one launch
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  const int l1v = level == 1 ? c->l1v_now : kL1Interleaved;
+  const int l1v = level == 1 ? c->l1v_now : kL1Chunked;
   if ((s = launch_level(L, c->opts.precision, level == 1 ? c->citest_grid_l1[l1v] : c->citest_grid[level], l1v,
                         c->stream)) != HPC_OK)
     return s;
@@ -388,7 +388,7 @@ bool capturable(cudaStream_t s) { return s != nullptr && s != cudaStreamLegacy &
 // degree of the context's last run (the default, interleaved, before any run).
 int l1_variant_of(const TuneEntry &e) {
   if (e.tile_cap <= 0) return kL1Interleaved;
-  if (e.l1_lanes == 1) return kL1Chunked;
+  if (e.edge_lanes == 1) return kL1Chunked;
   return e.l1_prefetch ? kL1Prefetch : kL1Interleaved;
 }
 
@@ -850,7 +850,7 @@ hpc_status hpc_ctx_set_tune(hpc_ctx *c, const hpc_tune_params *force) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
   if (force && !tune_params_valid(force)) {
-    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32, l1_prefetch 0 or 1",
+    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, edge_lanes 1 or 32, l1_prefetch 0 or 1",
               kTuneMaxCap);
     return HPC_ERR_INVALID_ARG;
   }
@@ -1485,7 +1485,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   // (35 KB per thread) would otherwise be reserved for the whole device
   for (int l = 1; l <= c->rec_ids; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
   for (int v = 0; v < 3; ++v) c->citest_grid_l1[v] = citest_grid(o.precision, 1, c->device, v);
-  retest_setup();
+  if (c->rec_ids > 16) retest_setup();  // the re-test kernel of levels 17-32
   if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, cor, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, cor, "cor32")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->adj, adj, "adjacency")) != HPC_OK) return fail(s);

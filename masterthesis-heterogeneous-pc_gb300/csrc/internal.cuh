@@ -70,15 +70,16 @@ struct LaunchCounters {
 // Tile policy of a level's CI tests (set by the autotuner, else the defaults):
 // tile_cap bounds the consecutive tests a lane takes per tile (the subset chunk),
 // tiles_per_lane is the target number of tiles per lane of the grid (balance), and
-// l1_lanes picks level 1's mapping: 32 = the warp's lanes interleaved over one edge's
-// tests, 1 = each lane a chunk of consecutive tests (the levels >= 2 mapping).
+// edge_lanes picks level 1's mapping: 32 = the warp's lanes interleaved over one
+// edge's tests, 1 = each lane a chunk of consecutive tests (the mapping of the higher
+// levels).
 struct TuneEntry {
-  int tile_cap, tiles_per_lane, l1_lanes, l1_prefetch;
+  int tile_cap, tiles_per_lane, edge_lanes, l1_prefetch;
 };
 // level-1 kernel variants: lanes interleaved over an edge, the same with the next
 // position's entries loaded a step ahead, each lane a chunk of consecutive tests
 constexpr int kL1Interleaved = 0, kL1Prefetch = 1, kL1Chunked = 2;
-constexpr int kTuneDefaultCap = 64, kTuneDefaultTpl = 4, kTuneDefaultL1Lanes = 32, kTuneMaxCap = 65536;
+constexpr int kTuneDefaultCap = 64, kTuneDefaultTpl = 4, kTuneDefaultEdgeLanes = 32, kTuneMaxCap = 65536;
 // table of a context: [p bucket][level][degree bucket]; bucket = bit length, capped
 constexpr int kTunePB = 32, kTuneDB = 18;
 __host__ __device__ __forceinline__ int tune_bucket(long long v, int cap) {

@@ -23,7 +23,7 @@ size_t index_of(int pb, int level, int db) { return ((size_t)pb * kLv + level) *
 
 bool valid_params(const hpc_tune_params &p) {
   return p.tile_cap >= 1 && p.tile_cap <= kTuneMaxCap && p.tiles_per_lane >= 1 && p.tiles_per_lane <= 64 &&
-         (p.l1_lanes == 1 || p.l1_lanes == 32) && (p.l1_prefetch == 0 || p.l1_prefetch == 1);
+         (p.edge_lanes == 1 || p.edge_lanes == 32) && (p.l1_prefetch == 0 || p.l1_prefetch == 1);
 }
 
 hpc_status check_key(int64_t p, int level, int max_degree) {
@@ -37,7 +37,7 @@ hpc_status check_key(int64_t p, int level, int max_degree) {
 }  // namespace
 
 TuneEntry tune_entry_of(const hpc_tune_params &p) {
-  return TuneEntry{p.tile_cap, p.tiles_per_lane, p.l1_lanes, p.l1_prefetch};
+  return TuneEntry{p.tile_cap, p.tiles_per_lane, p.edge_lanes, p.l1_prefetch};
 }
 
 bool tune_params_valid(const hpc_tune_params *p) { return p && valid_params(*p); }
@@ -74,7 +74,7 @@ hpc_status hpc_tune_set(int64_t p, int level, int max_degree, const hpc_tune_par
   hpc_status s = check_key(p, level, max_degree);
   if (s != HPC_OK) return s;
   if (prm && !valid_params(*prm)) {
-    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, l1_lanes 1 or 32, l1_prefetch 0 or 1",
+    set_error("tile policy needs 1 <= tile_cap <= %d, 1 <= tiles_per_lane <= 64, edge_lanes 1 or 32, l1_prefetch 0 or 1",
               kTuneMaxCap);
     return HPC_ERR_INVALID_ARG;
   }
@@ -97,7 +97,7 @@ hpc_status hpc_tune_lookup(int64_t p, int level, int max_degree, hpc_tune_params
   const bool have = e.tile_cap > 0;
   out->tile_cap = have ? e.tile_cap : kTuneDefaultCap;
   out->tiles_per_lane = have ? e.tiles_per_lane : kTuneDefaultTpl;
-  out->l1_lanes = have ? e.l1_lanes : kTuneDefaultL1Lanes;
+  out->edge_lanes = have ? e.edge_lanes : kTuneDefaultEdgeLanes;
   out->l1_prefetch = have ? e.l1_prefetch : 0;
   if (found) *found = have ? 1 : 0;
   return HPC_OK;
@@ -111,7 +111,7 @@ hpc_status hpc_tune_clear(void) {
 }
 
 // Text file: a header line, then one line per entry:
-//   p_bucket level degree_bucket tile_cap tiles_per_lane l1_lanes l1_prefetch
+//   p_bucket level degree_bucket tile_cap tiles_per_lane edge_lanes l1_prefetch
 hpc_status hpc_tune_save(const char *path) {
   if (!path) {
     set_error("null path");
@@ -131,7 +131,7 @@ hpc_status hpc_tune_save(const char *path) {
       for (int db = 0; db < kTuneDB; ++db) {
         const TuneEntry &e = t[index_of(pb, l, db)];
         if (e.tile_cap > 0)
-          std::fprintf(f, "%d %d %d %d %d %d %d\n", pb, l, db, e.tile_cap, e.tiles_per_lane, e.l1_lanes, e.l1_prefetch);
+          std::fprintf(f, "%d %d %d %d %d %d %d\n", pb, l, db, e.tile_cap, e.tiles_per_lane, e.edge_lanes, e.l1_prefetch);
       }
   const bool ok = std::fclose(f) == 0;
   if (!ok) {

@@ -71,7 +71,7 @@ class Served(C.Structure):
 
 
 class TuneParams(C.Structure):
-    _fields_ = [("tile_cap", C.c_int), ("tiles_per_lane", C.c_int), ("l1_lanes", C.c_int), ("l1_prefetch", C.c_int)]
+    _fields_ = [("tile_cap", C.c_int), ("tiles_per_lane", C.c_int), ("edge_lanes", C.c_int), ("l1_prefetch", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -146,9 +146,9 @@ _SIGS = {
 
 # ---- tile policy and autotuner (hpc_tune_* / hpc_autotune) ----------------------
 
-def tune_set(p, level, max_degree, tile_cap=None, tiles_per_lane=4, l1_lanes=32, l1_prefetch=0):
+def tune_set(p, level, max_degree, tile_cap=None, tiles_per_lane=4, edge_lanes=32, l1_prefetch=0):
     """Set (tile_cap given) or erase (None) the tile policy of a key's buckets."""
-    prm = None if tile_cap is None else C.byref(TuneParams(tile_cap, tiles_per_lane, l1_lanes, l1_prefetch))
+    prm = None if tile_cap is None else C.byref(TuneParams(tile_cap, tiles_per_lane, edge_lanes, l1_prefetch))
     _check(lib().hpc_tune_set(int(p), int(level), int(max_degree), prm))
 
 
@@ -172,7 +172,7 @@ def tune_load(path):
 
 
 def _params(c):
-    return TuneParams(c["tile_cap"], c.get("tiles_per_lane", 4), c.get("l1_lanes", 32), c.get("l1_prefetch", 0))
+    return TuneParams(c["tile_cap"], c.get("tiles_per_lane", 4), c.get("edge_lanes", 32), c.get("l1_prefetch", 0))
 
 
 def _set_tune(h, policy):
@@ -355,7 +355,7 @@ class SkeletonCalculator:
         _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
 
     def set_tune(self, policy):
-        """Force a tile policy ({"tile_cap", "tiles_per_lane", "l1_lanes"}) on every level; None = the table."""
+        """Force a tile policy ({"tile_cap", "tiles_per_lane", "edge_lanes"}) on every level; None = the table."""
         _set_tune(self._h, policy)
 
     def autotune(self, candidates=None, reps=1):
@@ -482,7 +482,7 @@ class SkeletonBatch:
         _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
 
     def set_tune(self, policy):
-        """Force a tile policy ({"tile_cap", "tiles_per_lane", "l1_lanes"}) on every level; None = the table."""
+        """Force a tile policy ({"tile_cap", "tiles_per_lane", "edge_lanes"}) on every level; None = the table."""
         _set_tune(self._h, policy)
 
     def autotune(self, candidates=None, reps=1):

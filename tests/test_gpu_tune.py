@@ -14,12 +14,12 @@ pytestmark = pytest.mark.gpu
 
 POLICIES = [
     None,                                                                        # table / defaults
-    {"tile_cap": 1, "tiles_per_lane": 1, "l1_lanes": 32, "l1_prefetch": 0},      # one test per lane per tile
-    {"tile_cap": 1024, "tiles_per_lane": 8, "l1_lanes": 1, "l1_prefetch": 0},    # long chunks, chunked level 1
-    {"tile_cap": 16, "tiles_per_lane": 64, "l1_lanes": 1, "l1_prefetch": 0},
-    {"tile_cap": 65536, "tiles_per_lane": 1, "l1_lanes": 32, "l1_prefetch": 0},  # a few huge tiles
-    {"tile_cap": 256, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 1},    # level 1 loads a step ahead
-    {"tile_cap": 2, "tiles_per_lane": 2, "l1_lanes": 32, "l1_prefetch": 1},
+    {"tile_cap": 1, "tiles_per_lane": 1, "edge_lanes": 32, "l1_prefetch": 0},      # one test per lane per tile
+    {"tile_cap": 1024, "tiles_per_lane": 8, "edge_lanes": 1, "l1_prefetch": 0},    # long chunks, chunked level 1
+    {"tile_cap": 16, "tiles_per_lane": 64, "edge_lanes": 1, "l1_prefetch": 0},
+    {"tile_cap": 65536, "tiles_per_lane": 1, "edge_lanes": 32, "l1_prefetch": 0},  # a few huge tiles
+    {"tile_cap": 256, "tiles_per_lane": 4, "edge_lanes": 32, "l1_prefetch": 1},    # level 1 loads a step ahead
+    {"tile_cap": 2, "tiles_per_lane": 2, "edge_lanes": 32, "l1_prefetch": 1},
 ]
 
 
@@ -60,9 +60,9 @@ def test_autotune_stores_per_level_choices(hub_case, tmp_path):
     sk = hg.SkeletonCalculator(p, n, alpha=alpha, max_level=ml, precision=hg.PREC_MIXED)
     sk.add_correlation_matrix(Cm)
     st0 = sk.run()
-    cands = [{"tile_cap": 16, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 0},
-             {"tile_cap": 256, "tiles_per_lane": 2, "l1_lanes": 1, "l1_prefetch": 0},
-             {"tile_cap": 64, "tiles_per_lane": 8, "l1_lanes": 32, "l1_prefetch": 1}]
+    cands = [{"tile_cap": 16, "tiles_per_lane": 4, "edge_lanes": 32, "l1_prefetch": 0},
+             {"tile_cap": 256, "tiles_per_lane": 2, "edge_lanes": 1, "l1_prefetch": 0},
+             {"tile_cap": 64, "tiles_per_lane": 8, "edge_lanes": 32, "l1_prefetch": 1}]
     chosen, entries = sk.autotune(cands, reps=2)
     assert entries == len([s for s in st0 if s["level"] >= 1 and s["potential_tests"] > 0]) > 0
     for s in st0:

@@ -15,13 +15,13 @@ def _clean_table():
 
 def test_defaults_without_entries():
     pol, found = hg.tune_lookup(2000, 1, 237)
-    assert not found and pol == {"tile_cap": 64, "tiles_per_lane": 4, "l1_lanes": 32, "l1_prefetch": 0}
+    assert not found and pol == {"tile_cap": 64, "tiles_per_lane": 4, "edge_lanes": 32, "l1_prefetch": 0}
 
 
 def test_buckets_and_erase():
     hg.tune_set(2000, 2, 100, 256, 8, 1)
     # same buckets: p in [1024, 2047], degree in [64, 127]
-    assert hg.tune_lookup(1024, 2, 64) == ({"tile_cap": 256, "tiles_per_lane": 8, "l1_lanes": 1, "l1_prefetch": 0},
+    assert hg.tune_lookup(1024, 2, 64) == ({"tile_cap": 256, "tiles_per_lane": 8, "edge_lanes": 1, "l1_prefetch": 0},
                                            True)
     assert hg.tune_lookup(2047, 2, 127)[1]
     # other buckets or levels
@@ -40,9 +40,9 @@ def test_file_round_trip(tmp_path):
     hg.tune_clear()
     assert not hg.tune_lookup(300, 7, 20)[1]
     hg.tune_load(path)
-    assert hg.tune_lookup(15000, 1, 13000) == ({"tile_cap": 1024, "tiles_per_lane": 2, "l1_lanes": 32, "l1_prefetch": 1},
+    assert hg.tune_lookup(15000, 1, 13000) == ({"tile_cap": 1024, "tiles_per_lane": 2, "edge_lanes": 32, "l1_prefetch": 1},
                                                True)
-    assert hg.tune_lookup(300, 7, 20) == ({"tile_cap": 16, "tiles_per_lane": 16, "l1_lanes": 1, "l1_prefetch": 0}, True)
+    assert hg.tune_lookup(300, 7, 20) == ({"tile_cap": 16, "tiles_per_lane": 16, "edge_lanes": 1, "l1_prefetch": 0}, True)
 
 
 @pytest.mark.parametrize("args", [(2000, 1, 10, 0, 4, 32), (2000, 1, 10, 65537, 4, 32), (2000, 1, 10, 64, 0, 32),
