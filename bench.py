@@ -100,7 +100,8 @@ def run_c3(args, wl):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
-    p, n = wl["p"], wl["n"]
+    p = wl["p"] if args.p is None else args.p
+    n = wl["n"]
     max_level = wl["max_level"] if args.max_level is None else args.max_level
     X = hg.sem_generate(p, n, wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"], wl["seed"],
                         dtype=np.float32)
@@ -613,6 +614,7 @@ def main():
     ap.add_argument("--count", type=int, default=None, help="c4: number of instances (default 512)")
     ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
     ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3)")
+    ap.add_argument("--p", type=int, default=None, help="c3: variables (default 15000; smaller for profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile policy (no hpc_autotune)")
     ap.add_argument("--tune-file", default=None,
                     help="tile-policy table: loaded instead of autotuning when it exists, else written after it")
