@@ -892,16 +892,20 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
         }
         {
           // lanes on the same edge learn of its removal in this step; one of them
-          // claims the edge and keeps its record for the flush
+          // claims the edge and keeps its record for the flush (the lanes' edges are
+          // grouped only in the steps where some lane removes)
           const unsigned act = __activemask();
-          const unsigned grp = __match_any_sync(act, (unsigned)(t - (unsigned long long)rank));
-          const unsigned rmask = __ballot_sync(act, rm) & grp;
-          if (rmask) {
-            if (lane == __ffs(rmask) - 1 && claim_edge(*I, i, j)) {
-              push_pending<1>(pend, np, *I, b, level, i, j, &k, 1, pv_rm);
-              skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
+          const unsigned rall = __ballot_sync(act, rm);
+          if (rall) {
+            const unsigned grp = __match_any_sync(act, (unsigned)(t - (unsigned long long)rank));
+            const unsigned rmask = rall & grp;
+            if (rmask) {
+              if (lane == __ffs(rmask) - 1 && claim_edge(*I, i, j)) {
+                push_pending<1>(pend, np, *I, b, level, i, j, &k, 1, pv_rm);
+                skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
+              }
+              live = false;
             }
-            live = false;
           }
         }
         // a removed edge is left at once: the lane moves to its first position of
