@@ -89,3 +89,30 @@ def test_invalid_arguments_rejected():
         hg.SkeletonCalculator(10, 100, alpha=0.0)
     with pytest.raises(hg.HpcError):
         hg.SkeletonCalculator(10, 100, max_level=hg.HPC_MAX_LEVEL + 1)
+
+
+def _footprint(p, n, precision=hg.PREC_MIXED, max_level=4):
+    import ctypes as C
+    o = hg.Opts()
+    hg.lib().hpc_opts_default(C.byref(o))
+    o.precision, o.max_level = precision, max_level
+    b = C.c_int64(0)
+    st = hg.lib().hpc_ctx_footprint(p, n, C.byref(o), C.byref(b))
+    return st, b.value
+
+
+def test_footprint_follows_the_layout():
+    """The device bytes the server admits a request by (hpc_ctx_footprint): they grow with
+    p and n, tensor-core mode holds the split operands and the re-test queue instead of
+    the FP64 matrix, and records grow with the max level (one id slot per level)."""
+    st, small = _footprint(100, 1000)
+    assert st == 0 and small > 0
+    assert _footprint(2000, 1000)[1] > small and _footprint(100, 5000)[1] > small
+    p, n = 2000, 5000
+    fp64 = _footprint(p, n, hg.PREC_FP64)[1]
+    mixed = _footprint(p, n, hg.PREC_MIXED)[1]
+    tc = _footprint(p, n, hg.PREC_MIXED_TC)[1]
+    assert mixed - fp64 == p * p * 4                       # the FP32 copy
+    assert tc > mixed - p * p * 8                          # split operands + re-test queue replace cor64
+    assert _footprint(p, n, hg.PREC_MIXED, -1)[1] > _footprint(p, n, hg.PREC_MIXED, 4)[1]
+    assert _footprint(1, n)[0] == 1 and _footprint(p, 3)[0] == 1  # HPC_ERR_INVALID_ARG
