@@ -159,6 +159,21 @@ def run_c3(args, wl):
     step_ms = float(np.median(ms))
     # accuracy of the tensor-core correlation against an FP64 Gram of the same data
     acc = correlation_error(hg, sk.correlation_f32(), p, n, Xd, stream)
+    cross = None
+    if args.cross_check:
+        # the plain path (FP64 Gram, every test in FP64) on the same observations: the
+        # mixed-precision skeleton must be the same edge set, level by level
+        fp = hg.SkeletonCalculator(p, n, alpha=wl["alpha"], max_level=max_level, precision=hg.PREC_FP64)
+        fp.set_stream(stream.cuda_stream)
+        fp.add_observations_device(Xd.data_ptr(), np.float32)
+        t0 = time.perf_counter()
+        st_fp = fp.run()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        cross = {"same_skeleton_as_fp64_path": bool(np.array_equal(fp.adjacency(), adj)),
+                 "same_edges_per_level": [a["edges_after"] for a in st_fp] == [b["edges_after"] for b in st],
+                 "fp64_path_s": dt}
+        fp.close()
     line = {"metric": "skeletons/sec", "value": 1e3 / step_ms, "unit": "skeletons/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16x4/f32/f64",
@@ -177,7 +192,7 @@ def run_c3(args, wl):
                        for q, s_ in enumerate(st)],
             "level_ms_note": "per-level device time from one more skeleton run kernel by kernel (not graph-replayed)",
             "next_level": {"level": next_level, "potential_tests": t_next, "max_degree": int(d.max())},
-            "accuracy": acc, "clocks": clk, "tile_policy": tuned}
+            "accuracy": acc, "clocks": clk, "tile_policy": tuned, "cross_check": cross}
     print(json.dumps(line), flush=True)
 
 
@@ -615,6 +630,8 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
     ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3)")
     ap.add_argument("--p", type=int, default=None, help="c3: variables (default 15000; smaller for profiling)")
+    ap.add_argument("--cross-check", action="store_true",
+                    help="c3: also run the plain FP64 path once and compare the skeletons")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile policy (no hpc_autotune)")
     ap.add_argument("--tune-file", default=None,
                     help="tile-policy table: loaded instead of autotuning when it exists, else written after it")
