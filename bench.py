@@ -555,6 +555,8 @@ def c4_cpu_sample(wl, k):
 
 def run_reference_c4(args, wl):
     k = min(wl["count"], C4_CPU_SAMPLE)
+    for _ in range(args.warmup):
+        c4_cpu_sample(wl, k)
     times, tests = [], 0
     for _ in range(args.steps):
         v, dt, tests, _, cores = c4_cpu_sample(wl, k)
