@@ -148,7 +148,7 @@ def run_c3(args, wl):
     nb, nbc = p_pad // 128, p_pad // 256
     tiles = sum(nbc - bi // 2 for bi in range(nb))  # 128 x 256 tiles reaching the upper triangle
     gram_issued = tiles * 2.0 * 128 * 256 * 4 * n_pad  # four BF16 products
-    gram_alg = 3.0 * n * p * (p + 1)                  # three products, the survey's count
+    gram_alg = 3.0 * n * p * (p + 1)                  # algorithmic count: hi.hi + hi.lo + lo.hi, upper triangle
     g_ms = float(np.median(gram_ms))
     adj = sk.adjacency()
     d = adj.sum(1).astype(np.int64)
@@ -315,7 +315,7 @@ def run_c5(args, wl):
 
 
 def c4_roofline(levels, timings):
-    """The survey's byte model for the CI tests (4 l(l+3)/2 bytes of FP32 gathers per
+    """The algorithmic byte model of the CI tests (4 l(l+3)/2 bytes of FP32 gathers per
     executed test; the per-edge bytes are left out) over the level kernels' CUDA-event
     times: per level and for levels >= 1 together."""
     peaks = load_peaks()
