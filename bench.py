@@ -259,6 +259,14 @@ def c4_instances(wl, count=None):
     return ps, ns, degs, alphas
 
 
+def c4_instance_data(wl, b):
+    """FP32 observations (p_b, n_b) of instance b of the batched workload."""
+    import heterogpc as hg
+    ps, ns, degs, _ = c4_instances(wl)
+    return hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, float(degs[b]), 2, wl["w_lo"], wl["w_hi"],
+                           wl["seed"] * 100000 + b, dtype=np.float32)
+
+
 def run_c5(args, wl):
     """Served skeletons: requests are submitted at their Poisson arrival times to the
     continuous-batching server; value = requests / (last completion - first arrival)."""
@@ -314,47 +322,81 @@ def run_c5(args, wl):
     print(json.dumps(line), flush=True)
 
 
-def c4_roofline(levels, timings):
-    """The algorithmic byte model of the CI tests (4 l(l+3)/2 bytes of FP32 gathers per
-    executed test; the per-edge bytes are left out) over the level kernels' CUDA-event
-    times: per level and for levels >= 1 together."""
-    peaks = load_peaks()
-    per, tot_b, tot_ms = [], 0, 0.0
-    for s_ in levels:
-        l = s_["level"]
-        ms = timings["test_ms"][l] if l < len(timings["test_ms"]) else 0.0
-        if l == 0 or ms <= 0:
-            continue
-        b = s_["executed_tests"] * 4 * l * (l + 3) // 2
-        per.append({"level": l, "achieved_gbs": b / 1e9 / (ms / 1e3), "ms": ms})
-        tot_b += b
-        tot_ms += ms
-    ach = tot_b / 1e9 / (tot_ms / 1e3) if tot_ms > 0 else 0.0
-    return {"kernel": "level kernels, levels >= 1, all 512 instances per launch", "bound": "hbm",
-            "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-            "peak_source": peaks["source"] + " (hbm_gbs)", "model": "4 l(l+3)/2 bytes per executed test",
-            "per_level": per}
-
-
-def c4_cpu_baseline(args, wl, bt):
-    if args.no_cpu_baseline:
+def c4_golden():
+    """The committed oracle results of the batched workload (tests/golden/c4_golden.json),
+    or None when absent; its per-instance oracle seconds order the CPU samples."""
+    path = os.path.join(ROOT, "tests", "golden", "c4_golden.json")
+    if not os.path.exists(path):
         return None
-    import hpc_build
-    hpc_build.build_oracle()
-    k = min(bt.count, C4_CPU_SAMPLE)
-    value, dt, tests, edges, cores = c4_cpu_sample(wl, k)
-    same = all(np.array_equal(edges[b], bt.adjacency(b)) for b in range(k))
-    return {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
-            "sample": "the first %d of the 512 instances, one after another (%.1f s); later instances cost far "
-                      "more on the CPU (instance 5, p=782, runs for minutes), so this rate flatters the CPU" % (k, dt),
-            "ci_tests_per_sec": tests / dt, "same_skeletons_as_gpu": bool(same)}
+    with open(path) as f:
+        return json.load(f)
+
+
+def c4_slices(count, costs, k):
+    """Instances in k slices of equal share of the cost: instance ranks in decreasing cost
+    order taken round robin (rank r goes to slice r mod k), so every slice is a systematic
+    sample of the whole batch's cost distribution."""
+    order = sorted(range(count), key=lambda b: -costs[b]) if costs else list(range(count))
+    return [order[q::k] for q in range(k)]
+
+
+def level_model_bytes(degs, level, executed, p, lane_bytes=4):
+    """Algorithmic bytes of one level kernel (l >= 1) of one instance: the snapshot rebuild
+    (the p x W adjacency words read, neighbour ids written, degrees and offsets) plus
+    l(l+3)/2 correlation entries per executed test and (2 + d_i) words per row that has
+    tests (r_ij, degree, neighbour list)."""
+    W = (p + 31) // 32
+    has = degs - 1 >= level
+    edge_bytes = int((degs[has] * (2 + degs[has])).sum()) * 4
+    rebuild = (p * W + int(degs.sum()) + 2 * p) * 4 + (p + 1) * 8
+    return executed * lane_bytes * level * (level + 3) // 2 + edge_bytes + rebuild
+
+
+def popcount_rows(words, p, W):
+    """Per-row popcounts of a p x W uint32 bitmask."""
+    b = np.unpackbits(np.ascontiguousarray(words).view(np.uint8)).reshape(p, W * 32)
+    return b.sum(1).astype(np.int64)
+
+
+def bits_to_matrix(words, p):
+    """p x p 0/1 matrix of a p x ceil(p/32) uint32 bitmask (bit j % 32 of word j / 32)."""
+    W = (p + 31) // 32
+    m = np.unpackbits(np.ascontiguousarray(words).view(np.uint8), bitorder="little").reshape(p, W * 32)
+    return m[:, :p]
+
+
+def c4_level_bytes(bt):
+    """Per-level algorithmic bytes of the batch's level kernels, from one instrumented run
+    level by level (each level's degrees read from the adjacency bitmask before it)."""
+    off = bt.adjacency_words()
+    bt.reset()
+    out = {}
+    bt.calc_level(0)
+    for lv in range(1, 33):
+        bits, _ = bt.adjacency_bits()
+        st = bt.calc_level(lv)
+        if st["potential_tests"] == 0:
+            break
+        tot = 0
+        for b in range(bt.count):
+            p = int(bt.ps[b])
+            W = (p + 31) // 32
+            degs = popcount_rows(bits[off[b]:off[b + 1]], p, W)
+            ex = bt.instance_levels(b)
+            executed = ex[lv]["executed_tests"] if lv < len(ex) else 0
+            tot += level_model_bytes(degs, lv, executed, p)
+        out[lv] = tot
+    return out
 
 
 def run_c4(args, wl):
-    """Batched skeletons: one context, every level kernel launched once for all 512
-    instances; a step is correlation (split-BF16 tensor-core Gram) + all levels of
-    every instance from observations resident in HBM. Compared with the plain
-    single-instance FP64 path (FP64 Gram, FP64 tests) run instance by instance."""
+    """Batched skeletons (the configuration the metric is quoted on): 512 instances in one
+    context, every level kernel launched once for all of them. A step is the tensor-core
+    correlation of every instance's observations (resident in HBM) plus every level of
+    every instance and the FP64 p-values of the removals, queued on one stream; CUDA events
+    time each step. Compared with the plain single-instance FP64 path on the same
+    instances, timed the same way (contexts created and sized before timing, CUDA events
+    around each instance's correlation and skeleton)."""
     import torch
 
     import heterogpc as hg
@@ -367,71 +409,287 @@ def run_c4(args, wl):
     ps, ns, degs, alphas = c4_instances(wl, args.count)
     bt = hg.SkeletonBatch(ps, ns, alphas, max_level=wl["max_level"], precision=hg.PREC_MIXED_TC)
     bt.set_stream(stream.cuda_stream)
-    packed = np.empty(int(bt.obs_off[-1]), np.float32)
+    total_obs = int(bt.obs_off[-1])
+    host = torch.empty(total_obs, dtype=torch.float32, pin_memory=True)
+    hv = host.numpy()
     for b in range(bt.count):
-        X = hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, float(degs[b]), 2, wl["w_lo"], wl["w_hi"],
-                            wl["seed"] * 100000 + b, dtype=np.float32)
-        packed[bt.obs_off[b]:bt.obs_off[b + 1]] = X.reshape(-1)
-    Xd = torch.from_numpy(packed).to(dev)
+        hv[bt.obs_off[b]:bt.obs_off[b + 1]] = c4_instance_data(wl, b).reshape(-1)
+    Xd = host.to(dev)
     flush = L2Flush(torch, dev)
 
-    def step():
+    def queue_step():
         bt.add_observations_device(Xd.data_ptr(), np.float32)
-        return bt.run()
+        bt.run_async()
 
     for _ in range(args.warmup):
-        step()
+        queue_step()
+        bt.wait()
     tuned = autotune_setup(args, bt, None, 2)
-    step()
+    queue_step()
+    bt.wait()
     torch.cuda.synchronize()
-    ms, tests = [], 0
+    launches0 = bt.timings()["launches"]
     clocks = ClockSampler(0)
     clocks.start()
+    torch.cuda.synchronize()
+    evs = []
     for _ in range(args.steps):
         flush()
         a, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        st = step()
+        queue_step()
         b_.record(stream)
-        b_.synchronize()
-        ms.append(a.elapsed_time(b_))
-        tests = sum(s_["executed_tests"] for s_ in st)
-    clk = clocks.stop()
-    t_cor = bt.timings()
-    value = bt.count * args.steps / (sum(ms) / 1e3)
-    # plain single-instance FP64 path, instance by instance (a bounded sample)
-    k_plain = min(bt.count, args.plain_sample)
-    t0 = time.perf_counter()
-    for b in range(k_plain):
-        sk = hg.SkeletonCalculator(int(ps[b]), int(ns[b]), alpha=float(alphas[b]), max_level=wl["max_level"],
-                                   precision=hg.PREC_FP64)
-        sk.add_observations_device(Xd.data_ptr() + int(bt.obs_off[b]) * 4, np.float32)
-        sk.run()
-        sk.close()
+        evs.append((a, b_))
+    st = bt.wait()
     torch.cuda.synchronize()
-    plain = k_plain / (time.perf_counter() - t0)
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b_) for a, b_ in evs]
+    launches = bt.timings()["launches"] - launches0
+    value = bt.count * args.steps / (sum(ms) / 1e3)
+    tests = sum(s_["executed_tests"] for s_ in st)
+    # the timed result against the committed oracle results (every instance)
+    gold = c4_golden()
+    parity = None
+    if gold and bt.count == len(gold["instances"]):
+        bits, off = bt.adjacency_bits()
+        same = sum(int(c4_adj_sha(bits_to_matrix(bits[off[b]:off[b + 1]], int(ps[b]))) == g["adj_sha256"])
+                   for b, g in enumerate(gold["instances"]))
+        parity = {"instances_equal_to_oracle": same, "instances": bt.count}
+
+    # per-kernel device times: one more step kernel by kernel (graph replays are timed whole)
+    bt.set_graphs(False)
+    flush()
+    queue_step()
+    bt.wait()
+    torch.cuda.synchronize()
+    t_k = bt.timings()
+    bt.set_graphs(True)
+
+    # e2e through the C ABI from pinned host memory: H2D of every instance's observations,
+    # correlation, all levels, record p-values, D2H of every adjacency bitmask and all
+    # separation-set records
+    words = int(bt.adjacency_words()[-1])
+    bits_h = torch.empty(words, dtype=torch.int32, pin_memory=True)
+    nrec = int(bt.record_prefix()[-1])
+    rec_cap = nrec + 4096
+    recs = hg.record_buffer(rec_cap)
+    e2e_t = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        bt.add_observations_ptr(host.data_ptr(), np.float32)
+        bt.run()
+        bt.adjacency_bits_into(bits_h.data_ptr(), words)
+        pre = bt.all_sepset_records_into(recs, rec_cap)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            e2e_t.append(time.perf_counter() - t0)
+        nrec = int(pre[-1])
+    e2e = {"value": bt.count * len(e2e_t) / sum(e2e_t), "unit": "skeletons/s", "h2d_bytes_per_step": total_obs * 4,
+           "d2h_bytes_per_step": words * 4 + nrec * bt.record_stride_bytes() + 16 * bt.count,
+           "path": "hpc_correlation_f32 (host observations) + hpc_run_skeleton + hpc_batch_get_adjacency_bits + "
+                   "hpc_batch_get_all_sepset_records, host wall clock per step"}
+
+    # the plain single-instance FP64 path on the same instances, like for like
+    plain = c4_plain_path(wl, hg, torch, stream, ps, ns, alphas, Xd, bt.obs_off, flush)
+
+    # roofline of the dominant kernel: the level kernel with the longest device time
+    peaks = load_peaks()
+    lb = c4_level_bytes(bt)
+    test_ms = t_k["test_ms"]
+    lv_dom = max(lb, key=lambda l: test_ms[l]) if lb else 1
+    ach = lb.get(lv_dom, 0) / 1e9 / (test_ms[lv_dom] / 1e3) if test_ms[lv_dom] > 0 else 0.0
+    all_b = sum(lb.values())
+    all_ms = sum(test_ms[l] for l in lb)
+    gram_alg = sum(3.0 * int(n) * int(p) * (int(p) + 1) for p, n in zip(ps, ns))
+    roofline = {"kernel": "level_kernel<%d> (level %d of all %d instances: rebuild, scan, CI tests)"
+                          % (lv_dom, lv_dom, bt.count),
+                "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (hbm_gbs, burst)",
+                "traffic": traffic_from_profile("c4_level_kernel_l%d" % lv_dom),
+                "algorithmic_bytes_per_launch": int(lb.get(lv_dom, 0)), "launch_ms": test_ms[lv_dom],
+                "all_levels": {"algorithmic_bytes": int(all_b), "kernel_ms": all_ms,
+                               "frac": all_b / 1e9 / (all_ms / 1e3) / peaks["hbm_gbs"] if all_ms > 0 else None},
+                "per_level": [{"level": l, "bytes": int(lb[l]), "ms": test_ms[l],
+                               "achieved_gbs": lb[l] / 1e9 / (test_ms[l] / 1e3) if test_ms[l] > 0 else None}
+                              for l in sorted(lb)]}
+    gram = {"ms": t_k["gram_ms"], "algorithmic_tflops": gram_alg / (t_k["gram_ms"] / 1e3) / 1e12,
+            "frac_of_bf16_peak": gram_alg / (t_k["gram_ms"] / 1e3) / 1e12 / peaks["bf16_tflops"],
+            "count": "3 n p (p + 1) BF16 flops per instance (hi.hi + hi.lo + lo.hi, upper triangle)",
+            "standardise_ms": t_k["standardise_ms"]}
     line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sum(ms) / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x4/f32/f64",
-            "data": "synthetic (seeded linear-Gaussian SEM)",
-            "config": {"workload": "c4", "instances": bt.count, "p": list(wl["p"]), "n": list(wl["n"]),
-                       "degree": list(wl["degree"]), "alphas": list(wl["alphas"]), "max_level": wl["max_level"],
-                       "precision": "tensor-core split-BF16 Gram, FP32 tests, FP64 re-tests",
-                       "l2": L2Flush.desc},
-            "ci_tests_per_step": tests, "correlation_ms": t_cor["standardise_ms"] + t_cor["gram_ms"],
-            "skeleton_ms": t_cor["skeleton_ms"],
-            "plain_gpu_path": {"skeletons_per_sec": plain, "sample": "%d instances, one context each" % k_plain,
-                               "precision": "fp64"},
-            "speedup_vs_plain": value / plain, "clocks": clk, "tile_policy": tuned,
-            "cpu_baseline": c4_cpu_baseline(args, wl, bt),
-            "roofline": c4_roofline(st, t_cor),
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3+f32+f64",
+            "data": "synthetic (seeded linear-Gaussian SEM, FP32 samples)",
+            "config": c4_config(wl, bt.count),
+            "precision": "tensor-core split-BF16 Gram, FP32 tests, FP64 re-tests within 1e-3 relative |z| of the "
+                         "threshold (decisions exact)",
+            "l2": L2Flush.desc,
+            "step": "correlation (standardise + tensor-core Gram) + every level of every instance + FP64 p-values "
+                    "of the removals, observations resident in HBM",
+            "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+            "ci_tests_per_step": tests, "ci_tests_per_sec": tests * args.steps / (sum(ms) / 1e3),
+            "gpu_launches": int(launches), "e2e": e2e, "roofline": roofline, "gram": gram,
+            "plain_gpu_path": plain, "speedup_vs_plain": value / plain["skeletons_per_sec"],
+            "e2e_speedup_vs_plain": e2e["value"] / plain["skeletons_per_sec"],
+            "parity": parity, "clocks": clk, "tile_policy": tuned,
+            "kernel_ms": {"standardise": t_k["standardise_ms"], "gram": t_k["gram_ms"],
+                          "levels": {str(l): test_ms[l] for l in range(len(test_ms)) if test_ms[l] > 0}},
             "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
                         "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
-                        "retests": s_["retests"], "edges_after": s_["edges_after"],
-                        "test_ms": t_cor["test_ms"][s_["level"]] if s_["level"] < len(t_cor["test_ms"]) else None}
-                       for s_ in st]}
+                        "retests": s_["retests"], "edges_after": s_["edges_after"]} for s_ in st]}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = c4_cpu_baseline(wl, bt.count)
     print(json.dumps(line), flush=True)
 
+
+def c4_adj_sha(adj):
+    """SHA-256 of the upper triangle (i < j, row by row) of a 0/1 matrix, bit-packed (the
+    hash the committed oracle results hold)."""
+    import hashlib
+    p = adj.shape[0]
+    iu = np.triu_indices(p, 1)
+    return hashlib.sha256(np.packbits(np.asarray(adj)[iu] != 0).tobytes()).hexdigest()
+
+
+def c4_config(wl, count):
+    return {"workload": "c4", "instances": count, "p": list(wl["p"]), "n": list(wl["n"]),
+            "degree": list(wl["degree"]), "alphas": list(wl["alphas"]), "max_level": wl["max_level"],
+            "graph": "Erdos-Renyi", "weights": [wl["w_lo"], wl["w_hi"]], "seed": wl["seed"]}
+
+
+def c4_plain_path(wl, hg, torch, stream, ps, ns, alphas, Xd, obs_off, flush):
+    """The plain single-instance FP64 path (FP64 Gram, every CI test in FP64), one context
+    per instance, all created and sized (one run each) before timing; then every instance's
+    correlation + skeleton + record p-values queued on the same stream with CUDA events
+    around each. Returns skeletons/s over the GPU time of all instances."""
+    count = len(ps)
+    ctxs = []
+    for b in range(count):
+        sk = hg.SkeletonCalculator(int(ps[b]), int(ns[b]), alpha=float(alphas[b]), max_level=wl["max_level"],
+                                   precision=hg.PREC_FP64)
+        sk.set_stream(stream.cuda_stream)
+        sk.add_observations_device(Xd.data_ptr() + int(obs_off[b]) * 4, np.float32)
+        sk.run()
+        ctxs.append(sk)
+    torch.cuda.synchronize()
+    flush()
+    evs = []
+    for b, sk in enumerate(ctxs):
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        sk.add_observations_device(Xd.data_ptr() + int(obs_off[b]) * 4, np.float32)
+        sk.run_async()
+        e.record(stream)
+        evs.append((a, e))
+    for sk in ctxs:
+        sk.wait()
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(e) for a, e in evs]
+    for sk in ctxs:
+        sk.close()
+    return {"skeletons_per_sec": count / (sum(ms) / 1e3), "ms_all_instances": sum(ms),
+            "precision": "fp64 (FP64 Gram, every CI test in FP64)",
+            "timing": "CUDA events around each instance's correlation + skeleton + record p-values, all instances "
+                      "queued back to back on one stream, contexts created and sized before timing"}
+
+
+def c4_cpu_work(b, threads):
+    """The oracle (the reference CPU path restated) on instance b: data made by the oracle
+    library's copy of the generator, FP64 correlation, skeleton. Returns (seconds of the
+    skeleton, executed tests, adjacency hash)."""
+    from oracle import oracle as orc
+    wl = WORKLOADS["c4"]
+    ps, ns, degs, alphas = c4_instances(wl)
+    X = orc.sem_generate(int(ps[b]), int(ns[b]), 0, float(degs[b]), 2, wl["w_lo"], wl["w_hi"],
+                         wl["seed"] * 100000 + b, dtype=np.float32)
+    Cm = orc.correlation(X.astype(np.float64))
+    t0 = time.perf_counter()
+    res = orc.run(Cm, int(ns[b]), float(alphas[b]), wl["max_level"], threads=threads)
+    dt = time.perf_counter() - t0
+    return dt, sum(l["executed_tests"] for l in res.levels), c4_adj_sha(res.adj)
+
+
+def c4_cpu_slice(slice_, cores):
+    """The oracle over a slice of instances one after another, each on all host cores
+    (its OpenMP row loop, as the reference's --cpu-only path runs one problem):
+    (seconds, tests, {instance: adjacency hash})."""
+    tot, tests, hashes = 0.0, 0, {}
+    for b in slice_:
+        dt, t, h = c4_cpu_work(b, cores)
+        tot += dt
+        tests += t
+        hashes[b] = h
+    return tot, tests, hashes
+
+
+# budget of the CPU legs: about 20 s of CPU work for the cpu_baseline sample and per
+# reference step; the slices are systematic samples of the batch's cost distribution
+C4_CPU_SAMPLE_S = 20.0
+
+
+def c4_cpu_plan(count, cores, budget_s):
+    """Slices of the batch for the CPU legs: the committed oracle results give every
+    instance's single-thread cost (measured on the machine that made them); a slice holds
+    about budget_s seconds of work on `cores` cores at a parallel efficiency of the row
+    loop taken as 0.6."""
+    gold = c4_golden()
+    costs = [g["oracle_s"] for g in gold["instances"]] if gold and "oracle_s" in gold["instances"][0] else None
+    total = sum(costs) if costs else None
+    k = max(1, int(np.ceil(total / (budget_s * cores * 0.6)))) if total else 32
+    return c4_slices(count, costs, k), total
+
+
+def c4_cpu_baseline(wl, count):
+    cores = os.cpu_count()
+    slices, _ = c4_cpu_plan(count, cores, C4_CPU_SAMPLE_S)
+    sl = slices[len(slices) // 2]
+    dt, tests, _ = c4_cpu_slice(sl, cores)
+    return {"value": len(sl) / dt, "unit": "skeletons/s", "cores": cores, "kind": "port",
+            "sample": "%d of the %d instances (one of %d slices; a slice takes every %d-th instance in decreasing "
+                      "order of the oracle's cost, a systematic sample of the batch), one after another, each on "
+                      "all %d cores; %.1f s" % (len(sl), count, len(slices), len(slices), cores, dt),
+            "ci_tests_per_sec": tests / dt}
+
+
+def run_reference_c4(args, wl):
+    """The reference CPU path (the oracle port; the reference's own sources cannot be built
+    on the GPU host) on the batched workload: each timed step runs one slice of the batch
+    (a systematic sample of its cost distribution, sized to about 20 s on the host's
+    cores); the K timed steps take K different slices. Warm-up steps run a few of the
+    cheapest instances."""
+    cores = os.cpu_count()
+    count = wl["count"]
+    slices, _ = c4_cpu_plan(count, cores, C4_CPU_SAMPLE_S)
+    gold = c4_golden()
+    cheap = sorted(range(count), key=lambda b: gold["instances"][b].get("oracle_s", 0))[:4] if gold else [0, 1]
+    for _ in range(args.warmup):
+        c4_cpu_slice(cheap, cores)
+    times, tests, done, same = [], 0, 0, 0
+    for k in range(args.steps):
+        sl = slices[(len(slices) // 2 + k) % len(slices)]
+        dt, t, hashes = c4_cpu_slice(sl, cores)
+        times.append(dt)
+        tests += t
+        done += len(sl)
+        if gold:
+            same += sum(1 for b, h in hashes.items() if gold["instances"][b]["adj_sha256"] == h)
+    value = done / sum(times)
+    line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded linear-Gaussian SEM, FP32 samples)", "impl": "reference",
+            "config": c4_config(wl, count),
+            "ci_tests_per_step": tests / args.steps, "ci_tests_per_sec": tests / sum(times),
+            "cpu_baseline": {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
+                             "sample": "each step one slice of about %d of the %d instances (every %d-th instance in "
+                                       "decreasing order of the oracle's cost: a systematic sample of the batch), "
+                                       "%d different slices over the steps (%d instances), each instance on all %d "
+                                       "cores" % (len(slices[0]), count, len(slices), min(args.steps, len(slices)),
+                                                  done, cores),
+                             "projected_full_batch_s": sum(times) / done * count if done else None},
+            "parity": {"instances_equal_to_committed_oracle_results": same, "instances": done} if gold else None,
+            "e2e": {"value": value, "unit": "skeletons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def load_peaks():
@@ -527,58 +785,18 @@ def traffic_from_profile(kernel):
     return ent.get("dram_bytes_per_launch") if ent else None
 
 
-# CPU-baseline sample of c4: the oracle's cost per instance ranges from 0.1 s to minutes
-# (levels up to 16 on some instances); the first five instances take about 2 s
-C4_CPU_SAMPLE = 5
-
-
-def c4_cpu_sample(wl, k):
-    """The oracle (the reference's CPU path restated, all host cores) on the first k
-    instances of the c4 batch, one after another: (skeletons/s, seconds, tests, edges
-    per instance). The bounded sample keeps the run to seconds."""
-    import heterogpc as hg
-    from oracle import oracle as orc
-    ps, ns, degs, alphas = c4_instances(wl)
-    cores = os.cpu_count()
-    tot, tests, edges = 0.0, 0, []
-    for b in range(k):
-        X = hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, float(degs[b]), 2, wl["w_lo"], wl["w_hi"],
-                            wl["seed"] * 100000 + b, dtype=np.float32)
-        Cm = orc.correlation(X.astype(np.float64))
-        t0 = time.perf_counter()
-        res = orc.run(Cm, int(ns[b]), float(alphas[b]), wl["max_level"], threads=cores)
-        tot += time.perf_counter() - t0
-        tests += sum(l["executed_tests"] for l in res.levels)
-        edges.append(res.adj)
-    return k / tot, tot, tests, edges, cores
-
-
-def run_reference_c4(args, wl):
-    k = min(wl["count"], C4_CPU_SAMPLE)
-    for _ in range(args.warmup):
-        c4_cpu_sample(wl, k)
-    times, tests = [], 0
-    for _ in range(args.steps):
-        v, dt, tests, _, cores = c4_cpu_sample(wl, k)
-        times.append(dt)
-    value = k * args.steps / sum(times)
-    line = {"metric": "skeletons/sec", "value": value, "unit": "skeletons/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded linear-Gaussian SEM)", "impl": "reference",
-            "config": {"workload": "c4", "instances": wl["count"], "p": list(wl["p"]), "n": list(wl["n"])},
-            "ci_tests_per_step": tests, "ci_tests_per_sec": tests * args.steps / sum(times),
-            "cpu_baseline": {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
-                             "sample": "the first %d of the 512 instances, one after another, per step (later "
-                                       "instances cost far more on the CPU)" % k},
-            "e2e": {"value": value, "unit": "skeletons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+def single_config(workload, wl):
+    """The config of a single-instance workload (the same keys on both arms)."""
+    return {"workload": workload, "p": wl["p"], "n": wl["n"], "graph": "Erdos-Renyi" if wl["graph"] == 0 else
+            "preferential attachment", "degree": wl["degree"], "alpha": wl["alpha"], "max_level": wl["max_level"],
+            "weights": [wl["w_lo"], wl["w_hi"]], "seed": wl["seed"], "samples": wl.get("dtype", "f32")}
 
 
 def run_reference(args, wl, rank, world):
     if rank != 0:
         return
-    import heterogpc as hg
+    # the product library is not loaded on this arm: the data come from the oracle
+    # library's copy of the generator (the same bytes)
     from oracle import oracle as orc
 
     import hpc_build
@@ -592,8 +810,8 @@ def run_reference(args, wl, rank, world):
                           "about 5e6 tests/s on 16 cores)" % args.workload}), flush=True)
         return
     xdt = np.float64 if wl.get("dtype") == "f64" else np.float32
-    X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
-                        wl["seed"], dtype=xdt)
+    X = orc.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
+                         wl["seed"], dtype=xdt)
     Cm = orc.correlation(X.astype(np.float64))
     cores = os.cpu_count()
     for _ in range(args.warmup):
@@ -610,8 +828,7 @@ def run_reference(args, wl, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded linear-Gaussian SEM)", "impl": "reference",
-            "config": dict(workload=args.workload, **{k: wl[k] for k in ("p", "n", "degree", "alpha", "max_level")},
-                           parallelism="replicas"),
+            "config": single_config(args.workload, wl),
             "ci_tests_per_step": tests, "ci_tests_per_sec": tests * args.steps / total,
             "cpu_baseline": {"value": value, "unit": "skeletons/s", "cores": cores, "kind": "port",
                              "sample": "the full skeleton phase (levels 0-%d) of the workload per step"
@@ -626,10 +843,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=None, help="c4: number of instances (default 512)")
-    ap.add_argument("--plain-sample", type=int, default=64, help="c4: instances timed on the plain path")
     ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3)")
     ap.add_argument("--p", type=int, default=None, help="c3: variables (default 15000; smaller for profiling)")
     ap.add_argument("--cross-check", action="store_true",
@@ -827,9 +1043,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded linear-Gaussian SEM, %s samples)" % ("FP64" if xdt == np.float64 else "FP32"),
-            "config": dict(workload=args.workload, p=p, n=n, degree=wl["degree"], alpha=wl["alpha"],
-                           max_level=wl["max_level"], precision="mixed (FP32 tests, FP64 re-tests)",
-                           l2=L2Flush.desc, parallelism="replicas"),
+            "config": single_config(args.workload, wl),
+            "precision": "mixed (FP32 tests, FP64 re-tests)", "l2": L2Flush.desc, "parallelism": "replicas",
             "ci_tests_per_step": tests_per_step, "ci_tests_per_sec": tests_per_step * args.steps * world / (total_ms / 1e3),
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "levels": [{k: s_[k] for k in ("level", "max_degree", "potential_tests", "executed_tests", "retests",

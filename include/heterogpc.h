@@ -180,10 +180,14 @@ hpc_status hpc_run_skeleton(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *
  * counter reset and the captured level sequence are queued on the context's stream
  * and the call returns; hpc_wait synchronises and returns what hpc_run_skeleton
  * would have. Runs of the same context queue behind each other, so a caller can keep
- * the GPU busy across skeletons. Needs a known opts.max_level; the first run of a
- * context (which sizes the neighbour lists) and runs that cannot be captured (legacy
- * default stream, graphs disabled) are run synchronously inside the call. No
- * counterpart in the reference, which runs one skeleton per process. */
+ * the GPU busy across skeletons. The first run of a context (which sizes the
+ * neighbour lists and, with max_level = -1, finds how many levels the data need) and
+ * runs that cannot be captured (legacy default stream, graphs disabled) are run
+ * synchronously inside the call. With max_level = -1 later runs queue the levels the
+ * previous run needed; hpc_wait continues level by level if the data reach further.
+ * Every skeleton run ends with the FP64 p-values of its removals (pmax), so records
+ * read afterwards need no further device work. No counterpart in the reference,
+ * which runs one skeleton per process. */
 hpc_status hpc_run_skeleton_async(hpc_ctx *ctx);
 hpc_status hpc_wait(hpc_ctx *ctx, hpc_level_stats *stats, int cap, int *levels_run);
 
@@ -265,6 +269,19 @@ hpc_status hpc_batch_get_adjacency(hpc_ctx *ctx, int idx, uint8_t *adj_host);
 hpc_status hpc_batch_edge_count(hpc_ctx *ctx, int idx, int64_t *edges);
 hpc_status hpc_batch_get_sepset_records(hpc_ctx *ctx, int idx, hpc_sepset_record *out, int64_t cap,
                                         int64_t *count);
+/* The same from record `first` on (for reading millions of records in chunks). */
+hpc_status hpc_batch_get_sepset_records_from(hpc_ctx *ctx, int idx, int64_t first, hpc_sepset_record *out,
+                                             int64_t cap, int64_t *count);
+/* Results of every instance in one copy each, for callers that read a whole batch:
+ * the live adjacency as bitmasks (instance b's p_b rows of W_b = ceil(p_b / 32) 32-bit
+ * words start at word_offsets[b]; bit j % 32 of word j / 32 of row i set = edge i-j
+ * kept; count + 1 offsets, the last the total) ... */
+hpc_status hpc_batch_adjacency_words(hpc_ctx *ctx, int64_t *word_offsets);
+hpc_status hpc_batch_get_adjacency_bits(hpc_ctx *ctx, uint32_t *bits_host, int64_t words);
+/* ... and the separation-set records of all instances back to back: instance b's are
+ * out[prefix[b] .. prefix[b + 1]) (prefix: count + 1 entries, always written; at most
+ * cap records copied, none when out is NULL). */
+hpc_status hpc_batch_get_all_sepset_records(hpc_ctx *ctx, hpc_sepset_record *out, int64_t cap, int64_t *prefix);
 
 /* ---- serving ----------------------------------------------------------------
  * Continuous batching of skeleton requests (no reference counterpart). A

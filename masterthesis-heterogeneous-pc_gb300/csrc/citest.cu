@@ -1,6 +1,8 @@
 // Level-l CI tests (l >= 1): the re-test and record kernels, the level-kernel
 // instantiations of levels 1-8 and the launchers (the level kernels' device code is in
 // citest.cuh).
+#include <algorithm>
+
 #include "citest.cuh"
 
 namespace hpc {
@@ -30,6 +32,20 @@ __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count
       h->pmax = pv;
       if (!(pv >= I.alpha)) atomicOr(&I.g->err, kErrBandViolation);
     }
+  }
+}
+
+// Records of all instances compacted into one buffer: one warp per record, its
+// words copied by the lanes (record r of the output belongs to the instance b with
+// prefix[b] <= r < prefix[b + 1]).
+__global__ void gather_records_kernel(const Inst *__restrict__ inst, int count, const long long *__restrict__ prefix,
+                                      long long total, int stride, int32_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < total; r += nw) {
+    const int b = find_inst(prefix, count, r);
+    const int32_t *src = inst[b].recs + (r - prefix[b]) * (long long)stride;
+    for (int w = lane; w < stride; w += 32) out[r * (long long)stride + w] = src[w];
   }
 }
 
@@ -158,6 +174,15 @@ hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s) {
   finalize_records_kernel<<<152 * 2, 128, 0, s>>>(inst, count);
   HPC_LAUNCH_CHECK("finalize_records_kernel");
+  return HPC_OK;
+}
+
+hpc_status launch_gather_records(const Inst *inst, int count, const long long *prefix, long long total, int stride,
+                                 int32_t *out, cudaStream_t s) {
+  if (total <= 0) return HPC_OK;
+  const long long blocks = std::min<long long>((total + 7) / 8, 152 * 8);
+  gather_records_kernel<<<(unsigned)blocks, 256, 0, s>>>(inst, count, prefix, total, stride, out);
+  HPC_LAUNCH_CHECK("gather_records_kernel");
   return HPC_OK;
 }
 

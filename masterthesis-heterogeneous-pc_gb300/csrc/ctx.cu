@@ -246,7 +246,6 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += queue ? 2 : 1;
-  c->records_final = false;
   return HPC_OK;
 }
 
@@ -365,6 +364,10 @@ hpc_status global_errors(hpc_ctx *c) {
       set_error("instance %d: a bounded device wait timed out", b);
       return HPC_ERR_TIMEOUT;
     }
+    if (err & kErrBandViolation) {
+      set_error("instance %d: an FP32 removal was not confirmed in FP64 (error bound violated)", b);
+      return HPC_ERR_NUMERIC;
+    }
   }
   return HPC_OK;
 }
@@ -418,10 +421,15 @@ hpc_status sync_tune(hpc_ctx *c) {
 
 // Run levels first..last with one host sync at the end; the whole sequence 0..last
 // is captured once into a CUDA graph and replayed while the buffers stay in place.
-hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait = true) {
+// `finalize` appends the FP64 p-values of the FP32-decided removals (and their FP64
+// confirmation where the instance has an FP64 matrix) to the sequence, as the
+// reference writes pMax inside its levels (src/executor/testing/cpuUtil.cpp:23-48);
+// the kernel skips records already finalised, so every chunk of a run may end with it.
+hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait = true, bool finalize = false) {
   hpc_status s;
   if ((s = sync_tune(c)) != HPC_OK) return s;
   c->l1v_now = level1_variant(c);
+  finalize = finalize && last >= 1 && c->recs;
   auto enqueue_all = [&](bool timed) -> hpc_status {
     if (first == 0) {  // a skeleton from the start: its counters and records begin at zero
       HPC_CUDA(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters) * (size_t)c->count * kLevels, c->stream));
@@ -432,11 +440,17 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
                              sizeof(SegAgg) * (size_t)c->total_segs * (size_t)(last - first + 1), c->stream));
     for (int l = first; l <= last; ++l)
       if ((s = enqueue_level(c, l, timed)) != HPC_OK) return s;
+    if (finalize) {
+      if ((s = launch_finalize_records(c->inst, c->count, c->stream)) != HPC_OK) return s;
+      c->timings.launches += 1;
+    }
     return HPC_OK;
   };
+  if (last >= 1) c->records_final = finalize;
   if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
-                       c->graph_version == c->inst_version && c->graph_l1v == c->l1v_now;
+                       c->graph_version == c->inst_version && c->graph_l1v == c->l1v_now &&
+                       c->graph_final == finalize;
     if (!valid) {
       if (c->graph) cudaGraphExecDestroy(c->graph);
       c->graph = nullptr;
@@ -461,6 +475,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
       c->graph_stream = c->stream;
       c->graph_version = c->inst_version;
       c->graph_l1v = c->l1v_now;
+      c->graph_final = finalize;
     }
     HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
     c->timings.launches += c->graph_launches;
@@ -803,6 +818,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->meta);
   dev_free(c->meta_denom);
   dev_free(c->tune_dev);
+  dev_free(c->rec_stage);
+  dev_free(c->rec_prefix_dev);
   delete[] c->ctr_host;
   delete[] c->gctr_host;
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -1054,6 +1071,41 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
   return collect_level(c, level, st);
 }
 
+// Levels first..top in chunks with a host check in between, until a level has no
+// tests: a known max level runs as one chunk (one graph replay from level 0); "until
+// exhausted" starts with the previous run's extent (exhaust_top) as one chunk and
+// continues four levels at a time. *last_run: the last level run; *overflow: the
+// neighbour lists were too small (the caller resizes and reruns).
+static hpc_status run_chunks(hpc_ctx *c, int first, int top, int *last_run, bool *overflow) {
+  hpc_status s;
+  const bool known = c->opts.max_level >= 0;
+  *overflow = false;
+  *last_run = first - 1;
+  bool done = false;
+  while (!done && first <= top) {
+    int last = std::min(top, first + 3);
+    if (known) last = top;
+    else if (first == 0 && c->exhaust_top >= 1) last = std::min(top, c->exhaust_top);
+    if ((s = run_levels(c, first, last, known || first == 0, true, true)) != HPC_OK) return s;
+    *last_run = last;
+    if (any_csr_overflow(c)) {
+      *overflow = true;
+      return HPC_OK;
+    }
+    if ((s = global_errors(c)) != HPC_OK) return s;
+    done = last >= 1 && !any_work(c, last);
+    first = last + 1;
+  }
+  return HPC_OK;
+}
+
+// the first level >= 1 without tests (where a run until exhausted stops), else last
+static int exhausted_at(hpc_ctx *c, int last) {
+  for (int l = 1; l <= last; ++l)
+    if (!any_work(c, l)) return l;
+  return last;
+}
+
 hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
@@ -1082,10 +1134,6 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
     if (levels_run) *levels_run = ran;
     return HPC_OK;
   }
-  // A known max level runs as one sequence (one graph replay, one sync); "until
-  // exhausted" runs in chunks of four levels with a check in between.
-  const bool known = c->opts.max_level >= 0;
-  const int chunk = known ? top + 1 : 4;
   HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
   for (int attempt = 0; attempt < 2; ++attempt) {
     ran = 0;
@@ -1099,20 +1147,9 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
       if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
       first = 1;
     }
-    bool overflow = false, done = false;
+    bool overflow = false;
     int last_run = first - 1;
-    while (!done && first <= top) {
-      const int last = std::min(top, first + chunk - 1);
-      if ((s = run_levels(c, first, last, known)) != HPC_OK) return s;
-      last_run = last;
-      if (any_csr_overflow(c)) {
-        overflow = true;
-        break;
-      }
-      if ((s = global_errors(c)) != HPC_OK) return s;
-      done = last >= 1 && !any_work(c, last);
-      first = last + 1;
-    }
+    if ((s = run_chunks(c, first, top, &last_run, &overflow)) != HPC_OK) return s;
     if (overflow) {
       // the data changed since the buffers were sized: resize from level 0 and rerun
       bool changed;
@@ -1121,6 +1158,7 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
       continue;
     }
     c->next_level = last_run + 1;
+    if (c->opts.max_level < 0) c->exhaust_top = exhausted_at(c, last_run);
     HPC_CUDA(cudaEventRecord(c->evr[1], c->stream));
     HPC_CUDA(cudaEventSynchronize(c->evr[1]));
     float tr = 0.f;
@@ -1144,24 +1182,23 @@ hpc_status hpc_run_skeleton_async(hpc_ctx *c) {
     set_error("run before a correlation matrix was computed or loaded");
     return HPC_ERR_STATE;
   }
-  if (c->opts.max_level < 0) {
-    set_error("an asynchronous run needs a known max_level");
-    return HPC_ERR_INVALID_ARG;
-  }
-  const int top = c->opts.max_level;
-  if (!(c->colidx && c->recs) || !c->graphs_enabled || !capturable(c->stream)) {
-    // the first run sizes the neighbour lists; uncapturable streams run eagerly
+  const bool known = c->opts.max_level >= 0;
+  if (!(c->colidx && c->recs) || !c->graphs_enabled || !capturable(c->stream) || (!known && c->exhaust_top < 1)) {
+    // the first run sizes the neighbour lists (and, until exhausted, finds the extent
+    // of the levels); uncapturable streams run eagerly
     c->async_pending = false;
     if ((s = hpc_ctx_reset(c)) != HPC_OK) return s;
     return hpc_run_skeleton(c, nullptr, 0, nullptr);
   }
+  // until exhausted: the previous run's extent, continued by hpc_wait if the data now
+  // reach further
+  const int top = known ? c->opts.max_level : c->exhaust_top;
   for (auto &h : c->ih) h.edges = h.p * (h.p - 1) / 2;
   HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
-  if ((s = run_levels(c, 0, top, true, false)) != HPC_OK) return s;
+  if ((s = run_levels(c, 0, top, true, false, true)) != HPC_OK) return s;
   HPC_CUDA(cudaEventRecord(c->evr[1], c->stream));
   c->async_pending = true;
   c->async_top = top;
-  c->records_final = false;
   c->next_level = 0;
   return HPC_OK;
 }
@@ -1181,7 +1218,24 @@ hpc_status hpc_wait(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run
       return hpc_run_skeleton(c, stats, cap, levels_run);
     }
     if ((s = global_errors(c)) != HPC_OK) return s;
-    c->next_level = c->async_top + 1;
+    int last_run = c->async_top;
+    if (c->opts.max_level < 0) {
+      if (last_run < HPC_MAX_LEVEL && any_work(c, last_run)) {
+        // the data reach beyond the previous run's extent: continue from here
+        bool overflow = false;
+        if ((s = run_chunks(c, c->async_top + 1, HPC_MAX_LEVEL, &last_run, &overflow)) != HPC_OK) return s;
+        if (overflow) {
+          bool changed;
+          if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
+          if ((s = hpc_ctx_reset(c)) != HPC_OK) return s;
+          return hpc_run_skeleton(c, stats, cap, levels_run);
+        }
+        HPC_CUDA(cudaEventRecord(c->evr[1], c->stream));
+        HPC_CUDA(cudaEventSynchronize(c->evr[1]));
+      }
+      c->exhaust_top = exhausted_at(c, last_run);
+    }
+    c->next_level = last_run + 1;
     float tr = 0.f;
     HPC_CUDA(cudaEventElapsedTime(&tr, c->evr[0], c->evr[1]));
     c->timings.skeleton_ms = tr;
@@ -1272,13 +1326,14 @@ static hpc_status finalize_records(hpc_ctx *c) {
   return HPC_OK;
 }
 
-hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *out, int64_t cap, int64_t *count) {
+hpc_status hpc_batch_get_sepset_records_from(hpc_ctx *c, int idx, int64_t first, hpc_sepset_record *out, int64_t cap,
+                                             int64_t *count) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
   if ((s = settle(c)) != HPC_OK) return s;
   if ((s = check_index(c, idx)) != HPC_OK) return s;
-  if (!count) {
-    set_error("null count pointer");
+  if (!count || first < 0) {
+    set_error(!count ? "null count pointer" : "negative first record");
     return HPC_ERR_INVALID_ARG;
   }
   if ((s = finalize_records(c)) != HPC_OK) return s;
@@ -1288,12 +1343,12 @@ hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *
   const InstHost &h = c->ih[idx];
   const long long n = c->recs ? std::min<long long>((long long)g.rec_count, h.rec_cap) : 0;
   *count = n;
-  if (out && cap > 0 && n > 0) {
-    const int64_t k = std::min<int64_t>(cap, n);
+  if (out && cap > 0 && first < n) {
+    const int64_t k = std::min<int64_t>(cap, n - first);
     const int stride = rec_stride_words(c->rec_ids);
     std::vector<int32_t> raw((size_t)k * stride);
-    HPC_CUDA(cudaMemcpyAsync(raw.data(), c->recs + h.rec_off, sizeof(int32_t) * raw.size(), cudaMemcpyDeviceToHost,
-                             c->stream));
+    HPC_CUDA(cudaMemcpyAsync(raw.data(), c->recs + h.rec_off + first * stride, sizeof(int32_t) * raw.size(),
+                             cudaMemcpyDeviceToHost, c->stream));
     HPC_CUDA(cudaStreamSynchronize(c->stream));
     for (int64_t r = 0; r < k; ++r) {  // packed records -> hpc_sepset_record
       const int32_t *rec = raw.data() + (size_t)r * stride;
@@ -1311,8 +1366,104 @@ hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *
   return HPC_OK;
 }
 
+hpc_status hpc_batch_get_sepset_records(hpc_ctx *c, int idx, hpc_sepset_record *out, int64_t cap, int64_t *count) {
+  return hpc_batch_get_sepset_records_from(c, idx, 0, out, cap, count);
+}
+
 hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t cap, int64_t *count) {
   return hpc_batch_get_sepset_records(c, 0, out, cap, count);
+}
+
+hpc_status hpc_batch_adjacency_words(hpc_ctx *c, int64_t *word_offsets) {
+  if (!c || !word_offsets) {
+    set_error("null argument");
+    return HPC_ERR_INVALID_ARG;
+  }
+  for (int b = 0; b < c->count; ++b) word_offsets[b] = c->ih[b].adj_off;
+  word_offsets[c->count] = c->total_words;
+  return HPC_OK;
+}
+
+hpc_status hpc_batch_get_adjacency_bits(hpc_ctx *c, uint32_t *out, int64_t words) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
+  if (!out || words < c->total_words) {
+    set_error(!out ? "null output pointer" : "output holds %lld words, the adjacency needs %lld", (long long)words,
+              (long long)c->total_words);
+    return HPC_ERR_INVALID_ARG;
+  }
+  if (c->next_level == 0) {  // nothing run yet: the complete graph
+    for (int b = 0; b < c->count; ++b) {
+      const InstHost &h = c->ih[b];
+      for (int64_t i = 0; i < h.p; ++i)
+        for (int w = 0; w < h.W; ++w) {
+          uint32_t v = 0;
+          for (int q = 0; q < 32; ++q) {
+            const int64_t j = (int64_t)w * 32 + q;
+            if (j < h.p && j != i) v |= 1u << q;
+          }
+          out[h.adj_off + i * h.W + w] = v;
+        }
+    }
+    return HPC_OK;
+  }
+  HPC_CUDA(cudaMemcpyAsync(out, c->adj, sizeof(uint32_t) * (size_t)c->total_words, cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
+hpc_status hpc_batch_get_all_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t cap, int64_t *prefix) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
+  if (!prefix) {
+    set_error("null prefix pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  if ((s = finalize_records(c)) != HPC_OK) return s;
+  HPC_CUDA(cudaMemcpyAsync(c->gctr_host, c->gctr, sizeof(DevGlobal) * (size_t)c->count, cudaMemcpyDeviceToHost,
+                           c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<long long> pre((size_t)c->count + 1, 0);
+  for (int b = 0; b < c->count; ++b) {
+    const long long n = c->recs ? std::min<long long>((long long)c->gctr_host[b].rec_count, c->ih[b].rec_cap) : 0;
+    pre[b + 1] = pre[b] + n;
+  }
+  for (int b = 0; b <= c->count; ++b) prefix[b] = pre[b];
+  const long long total = pre[c->count];
+  if (!out || cap <= 0 || total == 0) return HPC_OK;
+  const int stride = rec_stride_words(c->rec_ids);
+  if (c->rec_stage_words < total * stride) {
+    dev_free(c->rec_stage);
+    c->rec_stage_words = 0;
+    if ((s = dev_alloc(&c->rec_stage, total * stride, "record staging")) != HPC_OK) return s;
+    c->rec_stage_words = total * stride;
+  }
+  if (!c->rec_prefix_dev && (s = dev_alloc(&c->rec_prefix_dev, c->count + 1, "record prefix")) != HPC_OK) return s;
+  HPC_CUDA(cudaMemcpyAsync(c->rec_prefix_dev, pre.data(), sizeof(long long) * pre.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  if ((s = launch_gather_records(c->inst, c->count, c->rec_prefix_dev, total, stride, c->rec_stage, c->stream)) !=
+      HPC_OK)
+    return s;
+  c->timings.launches += 1;
+  const long long k = std::min<long long>(cap, total);
+  std::vector<int32_t> raw((size_t)(k * stride));
+  HPC_CUDA(cudaMemcpyAsync(raw.data(), c->rec_stage, sizeof(int32_t) * raw.size(), cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  for (long long r = 0; r < k; ++r) {
+    const int32_t *rec = raw.data() + (size_t)r * stride;
+    RecHead head;
+    std::memcpy(&head, rec, sizeof(head));
+    hpc_sepset_record &o = out[r];
+    o.i = head.i;
+    o.j = head.j;
+    o.level = head.level;
+    o.pad = 0;
+    o.pmax = head.pmax;
+    for (int q = 0; q < HPC_MAX_LEVEL; ++q) o.ids[q] = q < c->rec_ids ? rec[kRecHeadWords + q] : -1;
+  }
+  return HPC_OK;
 }
 
 hpc_status hpc_get_sepsets(hpc_ctx *c, int32_t *out, int max_cond) {

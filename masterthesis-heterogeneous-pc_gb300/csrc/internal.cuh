@@ -264,6 +264,10 @@ hpc_status launch_level(const Launch &L, int precision, int grid, int l1_variant
 hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s);
 void retest_setup();  // once per context creation, before any launch_retest
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
+// every instance's records packed back to back: instance b's first record goes to
+// record slot prefix[b] of out (stride words each); prefix has count + 1 entries
+hpc_status launch_gather_records(const Inst *inst, int count, const long long *prefix, long long total, int stride,
+                                 int32_t *out, cudaStream_t s);
 int citest_grid(int precision, int level, int device, int l1_variant = kL1Interleaved);
 
 // process-wide tile-policy table (tune.cu)
@@ -353,6 +357,7 @@ struct hpc_ctx {
   int l1_max_deg = -1;            // level-1 max degree of the last run (keys level 1's kernel choice)
   int l1v_now = 0;                // the level-1 kernel variant of the runs being queued
   int graph_l1v = 0;              // ... and of the captured graph
+  bool graph_final = false;       // the captured graph ends with the record finalisation
   cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
   cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
   cudaEvent_t evr[2] = {nullptr, nullptr};      // whole skeleton run
@@ -363,4 +368,13 @@ struct hpc_ctx {
   bool records_final = true;     // the records' FP32 p-values have been evaluated in FP64
   bool async_pending = false;    // an hpc_run_skeleton_async run not yet collected by hpc_wait
   int async_top = -1;
+  // runs "until exhausted" (max_level -1): the last level of the previous such run (its
+  // first level without tests), so that the next run queues levels 0..exhaust_top as one
+  // sequence (one graph replay, one sync) and only continues level by level if the data
+  // now reach further; -1 before the first run
+  int exhaust_top = -1;
+  // whole-batch record retrieval: compacted copy of every instance's records
+  int32_t *rec_stage = nullptr;
+  long long rec_stage_words = 0;
+  long long *rec_prefix_dev = nullptr;  // count + 1
 };

@@ -133,6 +133,11 @@ _SIGS = {
     "hpc_batch_get_adjacency": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "hpc_batch_edge_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]),
     "hpc_batch_get_sepset_records": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "hpc_batch_get_sepset_records_from": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_int64,
+                                                    C.POINTER(C.c_int64)]),
+    "hpc_batch_adjacency_words": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_batch_get_adjacency_bits": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "hpc_batch_get_all_sepset_records": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "hpc_tune_set": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.POINTER(TuneParams)]),
     "hpc_tune_lookup": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.POINTER(TuneParams), C.POINTER(C.c_int)]),
     "hpc_tune_clear": (C.c_int, []),
@@ -254,6 +259,25 @@ def sem_generate(p, n, graph=GRAPH_ER, degree=2.0, pa_parents=2, w_lo=0.1, w_hi=
                                   _ptr(dag) if dag is not None else None, None))
     X = X64 if X64 is not None else X32
     return (X, dag) if want_dag else X
+
+
+RECORD_DTYPE = np.dtype([("i", np.int32), ("j", np.int32), ("level", np.int32), ("pad", np.int32),
+                         ("pmax", np.float64), ("ids", np.int32, (HPC_MAX_LEVEL,))])
+
+
+def record_chunks(h, idx=0, chunk=1 << 22):
+    """Separation-set records of instance idx as numpy structured arrays (RECORD_DTYPE),
+    chunk by chunk (hpc_batch_get_sepset_records_from)."""
+    n = C.c_int64(0)
+    _check(lib().hpc_batch_get_sepset_records_from(h, idx, 0, None, 0, C.byref(n)))
+    total = n.value
+    buf = (SepsetRecord * max(1, min(chunk, total)))()
+    first = 0
+    while first < total:
+        k = min(chunk, total - first)
+        _check(lib().hpc_batch_get_sepset_records_from(h, idx, first, buf, k, C.byref(n)))
+        yield np.frombuffer(buf, dtype=RECORD_DTYPE, count=k).copy()
+        first += k
 
 
 class SkeletonCalculator:
@@ -419,6 +443,11 @@ class SkeletonCalculator:
         return [(r.i, r.j, r.level, tuple(r.ids[:r.level]), r.pmax) for r in recs[:n.value]]
 
 
+def record_buffer(n):
+    """A ctypes array of n hpc_sepset_record (for the *_into record calls)."""
+    return (SepsetRecord * max(1, int(n)))()
+
+
 class SkeletonBatch:
     """Many independent skeleton problems in one context: every level kernel runs
     once for all of them (hpc_batch_* in include/heterogpc.h)."""
@@ -432,6 +461,7 @@ class SkeletonBatch:
         lib().hpc_opts_default(C.byref(o))
         o.device, o.max_level, o.precision, o.retest_margin, o.verbose = device, max_level, precision, \
             retest_margin, int(verbose)
+        self.max_level = int(max_level)
         self.alphas = None if alphas is None else np.ascontiguousarray(alphas, dtype=np.float64)
         h = C.c_void_p()
         _check(lib().hpc_batch_create(C.byref(h), self.count, _ptr(self.ps), _ptr(self.ns),
@@ -468,6 +498,17 @@ class SkeletonBatch:
     def add_observations_device(self, ptr, dtype):
         fn = lib().hpc_correlation_device_f32 if dtype == np.float32 else lib().hpc_correlation_device_f64
         _check(fn(self._h, C.c_void_p(ptr)))
+
+    def add_observations_ptr(self, ptr, dtype):
+        """Packed observations in host memory at ptr (e.g. pinned), copied inside the call."""
+        fn = lib().hpc_correlation_f32 if dtype == np.float32 else lib().hpc_correlation_f64
+        _check(fn(self._h, C.c_void_p(ptr)))
+
+    def calc_level(self, level):
+        """One level of every instance (hpc_run_level); summed statistics."""
+        st = LevelStats()
+        _check(lib().hpc_run_level(self._h, int(level), C.byref(st)))
+        return st.as_dict()
 
     def add_correlation_matrices(self, mats):
         packed = np.empty(int(self.cor_off[-1]), np.float64)
@@ -522,6 +563,63 @@ class SkeletonBatch:
         k = C.c_int(0)
         _check(lib().hpc_batch_level_stats(self._h, idx, arr, cap, C.byref(k)))
         return [arr[i].as_dict() for i in range(k.value)]
+
+    def run_async(self):
+        """Queue the whole batch's skeleton and return (hpc_run_skeleton_async)."""
+        _check(lib().hpc_run_skeleton_async(self._h))
+
+    def wait(self):
+        cap = HPC_MAX_LEVEL + 1
+        arr = (LevelStats * cap)()
+        ran = C.c_int(0)
+        _check(lib().hpc_wait(self._h, arr, cap, C.byref(ran)))
+        self.level_stats = [arr[i].as_dict() for i in range(ran.value)]
+        return self.level_stats
+
+    def adjacency_words(self):
+        """Word offsets (count + 1) of every instance's bitmask in adjacency_bits()."""
+        off = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_adjacency_words(self._h, _ptr(off)))
+        return off
+
+    def adjacency_bits_into(self, ptr, words):
+        """Every instance's adjacency bitmask into caller memory (uint32 words at ptr)."""
+        _check(lib().hpc_batch_get_adjacency_bits(self._h, C.c_void_p(ptr), int(words)))
+
+    def adjacency_bits(self):
+        off = self.adjacency_words()
+        out = np.empty(int(off[-1]), np.uint32)
+        self.adjacency_bits_into(out.ctypes.data, out.size)
+        return out, off
+
+    def record_prefix(self):
+        """Exclusive prefix (count + 1) of the instances' separation-set record counts."""
+        pre = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_get_all_sepset_records(self._h, None, 0, _ptr(pre)))
+        return pre
+
+    def record_stride_bytes(self):
+        """Device bytes of one packed record (head + one id slot per level up to max_level)."""
+        ids = HPC_MAX_LEVEL if self.max_level < 0 else min(max(self.max_level, 1), HPC_MAX_LEVEL)
+        return 4 * (6 + ((ids + 1) & ~1))
+
+    def all_sepset_records_into(self, recs, cap):
+        """Every instance's records into a ctypes SepsetRecord array; returns the prefix."""
+        pre = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_get_all_sepset_records(self._h, recs, int(cap), _ptr(pre)))
+        return pre
+
+    def all_sepset_records(self):
+        """{instance: [(i, j, level, ids, pmax), ...]} of every instance in one copy."""
+        pre = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_get_all_sepset_records(self._h, None, 0, _ptr(pre)))
+        total = int(pre[-1])
+        recs = (SepsetRecord * max(1, total))()
+        pre = self.all_sepset_records_into(recs, total)
+        out = {}
+        for b in range(self.count):
+            out[b] = [(r.i, r.j, r.level, tuple(r.ids[:r.level]), r.pmax) for r in recs[int(pre[b]):int(pre[b + 1])]]
+        return out
 
     def sepset_records(self, idx):
         n = C.c_int64(0)

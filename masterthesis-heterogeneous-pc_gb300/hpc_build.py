@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["citest_l17.cu", "citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
-              "noalloc.cu", "tune.cu"]
+              "noalloc.cu", "tune.cu", "compat.cu"]
 HOST_SOURCES = ["semgen.cpp", "serve.cpp"]
 
 
@@ -41,7 +41,7 @@ def _newer(out, deps):
 
 
 def _headers():
-    hs = [os.path.join(INCLUDE, "heterogpc.h")]
+    hs = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     hs += [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".hpp", ".h"))]
     return hs
@@ -95,11 +95,15 @@ def build_cli(so):
 
 
 def build_oracle():
+    """oracle/liboracle.so: the CPU restatement, plus the seeded SEM generator (host code,
+    so that CPU-only legs can make the workloads' data without loading the product)."""
     so = os.path.join(ORACLE, "liboracle.so")
     src = os.path.join(ORACLE, "oracle.cpp")
-    deps = [src, os.path.join(ORACLE, "pinv_sym.hpp")]
+    sem = os.path.join(HOST, "semgen.cpp")
+    deps = [src, sem, os.path.join(ORACLE, "pinv_sym.hpp"), os.path.join(INCLUDE, "heterogpc.h")]
     if not _newer(so, deps):
-        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared", src, "-o", so])
+        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared", "-I", INCLUDE, src, sem,
+              "-o", so, "-lpthread"])
     return so
 
 

@@ -308,20 +308,178 @@ int orc_correlation(const double *X, int64_t n, int64_t p, int ref_compat, doubl
       sd[v] = std::sqrt(ss / (double)(n - 1));
   }
   const double denom = ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
-#pragma omp parallel for schedule(dynamic, 4)
-  for (int64_t a = 0; a < p; ++a) {
-    const double *xa = X + a * n;
-    for (int64_t b = a; b < p; ++b) {
-      const double *xb = X + b * n;
-      double s = 0.0;
-      for (int64_t k = 0; k < n; ++k) {
-        if (!(std::isnan(xa[k]) || std::isnan(xb[k])))
-          s += ((xa[k] - mean[a]) / sd[a]) * ((xb[k] - mean[b]) / sd[b]);
+  // corHelper.cu:98-106 evaluates ((x_a - mean_a) / sd_a) * ((x_b - mean_b) / sd_b) per
+  // sample, skipping samples where either value is NaN. Each factor is formed here once
+  // per variable (the same operations, so the same doubles) and the NaN skip kept as a
+  // mask; the per-pair sum runs over k in order, as there.
+  std::vector<double> z((size_t)(n * p));
+  std::vector<uint8_t> miss((size_t)(n * p));
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < p; ++v)
+    for (int64_t k = 0; k < n; ++k) {
+      const double x = X[v * n + k];
+      miss[v * n + k] = std::isnan(x) ? 1 : 0;
+      z[v * n + k] = (x - mean[v]) / sd[v];
+    }
+  constexpr int64_t kTile = 16;
+  const int64_t nt = (p + kTile - 1) / kTile;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t t = 0; t < nt * nt; ++t) {
+    const int64_t ta = t / nt, tb = t % nt;
+    if (tb < ta) continue;
+    for (int64_t a = ta * kTile; a < std::min(p, (ta + 1) * kTile); ++a) {
+      const double *za = z.data() + a * n;
+      const uint8_t *ma = miss.data() + a * n;
+      for (int64_t b = std::max(a, tb * kTile); b < std::min(p, (tb + 1) * kTile); ++b) {
+        const double *zb = z.data() + b * n;
+        const uint8_t *mb = miss.data() + b * n;
+        double s = 0.0;
+        for (int64_t k = 0; k < n; ++k)
+          if (!(ma[k] | mb[k])) s += za[k] * zb[k];
+        C[a * p + b] = C[b * p + a] = s / denom;
       }
-      C[a * p + b] = C[b * p + a] = s / denom;
     }
   }
   return 0;
+}
+
+// Re-test of stored separation sets in FP64 with the reference's formulas
+// (cpuInd.cpp:8-38): ok[t] = 1 iff p >= alpha for edge (i, j) given ids. ijl holds
+// (i, j, level) per record, ids max_ids slots per record.
+void orc_verify_sepsets(const double *C, int64_t p, int n, double alpha, int64_t k, const int32_t *ijl,
+                        const int32_t *ids, int max_ids, uint8_t *ok) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t t = 0; t < k; ++t) {
+    const int64_t i = ijl[3 * t], j = ijl[3 * t + 1];
+    const int l = ijl[3 * t + 2];
+    const int32_t *S = ids + t * max_ids;
+    double pv;
+    if (l == 0) {
+      pv = calc_pvalue(C[std::max(i, j) * p + std::min(i, j)], n);
+    } else if (l == 1) {
+      pv = pval_l1(C[i * p + j], C[i * p + S[0]], C[j * p + S[0]], n);
+    } else {
+      const int kk = l + 2;
+      std::vector<int64_t> V((size_t)kk);
+      V[0] = i;
+      V[1] = j;
+      for (int q = 0; q < l; ++q) V[2 + q] = S[q];
+      std::sort(V.begin() + 2, V.end());
+      std::vector<double> M((size_t)(kk * kk));
+      for (int a = 0; a < kk; ++a)
+        for (int b = 0; b < kk; ++b) M[a * kk + b] = a == b ? 1.0 : C[V[a] * p + V[b]];
+      pv = pval_ln(M.data(), kk, n);
+    }
+    ok[t] = pv >= alpha ? 1 : 0;
+  }
+}
+
+namespace {
+// |r| at which calc_pvalue == alpha (p is decreasing in |r|); 2 when every r is removed
+double r_crit_of(double alpha, int n) {
+  double lo = 0.0, hi = kCutThr;
+  if (calc_pvalue(hi, n) >= alpha) return 2.0;
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (calc_pvalue(mid, n) >= alpha) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// Does the subset S (|S| = l >= 2) separate i and j? The partial correlation by
+// Cholesky of the S block in FP64; where the block is ill-conditioned or |r| lies within
+// 1e-8 relative of r_crit, the reference's pinv formula (pval_ln) decides.
+bool separates(const double *C, int64_t p, int n, double alpha, double rc, int64_t i, int64_t j, const int *S,
+               int l) {
+  double Lm[kMaxLevel * kMaxLevel], wx[kMaxLevel], wy[kMaxLevel];
+  bool ok = true;
+  for (int r = 0; r < l && ok; ++r) {
+    double vx = C[i * p + S[r]], vy = C[j * p + S[r]], d = 1.0;
+    for (int c = 0; c < r; ++c) {
+      double v = C[(int64_t)S[c] * p + S[r]];
+      for (int q = 0; q < c; ++q) v -= Lm[r * kMaxLevel + q] * Lm[c * kMaxLevel + q];
+      v /= Lm[c * kMaxLevel + c];
+      Lm[r * kMaxLevel + c] = v;
+      d -= v * v;
+      vx -= v * wx[c];
+      vy -= v * wy[c];
+    }
+    if (!(d > 1e-8)) ok = false;
+    else {
+      Lm[r * kMaxLevel + r] = std::sqrt(d);
+      wx[r] = vx / Lm[r * kMaxLevel + r];
+      wy[r] = vy / Lm[r * kMaxLevel + r];
+    }
+  }
+  if (ok) {
+    double ax = 1.0, ay = 1.0, b = C[i * p + j];
+    for (int q = 0; q < l; ++q) {
+      ax -= wx[q] * wx[q];
+      ay -= wy[q] * wy[q];
+      b -= wx[q] * wy[q];
+    }
+    if (ax > 1e-8 && ay > 1e-8 && std::isfinite(b)) {
+      const double r = std::fabs(b / std::sqrt(ax * ay));
+      if (r < rc * (1.0 - 1e-8)) return true;
+      if (r > rc * (1.0 + 1e-8)) return false;
+    }
+  }
+  const int kk = l + 2;
+  std::vector<int64_t> V((size_t)kk);
+  V[0] = i;
+  V[1] = j;
+  for (int q = 0; q < l; ++q) V[2 + q] = S[q];
+  std::vector<double> M((size_t)(kk * kk));
+  for (int a = 0; a < kk; ++a)
+    for (int b = 0; b < kk; ++b) M[a * kk + b] = a == b ? 1.0 : C[V[a] * p + V[b]];
+  return pval_ln(M.data(), kk, n) >= alpha;
+}
+}  // namespace
+
+// Exhaustive check of edges kept at `level`: for edge (i, j) every level-subset of
+// i's snapshot neighbours other than j, and of j's other than i (adj_before: the p x p
+// adjacency at the level start), is tested in FP64; status[t] = 0 no subset separates,
+// 1 a subset separates (the edge should have been removed), 2 not checked (more than
+// max_subsets subsets in a direction).
+void orc_check_retained(const double *C, int64_t p, int n, double alpha, int level, const uint8_t *adj_before,
+                        int64_t k, const int32_t *edges, int64_t max_subsets, int8_t *status) {
+  const double rc = r_crit_of(alpha, n);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t t = 0; t < k; ++t) {
+    const int64_t ends[2] = {edges[2 * t], edges[2 * t + 1]};
+    std::vector<int> nb[2];
+    for (int e = 0; e < 2; ++e)
+      for (int64_t v = 0; v < p; ++v)
+        if (adj_before[ends[e] * p + v] && v != ends[1 - e]) nb[e].push_back((int)v);
+    int8_t st = 0;
+    for (int e = 0; e < 2 && st == 0; ++e)
+      if ((int)nb[e].size() >= level && binom((int)nb[e].size(), level) > (uint64_t)max_subsets) st = 2;
+    for (int e = 0; e < 2 && st == 0; ++e) {
+      const int m = (int)nb[e].size();
+      if (m < level) continue;
+      const int64_t i = ends[e], j = ends[1 - e];
+      if (level == 1) {
+        for (int q = 0; q < m && st == 0; ++q)
+          if (pval_l1(C[i * p + j], C[i * p + nb[e][q]], C[j * p + nb[e][q]], n) >= alpha) st = 1;
+        continue;
+      }
+      int pos[kMaxLevel], S[kMaxLevel];
+      for (int q = 0; q < level; ++q) pos[q] = q;
+      for (;;) {
+        for (int q = 0; q < level; ++q) S[q] = nb[e][pos[q]];
+        if (separates(C, p, n, alpha, rc, i, j, S, level)) {
+          st = 1;
+          break;
+        }
+        int q = level - 1;
+        while (q >= 0 && pos[q] == m - level + q) --q;
+        if (q < 0) break;
+        ++pos[q];
+        for (int r = q + 1; r < level; ++r) pos[r] = pos[r - 1] + 1;
+      }
+    }
+    status[t] = st;
+  }
 }
 
 // skeleton.cpp:152-190 level loop; max_level < 0 runs until a level has no test.

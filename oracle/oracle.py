@@ -55,6 +55,12 @@ def lib():
         L.orc_records.restype = C.c_int64
         L.orc_records.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int64]
         L.orc_l0_deleted.argtypes = [C.c_void_p, C.c_int64, C.c_int64]
+        L.orc_verify_sepsets.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_double, C.c_int64, C.c_void_p,
+                                         C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_check_retained.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_double, C.c_int, C.c_void_p,
+                                         C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+        L.hpc_sem_generate.restype = C.c_int
+        L.hpc_sem_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _orc = L
     return _orc
 
@@ -71,6 +77,25 @@ def ref_lib():
                               C.c_void_p]
         _ref = L
     return _ref
+
+
+class _SemParams(C.Structure):
+    _fields_ = [("p", C.c_int64), ("n", C.c_int64), ("graph", C.c_int), ("degree", C.c_double),
+                ("pa_parents", C.c_int), ("w_lo", C.c_double), ("w_hi", C.c_double), ("seed", C.c_uint64)]
+
+
+def sem_generate(p, n, graph=0, degree=2.0, pa_parents=2, w_lo=0.1, w_hi=1.0, seed=1, dtype=np.float64):
+    """The seeded SEM generator (masterthesis-heterogeneous-pc_gb300/host/semgen.cpp, host
+    code compiled into this library): the same bytes as the product's hpc_sem_generate,
+    for CPU-only legs that must not load the product library."""
+    prm = _SemParams(p, n, graph, degree, pa_parents, w_lo, w_hi, seed)
+    X = np.empty((p, n), dtype)
+    x64 = _p(X) if dtype == np.float64 else None
+    x32 = _p(X) if dtype == np.float32 else None
+    rc = lib().hpc_sem_generate(C.byref(prm), x64, x32, None, None)
+    if rc != 0:
+        raise ValueError("sem_generate rejected the parameters (%d)" % rc)
+    return X
 
 
 def calc_pvalue(r, n):
@@ -195,3 +220,50 @@ def verify_sepset(Cm, n_obs, alpha, i, j, ids):
         for b in range(a + 1, k):
             M[a, b] = M[b, a] = Cm[idx[a], idx[b]]
     return pval_ln(M, n_obs) >= alpha
+
+
+def verify_sepsets(Cm, n_obs, alpha, records):
+    """FP64 re-test of many stored separation sets at once: records is a list of
+    (i, j, level, ids); returns a bool array, True where p >= alpha given ids."""
+    Cm = np.ascontiguousarray(Cm, np.float64)
+    k = len(records)
+    if k == 0:
+        return np.zeros(0, bool)
+    mi = max(1, max(r[2] for r in records))
+    ijl = np.empty((k, 3), np.int32)
+    ids = np.full((k, mi), -1, np.int32)
+    for t, r in enumerate(records):
+        ijl[t] = (r[0], r[1], r[2])
+        ids[t, :r[2]] = r[3][:r[2]]
+    ok = np.zeros(k, np.uint8)
+    lib().orc_verify_sepsets(_p(Cm), Cm.shape[0], int(n_obs), float(alpha), k, _p(ijl), _p(ids), mi, _p(ok))
+    return ok.astype(bool)
+
+
+def check_retained(Cm, n_obs, alpha, level, adj_before, edges, max_subsets):
+    """Exhaustive FP64 check of kept edges (k x 2 array, i < j) at `level`: every subset of
+    either endpoint's snapshot neighbours (adj_before, the adjacency at the level start)
+    is tested. Returns per edge 0 = no subset separates, 1 = a subset separates,
+    2 = not checked (more than max_subsets subsets on a side)."""
+    Cm = np.ascontiguousarray(Cm, np.float64)
+    A = np.ascontiguousarray(adj_before, np.uint8)
+    E = np.ascontiguousarray(edges, np.int32).reshape(-1, 2)
+    st = np.zeros(len(E), np.int8)
+    lib().orc_check_retained(_p(Cm), Cm.shape[0], int(n_obs), float(alpha), int(level), _p(A), len(E), _p(E),
+                             int(max_subsets), _p(st))
+    return st
+
+
+def verify_record_array(Cm, n_obs, alpha, recs):
+    """verify_sepsets for a numpy structured array of records with fields i, j, level and
+    ids (one row per record, ids padded): True where p >= alpha given the stored set."""
+    Cm = np.ascontiguousarray(Cm, np.float64)
+    k = len(recs)
+    if k == 0:
+        return np.zeros(0, bool)
+    ijl = np.ascontiguousarray(np.stack([recs["i"], recs["j"], recs["level"]], axis=1), np.int32)
+    ids = np.ascontiguousarray(recs["ids"], np.int32)
+    ok = np.zeros(k, np.uint8)
+    lib().orc_verify_sepsets(_p(Cm), Cm.shape[0], int(n_obs), float(alpha), k, _p(ijl), _p(ids), ids.shape[1],
+                             _p(ok))
+    return ok.astype(bool)

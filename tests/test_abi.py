@@ -29,6 +29,23 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, name), name
 
 
+def test_reference_named_entry_points_exported():
+    """gpuPMCC and callCompact with the reference's C++ signatures (heterogpc_compat.h)."""
+    import ctypes
+    L = ctypes.CDLL(hg.LIB_PATH)
+    for mangled in ("_Z7gpuPMCCPKdmiPdib", "_Z11callCompactP7MMStateiiii"):
+        assert hasattr(L, mangled), mangled
+
+
+def test_compat_header_layout():
+    """MMState has the reference's member order (src/util/state.cuh:29-56)."""
+    src = open(os.path.join(ROOT, "include", "heterogpc_compat.h")).read()
+    body = src[src.index("struct MMState {"):src.index("};", src.index("struct MMState {"))]
+    members = re.findall(r"\b(\w+);", body)
+    assert members == ["ats", "pMax", "adj", "adj_compact", "cor", "sepSets", "p", "observations", "alpha",
+                       "maxCondSize", "max_adj", "lock", "maxLevel", "node_status", "gpu_done"]
+
+
 def test_binding_covers_header():
     assert declared_symbols() <= set(hg.exported_symbols()) | {"hpc_ctx_footprint"}
 
