@@ -58,7 +58,44 @@ WORKLOADS = {
     # level cap: at level 4 the hubs alone would need ~1e10 tests each (reported).
     "c3": dict(p=15000, n=3000, graph=1, degree=4.0, pa_parents=2, w_lo=0.2, w_hi=1.0, seed=3, alpha=0.05,
                max_level=3),
+    # input readers of the CLI on the wide workload's observations (3000 x 15000 FP32):
+    # CSV text against .npy binary (C order, FP32) and .npy (Fortran order, FP64)
+    "io": dict(p=15000, n=3000, graph=1, degree=4.0, pa_parents=2, w_lo=0.2, w_hi=1.0, seed=3),
 }
+
+
+def run_io(args, wl):
+    """Read rate of the CLI's input readers (heterogpc --io-benchmark) on the wide
+    workload's observations written as CSV and as .npy; host only, no GPU work."""
+    import re
+    import tempfile
+
+    import heterogpc as hg
+    import hpc_build
+    hpc_build.build_library()
+    exe = os.path.join(os.path.dirname(hg.LIB_PATH), "heterogpc")
+    X = hg.sem_generate(wl["p"], wl["n"], wl["graph"], wl["degree"], wl["pa_parents"], wl["w_lo"], wl["w_hi"],
+                        wl["seed"], dtype=np.float32)
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        files = {"csv": os.path.join(d, "x.csv"), "npy_f32_c": os.path.join(d, "x32.npy"),
+                 "npy_f64_fortran": os.path.join(d, "x64.npy")}
+        np.savetxt(files["csv"], X.T, delimiter=",", fmt="%.9g")
+        np.save(files["npy_f32_c"], np.ascontiguousarray(X.T))
+        np.save(files["npy_f64_fortran"], np.asfortranarray(X.T.astype(np.float64)))
+        for k, f in files.items():
+            rates = []
+            for _ in range(max(1, args.steps)):
+                r = subprocess.run([exe, "-i", f, "--io-benchmark"], capture_output=True, text=True, check=True)
+                m = re.search(r"in ([0-9.]+) s: ([0-9.]+) MB/s of file, ([0-9.]+) M values/s", r.stdout)
+                rates.append((float(m.group(1)), float(m.group(2)), float(m.group(3))))
+            best = min(rates)
+            out[k] = {"seconds": best[0], "file_mb_per_s": best[1], "mvalues_per_s": best[2],
+                      "file_bytes": os.path.getsize(f)}
+    line = {"metric": "input read rate", "value": out["npy_f32_c"]["mvalues_per_s"], "unit": "M values/s",
+            "higher_is_better": True, "config": {"workload": "io", "rows": wl["n"], "columns": wl["p"]},
+            "readers": out, "cores": os.cpu_count(), "note": "best of %d reads per file, page cache warm" % args.steps}
+    print(json.dumps(line), flush=True)
 
 
 def correlation_error(hg, c32, p, n, Xd, stream):
@@ -470,24 +507,24 @@ def run_c4(args, wl):
     # separation-set records
     words = int(bt.adjacency_words()[-1])
     bits_h = torch.empty(words, dtype=torch.int32, pin_memory=True)
-    nrec = int(bt.record_prefix()[-1])
-    rec_cap = nrec + 4096
-    recs = hg.record_buffer(rec_cap)
+    rec_words = int(bt.packed_words()[-1])
+    rec_cap = rec_words + 65536
+    recs_h = torch.empty(rec_cap, dtype=torch.int32, pin_memory=True)
     e2e_t = []
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         bt.add_observations_ptr(host.data_ptr(), np.float32)
         bt.run()
         bt.adjacency_bits_into(bits_h.data_ptr(), words)
-        pre = bt.all_sepset_records_into(recs, rec_cap)
+        w = bt.records_packed_into(recs_h.data_ptr(), rec_cap)
         torch.cuda.synchronize()
         if k >= args.warmup:
             e2e_t.append(time.perf_counter() - t0)
-        nrec = int(pre[-1])
+        rec_words = int(w[-1])
     e2e = {"value": bt.count * len(e2e_t) / sum(e2e_t), "unit": "skeletons/s", "h2d_bytes_per_step": total_obs * 4,
-           "d2h_bytes_per_step": words * 4 + nrec * bt.record_stride_bytes() + 16 * bt.count,
-           "path": "hpc_correlation_f32 (host observations) + hpc_run_skeleton + hpc_batch_get_adjacency_bits + "
-                   "hpc_batch_get_all_sepset_records, host wall clock per step"}
+           "d2h_bytes_per_step": words * 4 + rec_words * 4,
+           "path": "hpc_correlation_f32 (host observations, pinned) + hpc_run_skeleton + "
+                   "hpc_batch_get_adjacency_bits + hpc_batch_get_records_packed (pinned), host wall clock per step"}
 
     # the plain single-instance FP64 path on the same instances, like for like
     plain = c4_plain_path(wl, hg, torch, stream, ps, ns, alphas, Xd, bt.obs_off, flush)
@@ -861,6 +898,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if args.workload == "io":
+        if rank == 0:
+            run_io(args, wl)
+        return
     if args.impl == "reference":
         run_reference(args, wl, rank, world)
         return

@@ -282,6 +282,13 @@ hpc_status hpc_batch_get_adjacency_bits(hpc_ctx *ctx, uint32_t *bits_host, int64
  * out[prefix[b] .. prefix[b + 1]) (prefix: count + 1 entries, always written; at most
  * cap records copied, none when out is NULL). */
 hpc_status hpc_batch_get_all_sepset_records(hpc_ctx *ctx, hpc_sepset_record *out, int64_t cap, int64_t *prefix);
+/* ... or packed, for bulk transfer: record after record (instance by instance, each
+ * instance's in level order) the 32-bit words i, j, level, 0, pmax (a double in two
+ * words), then the `level` separating ids padded with -1 to an even count, i.e.
+ * 6 + 2 * ceil(level / 2) words per record; instance b's records start at word
+ * inst_words[b] (count + 1 entries, always written; the last is the total). At most
+ * cap_words words are copied, none when out is NULL. */
+hpc_status hpc_batch_get_records_packed(hpc_ctx *ctx, int32_t *out, int64_t cap_words, int64_t *inst_words);
 
 /* ---- serving ----------------------------------------------------------------
  * Continuous batching of skeleton requests (no reference counterpart). A
@@ -333,6 +340,20 @@ double hpc_pval_l1(double x1, double x2, double x3, int n_obs);
 double hpc_pval_ln(const double *M, int k, int n_obs);
 /* z_crit = Phi^-1(1 - alpha/2): p >= alpha  <=>  |z| <= z_crit. */
 double hpc_z_crit(double alpha);
+
+/* ---- test hooks ------------------------------------------------------------
+ * Failure injection on the host, for tests of the error paths (no counterpart in the
+ * reference, which exits the process on any CUDA error, src/util/cuda_util.cuh:28-50).
+ * hpc_debug_fail_allocation(k): the k-th device allocation of the library from now on
+ * fails with HPC_ERR_OOM (k = 0 clears it). hpc_debug_live_allocations: the library's
+ * device allocations currently held (a failed call must leave it unchanged).
+ * hpc_debug_set_barrier: the bound of the level kernels' grid-barrier waits
+ * (default 2e9 ns) and 0 or 1 arrivals added to their target -- with 1 the wait cannot
+ * complete, runs out after wait_ns, and the run returns HPC_ERR_TIMEOUT; the context
+ * works again after hpc_debug_set_barrier(ctx, 2000000000, 0) and hpc_ctx_reset. */
+hpc_status hpc_debug_fail_allocation(int64_t k);
+int64_t hpc_debug_live_allocations(void);
+hpc_status hpc_debug_set_barrier(hpc_ctx *ctx, int64_t wait_ns, int extra_arrivals);
 
 /* ---- synthetic data ------------------------------------------------------
  * Seeded linear-Gaussian SEM (no reference counterpart; the reference reads

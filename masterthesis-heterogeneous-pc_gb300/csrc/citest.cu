@@ -49,6 +49,36 @@ __global__ void gather_records_kernel(const Inst *__restrict__ inst, int count, 
   }
 }
 
+// Records of all instances in the packed form of hpc_batch_get_records_packed: record
+// r (instance b with pre[b] <= r < pre[b + 1]) has level l, found from the instance's
+// removals per level (records are appended level by level, so an instance's records of
+// level l follow those of lower levels), and goes to word
+//   inst_words[b] + sum_{l' < l} deleted(l') * w(l') + (rank within level l) * w(l),
+// w(l) = 6 + 2 ceil(l / 2). One warp per record.
+__global__ void pack_records_kernel(const Inst *__restrict__ inst, int count, const long long *__restrict__ pre,
+                                    const long long *__restrict__ inst_words, long long total,
+                                    int32_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < total; r += nw) {
+    const int b = find_inst(pre, count, r);
+    const Inst &I = inst[b];
+    const long long rr = r - pre[b];
+    long long cum = 0, words = inst_words[b];
+    int l = 1;
+    for (; l <= HPC_MAX_LEVEL; ++l) {
+      const long long d = (long long)I.ctr[l].deleted;
+      if (rr < cum + d) break;
+      cum += d;
+      words += d * (long long)(6 + ((l + 1) & ~1));
+    }
+    const int w = 6 + ((l + 1) & ~1);
+    const int32_t *src = I.recs + rr * (long long)I.rec_stride;
+    int32_t *dst = out + words + (rr - cum) * (long long)w;
+    for (int q = lane; q < w; q += 32) dst[q] = q < 6 + l ? src[q] : -1;
+  }
+}
+
 __device__ __forceinline__ double warp_dot(const double *__restrict__ x, const double *__restrict__ y, int64_t n) {
   const int lane = threadIdx.x & 31;
   double s = 0.0;
@@ -183,6 +213,15 @@ hpc_status launch_gather_records(const Inst *inst, int count, const long long *p
   const long long blocks = std::min<long long>((total + 7) / 8, 152 * 8);
   gather_records_kernel<<<(unsigned)blocks, 256, 0, s>>>(inst, count, prefix, total, stride, out);
   HPC_LAUNCH_CHECK("gather_records_kernel");
+  return HPC_OK;
+}
+
+hpc_status launch_pack_records(const Inst *inst, int count, const long long *prefix, const long long *inst_words,
+                               long long total, int32_t *out, cudaStream_t s) {
+  if (total <= 0) return HPC_OK;
+  const long long blocks = std::min<long long>((total + 7) / 8, 152 * 8);
+  pack_records_kernel<<<(unsigned)blocks, 256, 0, s>>>(inst, count, prefix, inst_words, total, out);
+  HPC_LAUNCH_CHECK("pack_records_kernel");
   return HPC_OK;
 }
 

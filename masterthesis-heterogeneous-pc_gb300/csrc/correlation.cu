@@ -89,16 +89,21 @@ __global__ void __launch_bounds__(kStdThreads) standardise_kernel(const TIn *__r
       sd_s = sqrt(tt / (double)(n - 1));
   }
   __syncthreads();
-  const double sd = sd_s;
+  // z = (x - mean) * (1 / sd): one FP64 multiply per sample instead of a division (FP64
+  // division is a long instruction sequence on this GPU, and this loop touches every
+  // sample of every variable); the values differ from (x - mean) / sd by at most an ulp
+  const double inv_sd = 1.0 / sd_s;
   if (!SPLIT) {
     for (long long k = threadIdx.x; k < n; k += kStdThreads) {
       const double xv = (double)x[k];
-      z[k] = isnan(xv) ? 0.0 : (xv - mean) / sd;
+      z[k] = isnan(xv) ? 0.0 : (xv - mean) * inv_sd;
     }
     return;
   }
   // split-BF16 operands of the tensor-core Gram: P = [hi|hi|lo|lo], Q = [hi|lo|hi|lo]
-  // of z / sqrt(n - 1), so that P Q^T is the correlation
+  // of z / sqrt(n - 1), so that P Q^T is the correlation. The split runs in FP32
+  // (hi = bf16(zs), lo = bf16(zs - hi), the subtraction exact in FP32): its error is
+  // the rounding of lo, as with an FP64 split, plus 2^-24 relative from zs itself.
   const double denom = a.ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
   const double scale = 1.0 / sqrt(denom);
   const long long n_pad = a.n_pad[b], K = a.kdim[b];
@@ -107,12 +112,12 @@ __global__ void __launch_bounds__(kStdThreads) standardise_kernel(const TIn *__r
     double zz = 0.0;
     if (k < n) {
       const double xv = (double)x[k];
-      zz = isnan(xv) ? 0.0 : (xv - mean) / sd;
+      zz = isnan(xv) ? 0.0 : (xv - mean) * inv_sd;
       z[k] = zz;
     }
-    const double zs = zz * scale;
-    const __nv_bfloat16 hi = __double2bfloat16(zs);
-    const __nv_bfloat16 lo = __double2bfloat16(zs - (double)__bfloat162float(hi));
+    const float zs = (float)(zz * scale);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(zs);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(zs - __bfloat162float(hi));
     pr[k] = hi;
     pr[n_pad + k] = hi;
     pr[2 * n_pad + k] = lo;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -89,9 +90,23 @@ cudaStream_t alloc_stream() {
   return streams[dev];
 }
 
+// Test hooks: the k-th device allocation from now fails (0 = none), and the number of
+// the library's device allocations currently live.
+std::atomic<long long> g_fail_alloc_in{0};
+std::atomic<long long> g_live_allocs{0};
+
 template <typename T>
 hpc_status dev_alloc(T **ptr, int64_t count, const char *what) {
   if (count <= 0) count = 1;
+  long long k = g_fail_alloc_in.load();
+  while (k > 0 && !g_fail_alloc_in.compare_exchange_weak(k, k - 1)) {
+  }
+  if (k == 1) {
+    *ptr = nullptr;
+    set_error("device allocation of %s (%lld bytes) failed: injected by hpc_debug_fail_allocation", what,
+              (long long)(sizeof(T) * count));
+    return HPC_ERR_OOM;
+  }
   cudaStream_t as = alloc_stream();
   cudaError_t e = cudaMallocAsync((void **)ptr, sizeof(T) * (size_t)count, as);
   if (e == cudaSuccess) e = cudaStreamSynchronize(as);
@@ -102,13 +117,17 @@ hpc_status dev_alloc(T **ptr, int64_t count, const char *what) {
               cudaGetErrorString(e));
     return HPC_ERR_OOM;
   }
+  g_live_allocs.fetch_add(1);
   return HPC_OK;
 }
 
 // Only after the context's own work that used ptr has completed.
 template <typename T>
 void dev_free(T *&ptr) {
-  if (ptr) cudaFreeAsync((void *)ptr, alloc_stream());
+  if (ptr) {
+    cudaFreeAsync((void *)ptr, alloc_stream());
+    g_live_allocs.fetch_sub(1);
+  }
   ptr = nullptr;
 }
 
@@ -206,6 +225,8 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.row_work_limit = std::min<unsigned long long>(1ull << 56, 0x7FFFFFFFFFFFFFFFull /
                                                                   (unsigned long long)std::max<long long>(1, c->total_rows));
   L.inst0 = c->inst_host[0];
+  L.wait_ns = c->wait_ns;
+  L.bar_extra = c->bar_extra;
   return L;
 }
 
@@ -1374,6 +1395,59 @@ hpc_status hpc_get_sepset_records(hpc_ctx *c, hpc_sepset_record *out, int64_t ca
   return hpc_batch_get_sepset_records(c, 0, out, cap, count);
 }
 
+hpc_status hpc_batch_get_records_packed(hpc_ctx *c, int32_t *out, int64_t cap_words, int64_t *inst_words) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if ((s = settle(c)) != HPC_OK) return s;
+  if (!inst_words) {
+    set_error("null inst_words pointer");
+    return HPC_ERR_INVALID_ARG;
+  }
+  if ((s = finalize_records(c)) != HPC_OK) return s;
+  if ((s = pull_counters(c)) != HPC_OK) return s;
+  // records and packed words per instance, from its removals per level (a level's
+  // removals are its records; level 0 writes none)
+  std::vector<long long> pre((size_t)c->count + 1, 0), wpre((size_t)c->count + 1, 0);
+  for (int b = 0; b < c->count; ++b) {
+    long long n = 0, w = 0;
+    for (int l = 1; l < kLevels && l < c->next_level; ++l) {
+      const long long d = (long long)c->ctr_host[(size_t)b * kLevels + l].deleted;
+      n += d;
+      w += d * (6 + ((l + 1) & ~1));
+    }
+    if (c->recs && n > std::min<long long>((long long)c->gctr_host[b].rec_count, c->ih[b].rec_cap)) {
+      set_error("instance %d: record counts disagree (%lld removals, %lld records)", b, n,
+                (long long)c->gctr_host[b].rec_count);
+      return HPC_ERR_STATE;
+    }
+    pre[b + 1] = pre[b] + (c->recs ? n : 0);
+    wpre[b + 1] = wpre[b] + (c->recs ? w : 0);
+  }
+  for (int b = 0; b <= c->count; ++b) inst_words[b] = wpre[b];
+  const long long total = pre[c->count], words = wpre[c->count];
+  if (!out || cap_words <= 0 || total == 0) return HPC_OK;
+  if (c->rec_stage_words < words) {
+    dev_free(c->rec_stage);
+    c->rec_stage_words = 0;
+    if ((s = dev_alloc(&c->rec_stage, words, "record staging")) != HPC_OK) return s;
+    c->rec_stage_words = words;
+  }
+  if (!c->rec_prefix_dev && (s = dev_alloc(&c->rec_prefix_dev, 2 * (c->count + 1), "record prefix")) != HPC_OK)
+    return s;
+  std::vector<long long> both(pre);
+  both.insert(both.end(), wpre.begin(), wpre.end());
+  HPC_CUDA(cudaMemcpyAsync(c->rec_prefix_dev, both.data(), sizeof(long long) * both.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  if ((s = launch_pack_records(c->inst, c->count, c->rec_prefix_dev, c->rec_prefix_dev + c->count + 1, total,
+                               c->rec_stage, c->stream)) != HPC_OK)
+    return s;
+  c->timings.launches += 1;
+  HPC_CUDA(cudaMemcpyAsync(out, c->rec_stage, sizeof(int32_t) * (size_t)std::min<long long>(cap_words, words),
+                           cudaMemcpyDeviceToHost, c->stream));
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  return HPC_OK;
+}
+
 hpc_status hpc_batch_adjacency_words(hpc_ctx *c, int64_t *word_offsets) {
   if (!c || !word_offsets) {
     set_error("null argument");
@@ -1440,7 +1514,8 @@ hpc_status hpc_batch_get_all_sepset_records(hpc_ctx *c, hpc_sepset_record *out, 
     if ((s = dev_alloc(&c->rec_stage, total * stride, "record staging")) != HPC_OK) return s;
     c->rec_stage_words = total * stride;
   }
-  if (!c->rec_prefix_dev && (s = dev_alloc(&c->rec_prefix_dev, c->count + 1, "record prefix")) != HPC_OK) return s;
+  if (!c->rec_prefix_dev && (s = dev_alloc(&c->rec_prefix_dev, 2 * (c->count + 1), "record prefix")) != HPC_OK)
+    return s;
   HPC_CUDA(cudaMemcpyAsync(c->rec_prefix_dev, pre.data(), sizeof(long long) * pre.size(), cudaMemcpyHostToDevice,
                            c->stream));
   if ((s = launch_gather_records(c->inst, c->count, c->rec_prefix_dev, total, stride, c->rec_stage, c->stream)) !=
@@ -1491,6 +1566,28 @@ hpc_status hpc_get_sepsets(hpc_ctx *c, int32_t *out, int max_cond) {
   for (int64_t i = 0; i < p; ++i)
     for (int64_t j = i + 1; j < p; ++j)
       if (!adj[i * p + j] && !later[i * p + j]) out[(i * p + j) * max_cond] = -2;
+  return HPC_OK;
+}
+
+hpc_status hpc_debug_fail_allocation(int64_t k) {
+  if (k < 0) return HPC_ERR_INVALID_ARG;
+  g_fail_alloc_in.store(k);
+  return HPC_OK;
+}
+
+int64_t hpc_debug_live_allocations(void) { return g_live_allocs.load(); }
+
+hpc_status hpc_debug_set_barrier(hpc_ctx *c, int64_t wait_ns, int extra_arrivals) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (wait_ns < 1000 || wait_ns > 10000000000ll || extra_arrivals < 0 || extra_arrivals > 1) {
+    set_error("barrier wait needs 1 us <= wait_ns <= 10 s and extra_arrivals 0 or 1");
+    return HPC_ERR_INVALID_ARG;
+  }
+  if ((s = settle(c)) != HPC_OK) return s;
+  c->wait_ns = (unsigned long long)wait_ns;
+  c->bar_extra = (unsigned int)extra_arrivals;
+  ++c->inst_version;  // launch parameters: graphs are captured anew
   return HPC_OK;
 }
 

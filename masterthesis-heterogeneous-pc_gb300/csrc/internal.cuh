@@ -178,6 +178,8 @@ struct Launch {
   unsigned long long row_work_limit;  // a row with this many CI tests or more is a work overflow
                                       // (rows x limit < 2^63: the level's total fits)
   Inst inst0;                       // inst[0] by value: read from the parameter bank when count == 1
+  unsigned long long wait_ns;       // bound of the grid barriers' waits (2 s)
+  unsigned int bar_extra;           // arrivals added to the barrier target (0; tests raise it)
 };
 
 // Instance b's descriptor: the launch's parameter copy for a single instance (no
@@ -268,6 +270,9 @@ hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
 // record slot prefix[b] of out (stride words each); prefix has count + 1 entries
 hpc_status launch_gather_records(const Inst *inst, int count, const long long *prefix, long long total, int stride,
                                  int32_t *out, cudaStream_t s);
+// every instance's records in the packed form of hpc_batch_get_records_packed
+hpc_status launch_pack_records(const Inst *inst, int count, const long long *prefix, const long long *inst_words,
+                               long long total, int32_t *out, cudaStream_t s);
 int citest_grid(int precision, int level, int device, int l1_variant = kL1Interleaved);
 
 // process-wide tile-policy table (tune.cu)
@@ -367,6 +372,8 @@ struct hpc_ctx {
   int next_level = 0;
   bool records_final = true;     // the records' FP32 p-values have been evaluated in FP64
   bool async_pending = false;    // an hpc_run_skeleton_async run not yet collected by hpc_wait
+  unsigned long long wait_ns = 2000000000ull;  // grid-barrier wait bound of the level kernels
+  unsigned int bar_extra = 0;    // test hook: arrivals added to the barrier target
   int async_top = -1;
   // runs "until exhausted" (max_level -1): the last level of the previous such run (its
   // first level without tests), so that the next run queues levels 0..exhaust_top as one
@@ -376,5 +383,5 @@ struct hpc_ctx {
   // whole-batch record retrieval: compacted copy of every instance's records
   int32_t *rec_stage = nullptr;
   long long rec_stage_words = 0;
-  long long *rec_prefix_dev = nullptr;  // count + 1
+  long long *rec_prefix_dev = nullptr;  // 2 x (count + 1): record and packed-word prefixes
 };

@@ -24,8 +24,10 @@
 //    (different streams, or different host threads) race on the array; order
 //    them on one stream or serialise them.
 //  * The shapes the grouped kernels read (offsets, sizes, tile counts) also live in
-//    a file-scope __device__ struct, written with cudaMemcpyToSymbolAsync on the
-//    caller's stream, and are shared between calls the same way.
+//    a file-scope __device__ struct, written by a one-thread kernel (the values
+//    travel as its launch parameter, so no host memory is copied and the call does
+//    not wait for the stream) on the caller's stream, and are shared between calls
+//    the same way.
 //  * No cudaMalloc, cudaFree or allocating library routine is called.
 #include <cuda_runtime.h>
 
@@ -48,6 +50,9 @@ struct NoallocMeta {
   double denom;
 };
 static __device__ NoallocMeta g_meta;
+
+// writes the shapes of this call where the grouped kernels read them
+__global__ void set_meta_kernel(NoallocMeta m) { g_meta = m; }
 
 std::mutex g_scratch_mu;
 double *g_scratch_addr[kMaxDevices] = {};
@@ -119,8 +124,8 @@ extern "C" hpc_status hpc_correlation_noalloc_f64(const double *X_dev, int64_t n
   m.tile_prefix[1] = gram_f64_tiles(p);
   m.p = p;
   m.denom = ref_compat_sd ? (double)((float)n_obs - 1.f) : (double)(n_obs - 1);
-  // pageable source: the copy has read `m` when the call returns
-  HPC_CUDA(cudaMemcpyToSymbolAsync(g_meta, &m, sizeof(m), 0, cudaMemcpyHostToDevice, st));
+  set_meta_kernel<<<1, 1, 0, st>>>(m);
+  HPC_LAUNCH_CHECK("set_meta_kernel");
   StdArgs sa{};
   sa.count = 1;
   sa.row_prefix = md->row_prefix;

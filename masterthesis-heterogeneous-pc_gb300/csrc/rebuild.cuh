@@ -35,20 +35,22 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
 }
 
 // Grid-wide barrier of a cooperative launch (all blocks co-resident). `epoch` counts
-// the barriers this block has passed. The wait is bounded (2 s of %globaltimer): on
-// expiry the kernel's error flag is set and false is returned; the caller returns.
+// the barriers this block has passed. The wait is bounded (L.wait_ns of %globaltimer,
+// 2 s by default): on expiry the kernel's error flag is set and false is returned; the
+// caller returns. L.bar_extra (0 outside tests) raises the arrival target, so that a
+// test can make the wait run out without anything faulting.
 __device__ __forceinline__ bool grid_barrier(const Launch &L, unsigned int &epoch) {
   __shared__ int s_ok;
   __syncthreads();
   ++epoch;
   if (threadIdx.x == 0) {
-    const unsigned int target = epoch * gridDim.x;
+    const unsigned int target = epoch * gridDim.x + L.bar_extra;
     __threadfence();
     atomicAdd(&L.lc->bar, 1u);
     int ok = 1;
     const unsigned long long t0 = globaltimer_ns();
     while (ld_acquire_u32(&L.lc->bar) < target) {
-      if (globaltimer_ns() - t0 > 2000000000ull) {
+      if (globaltimer_ns() - t0 > L.wait_ns) {
         ok = 0;
         atomicOr(&inst_of(L, 0)->g->err, kErrTimeout);
         break;

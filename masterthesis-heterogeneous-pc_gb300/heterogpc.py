@@ -117,6 +117,9 @@ _SIGS = {
     "hpc_pval_l1": (C.c_double, [C.c_double, C.c_double, C.c_double, C.c_int]),
     "hpc_pval_ln": (C.c_double, [C.c_void_p, C.c_int, C.c_int]),
     "hpc_z_crit": (C.c_double, [C.c_double]),
+    "hpc_debug_fail_allocation": (C.c_int, [C.c_int64]),
+    "hpc_debug_live_allocations": (C.c_int64, []),
+    "hpc_debug_set_barrier": (C.c_int, [C.c_void_p, C.c_int64, C.c_int]),
     "hpc_sem_generate": (C.c_int, [C.POINTER(SemParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hpc_server_opts_default": (C.c_int, [C.POINTER(ServerOpts)]),
     "hpc_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(ServerOpts)]),
@@ -136,6 +139,7 @@ _SIGS = {
     "hpc_batch_get_sepset_records_from": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_int64,
                                                     C.POINTER(C.c_int64)]),
     "hpc_batch_adjacency_words": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hpc_batch_get_records_packed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "hpc_batch_get_adjacency_bits": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "hpc_batch_get_all_sepset_records": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "hpc_tune_set": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.POINTER(TuneParams)]),
@@ -378,6 +382,10 @@ class SkeletonCalculator:
     def set_graphs(self, enable):
         _check(lib().hpc_ctx_set_graphs(self._h, int(bool(enable))))
 
+    def set_barrier(self, wait_ns, extra_arrivals):
+        """Test hook (hpc_debug_set_barrier): grid-barrier wait bound and added arrivals."""
+        _check(lib().hpc_debug_set_barrier(self._h, int(wait_ns), int(extra_arrivals)))
+
     def set_tune(self, policy):
         """Force a tile policy ({"tile_cap", "tiles_per_lane", "edge_lanes"}) on every level; None = the table."""
         _set_tune(self._h, policy)
@@ -591,6 +599,35 @@ class SkeletonBatch:
         out = np.empty(int(off[-1]), np.uint32)
         self.adjacency_bits_into(out.ctypes.data, out.size)
         return out, off
+
+    def packed_words(self):
+        """Word offsets (count + 1) of every instance's packed records."""
+        w = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_get_records_packed(self._h, None, 0, _ptr(w)))
+        return w
+
+    def records_packed_into(self, ptr, cap_words):
+        """Every instance's records in the packed form into caller memory at ptr (int32
+        words); returns the instances' word offsets."""
+        w = np.empty(self.count + 1, np.int64)
+        _check(lib().hpc_batch_get_records_packed(self._h, C.c_void_p(ptr), int(cap_words), _ptr(w)))
+        return w
+
+    def records_packed(self):
+        """{instance: [(i, j, level, ids, pmax), ...]} decoded from the packed copy."""
+        w = self.packed_words()
+        buf = np.empty(max(1, int(w[-1])), np.int32)
+        w = self.records_packed_into(buf.ctypes.data, buf.size)
+        out = {}
+        for b in range(self.count):
+            recs, q = [], int(w[b])
+            while q < int(w[b + 1]):
+                i, j, lev = int(buf[q]), int(buf[q + 1]), int(buf[q + 2])
+                pmax = float(buf[q + 4:q + 6].view(np.float64)[0])
+                recs.append((i, j, lev, tuple(int(x) for x in buf[q + 6:q + 6 + lev]), pmax))
+                q += 6 + 2 * ((lev + 1) // 2)
+            out[b] = recs
+        return out
 
     def record_prefix(self):
         """Exclusive prefix (count + 1) of the instances' separation-set record counts."""

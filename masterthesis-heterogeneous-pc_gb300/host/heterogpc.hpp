@@ -54,6 +54,12 @@ namespace CSVParser {
 std::shared_ptr<Matrix> read_csv_to_mat(const std::string &filename, std::vector<std::string> &column_names);
 }  // namespace CSVParser
 
+namespace NPYLoader {
+// binary input (no reference counterpart): a 2-D float64/float32 .npy file, rows =
+// observations, columns = variables, read into the column-major layout above
+std::shared_ptr<Matrix> read_npy_to_mat(const std::string &filename);
+}  // namespace NPYLoader
+
 namespace CPU {
 double calcPValue(double r, int sampleSize);
 double pValL1(double x1, double x2, double x3, int sampleSize);

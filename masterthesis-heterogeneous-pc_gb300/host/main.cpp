@@ -3,6 +3,8 @@
 // --power9-ats, -t) are accepted; every CI test here runs on the GPU work queue,
 // so they change nothing and a note says so. New: --precision fp64|mixed|mixed-tc,
 // --autotune and --tune-file (the CI tests' tile policy, hpc_autotune / hpc_tune_*).
+#include <chrono>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -52,6 +54,7 @@ const std::vector<Opt> kOpts = {
     {"precision", 0, true, false, "CI-test precision: fp64, mixed (default) or mixed-tc", "mixed"},
     {"autotune", 0, false, false, "time the tile-policy candidates on this input before the run", ""},
     {"tune-file", 0, true, false, "tile-policy table: loaded before the run, written after --autotune", ""},
+    {"io-benchmark", 0, false, false, "only read the input file (.csv or .npy) and report the read rate", ""},
 };
 
 const Opt *find_long(const std::string &n) {
@@ -191,6 +194,29 @@ int main(int argc, char const *argv[]) {
                  "every CI test runs on the GPU work queue\n";
   if (gpus.size() > 1) std::cerr << "note: one GPU per process; using device " << gpus.front() << "\n";
 
+  if (vm.count("io-benchmark")) {
+    // the input reader alone: values and megabytes of the file per second
+    try {
+      SkeletonCalculator probe(maxLevel, alpha, false, "", numberOfThreads, false);
+      FILE *fh = std::fopen(inputFile.c_str(), "rb");
+      long long fbytes = 0;
+      if (fh) {
+        std::fseek(fh, 0, SEEK_END);
+        fbytes = std::ftell(fh);
+        std::fclose(fh);
+      }
+      const auto t0 = std::chrono::steady_clock::now();
+      auto m = probe.read_csv_file(inputFile);
+      const double s_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      std::printf("read %lld x %lld values from %lld bytes in %.3f s: %.1f MB/s of file, %.1f M values/s\n",
+                  (long long)m->n_rows, (long long)m->n_cols, fbytes, s_, fbytes / s_ / 1e6,
+                  (double)(m->n_rows * m->n_cols) / s_ / 1e6);
+    } catch (const HpcException &e) {
+      std::cerr << "Error: " << e.what() << "\n";
+      return 2;
+    }
+    return 0;
+  }
   try {
     // the tile-policy table is read first (a bad file fails before any GPU work)
     const std::string tuneFile = vm.count("tune-file") ? get("tune-file") : "";

@@ -57,6 +57,8 @@ void SkeletonCalculator::set_precision(int precision) { precision_ = precision; 
 
 std::shared_ptr<Matrix> SkeletonCalculator::read_csv_file(const std::string &input_file) {
   if (verbose_) std::cout << "Reading file: " << input_file << std::endl;
+  if (input_file.size() > 4 && input_file.compare(input_file.size() - 4, 4, ".npy") == 0)
+    return NPYLoader::read_npy_to_mat(input_file);  // binary input, no reference counterpart
   if (input_file.find(".csv") == std::string::npos) {
     std::cout << "Cannot process file '" << input_file << "'." << std::endl;
     std::cout << "Has to be .csv format." << std::endl;

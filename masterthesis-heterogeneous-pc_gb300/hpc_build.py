@@ -82,7 +82,7 @@ def build_library(jobs=8):
     return so
 
 
-CLI_SOURCES = ["main.cpp", "skeleton.cpp", "csv.cpp"]
+CLI_SOURCES = ["main.cpp", "skeleton.cpp", "csv.cpp", "npy.cpp"]
 
 
 def build_cli(so):

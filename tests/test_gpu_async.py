@@ -46,10 +46,17 @@ def test_async_matches_sync_and_oracle(precision):
     sk.close()
 
 
-def test_async_needs_known_max_level():
+def test_async_until_exhausted_after_a_first_run():
+    """max_level -1: the first run_async runs synchronously (it finds the extent of the
+    levels), later ones are queued; results equal the oracle's."""
     X = gen(dict(p=30, n=400, graph=hg.GRAPH_ER, degree=2.0, seed=7))
+    Cm = orc.correlation(X)
+    want = orc.run(Cm, X.shape[1], 0.05, -1)
     sk = hg.SkeletonCalculator(X.shape[0], X.shape[1], alpha=0.05, max_level=-1, precision=hg.PREC_MIXED)
     sk.add_observations(X)
-    with pytest.raises(hg.HpcError):
+    for _ in range(3):
         sk.run_async()
+    st = sk.wait()
+    assert np.array_equal(sk.adjacency(), want.adj)
+    assert [s["edges_after"] for s in st] == [l["edges_after"] for l in want.levels][:len(st)]
     sk.close()

@@ -65,3 +65,26 @@ def test_batch_correlation_input():
     for b in range(bt.count):
         want = orc.run(mats[b], int(ns[b]), float(alphas[b]), 4)
         assert np.array_equal(bt.adjacency(b), want.adj)
+
+
+def test_whole_batch_result_copies():
+    """Adjacency bitmasks and records of every instance in one copy each (plain, packed
+    and per instance agree)."""
+    ps, ns, alphas, Xs = make_batch(12, seed=4)
+    bt = hg.SkeletonBatch(ps, ns, alphas, max_level=-1, precision=hg.PREC_MIXED_TC)
+    bt.add_observations(bt.pack(Xs))
+    bt.run()
+    bits, off = bt.adjacency_bits()
+    allrec = bt.all_sepset_records()
+    packed = bt.records_packed()
+    for b in range(bt.count):
+        p = int(ps[b])
+        W = (p + 31) // 32
+        m = np.unpackbits(bits[off[b]:off[b + 1]].view(np.uint8), bitorder="little").reshape(p, W * 32)[:, :p]
+        assert np.array_equal(m, bt.adjacency(b))
+        one = bt.sepset_records(b)
+        assert allrec[b] == one
+        assert [(i, j, lev, ids) for i, j, lev, ids, _ in packed[b]] == [(i, j, lev, ids) for i, j, lev, ids, _
+                                                                          in one]
+        assert [pm for *_, pm in packed[b]] == [pm for *_, pm in one]
+        assert [lev for _, _, lev, _, _ in packed[b]] == sorted(lev for _, _, lev, _, _ in packed[b])

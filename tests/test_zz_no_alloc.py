@@ -23,17 +23,17 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12  # the correlation tolerance used by the other GPU tests
 
 
-def _reference_correlation(Xd, p, n):
-    sk = hg.SkeletonCalculator(p, n, precision=hg.PREC_FP64)
+def _reference_correlation(Xd, p, n, ref_compat=False):
+    sk = hg.SkeletonCalculator(p, n, precision=hg.PREC_FP64, ref_compat_sd=ref_compat)
     sk.add_observations_device(Xd.data_ptr(), np.float64)
     out = sk.correlation()
     sk.close()
     return out
 
 
-def _noalloc(Xd, p, n, Cd, stream):
-    return hg.lib().hpc_correlation_noalloc_f64(C.c_void_p(Xd.data_ptr()), n, p, 0, C.c_void_p(Cd.data_ptr()),
-                                                C.c_void_p(stream))
+def _noalloc(Xd, p, n, Cd, stream, ref_compat=0):
+    return hg.lib().hpc_correlation_noalloc_f64(C.c_void_p(Xd.data_ptr()), n, p, int(ref_compat),
+                                                C.c_void_p(Cd.data_ptr()), C.c_void_p(stream) if stream else None)
 
 
 def test_noalloc_matches_allocating_entry_point_twice():
@@ -52,6 +52,32 @@ def test_noalloc_matches_allocating_entry_point_twice():
         stream.synchronize()
         got = Cd.cpu().numpy()
         want = _reference_correlation(Xd, p, n)
+        assert np.isfinite(got).all()
+        assert np.abs(got - want).max() <= TOL
+
+
+@pytest.mark.parametrize("ref_compat,missing,default_stream", [(1, False, False), (0, True, False),
+                                                              (1, True, True)])
+def test_noalloc_variants_twice(ref_compat, missing, default_stream):
+    """The float-rounded standard deviation (ref_compat_sd = 1), observations with
+    missing samples and the default stream (NULL), each on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = None if default_stream else torch.cuda.Stream(device=dev)
+    for p, n, seed in [(40, 600, 5), (72, 1100, 6)]:
+        X = hg.sem_generate(p, n, hg.GRAPH_ER, 3.0, seed=seed)
+        if missing:
+            X[2, ::13] = np.nan
+            X[p - 1, 5::17] = np.nan
+        Xd = torch.from_numpy(X).to(dev)
+        Cd = torch.full((p, p), float("nan"), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        st = _noalloc(Xd, p, n, Cd, stream.cuda_stream if stream else None, ref_compat)
+        assert st == 0, hg.lib().hpc_last_error_string()
+        torch.cuda.synchronize()
+        got = Cd.cpu().numpy()
+        want = _reference_correlation(Xd, p, n, bool(ref_compat))
         assert np.isfinite(got).all()
         assert np.abs(got - want).max() <= TOL
 
