@@ -291,33 +291,36 @@ hpc_status hpc_batch_get_all_sepset_records(hpc_ctx *ctx, hpc_sepset_record *out
 hpc_status hpc_batch_get_records_packed(hpc_ctx *ctx, int32_t *out, int64_t cap_words, int64_t *inst_words);
 
 /* ---- serving ----------------------------------------------------------------
- * Continuous batching of skeleton requests (no reference counterpart). A
- * scheduler thread admits the requests that have arrived, in arrival order, as one
- * batch (a context whose level kernels run once for all its instances) while the
- * device bytes in flight (hpc_ctx_footprint per request) stay within budget_bytes
- * and fewer than max_inflight batches run; every batch runs on its own worker
- * thread and CUDA stream, so batches admitted while others are on the GPU overlap
- * with them. Each request's data stay resident on the device until its batch is
- * done. */
+ * Continuous batching of skeleton requests (no reference counterpart; the
+ * reference's level loop is src/independence/skeleton.cpp:152-190). One engine
+ * thread runs steps: in a step, the requests standing at the same level share one
+ * launch of that level's kernels (the kernels run over a table of instances), and
+ * requests at different levels run as consecutive launches of the step. After each
+ * step every request moves on to its next level or completes, and requests that
+ * arrived meanwhile are admitted -- in arrival order, while the device bytes of the
+ * admitted requests (hpc_ctx_footprint without the re-test queue, which the engine
+ * shares) stay within budget_bytes -- and join at level 0 in the next step, while
+ * the others continue. Each request's data stay resident on the device from its
+ * admission to its completion. */
 typedef struct hpc_server hpc_server;
 typedef struct hpc_server_opts {
   int device;
   int precision;          /* default HPC_PREC_MIXED_TC */
-  int max_level;          /* default 4 */
+  int max_level;          /* default 4; -1 = until no edge has enough neighbours */
   int64_t budget_bytes;   /* device bytes admitted at once (default 150 GB) */
-  int max_batch;          /* requests per batch (default 64) */
-  int max_inflight;       /* batches on the device at once (default 4) */
+  int max_batch;          /* most requests on the device at once (default 256) */
+  int max_inflight;       /* most requests admitted between two steps (default 32) */
 } hpc_server_opts;
 typedef struct hpc_served {
   int64_t id;
   int32_t status;         /* hpc_status of the request */
   int32_t levels;         /* levels run */
   int64_t edges;          /* undirected edges of its skeleton */
-  double queue_ms;        /* submit -> its batch started */
-  double run_ms;          /* batch start -> results copied */
+  double queue_ms;        /* submit -> admitted */
+  double run_ms;          /* admitted -> results copied */
   double latency_ms;      /* submit -> results copied */
-  int32_t batch_size;
-  int32_t pad;
+  int32_t batch_size;     /* most requests that shared one of its level launches */
+  int32_t joined;         /* requests already running when it was admitted */
 } hpc_served;
 hpc_status hpc_server_opts_default(hpc_server_opts *opts);
 hpc_status hpc_server_create(hpc_server **out, const hpc_server_opts *opts);

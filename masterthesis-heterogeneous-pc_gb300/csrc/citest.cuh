@@ -293,11 +293,13 @@ struct Fact {
 // i, j and the unchanged first ci members of S). Returns 1 = remove, 0 = keep,
 // 2 = undecided (re-test in FP64): |r| is compared with r_c outside a band of
 // margin_r + 8 * ke(l) / smallest pivot. *rr_out receives |r|.
+// The entries are read from C at [x * stride + y]: the instance's FP32 matrix with
+// variable ids (C = cor32, stride = p, xi = i, xj = j, xs = ids), or a row's block
+// staged in shared memory with block-local indices (a generic pointer; the same FP32
+// values, so the same decisions).
 template <int LA>
-__device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j, const int *ids, int l, int ci,
-                                            Fact<LA> &F, float *rr_out) {
-  const float *__restrict__ C = I.cor32;
-  const int64_t p = I.p;
+__device__ __forceinline__ int test_f32_inc(const Inst &I, const float *__restrict__ C, int64_t stride, int64_t xi,
+                                            int64_t xj, const int *xs, int l, int ci, Fact<LA> &F, float *rr_out) {
   // unrolled levels (LA <= 8): all entries the changed rows need are gathered before
   // any arithmetic (one round of independent loads instead of one per factor row); the
   // generic level kernel loads row by row (its 16-wide arrays would live in local
@@ -309,27 +311,27 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
 #pragma unroll (kUnr<LA>)
     for (int r = 0; r < LA; ++r) {
       if (r >= ci && r < l) {
-        const int idr = ids[r];
-        gx[r] = __ldg(C + i * p + idr);
-        gy[r] = __ldg(C + j * p + idr);
+        const int64_t xr = xs[r];
+        gx[r] = C[xi * stride + xr];
+        gy[r] = C[xj * stride + xr];
 #pragma unroll (kUnr<LA>)
         for (int c = 0; c < LA; ++c)
-          if (c < r) gs[r * (r - 1) / 2 + c] = __ldg(C + (int64_t)ids[c] * p + idr);
+          if (c < r) gs[r * (r - 1) / 2 + c] = C[(int64_t)xs[c] * stride + xr];
       }
     }
   }
-  const float rij = __ldg(C + i * p + j);
+  const float rij = C[xi * stride + xj];
 #pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r) {
     if (r >= ci && r < l) {
-      const int idr = ids[r];
+      const int64_t xr = xs[r];
       float vx, vy;
       if constexpr (kGather) {
         vx = gx[r];
         vy = gy[r];
       } else {
-        vx = __ldg(C + i * p + idr);
-        vy = __ldg(C + j * p + idr);
+        vx = C[xi * stride + xr];
+        vy = C[xj * stride + xr];
       }
       float d = 1.0f;
 #pragma unroll (kUnr<LA>)
@@ -339,7 +341,7 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
           if constexpr (kGather)
             v = gs[r * (r - 1) / 2 + c];
           else
-            v = __ldg(C + (int64_t)ids[c] * p + idr);
+            v = C[(int64_t)xs[c] * stride + xr];
 #pragma unroll (kUnr<LA>)
           for (int q = 0; q < LA; ++q)
             if (q < c) v -= F.Lm[r * (r + 1) / 2 + q] * F.Lm[c * (c + 1) / 2 + q];
@@ -378,6 +380,30 @@ __device__ __forceinline__ int test_f32_inc(const Inst &I, int64_t i, int64_t j,
   const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
   if (!(fabsf(dist) > band)) return 2;
   return dist < 0.0f ? 1 : 0;
+}
+
+// Rows of degree up to kBlkD have their correlation block -- the row variable and its
+// neighbours, (d + 1)^2 FP32 entries -- staged in shared memory by the warp whose tile
+// starts in the row (levels 2-16 of the mixed-precision kernels): every test of the row
+// reads only that block (the row, the edge's other end and the conditioning set are all
+// among them), so the gathers of a test come from shared memory instead of L2/HBM.
+// Block-local index 0 is the row itself, k + 1 its k-th neighbour in the snapshot.
+constexpr int kBlkD = 31, kBlkS = kBlkD + 1;
+
+// Stage the block of row i of instance I (whole warp, converged; d + 1 <= 32 lanes hold
+// the block's variable ids): row a of the block is one gather of d + 1 entries.
+__device__ __forceinline__ void stage_block(const Inst &I, int64_t i, int d, float *__restrict__ B) {
+  const int lane = threadIdx.x & 31;
+  const int base = I.rowptr[i];
+  const int gid = lane == 0 ? (int)i : (lane <= d ? I.colidx[base + lane - 1] : 0);
+  const float *__restrict__ C = I.cor32;
+  __syncwarp();
+#pragma unroll 4
+  for (int a = 0; a <= d; ++a) {
+    const int ga = __shfl_sync(0xffffffffu, gid, a);
+    if (lane <= d) B[a * kBlkS + lane] = __ldg(C + (int64_t)ga * I.p + gid);
+  }
+  __syncwarp();
 }
 
 __device__ __forceinline__ int64_t find_row(const unsigned long long *row_work, int64_t p, unsigned long long t) {
@@ -625,6 +651,12 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   __shared__ PendRem<LA> s_pend[kThreads / 32][kPend];
   __shared__ int s_np[kThreads / 32];
+  // the staged correlation block of the warp (levels 2-16, mixed precision)
+  constexpr bool kBlk = MIXED && LT >= 2 && LT <= 16;
+  __shared__ float s_blk[kBlk ? kThreads / 32 : 1][kBlk ? kBlkS * kBlkS : 1];
+  float *blk = s_blk[kBlk ? wib : 0];
+  int64_t blk_i = -1;  // row and instance of the staged block
+  int blk_b = -1;
   PendRem<LA> *pend = s_pend[wib];
   int *np = s_np + wib;
   if (lane == 0) *np = 0;
@@ -658,6 +690,14 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
     const Inst *I = inst_of(L, b);
     unsigned long long base_t = L.work_prefix[b];
     const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
+    if (kBlk && (i0 != blk_i || b != blk_b)) {  // the block of the tile's first row
+      const int d0 = I->deg[i0];
+      if (d0 <= kBlkD) {
+        stage_block(*I, i0, d0, blk);
+        blk_i = i0;
+        blk_b = b;
+      }
+    }
     const bool active = t < tend;
     const bool same = t < L.work_prefix[b + 1];
     int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
@@ -690,7 +730,17 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
             if (q < l && q >= ci) ids[q] = I->colidx[base + pos[q] + (pos[q] >= s ? 1 : 0)];
           int res = 2;
           float rr = 0.f;
-          if (MIXED) res = test_f32_inc<LA>(*I, i, j, ids, l, ci, F, &rr);
+          if (MIXED) {
+            if (kBlk && i == blk_i && b == blk_b) {  // from the staged block, block-local indices
+              int lids[LA];
+#pragma unroll (kUnr<LA>)
+              for (int q = 0; q < LA; ++q)
+                if (q < l) lids[q] = pos[q] + (pos[q] >= s ? 1 : 0) + 1;
+              res = test_f32_inc<LA>(*I, blk, kBlkS, 0, s + 1, lids, l, ci, F, &rr);
+            } else {
+              res = test_f32_inc<LA>(*I, I->cor32, I->p, i, j, ids, l, ci, F, &rr);
+            }
+          }
           ci = l;
           ++executed;
           ++tested_edge;

@@ -591,6 +591,21 @@ long long retest_queue_cap(long long sum_p2) {
   return std::min<long long>(16ll << 20, std::max<long long>(1ll << 20, sum_p2 / 16));
 }
 
+// The deferred FP64 re-test queue, allocated before the first run of a context
+// without an FP64 matrix (tensor-core mode); contexts whose levels run elsewhere (the
+// server's shared launches bring their own queue) never allocate it.
+hpc_status ensure_rq(hpc_ctx *c) {
+  if (c->rq || c->cor64_valid) return HPC_OK;
+  long long p2 = 0;
+  for (const auto &h : c->ih) p2 += h.p * h.p;
+  const long long cap = retest_queue_cap(p2);
+  hpc_status s;
+  if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
+  c->rq_cap = cap;
+  ++c->inst_version;  // a captured graph holds the queue pointer
+  return HPC_OK;
+}
+
 hpc_status after_correlation(hpc_ctx *c) {
   c->have_cor = true;
   hpc_status s = write_inst_table(c);
@@ -631,13 +646,6 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
       HPC_CUDA(cudaMemcpyAsync(c->tc_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
                                c->stream));
       HPC_CUDA(cudaStreamSynchronize(c->stream));
-    }
-    if (!c->rq) {
-      long long p2 = 0;
-      for (const auto &h : c->ih) p2 += h.p * h.p;
-      const long long cap = retest_queue_cap(p2);
-      if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
-      c->rq_cap = cap;
     }
     if ((s = launch_standardise(X, f32, sa, sa.count ? c->total_rows : 0, c->Z, c->tcP, c->tcQ, c->stream)) != HPC_OK)
       return s;
@@ -727,6 +735,16 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
                   const hpc_opts *opts);
 
 }  // namespace
+
+// for the server's shared launches (serve.cu)
+hpc_status ctx_size_after_level0(hpc_ctx *c) {
+  bool changed = false;
+  return ensure_capacity(c, &changed);
+}
+long long ctx_retest_queue_bytes(long long sum_p2) {
+  return retest_queue_cap(sum_p2) * (long long)sizeof(RetestItem);
+}
+
 }  // namespace hpc
 
 using namespace hpc;
@@ -1078,6 +1096,7 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     set_error("level %d above the context's max_level %d", level, c->opts.max_level);
     return HPC_ERR_INVALID_ARG;
   }
+  if ((s = ensure_rq(c)) != HPC_OK) return s;
   if (level == 1) {
     bool changed = false;
     if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
@@ -1155,6 +1174,7 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
     if (levels_run) *levels_run = ran;
     return HPC_OK;
   }
+  if ((s = ensure_rq(c)) != HPC_OK) return s;
   HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
   for (int attempt = 0; attempt < 2; ++attempt) {
     ran = 0;
@@ -1211,6 +1231,7 @@ hpc_status hpc_run_skeleton_async(hpc_ctx *c) {
     if ((s = hpc_ctx_reset(c)) != HPC_OK) return s;
     return hpc_run_skeleton(c, nullptr, 0, nullptr);
   }
+  if ((s = ensure_rq(c)) != HPC_OK) return s;
   // until exhausted: the previous run's extent, continued by hpc_wait if the data now
   // reach further
   const int top = known ? c->opts.max_level : c->exhaust_top;

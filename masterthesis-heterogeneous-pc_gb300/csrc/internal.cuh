@@ -283,6 +283,12 @@ long long tune_version();
 void tune_store(int64_t p, int level, int max_degree, const TuneEntry &e);
 TuneEntry tune_get(int p_bucket, int level, int deg_bucket);  // by bucket indices
 
+// used by the server's shared launches (serve.cu): a context's neighbour-list and
+// record buffers sized from its level-0 counters (ctr_host filled by the caller), and
+// the bytes of the re-test queue a context of sum p^2 would hold
+hpc_status ctx_size_after_level0(hpc_ctx *c);
+long long ctx_retest_queue_bytes(long long sum_p2);
+
 // per-instance host bookkeeping
 struct InstHost {
   int64_t p = 0, n = 0;

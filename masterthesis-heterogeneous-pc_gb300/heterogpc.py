@@ -67,7 +67,7 @@ class ServerOpts(C.Structure):
 class Served(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("levels", C.c_int32), ("edges", C.c_int64),
                 ("queue_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
-                ("batch_size", C.c_int32), ("pad", C.c_int32)]
+                ("batch_size", C.c_int32), ("joined", C.c_int32)]
 
 
 class TuneParams(C.Structure):
@@ -669,8 +669,8 @@ class SkeletonBatch:
 class SkeletonServer:
     """Continuous-batching skeleton server (hpc_server_* in include/heterogpc.h)."""
 
-    def __init__(self, precision=PREC_MIXED_TC, max_level=4, budget_bytes=150 * 10**9, max_batch=64,
-                 max_inflight=4, device=0):
+    def __init__(self, precision=PREC_MIXED_TC, max_level=4, budget_bytes=150 * 10**9, max_batch=256,
+                 max_inflight=32, device=0):
         o = ServerOpts()
         lib().hpc_server_opts_default(C.byref(o))
         o.device, o.precision, o.max_level = device, precision, max_level
@@ -699,7 +699,8 @@ class SkeletonServer:
         for r in arr[:k.value]:
             X, adj = self._keep.pop(r.id)
             out.append(dict(id=r.id, status=r.status, levels=r.levels, edges=r.edges, queue_ms=r.queue_ms,
-                            run_ms=r.run_ms, latency_ms=r.latency_ms, batch_size=r.batch_size, adjacency=adj))
+                            run_ms=r.run_ms, latency_ms=r.latency_ms, batch_size=r.batch_size, joined=r.joined,
+                            adjacency=adj))
         return out
 
     def drain(self):

@@ -22,8 +22,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["citest_l17.cu", "citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
-              "noalloc.cu", "tune.cu", "compat.cu"]
-HOST_SOURCES = ["semgen.cpp", "serve.cpp"]
+              "noalloc.cu", "tune.cu", "compat.cu", "serve.cu"]
+HOST_SOURCES = ["semgen.cpp"]
 
 
 def _run(cmd):

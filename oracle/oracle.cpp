@@ -103,6 +103,7 @@ struct State {
   int64_t p = 0;
   int n = 0;
   double alpha = 0.05;
+  double r_crit = 2.0;              // |r| with calc_pvalue == alpha
   std::vector<double> cor;          // p x p row-major
   std::vector<uint8_t> adj;         // p x p, live
   std::vector<std::vector<int>> compact;  // snapshot neighbour lists (ascending)
@@ -168,8 +169,71 @@ void test_l1(State &s, int row, int col_slot) {
   s.tests.fetch_add(tests, std::memory_order_relaxed);
 }
 
-// cpuRowTests.cpp:58-136 for any level (as cpuWorkstealingTests.cpp:39-112),
-// subsets in ascending rank order as the row variant.
+// |r| at which calc_pvalue == alpha (p is decreasing in |r|); 2 when every r is removed
+double r_crit_for(double alpha, int n) {
+  double lo = 0.0, hi = kCutThr;
+  if (calc_pvalue(hi, n) >= alpha) return 2.0;
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (calc_pvalue(mid, n) >= alpha) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// The test's decision p >= alpha from the k x k submatrix M (ordered i, j, S), with the
+// reference's pinv formula (cpuInd.cpp:29-38) wherever it can matter: the partial
+// correlation is formed by Cholesky of the S block in FP64 and decides only when the
+// block is well conditioned (every pivot above 1e-8) and |r| lies outside 1e-8 relative
+// of r_crit (p is monotone in |r|); otherwise, and for the p-value of every removal
+// (*pv), pval_ln decides. A Cholesky |r| of a well-conditioned block differs from the
+// pinv one by orders of magnitude less than that band, so the decisions are pval_ln's.
+bool test_removes(const double *M, int k, int n, double alpha, double rc, double *pv) {
+  const int l = k - 2;
+  double Lm[kMaxLevel * kMaxLevel], wx[kMaxLevel], wy[kMaxLevel];
+  bool ok = true;
+  for (int i = 0; i < k * k && ok; ++i) ok = !std::isnan(M[i]);
+  for (int r = 0; r < l && ok; ++r) {
+    double vx = M[(r + 2) * k + 0], vy = M[(r + 2) * k + 1], d = 1.0;
+    for (int c = 0; c < r; ++c) {
+      double v = M[(c + 2) * k + (r + 2)];
+      for (int q = 0; q < c; ++q) v -= Lm[r * kMaxLevel + q] * Lm[c * kMaxLevel + q];
+      v /= Lm[c * kMaxLevel + c];
+      Lm[r * kMaxLevel + c] = v;
+      d -= v * v;
+      vx -= v * wx[c];
+      vy -= v * wy[c];
+    }
+    if (!(d > 1e-8)) {
+      ok = false;
+      break;
+    }
+    Lm[r * kMaxLevel + r] = std::sqrt(d);
+    wx[r] = vx / Lm[r * kMaxLevel + r];
+    wy[r] = vy / Lm[r * kMaxLevel + r];
+  }
+  if (ok) {
+    double ax = 1.0, ay = 1.0, b = M[1];
+    for (int q = 0; q < l; ++q) {
+      ax -= wx[q] * wx[q];
+      ay -= wy[q] * wy[q];
+      b -= wx[q] * wy[q];
+    }
+    if (ax > 1e-8 && ay > 1e-8) {
+      const double r = std::fabs(b / std::sqrt(ax * ay));
+      if (r > rc * (1.0 + 1e-8)) return false;  // p < alpha: kept, no p-value needed
+      if (r < rc * (1.0 - 1e-8)) {
+        *pv = pval_ln(M, k, n);
+        return true;
+      }
+    }
+  }
+  *pv = pval_ln(M, k, n);
+  return *pv >= alpha;
+}
+
+// cpuRowTests.cpp:58-136 for any level (as cpuWorkstealingTests.cpp:39-112), subsets in
+// ascending rank order as the row variant: the first subset by ith_combination
+// (cuda_util.cu:34-50), each further one as the lexicographic successor (the next rank).
 void test_ln(State &s, int level, int row, int col_slot) {
   const std::vector<int> &nb = s.compact[row];
   int row_count = (int)nb.size();
@@ -177,15 +241,21 @@ void test_ln(State &s, int level, int row, int col_slot) {
   int col = nb[col_slot];
   int row_neighbours = row_count - 1;
   uint64_t count = binom(row_neighbours, level);
-  int sep[kMaxLevel];
+  int pos[kMaxLevel], sep[kMaxLevel];
   const int k = level + 2;
   double M[(kMaxLevel + 2) * (kMaxLevel + 2)];
   int64_t tests = 0;
   const int64_t p = s.p;
+  if (count > 0) ith_combination(pos, 0, level, row_neighbours);  // 1-based positions 1..level
   for (uint64_t t = 0; t < count; ++t) {
-    ith_combination(sep, t, level, row_neighbours);
+    if (t > 0) {  // lexicographic successor of pos over 1..row_neighbours
+      int q = level - 1;
+      while (q >= 0 && pos[q] == row_neighbours - level + q + 1) --q;
+      ++pos[q];
+      for (int r = q + 1; r < level; ++r) pos[r] = pos[r - 1] + 1;
+    }
     for (int ind = 0; ind < level; ++ind)
-      sep[ind] = (sep[ind] - 1 >= col_slot) ? nb[sep[ind]] : nb[sep[ind] - 1];
+      sep[ind] = (pos[ind] - 1 >= col_slot) ? nb[pos[ind]] : nb[pos[ind] - 1];
     for (int i = 0; i < k * k; ++i) M[i] = 0.0;
     for (int i = 0; i < k; ++i) M[i * k + i] = 1.0;
     M[1] = M[k] = s.cor[row * p + col];
@@ -197,8 +267,8 @@ void test_ln(State &s, int level, int row, int col_slot) {
       for (int j = i + 1; j < k; ++j)
         M[i * k + j] = M[j * k + i] = s.cor[(int64_t)sep[i - 2] * p + sep[j - 2]];
     ++tests;
-    double pv = pval_ln(M, k, s.n);
-    if (pv >= s.alpha) {
+    double pv = 0.0;
+    if (test_removes(M, k, s.n, s.alpha, s.r_crit, &pv)) {
       delete_edge(s, level, col, row, pv, sep);
       break;
     }
@@ -375,17 +445,6 @@ void orc_verify_sepsets(const double *C, int64_t p, int n, double alpha, int64_t
 }
 
 namespace {
-// |r| at which calc_pvalue == alpha (p is decreasing in |r|); 2 when every r is removed
-double r_crit_of(double alpha, int n) {
-  double lo = 0.0, hi = kCutThr;
-  if (calc_pvalue(hi, n) >= alpha) return 2.0;
-  for (int it = 0; it < 200; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (calc_pvalue(mid, n) >= alpha) lo = mid; else hi = mid;
-  }
-  return 0.5 * (lo + hi);
-}
-
 // Does the subset S (|S| = l >= 2) separate i and j? The partial correlation by
 // Cholesky of the S block in FP64; where the block is ill-conditioned or |r| lies within
 // 1e-8 relative of r_crit, the reference's pinv formula (pval_ln) decides.
@@ -443,7 +502,7 @@ bool separates(const double *C, int64_t p, int n, double alpha, double rc, int64
 // max_subsets subsets in a direction).
 void orc_check_retained(const double *C, int64_t p, int n, double alpha, int level, const uint8_t *adj_before,
                         int64_t k, const int32_t *edges, int64_t max_subsets, int8_t *status) {
-  const double rc = r_crit_of(alpha, n);
+  const double rc = r_crit_for(alpha, n);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t t = 0; t < k; ++t) {
     const int64_t ends[2] = {edges[2 * t], edges[2 * t + 1]};
@@ -491,6 +550,7 @@ orc_result *orc_run(const double *C, int64_t p, int n_obs, double alpha, int max
   s.p = p;
   s.n = n_obs;
   s.alpha = alpha;
+  s.r_crit = r_crit_for(alpha, n_obs);
   s.cor.assign(C, C + p * p);
   s.adj.assign((size_t)(p * p), 1);  // state.cu:31-36
   for (int64_t i = 0; i < p; ++i) s.adj[i * p + i] = 0;

@@ -12,10 +12,10 @@ the data, the number of edges after every level, the SHA-256 of the final adjace
 single-thread seconds (the CPU legs of bench.py order instances by it). The GPU test
 (tests/test_gpu_c4_parity.py) recomputes the same hashes from the device results.
 
-The oracle's cost per instance ranges from milliseconds to over an hour (levels up
-to 20 on the densest p ~ 800 instances), so the instances run in parallel, one per
-host core, most expensive first; finished instances are appended to a progress file
-next to the fixture so that an interrupted run resumes.
+The oracle's cost per instance ranges from milliseconds to minutes (levels up to 21
+on the p ~ 800 instances), so the instances run in parallel, one per host core, most
+expensive first; finished instances are appended to a progress file next to the
+fixture so that an interrupted run resumes.
 
 Run from the repository root:   python tests/golden/make_c4_golden.py [--jobs N]
 """

@@ -58,5 +58,6 @@ def test_async_until_exhausted_after_a_first_run():
         sk.run_async()
     st = sk.wait()
     assert np.array_equal(sk.adjacency(), want.adj)
-    assert [s["edges_after"] for s in st] == [l["edges_after"] for l in want.levels][:len(st)]
+    # the device's list ends with the first level without tests, the oracle's before it
+    assert [s["edges_after"] for s in st][:len(want.levels)] == [l["edges_after"] for l in want.levels]
     sk.close()
