@@ -50,7 +50,7 @@ WORKLOADS = {
     # [500, 20000], ER degree 3 / preferential attachment (2 parents) alternating,
     # alpha 0.01, FP32 data, admission under a 150 GB device budget
     "c5": dict(requests=2000, pool=400, rate=200.0, p=(30, 5000), n=(500, 20000), degree=3.0, pa_parents=2,
-               w_lo=0.1, w_hi=1.0, alpha=0.01, seed=5, budget=150 * 10**9, max_level=-1),
+               w_lo=0.1, w_hi=1.0, alpha=0.01, seed=5, budget=150 * 10**9, max_level=4),
     "c4": dict(count=512, p=(20, 800), n=(200, 8000), degree=(1.0, 5.0), w_lo=0.1, w_hi=1.0, seed=4,
                alphas=(0.01, 0.05), max_level=-1),
     # wide, hub-heavy: preferential attachment (2 parents per new node), p=15000, n=3000,
@@ -381,11 +381,15 @@ def c4_golden():
 
 
 def c4_slices(count, costs, k):
-    """Instances in k slices of equal share of the cost: instance ranks in decreasing cost
-    order taken round robin (rank r goes to slice r mod k), so every slice is a systematic
-    sample of the whole batch's cost distribution."""
+    """Instances in k slices of about equal cost: instances in decreasing cost order dealt
+    to the slices back and forth (0..k-1, then k-1..0, ...), so every slice is a
+    systematic sample of the whole batch's cost distribution."""
     order = sorted(range(count), key=lambda b: -costs[b]) if costs else list(range(count))
-    return [order[q::k] for q in range(k)]
+    out = [[] for _ in range(k)]
+    for r, b in enumerate(order):
+        q = r % k
+        out[q if (r // k) % 2 == 0 else k - 1 - q].append(b)
+    return out
 
 
 def level_model_bytes(degs, level, executed, p, lane_bytes=4):
@@ -481,6 +485,7 @@ def run_c4(args, wl):
     clocks.start()
     torch.cuda.synchronize()
     evs = []
+    torch.cuda.nvtx.range_push("timed")  # the launch-list profile filters on this range
     for _ in range(args.steps):
         flush()
         a, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -490,6 +495,7 @@ def run_c4(args, wl):
         evs.append((a, b_))
     st = bt.wait()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     ms = [a.elapsed_time(b_) for a, b_ in evs]
     launches = bt.timings()["launches"] - launches0
@@ -670,21 +676,22 @@ def c4_cpu_slice(slice_, cores):
     return tot, tests, hashes
 
 
-# budget of the CPU legs: about 20 s of CPU work for the cpu_baseline sample and per
-# reference step; the slices are systematic samples of the batch's cost distribution
+# budget of the CPU legs: about 20 s of CPU work for the cpu_baseline sample, at most 8 s
+# per reference step; the slices are systematic samples of the batch's cost distribution
 C4_CPU_SAMPLE_S = 20.0
+C4_REF_STEP_S = 8.0
 
 
-def c4_cpu_plan(count, cores, budget_s):
+def c4_cpu_plan(count, cores, budget_s, min_slices=1):
     """Slices of the batch for the CPU legs: the committed oracle results give every
     instance's single-thread cost (measured on the machine that made them); a slice holds
     about budget_s seconds of work on `cores` cores at a parallel efficiency of the row
-    loop taken as 0.6."""
+    loop taken as 0.6, and there are at least min_slices of them."""
     gold = c4_golden()
     costs = [g["oracle_s"] for g in gold["instances"]] if gold and "oracle_s" in gold["instances"][0] else None
     total = sum(costs) if costs else None
     k = max(1, int(np.ceil(total / (budget_s * cores * 0.6)))) if total else 32
-    return c4_slices(count, costs, k), total
+    return c4_slices(count, costs, max(k, min_slices)), total
 
 
 def c4_cpu_baseline(wl, count):
@@ -702,19 +709,22 @@ def c4_cpu_baseline(wl, count):
 def run_reference_c4(args, wl):
     """The reference CPU path (the oracle port; the reference's own sources cannot be built
     on the GPU host) on the batched workload: each timed step runs one slice of the batch
-    (a systematic sample of its cost distribution, sized to about 20 s on the host's
-    cores); the K timed steps take K different slices. Warm-up steps run a few of the
+    (a systematic sample of its cost distribution); the K timed steps take K different
+    slices, which together are the whole batch when a K-th of it fits C4_REF_STEP_S on
+    the host's cores, else a systematic sample of it. Warm-up steps run a few of the
     cheapest instances."""
     cores = os.cpu_count()
     count = wl["count"]
-    slices, _ = c4_cpu_plan(count, cores, C4_CPU_SAMPLE_S)
+    # K timed steps cover K slices; as many slices as steps (each about a K-th of the
+    # batch) unless that makes a step longer than C4_REF_STEP_S, then more, smaller ones
+    slices, _ = c4_cpu_plan(count, cores, C4_REF_STEP_S, min_slices=args.steps)
     gold = c4_golden()
     cheap = sorted(range(count), key=lambda b: gold["instances"][b].get("oracle_s", 0))[:4] if gold else [0, 1]
     for _ in range(args.warmup):
         c4_cpu_slice(cheap, cores)
     times, tests, done, same = [], 0, 0, 0
     for k in range(args.steps):
-        sl = slices[(len(slices) // 2 + k) % len(slices)]
+        sl = slices[k % len(slices)]
         dt, t, hashes = c4_cpu_slice(sl, cores)
         times.append(dt)
         tests += t
@@ -894,7 +904,7 @@ def main():
     ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=None, help="c4: number of instances (default 512)")
-    ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3); c5: (default none)")
+    ap.add_argument("--max-level", type=int, default=None, help="c3: level cap (default 3); c5: (default 4)")
     ap.add_argument("--p", type=int, default=None, help="c3: variables (default 15000; smaller for profiling)")
     ap.add_argument("--cross-check", action="store_true",
                     help="c3: also run the plain FP64 path once and compare the skeletons")

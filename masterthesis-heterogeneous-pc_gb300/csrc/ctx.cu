@@ -666,16 +666,30 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
   } else {
     if ((s = launch_standardise(X, f32, sa, c->total_rows, c->Z, nullptr, nullptr, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
-    if ((s = launch_gram_f64(c->Z, c->cor64, gram_args(c), c->tiles64, c->stream)) != HPC_OK) return s;
-    HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
-    c->timings.launches += 2;
     c->cor64_valid = true;
     c->cor32_rounded = true;
-    if (c->opts.precision == HPC_PREC_MIXED) {
-      long long tot = 0;
-      for (const auto &h : c->ih) tot += h.p * h.p;
-      if ((s = launch_to_f32(c->cor64, tot, c->cor32, c->stream)) != HPC_OK) return s;
-      c->timings.launches += 1;
+    // FP64-accurate correlation: on the tensor cores by exact digits where that serves
+    // (mixed precision, one instance of a few hundred variables or more), else the
+    // FP64 SIMT Gram (the plain path, batches, small problems)
+    const InstHost &h0 = c->ih[0];
+    if (c->opts.precision == HPC_PREC_MIXED && c->count == 1 && emu_eligible(h0.p, h0.n)) {
+      if (!c->emuD && (s = dev_alloc(&c->emuD, emu_digit_elems(h0.p, h0.n), "digit planes")) != HPC_OK) return s;
+      if (!c->emuE && (s = dev_alloc(&c->emuE, emu_p_pad(h0.p), "digit exponents")) != HPC_OK) return s;
+      if ((s = launch_gram_emu(c->Z, h0.p, h0.n, denom_of(c, h0.n), c->emuD, c->emuE, nullptr, c->cor64, c->cor32,
+                               &c->gctr[0].err, c->stream)) != HPC_OK)
+        return s;
+      HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+      c->timings.launches += 3;
+    } else {
+      if ((s = launch_gram_f64(c->Z, c->cor64, gram_args(c), c->tiles64, c->stream)) != HPC_OK) return s;
+      HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
+      c->timings.launches += 2;
+      if (c->opts.precision == HPC_PREC_MIXED) {
+        long long tot = 0;
+        for (const auto &h : c->ih) tot += h.p * h.p;
+        if ((s = launch_to_f32(c->cor64, tot, c->cor32, c->stream)) != HPC_OK) return s;
+        c->timings.launches += 1;
+      }
     }
   }
   HPC_CUDA(cudaEventRecord(c->evc[3], c->stream));
@@ -833,6 +847,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->Z);
   dev_free(c->tcP);
   dev_free(c->tcQ);
+  dev_free(c->emuD);
+  dev_free(c->emuE);
   dev_free(c->tc_maps);
   {
     uint8_t *xs = (uint8_t *)c->X_stage;

@@ -44,6 +44,7 @@
 #include <cuda_runtime.h>
 
 #include "internal.cuh"
+#include "tc_common.cuh"
 
 namespace hpc {
 namespace {
@@ -59,102 +60,6 @@ constexpr int kGroup = 4;        // k-blocks (16 MMAs) per accumulation group
 constexpr int kAccWarps = 8;     // two per TMEM lane quadrant, 128 columns each
 constexpr int kBand = 16;        // row blocks per band of the tile order (even)
 constexpr int kThreadsTc = 64 + 32 * kAccWarps;  // producer warp, MMA warp, accumulator warps
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait on the phase with the given parity; false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const unsigned long long t0 = global_ns();
-  for (;;) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - t0 > kWaitNs) return false;
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
-// 1024 bytes (stride byte offset), descriptor version bits 46-48 = 0b001.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)(16u >> 4) << 16;
-  d |= (uint64_t)(1024u >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-
-// Instruction descriptor of tcgen05.mma.kind::f16: D = F32, A = B = BF16, both
-// K-major, N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
-                            ((uint32_t)(TM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 
 // operand rows padded to the column-block size, so that every TMA box lies inside
 __host__ __device__ __forceinline__ int64_t tc_p_pad_dev(int64_t p) { return (p + TN - 1) / TN * TN; }
@@ -278,7 +183,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
 #pragma unroll
         for (int k = 0; k < TK / 16; ++k) {
           // 16 bf16 = 32 bytes further along K inside the 128-byte swizzled row
-          mma_bf16(dcol, smem_desc_sw128(a0 + k * 32), smem_desc_sw128(b0 + k * 32),
+          mma_bf16(dcol, smem_desc_sw128(a0 + k * 32), smem_desc_sw128(b0 + k * 32), idesc_bf16(TM, TN),
                    (kb > g * kGroup || k > 0) ? 1u : 0u);
         }
         mma_commit(&sm.empty[s]);
@@ -415,6 +320,12 @@ long long gram_tc_tiles(int64_t p) {
 }
 
 // Tensor maps of one instance's operands P and Q (tc_p_pad(p) rows of tc_k(n) bf16).
+// a 2-D BF16 tensor map (rows x K, K contiguous, 64-column x box_rows boxes, 128-byte
+// swizzle) for the other tensor-core kernels
+hpc_status tc_make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int64_t K, int box_rows) {
+  return make_map(m, base, rows, K, box_rows);
+}
+
 hpc_status tc_make_maps(CUtensorMap *mp, CUtensorMap *mq, const __nv_bfloat16 *P, const __nv_bfloat16 *Q,
                         int64_t p, int64_t n) {
   hpc_status st;

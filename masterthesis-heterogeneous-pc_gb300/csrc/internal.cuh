@@ -255,6 +255,16 @@ struct TcArgs {                     // grouped tensor-core Gram
   int *err;
 };
 hpc_status launch_gram_tc(float *C, const TcArgs &a, long long total_tiles, cudaStream_t s);
+hpc_status tc_make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int64_t K, int box_rows);
+// FP64-accurate Gram on the tensor cores (gram_emu.cu): C64 (and C32 when not null) =
+// Z^T Z / denom for one instance's standardised data Z (n x p, each variable
+// contiguous). D (digits) and E (exponents) are its work buffers of emu_digit_elems /
+// emu_p_pad elements.
+bool emu_eligible(int64_t p, int64_t n);
+int64_t emu_p_pad(int64_t p);
+int64_t emu_digit_elems(int64_t p, int64_t n);
+hpc_status launch_gram_emu(const double *Z, int64_t p, int64_t n, double denom, __nv_bfloat16 *D, int *E,
+                           CUtensorMap *map_host_scratch, double *C64, float *C32, int *err, cudaStream_t s);
 
 hpc_status launch_level0(const Launch &L, long long total_tiles, cudaStream_t s);
 hpc_status launch_degrees(const Launch &L, long long total_rows, cudaStream_t s);
@@ -317,6 +327,8 @@ struct hpc_ctx {
   float *cor32 = nullptr;         // sum p^2 (mixed modes)
   double *Z = nullptr;            // sum n * p
   __nv_bfloat16 *tcP = nullptr, *tcQ = nullptr;  // split-BF16 operands, sum p_pad * K'
+  __nv_bfloat16 *emuD = nullptr;  // exact digit planes of the FP64-accurate tensor-core Gram
+  int *emuE = nullptr;            // ... and the variables' exponents
   CUtensorMap *tc_maps = nullptr;  // device, 2 per instance
   void *X_stage = nullptr;        // device copy of host observations
   int64_t X_stage_bytes = 0;

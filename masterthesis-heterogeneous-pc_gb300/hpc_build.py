@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["citest_l17.cu", "citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
-              "noalloc.cu", "tune.cu", "compat.cu", "serve.cu"]
+              "noalloc.cu", "tune.cu", "compat.cu", "serve.cu", "gram_emu.cu"]
 HOST_SOURCES = ["semgen.cpp"]
 
 
@@ -107,15 +107,19 @@ def build_oracle():
     return so
 
 
+# where the reference tree is mounted in the build container (REF_ROOT overrides it)
+REFERENCE_MOUNT = "/root/reference"
+
+
 def build_reference_pin():
     """oracle/_ref/libref_cpu.so from the reference sources, only where they exist."""
-    ref = os.environ.get("REF_ROOT", "/root/reference")
+    ref = os.environ.get("REF_ROOT", REFERENCE_MOUNT)
     if not os.path.isdir(os.path.join(ref, "src")):
         return None
     out = os.path.join(ORACLE, "_ref", "libref_cpu.so")
     if os.path.exists(out):
         return out
-    _run(["bash", os.path.join(ORACLE, "build_ref.sh")])
+    _run(["bash", os.path.join(ORACLE, "build_ref.sh"), ref])
     return out
 
 

@@ -1,7 +1,8 @@
 #!/bin/bash
 # ORACLE -- test infrastructure only.
 # Builds oracle/_ref/libref_cpu.so from the reference's own CPU test sources where
-# they lie (REF_ROOT, default /root/reference), compiled against the stand-in
+# they lie (the reference tree's root: the first argument, else REF_ROOT; one of them
+# is required), compiled against the stand-in
 # headers in oracle/ref_shim/ (Armadillo pinv and Boost normal cdf restated), plus
 # oracle/ref_harness.cpp. Used only to pin the oracle and to make the golden
 # fixtures; the reference tree is not present where the GPU tests run. The
@@ -9,7 +10,8 @@
 # headers are force-included (-include) instead of editing its sources.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_ROOT="${REF_ROOT:-/root/reference}"
+REF_ROOT="${1:-${REF_ROOT:-}}"
+[ -n "$REF_ROOT" ] || { echo "usage: build_ref.sh <reference tree root> (or set REF_ROOT)" >&2; exit 2; }
 SRC="$REF_ROOT/src"
 OUT="$HERE/_ref"
 [ -d "$SRC" ] || { echo "reference sources not found at $SRC" >&2; exit 2; }

@@ -14,6 +14,17 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (run with -m gpu on a GB300)")
 
 
+def pytest_collection_modifyitems(config, items):
+    """Every GPU test ends within 10 minutes: where pytest-timeout is installed, a test
+    still running then has its stacks dumped and the process exits (the thread method,
+    which also ends a host thread waiting on the device)."""
+    if not config.pluginmanager.hasplugin("timeout"):
+        return
+    for item in items:
+        if item.get_closest_marker("gpu") and not item.get_closest_marker("timeout"):
+            item.add_marker(pytest.mark.timeout(600, method="thread"))
+
+
 @pytest.fixture(scope="session", autouse=True)
 def _built():
     """Build the library and the oracle once per session (no-op when up to date)."""

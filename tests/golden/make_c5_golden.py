@@ -1,7 +1,9 @@
 """Generate tests/golden/c5_golden.json: the oracle's skeletons of a set of served
 requests spanning the served workload's range (p up to 5000, n up to 20000, ER degree 3
 and preferential attachment with 2 parents per node -- hub-heavy --, weights
-+-[0.1, 1.0], alpha 0.01, FP32 data, levels until no edge has enough neighbours).
++-[0.1, 1.0], alpha 0.01, FP32 data, levels 0-4: the served workload's cap -- on the
+hub-heavy graphs the number of tests grows as C(d - 1, l) on the hubs' rows, so that
+"until exhausted" is out of reach for the CPU and the GPU alike).
 
 The data come from the library's seeded generator (host code, bit-identical on every
 host); the oracle (oracle/oracle.cpp) computes the FP64 correlation and the skeleton on
@@ -26,6 +28,7 @@ for _d in (ROOT, os.path.join(ROOT, "masterthesis-heterogeneous-pc_gb300")):
 
 OUT = os.path.join(HERE, "c5_golden.json")
 ALPHA = 0.01
+MAX_LEVEL = 4
 # (p, n, graph): the corners and the middle of p in [30, 5000] x n in [500, 20000]
 REQUESTS = [(5000, 20000, 0), (5000, 2000, 1), (3000, 20000, 1), (4000, 8000, 1), (1500, 15000, 1),
             (800, 500, 0), (30, 500, 1), (200, 20000, 0), (2500, 1000, 0), (5000, 5000, 1), (60, 12000, 1),
@@ -52,7 +55,7 @@ def main():
         t0 = time.perf_counter()
         Cm = orc.correlation(X.astype(np.float64))
         t1 = time.perf_counter()
-        res = orc.run(Cm, n, ALPHA, -1)
+        res = orc.run(Cm, n, ALPHA, MAX_LEVEL)
         t2 = time.perf_counter()
         rows.append(dict(q=q, p=p, n=n, graph="PA" if graph else "ER", data_sha256=data_sha(X),
                          adj_sha256=adjacency_sha(res.adj), edges=res.edges(),
@@ -61,7 +64,7 @@ def main():
               % (q, p, n, rows[-1]["graph"], res.edges(), len(res.levels), t1 - t0, t2 - t1), flush=True)
     with open(OUT, "w") as f:
         json.dump(dict(generator="tests/golden/make_c5_golden.py", expected_from="oracle (oracle/oracle.cpp, FP64)",
-                       alpha=ALPHA, requests=rows), f, separators=(",", ":"))
+                       alpha=ALPHA, max_level=MAX_LEVEL, requests=rows), f, separators=(",", ":"))
     print("wrote", OUT)
 
 

@@ -8,8 +8,9 @@ Inputs are seeded linear-Gaussian SEM data from the library's generator (bit-ide
 on every host; the fixture stores a SHA-256 of the data and of the FP64 correlation
 matrix so a host that disagrees is caught) or small matrices stored inline.
 
-Run from the repository root where the reference tree exists:
-    python tests/golden/make_golden.py
+Run from the repository root, naming the reference tree's root (its data/cooling_house.csv
+is one of the cases):
+    python tests/golden/make_golden.py <reference tree root>
 """
 import hashlib
 import json
@@ -25,7 +26,6 @@ sys.path.insert(0, os.path.join(ROOT, "masterthesis-heterogeneous-pc_gb300"))
 import heterogpc as hg  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 
-REF_DATA = "/root/reference/data/cooling_house.csv"
 
 # name, generator params, alpha, max_level
 GEN_CASES = [
@@ -71,6 +71,9 @@ def expected(Cm, n, alpha, max_level):
 
 
 def main():
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference tree root>")
+    ref_data = os.path.join(sys.argv[1], "data", "cooling_house.csv")
     if not orc.ref_available():
         sys.exit("oracle/_ref/libref_cpu.so missing: build it with oracle/build_ref.sh first")
     cases = []
@@ -98,8 +101,8 @@ def main():
         cases.append(dict(name=name, source="matrix", alpha=0.05, max_level=4, n_obs=base["n"],
                           cor=[[None if np.isnan(v) else float(v) for v in row] for row in Cm],
                           cor_sha256=sha(Cm), edges=edges, n_edges=len(edges), ref_sepsets=seps))
-    if os.path.exists(REF_DATA):
-        D = np.loadtxt(REF_DATA, delimiter=",").T.copy()
+    if os.path.exists(ref_data):
+        D = np.loadtxt(ref_data, delimiter=",").T.copy()
         Cm = orc.correlation(D)
         for alpha in (0.01, 0.05):
             edges, seps, mc = expected(Cm, D.shape[1], alpha, 4)

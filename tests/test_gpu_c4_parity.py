@@ -55,11 +55,10 @@ def test_c4_every_instance_equals_oracle():
                 bad.append(b)
         assert not bad, "rep %d: instances differing from the oracle: %s" % (rep, bad[:20])
     # every stored separation set of a sample of instances re-tests as independent in FP64
-    recs = bt.all_sepset_records()
     rng = np.random.default_rng(4)
     for b in sorted(rng.choice(len(ps), 64, replace=False)):
         Cm = orc.correlation(Xs[b].astype(np.float64))
-        rs = recs[b]
+        rs = bt.sepset_records(int(b))
         ok = orc.verify_sepsets(Cm, int(ns[b]), float(alphas[b]), [(i, j, lev, ids) for i, j, lev, ids, _ in rs])
         assert ok.all(), (b, [rs[t] for t in np.nonzero(~ok)[0][:5]])
         assert all(pm >= alphas[b] for *_, pm in rs)

@@ -72,7 +72,7 @@ def test_request_joins_a_running_batch_at_the_next_level():
     import time
     big = hg.sem_generate(900, 3000, hg.GRAPH_PA, 3.0, 2, 0.2, 1.0, 4242, dtype=np.float32)
     small = requests(10, seed=3)
-    alpha, ml = 0.01, -1
+    alpha, ml = 0.01, 4
     sv = hg.SkeletonServer(max_level=ml, max_batch=16, max_inflight=4)
     bid = sv.submit(big, alpha, want_adjacency=True)
     time.sleep(0.05)
@@ -111,15 +111,15 @@ C5 = _c5_fixture()
 @pytest.mark.skipif(C5 is None, reason="tests/golden/c5_golden.json not generated")
 def test_full_range_requests_equal_the_oracle():
     """Requests spanning the served workload's range (p up to 5000, n up to 20000,
-    hub-heavy preferential-attachment graphs), served together until exhausted, against
-    the committed oracle results (tests/golden/make_c5_golden.py)."""
+    hub-heavy preferential-attachment graphs), served together to the served workload's
+    level cap, against the committed oracle results (tests/golden/make_c5_golden.py)."""
     import os
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
     import make_c5_golden as g5
     from helpers import sha
     import bench
-    sv = hg.SkeletonServer(max_level=-1)
+    sv = hg.SkeletonServer(max_level=C5["max_level"])
     ids, data = [], []
     for row in C5["requests"]:
         X = g5.request_data(row["q"])
