@@ -1065,9 +1065,28 @@ def main():
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
     e2e_total = max_over_ranks(sum(e2e_t), dist, dev)
-    W = (p + 31) // 32
     e2e = {"value": replica_rate(world, args.steps, e2e_total), "unit": "skeletons/s", "h2d_bytes_per_step": p * p * 8,
-           "d2h_bytes_per_step": p * p}
+           "d2h_bytes_per_step": p * p,
+           "path": "hpc_load_correlation (pinned FP64 matrix) + hpc_run_skeleton + hpc_get_adjacency"}
+    # the same from observations (correlation included): H2D of the samples, the
+    # FP64-accurate correlation, all levels, the adjacency back
+    Xh = torch.from_numpy(X).pin_memory()
+    for _ in range(args.warmup):
+        sk.add_observations_ptr(Xh.data_ptr(), xdt)
+        sk.run()
+        sk.adjacency_into(adj_h.data_ptr())
+    torch.cuda.synchronize()
+    obs_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sk.add_observations_ptr(Xh.data_ptr(), xdt)
+        sk.run()
+        sk.adjacency_into(adj_h.data_ptr())
+        torch.cuda.synchronize()
+        obs_t.append(time.perf_counter() - t0)
+    e2e_obs = {"value": replica_rate(world, args.steps, max_over_ranks(sum(obs_t), dist, dev)), "unit": "skeletons/s",
+               "h2d_bytes_per_step": int(X.nbytes), "d2h_bytes_per_step": p * p,
+               "path": "hpc_correlation_f32/f64 (pinned observations) + hpc_run_skeleton + hpc_get_adjacency"}
 
     if rank != 0:
         if dist:
@@ -1114,8 +1133,10 @@ def main():
             "plain_gpu_path": {"skeletons_per_sec": args.steps / (sum(plain_ms) / 1e3),
                                "ms_per_step": sum(plain_ms) / args.steps, "precision": "fp64"},
             "correlation": {"ms": cor_ms, "gram_ms": cor_t["gram_ms"], "standardise_ms": cor_t["standardise_ms"],
-                            "kernel": "gram_f64_kernel", "fp64_gflops": gram_flops / (cor_t["gram_ms"] / 1e3) / 1e9},
-            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+                            "kernel": "gram_emu_kernel (exact BF16 digits)" if p >= 256 else "gram_f64_kernel",
+                            "fp64_equivalent_tflops": gram_flops / (cor_t["gram_ms"] / 1e3) / 1e12},
+            "roofline": roofline, "e2e": e2e, "e2e_from_observations": e2e_obs, "gpu_launches": int(launches),
+            "clocks": clk,
             "tile_policy": tuned}
     if not args.no_cpu_baseline:
         from oracle import oracle as orc

@@ -409,6 +409,12 @@ class SkeletonCalculator:
         _check(lib().hpc_load_correlation_device(self._h, C.c_void_p(ptr)))
         self.level_stats = []
 
+    def add_observations_ptr(self, ptr, dtype):
+        """Observations in host memory at ptr (e.g. pinned), column-major n x p."""
+        fn = lib().hpc_correlation_f32 if dtype == np.float32 else lib().hpc_correlation_f64
+        _check(fn(self._h, C.c_void_p(ptr)))
+        self.level_stats = []
+
     def add_correlation_matrix_ptr(self, ptr):
         """Host pointer (e.g. pinned memory) to a row-major p x p FP64 matrix."""
         _check(lib().hpc_load_correlation(self._h, C.c_void_p(ptr)))

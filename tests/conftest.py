@@ -15,14 +15,14 @@ def pytest_configure(config):
 
 
 def pytest_collection_modifyitems(config, items):
-    """Every GPU test ends within 10 minutes: where pytest-timeout is installed, a test
+    """Every GPU test ends within 5 minutes: where pytest-timeout is installed, a test
     still running then has its stacks dumped and the process exits (the thread method,
     which also ends a host thread waiting on the device)."""
     if not config.pluginmanager.hasplugin("timeout"):
         return
     for item in items:
         if item.get_closest_marker("gpu") and not item.get_closest_marker("timeout"):
-            item.add_marker(pytest.mark.timeout(600, method="thread"))
+            item.add_marker(pytest.mark.timeout(300, method="thread"))
 
 
 @pytest.fixture(scope="session", autouse=True)
