@@ -1,23 +1,28 @@
 #!/usr/bin/env python3
 """Benchmark of the PC-stable skeleton path on one GB300 (or N replicas).
 
-Workload (default, "c2"): linear-Gaussian SEM on a seeded Erdos-Renyi DAG, p=2000
-variables, expected degree 4, weights +-[0.1, 1.0], N(0,1) noise, n=5000 FP32 samples,
-alpha=0.01, levels 0..6, FP64-accurate correlation computed on the device.
+Workload (default, "c4" -- the configuration the metric is quoted on): 512 independent
+skeleton problems, p ~ U[20, 800], n ~ U[200, 8000], Erdos-Renyi DAGs of expected degree
+~ U[1, 5], weights +-[0.1, 1.0], N(0,1) noise, FP32 samples, alpha 0.01 / 0.05
+alternating, levels until no edge has enough neighbours, all in one batch context.
 
-A step is one skeleton discovery on a correlation matrix resident in HBM: levels
-0..6 (snapshots, CI tests, removals, separation sets), i.e. the region the reference
-times (src/independence/skeleton.cpp:167-180). The correlation of the step's data is
-computed once beforehand on the device and reported separately.
+A step is the tensor-core correlation of every instance's observations (resident in
+HBM) plus every level of every instance and the FP64 p-values of the removals (the
+region the reference times, src/independence/skeleton.cpp:167-180, plus the
+correlation), queued on one stream and timed with CUDA events; L2 is flushed before
+every step.
 
-  value   skeletons/s with the correlation resident in HBM (CUDA events, L2 flushed
-          before every step because the 48 MB of correlation fits in L2)
-  e2e     the same through the C ABI from pinned host memory: H2D of the FP64
-          correlation, all levels, D2H of the adjacency bitmask
+  value   skeletons/s of the batch (CUDA events)
+  e2e     the same through the C ABI from pinned host memory: H2D of the observations,
+          the whole step, D2H of every adjacency bitmask and every separation set
+  plain_gpu_path  the plain single-instance FP64 path (FP64 Gram, every test in FP64) on
+          the same instances, timed the same way
   --impl reference   the reference's CPU path (the oracle restatement, all host cores)
+          on systematic slices of the same batch
 
-Multi-GPU: replicas only (the skeleton does not shard without an exchange step);
-under torchrun every rank runs the workload and rank 0 prints the aggregate.
+Other workloads (--workload): c1, c2 (single instances), c3 (wide, hub-heavy), c5
+(served request stream), io (input readers). Multi-GPU: replicas only (the skeleton does
+not shard without an exchange step).
 """
 import argparse
 import json

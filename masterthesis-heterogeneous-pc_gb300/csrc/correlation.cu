@@ -100,32 +100,34 @@ __global__ void __launch_bounds__(kStdThreads) standardise_kernel(const TIn *__r
     }
     return;
   }
-  // split-BF16 operands of the tensor-core Gram: P = [hi|hi|lo|lo], Q = [hi|lo|hi|lo]
-  // of z / sqrt(n - 1), so that P Q^T is the correlation. The split runs in FP32
-  // (hi = bf16(zs), lo = bf16(zs - hi), the subtraction exact in FP32): its error is
-  // the rounding of lo, as with an FP64 split, plus 2^-24 relative from zs itself.
+  // split-BF16 operand of the tensor-core Gram: two planes T = [hi | lo] of z / sqrt(n - 1)
+  // (the Gram's producer pairs the planes: hi.hi + hi.lo + lo.hi + lo.lo is the
+  // correlation). The split runs in FP32 (hi = bf16(zs), lo = bf16(zs - hi), the
+  // subtraction exact in FP32): its error is the rounding of lo, as with an FP64 split,
+  // plus 2^-24 relative from zs itself. Two consecutive samples per thread, so that the
+  // planes are written as 4-byte pairs.
   const double denom = a.ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
   const double scale = 1.0 / sqrt(denom);
   const long long n_pad = a.n_pad[b], K = a.kdim[b];
-  __nv_bfloat16 *pr = P + a.tc_off[b] + v * K, *qr = Q + a.tc_off[b] + v * K;
-  for (long long k = threadIdx.x; k < n_pad; k += kStdThreads) {
-    double zz = 0.0;
+  __nv_bfloat16 *pr = P + a.tc_off[b] + v * K;
+  for (long long k = 2 * (long long)threadIdx.x; k < n_pad; k += 2 * kStdThreads) {
+    double z0 = 0.0, z1 = 0.0;
     if (k < n) {
       const double xv = (double)x[k];
-      zz = isnan(xv) ? 0.0 : (xv - mean) * inv_sd;
-      z[k] = zz;
+      z0 = isnan(xv) ? 0.0 : (xv - mean) * inv_sd;
+      z[k] = z0;
     }
-    const float zs = (float)(zz * scale);
-    const __nv_bfloat16 hi = __float2bfloat16_rn(zs);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(zs - __bfloat162float(hi));
-    pr[k] = hi;
-    pr[n_pad + k] = hi;
-    pr[2 * n_pad + k] = lo;
-    pr[3 * n_pad + k] = lo;
-    qr[k] = hi;
-    qr[n_pad + k] = lo;
-    qr[2 * n_pad + k] = hi;
-    qr[3 * n_pad + k] = lo;
+    if (k + 1 < n) {
+      const double xv = (double)x[k + 1];
+      z1 = isnan(xv) ? 0.0 : (xv - mean) * inv_sd;
+      z[k + 1] = z1;
+    }
+    const float s0 = (float)(z0 * scale), s1 = (float)(z1 * scale);
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(s0, s1);
+    const float2 hf = __bfloat1622float2(hi);
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(s0 - hf.x, s1 - hf.y);
+    *reinterpret_cast<__nv_bfloat162 *>(pr + k) = hi;
+    *reinterpret_cast<__nv_bfloat162 *>(pr + n_pad + k) = lo;
   }
 }
 

@@ -631,14 +631,12 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
     if (!c->tcP) {
       long long tt = 0;
       for (const auto &h : c->ih) tt += tc_p_pad(h.p) * tc_k(h.n);
-      if ((s = dev_alloc(&c->tcP, tt, "tensor-core operand P")) != HPC_OK) return s;
-      if ((s = dev_alloc(&c->tcQ, tt, "tensor-core operand Q")) != HPC_OK) return s;
+      if ((s = dev_alloc(&c->tcP, tt, "tensor-core operand")) != HPC_OK) return s;
       HPC_CUDA(cudaMemsetAsync(c->tcP, 0, sizeof(__nv_bfloat16) * tt, c->stream));
-      HPC_CUDA(cudaMemsetAsync(c->tcQ, 0, sizeof(__nv_bfloat16) * tt, c->stream));
       std::vector<CUtensorMap> maps((size_t)(2 * c->count));
       for (int b = 0; b < c->count; ++b) {
         const InstHost &h = c->ih[b];
-        if ((s = tc_make_maps(&maps[2 * b], &maps[2 * b + 1], c->tcP + h.tc_off, c->tcQ + h.tc_off, h.p, h.n)) !=
+        if ((s = tc_make_maps(&maps[2 * b], &maps[2 * b + 1], c->tcP + h.tc_off, c->tcP + h.tc_off, h.p, h.n)) !=
             HPC_OK)
           return s;
       }
@@ -647,7 +645,7 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
                                c->stream));
       HPC_CUDA(cudaStreamSynchronize(c->stream));
     }
-    if ((s = launch_standardise(X, f32, sa, sa.count ? c->total_rows : 0, c->Z, c->tcP, c->tcQ, c->stream)) != HPC_OK)
+    if ((s = launch_standardise(X, f32, sa, sa.count ? c->total_rows : 0, c->Z, c->tcP, nullptr, c->stream)) != HPC_OK)
       return s;
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
     TcArgs ta{};
@@ -801,7 +799,7 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   int64_t b = 0;
   if (o->precision != HPC_PREC_MIXED_TC) b += p * p * 8;           // cor64
   if (o->precision != HPC_PREC_FP64) b += p * p * 4;               // cor32
-  if (o->precision == HPC_PREC_MIXED_TC) b += 2 * tc_p_pad(p) * tc_k(n) * 2;  // split operands
+  if (o->precision == HPC_PREC_MIXED_TC) b += tc_p_pad(p) * tc_k(n) * 2;      // split operand planes
   b += n * p * 8;                                                  // standardised data
   b += n * p * 4;                                                  // observation staging
   b += p * W * 4 + p * p;                                          // adjacency bits + bytes

@@ -6,10 +6,11 @@
 //
 //   z  = (x - mean) / sd / sqrt(n - 1)          (FP64, per variable)
 //   hi = bf16(z),  lo = bf16(z - hi)
-//   P  = [hi | hi | lo | lo],  Q = [hi | lo | hi | lo]    (K' = 4 * n_pad, K-major rows)
-//   C  = P Q^T = hi.hi + hi.lo + lo.hi + lo.lo            (FP32 accumulation in TMEM)
+//   T  = [hi | lo]                              (two planes of n_pad, K-major rows)
+//   C  = hi.hi + hi.lo + lo.hi + lo.lo          (FP32 accumulation in TMEM)
 //
-// so one BF16 GEMM with K' = 4n gives the products of the split. With lo.lo the
+// so one BF16 GEMM with K = 4 n_pad gives the products of the split: the producer reads
+// plane q >> 1 for A and plane q & 1 for B in the q-th quarter of K. With lo.lo the
 // product of the two 16-bit representations is complete and what is left is the
 // rounding of lo (2^-17 relative per value), which averages out over n samples;
 // without it a systematic error of about 2^-18 |r| remains. Tiles are 128 rows x 256
@@ -51,7 +52,8 @@ namespace {
 
 constexpr int TM = 128, TN = 256, TK = 64;  // tile: 128 x 256 outputs, 64 bf16 (128 B) of K per stage
 constexpr int kStages = 4;
-constexpr int kSlices = 4;       // K' = kSlices * n_pad: hi.hi, hi.lo, lo.hi, lo.lo
+constexpr int kSlices = 4;       // K = kSlices * n_pad: hi.hi, hi.lo, lo.hi, lo.lo
+constexpr int kPlanes = 2;       // the operand holds hi and lo
 constexpr int kStageBytesA = TM * TK * 2;   // 16 KB
 constexpr int kStageBytesB = TN * TK * 2;   // 32 KB
 constexpr int kStageBytes = kStageBytesA + kStageBytesB;
@@ -97,7 +99,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   long long t = tt - ta.tile_prefix[inst];
   const int64_t p = ta.p[inst];
   const int nbc = tc_col_blocks(p);
-  const int kblocks = (int)(kSlices * ((ta.n[inst] + TK - 1) / TK));
+  const int kbq = (int)((ta.n[inst] + TK - 1) / TK);  // k-blocks per product
+  const int64_t n_pad = (int64_t)kbq * TK;
+  const int kblocks = kSlices * kbq;
   const CUtensorMap *mapP = ta.maps + 2 * inst, *mapQ = ta.maps + 2 * inst + 1;
   float *__restrict__ C = Call + ta.c_off[inst];
   int *err = ta.err;
@@ -157,8 +161,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
       if (aborted(sm)) break;
       mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
-      tma_load_2d(sm.stage[s], mapP, kb * TK, bi * TM, &sm.full[s]);
-      tma_load_2d(sm.stage[s] + kStageBytesA, mapQ, kb * TK, bj * TN, &sm.full[s]);
+      const int q = kb / kbq, kq = (kb - q * kbq) * TK;  // product q: planes (q >> 1, q & 1)
+      tma_load_2d(sm.stage[s], mapP, (q >> 1) * (int)n_pad + kq, bi * TM, &sm.full[s]);
+      tma_load_2d(sm.stage[s] + kStageBytesA, mapQ, (q & 1) * (int)n_pad + kq, bj * TN, &sm.full[s]);
       ++issued;
     }
   } else if (warp == 1 && lane == 0) {
@@ -310,7 +315,7 @@ hpc_status make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int
 
 int64_t tc_n_pad(int64_t n) { return (n + TK - 1) / TK * TK; }
 int64_t tc_p_pad(int64_t p) { return tc_p_pad_dev(p); }
-int64_t tc_k(int64_t n) { return kSlices * tc_n_pad(n); }
+int64_t tc_k(int64_t n) { return kPlanes * tc_n_pad(n); }
 
 long long gram_tc_tiles(int64_t p) {
   const long long nb = tc_p_pad(p) / TM, nbc = tc_col_blocks(p);
@@ -319,7 +324,8 @@ long long gram_tc_tiles(int64_t p) {
   return t;
 }
 
-// Tensor maps of one instance's operands P and Q (tc_p_pad(p) rows of tc_k(n) bf16).
+// Tensor maps of one instance's operand planes (tc_p_pad(p) rows of tc_k(n) bf16), for
+// the A (128-row) and B (256-row) tiles; P and Q may be the same buffer.
 // a 2-D BF16 tensor map (rows x K, K contiguous, 64-column x box_rows boxes, 128-byte
 // swizzle) for the other tensor-core kernels
 hpc_status tc_make_map(CUtensorMap *m, const __nv_bfloat16 *base, int64_t rows, int64_t K, int box_rows) {

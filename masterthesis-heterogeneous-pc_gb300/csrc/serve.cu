@@ -51,7 +51,7 @@ struct Request {
   int levels = 0;
   int64_t edges = 0;
   int batch_size = 0;   // most requests in one of its level launches
-  int joined = 0;       // requests active when it was admitted
+  int joined = 0;       // requests already running when it was admitted
   // engine state
   hpc_ctx *ctx = nullptr;
   int next = 0;         // next level to run
@@ -342,9 +342,10 @@ void engine_loop(hpc_server *sv) {
         admitted.push_back(r);
       }
     }
+    const int running = (int)sv->active.size();  // requests that have run steps already
     for (Request *r : admitted) {
       r->t_start = clk::now();
-      r->joined = (int)sv->active.size();
+      r->joined = running;
       r->status = admit(sv, r);
       if (r->status != HPC_OK) finish(sv, r, &finished);
       else sv->active.push_back(r);

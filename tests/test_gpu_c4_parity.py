@@ -85,12 +85,13 @@ def test_c4_plain_fp64_path_on_64_instances():
 def test_c4_queued_runs_continue_past_the_previous_extent():
     """A run until exhausted queues the levels the previous run needed as one sequence;
     when the new data reach further, hpc_wait continues level by level. Here the first
-    run sees shallow data (ER degree 1) of the deep instances' shapes, then the real
-    observations are queued: the result is still the oracle's skeleton."""
+    run sees independent variables (no DAG edges: the skeleton is exhausted after level
+    1) of the deep instances' shapes, then the real observations are queued: the result
+    is still the oracle's skeleton."""
     wl, ps, ns, alphas, Xs = _data()
     idx = sorted(range(len(ps)), key=lambda b: -len(GOLD["instances"][b]["edges_per_level"]))[:8]
     bt = hg.SkeletonBatch(ps[idx], ns[idx], alphas[idx], max_level=-1, precision=hg.PREC_MIXED_TC)
-    shallow = [hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, 1.0, 2, 0.1, 1.0, 900 + b, dtype=np.float32)
+    shallow = [hg.sem_generate(int(ps[b]), int(ns[b]), hg.GRAPH_ER, 0.0, 2, 0.1, 1.0, 900 + b, dtype=np.float32)
                for b in idx]
     bt.add_observations(bt.pack(shallow))
     first = bt.run()

@@ -69,17 +69,14 @@ def test_request_joins_a_running_batch_at_the_next_level():
     """A long request runs level after level; requests submitted while it runs are
     admitted between its steps (joined > 0), share its level launches, and give the
     oracle's skeleton, as they do alone."""
-    import time
     big = hg.sem_generate(900, 3000, hg.GRAPH_PA, 3.0, 2, 0.2, 1.0, 4242, dtype=np.float32)
     small = requests(10, seed=3)
     alpha, ml = 0.01, 4
-    sv = hg.SkeletonServer(max_level=ml, max_batch=16, max_inflight=4)
+    # at most two admissions between steps: the later requests are admitted while the
+    # first ones run their levels
+    sv = hg.SkeletonServer(max_level=ml, max_batch=16, max_inflight=2)
     bid = sv.submit(big, alpha, want_adjacency=True)
-    time.sleep(0.05)
-    ids = []
-    for X in small:
-        ids.append(sv.submit(X, alpha, want_adjacency=True))
-        time.sleep(0.002)
+    ids = [sv.submit(X, alpha, want_adjacency=True) for X in small]
     sv.drain()
     done = {d["id"]: d for d in sv.poll()}
     assert done[bid]["status"] == 0
