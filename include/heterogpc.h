@@ -357,6 +357,18 @@ double hpc_z_crit(double alpha);
 hpc_status hpc_debug_fail_allocation(int64_t k);
 int64_t hpc_debug_live_allocations(void);
 hpc_status hpc_debug_set_barrier(hpc_ctx *ctx, int64_t wait_ns, int extra_arrivals);
+/* hpc_debug_set_order_from(level): the lowest level whose CI tests run in the set order
+ * (one Cholesky factor of a conditioning set serves every neighbour outside it), 2..32,
+ * or 0 for the edge order (each test factors its own set) at every level; process-wide,
+ * read when a level is launched. Both orders give the same skeleton; the default is 4. */
+hpc_status hpc_debug_set_order_from(int level);
+/* hpc_debug_set_retest_queue(ctx, entries): replace the context's FP64 re-test queue by
+ * one of `entries` entries (so that a test can make it overflow). When a set-order level
+ * finds the queue full, the run is repeated from level 0 in the edge order, whose tests
+ * re-test inline when the queue is full; hpc_debug_set_order_active then returns 0 for
+ * the context (1 while the set order is in use). */
+hpc_status hpc_debug_set_retest_queue(hpc_ctx *ctx, int64_t entries);
+int hpc_debug_set_order_active(hpc_ctx *ctx);
 
 /* ---- synthetic data ------------------------------------------------------
  * Seeded linear-Gaussian SEM (no reference counterpart; the reference reads

@@ -10,9 +10,8 @@ namespace {
 
 // p-values of the removals decided in FP32 (negative pmax), for every instance's
 // records: FP64 re-evaluation where the instance has an FP64 matrix -- a result below
-// alpha flags kErrBandViolation (the FP32 error bound did not hold) -- else the FP64
-// formula on the stored FP32 |r|. Run when the records are first read, not inside the
-// level loop.
+// alpha flags kErrBandViolation (the FP32 error bound did not hold) -- else the formula
+// in FP32 on the stored FP32 |r|. Run at the end of every skeleton run.
 __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count) {
   const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
   const unsigned long long nthreads = (unsigned long long)gridDim.x * blockDim.x;
@@ -25,7 +24,7 @@ __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count
       RecHead *h = reinterpret_cast<RecHead *>(rec);
       if (!(h->pmax < 0.0)) continue;
       if (!I.cor64) {
-        h->pmax = calc_pvalue64(-1.0 - h->pmax, I.n_obs);
+        h->pmax = (double)calc_pvalue32((float)(-1.0 - h->pmax), I.n_obs);
         continue;
       }
       const double pv = exact_pvalue<HPC_MAX_LEVEL>(I, h->i, h->j, rec + kRecHeadWords, h->level);
@@ -79,77 +78,156 @@ __global__ void pack_records_kernel(const Inst *__restrict__ inst, int count, co
   }
 }
 
-__device__ __forceinline__ double warp_dot(const double *__restrict__ x, const double *__restrict__ y, int64_t n) {
+__device__ __forceinline__ double warp_dot(const Inst &I, int64_t a, int64_t b) {
   const int lane = threadIdx.x & 31;
-  double s = 0.0;
-  for (int64_t k = lane; k < n; k += 32) s = fma(x[k], y[k], s);
+  double s = zdot(I, a, b, lane, 32);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
 }
 
-// FP64 re-tests deferred by the level kernels (instances without an FP64 matrix):
-// one warp per queued test forms the FP64 correlation entries it needs as dot
-// products of the FP64-standardised columns, lane 0 evaluates the reference formula.
-// Level-0 items set the kept bits of both triangles; level >= 1 items remove the edge.
-// The matrices live in dynamic shared memory sized by the launch's level ((l + 2)^2
-// doubles per warp: 2.6 KB at level 16, 9 KB at level 32), so the low levels, where
-// the re-tests are many, keep the SM's warps resident for the dot products.
+// FP64 re-tests deferred by the level kernels (instances without an FP64 matrix). A
+// re-test of level l needs the E = (l + 2)(l + 1) / 2 FP64 correlation entries among
+// i, j and S, each a dot product of two FP64-standardised columns (n samples). One warp
+// per dot product: the launch's first W items (W = min(queued, rq_vcap / E)) are cut
+// into W * E (item, entry) units over the grid, each warp writes its entry to the item's
+// scratch row and counts it done; the warp completing an item's last entry gathers the
+// row into its (l + 2)^2 matrix in shared memory and lane 0 evaluates the reference
+// formula. So a level with a few re-tests of many entries (the high levels) runs them
+// side by side instead of one warp stepping through 100+ dot products; items beyond the
+// scratch take a warp each. Level-0 items (one entry) set the kept bits of both
+// triangles; level >= 1 items remove the edge. The done counters return to zero when
+// their item is evaluated, ready for the next launch.
 // KM: the highest level of the launch's items (16 for levels up to 16, HPC_MAX_LEVEL
 // above), which sizes the FP64 fallback's local arrays.
 constexpr int kRetestWarps = 8;
+
+// the variable at position r of a re-test's matrix order (i, j, S)
+__device__ __forceinline__ int64_t retest_var(const RetestItem *it, int r) {
+  return r == 0 ? (int64_t)it->i : r == 1 ? (int64_t)it->j : (int64_t)it->ids[r - 2];
+}
+
+// entry e of the upper triangle of a k x k matrix, row by row: (r, c), r < c
+__device__ __forceinline__ void entry_rc(int e, int k, int &r, int &c) {
+  r = 0;
+  while (e >= k - 1 - r) {
+    e -= k - 1 - r;
+    ++r;
+  }
+  c = r + 1 + e;
+}
+
+// lane 0: the FP64 decision of item it from its matrix M (k x k, warp-filled)
+template <int KM>
+__device__ __forceinline__ void retest_decide(const Launch &L, const Inst &I, const RetestItem *it, int l, double *M) {
+  bool nan_p;
+  const double r = partial_r_of_matrix<KM>(M, l, &nan_p);
+  double pv;
+  const int64_t i = it->i, j = it->j;
+  if (decide_of_r(I, r, nan_p, &pv) && claim_edge(I, i, j)) write_record(I, L.level, i, j, it->ids, l, pv);
+}
+
 template <int KM>
 __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_constant__ Launch L) {
   extern __shared__ double retest_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int kmax = L.level + 2;
-  double *M = retest_smem + (size_t)wib * kmax * kmax;
+  const int l = L.level;
+  const int k = l + 2;
+  double *M = retest_smem + (size_t)wib * k * k;
   unsigned long long count = L.lc->rq_count;
   if (count > (unsigned long long)L.rq_cap) count = (unsigned long long)L.rq_cap;
   const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-  for (unsigned long long q = warp; q < count; q += nwarps) {
-    const RetestItem it = L.rq[q];
-    const Inst &I = *inst_of(L, it.inst);
-    const int64_t i = it.i, j = it.j, n = I.n_z;
-    const int l = it.level;
-    if (l == 0) {
-      const double r = warp_dot(I.Z + i * n, I.Z + j * n, n) / I.denom;
+  if (l == 0) {
+    for (unsigned long long q = warp; q < count; q += nwarps) {
+      const RetestItem *it = L.rq + q;
+      const Inst &I = *inst_of(L, it->inst);
+      const int64_t i = it->i, j = it->j;
+      const double r = warp_dot(I, i, j) / I.denom;
       double pv;
       if (lane == 0 && !decide_of_r(I, r, false, &pv)) {  // kept: both triangles' bits
         atomicOr(I.adj + i * I.W + (j >> 5), 1u << (j & 31));
         atomicOr(I.adj + j * I.W + (i >> 5), 1u << (i & 31));
       }
-      continue;
     }
-    if (!live_bit(I.adj, I.W, i, j)) continue;  // removed by another test meanwhile
-    const int k = l + 2;
-    int V[HPC_MAX_LEVEL + 2];
-    V[0] = (int)i;
-    V[1] = (int)j;
-    for (int t = 0; t < l; ++t) V[2 + t] = it.ids[t];
+    return;
+  }
+  const int E = k * (k - 1) / 2;
+  const unsigned long long W =
+      L.rq_val ? min(count, (unsigned long long)(L.rq_vcap / E)) : 0ull;  // items run entry by entry
+  const unsigned long long units = W * (unsigned long long)E;
+  for (unsigned long long u = warp; u < units; u += nwarps) {
+    const unsigned long long q = u / (unsigned long long)E;
+    const int e = (int)(u - q * (unsigned long long)E);
+    const RetestItem *it = L.rq + q;
+    const Inst &I = *inst_of(L, it->inst);
+    const int64_t i = it->i, j = it->j;
+    if (live_bit(I.adj, I.W, i, j)) {  // else removed meanwhile: nothing to compute
+      int r, c;
+      entry_rc(e, k, r, c);
+      const double v = warp_dot(I, retest_var(it, r), retest_var(it, c)) / I.denom;
+      if (lane == 0) L.rq_val[q * (unsigned long long)E + e] = v;
+    }
+    unsigned last = 0;
+    if (lane == 0) {
+      __threadfence();
+      last = atomicAdd(L.rq_done + q, 1u) == (unsigned)(E - 1);
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
+    // the item's last entry: gather its matrix and decide
+    __threadfence();
+    if (lane == 0) L.rq_done[q] = 0u;
+    if (!live_bit(I.adj, I.W, i, j)) continue;
+    for (int t = lane; t < k * k; t += 32) {
+      const int r = t / k, c = t - r * k;
+      double v = 1.0;
+      if (r != c) {
+        const int a = r < c ? r : c, b2 = r < c ? c : r;
+        const int eidx = a * k - a * (a + 1) / 2 + (b2 - a - 1);  // entry_rc's numbering
+        v = __ldcg(L.rq_val + q * (unsigned long long)E + eidx);
+      }
+      M[t] = v;
+    }
+    __syncwarp();
+    if (lane == 0) retest_decide<KM>(L, I, it, l, M);
+    __syncwarp();
+  }
+  // items beyond the scratch: a warp each
+  for (unsigned long long q = W + warp; q < count; q += nwarps) {
+    const RetestItem *it = L.rq + q;
+    const Inst &I = *inst_of(L, it->inst);
+    if (!live_bit(I.adj, I.W, it->i, it->j)) continue;  // removed by another test meanwhile
     for (int r = 0; r < k; ++r) {
       if (lane == 0) M[r * k + r] = 1.0;
       for (int c2 = r + 1; c2 < k; ++c2) {
-        const double v = warp_dot(I.Z + (int64_t)V[r] * n, I.Z + (int64_t)V[c2] * n, n) / I.denom;
+        const double v = warp_dot(I, retest_var(it, r), retest_var(it, c2)) / I.denom;
         if (lane == 0) M[r * k + c2] = M[c2 * k + r] = v;
       }
     }
     __syncwarp();
-    if (lane == 0) {
-      bool nan_p;
-      const double r = partial_r_of_matrix<KM>(M, l, &nan_p);
-      double pv;
-      if (decide_of_r(I, r, nan_p, &pv) && claim_edge(I, i, j)) write_record(I, L.level, i, j, it.ids, l, pv);
-    }
+    if (lane == 0) retest_decide<KM>(L, I, it, l, M);
     __syncwarp();
   }
 }
 
 template <bool MIXED>
 void *kernel_for(int level, int l1_variant) {
+  if (MIXED && l1_variant == kSetOrder && level >= 2 && level <= 16) {
+    switch (level) {
+      case 2: return (void *)level_kernel<2, true, kSetOrder>;
+      case 3: return (void *)level_kernel<3, true, kSetOrder>;
+      case 4: return (void *)level_kernel<4, true, kSetOrder>;
+      case 5: return (void *)level_kernel<5, true, kSetOrder>;
+      case 6: return (void *)level_kernel<6, true, kSetOrder>;
+      case 7: return (void *)level_kernel<7, true, kSetOrder>;
+      case 8: return (void *)level_kernel<8, true, kSetOrder>;
+      default: return level <= 12 ? level_kernel_9_12(level, true, true) : level_kernel_13_16(level, true, true);
+    }
+  }
   switch (level) {
     case 1:
+      if (MIXED && l1_variant == (kL1Interleaved | kQueueOnly)) return (void *)level_kernel<1, true, kL1Interleaved | kQueueOnly>;
+      if (MIXED && l1_variant == (kL1Prefetch | kQueueOnly)) return (void *)level_kernel<1, true, kL1Prefetch | kQueueOnly>;
       return l1_variant == kL1Chunked    ? (void *)level_kernel<1, MIXED, kL1Chunked>
              : l1_variant == kL1Prefetch ? (void *)level_kernel<1, MIXED, kL1Prefetch>
                                          : (void *)level_kernel<1, MIXED>;
@@ -161,8 +239,8 @@ void *kernel_for(int level, int l1_variant) {
     case 7: return (void *)level_kernel<7, MIXED>;
     case 8: return (void *)level_kernel<8, MIXED>;
     default:
-      return level <= 12 ? level_kernel_9_12(level, MIXED)
-                         : level <= 16 ? level_kernel_13_16(level, MIXED) : level_kernel_17_up(level, MIXED);
+      return level <= 12 ? level_kernel_9_12(level, MIXED, false)
+                         : level <= 16 ? level_kernel_13_16(level, MIXED, false) : level_kernel_17_up(level, MIXED);
   }
 }
 

@@ -67,14 +67,11 @@ __device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, 
 }
 
 // FP64 correlation entries of one instance: read from its FP64 matrix when there is
-// one, else the dot product of its FP64-standardised columns. Index order as the
+// one, else the dot product of its FP64-standardised columns (zdot). Index order as the
 // reference reads cor[row * p + col].
 __device__ __forceinline__ double exact_entry(const Inst &I, int64_t x, int64_t y) {
   if (I.cor64) return I.cor64[x * I.p + y];
-  const double *a = I.Z + x * I.n_z, *b = I.Z + y * I.n_z;
-  double s = 0.0;
-  for (int64_t k = 0; k < I.n_z; ++k) s = fma(a[k], b[k], s);
-  return s / I.denom;
+  return zdot(I, x, y, 0, 1) / I.denom;
 }
 
 // FP64 partial correlation of a k x k submatrix M (row-major, ordered i, j, S;
@@ -643,22 +640,31 @@ __device__ __forceinline__ void skip_tiles_of_edge(const Launch &L, unsigned lon
   if (target > nwarps) atomicMax(&L.lc->tile_next, target - nwarps);
 }
 
+// Shared memory of a level kernel's CI-test phase: per warp, the pending removals and
+// (levels 2-16, mixed precision) the staged correlation block.
 template <int LT, bool MIXED>
-__device__ __forceinline__ void tests_generic(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te) {
+struct TestSmem {
+  static constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
+  static constexpr bool kBlk = MIXED && LT >= 2 && LT <= 16;
+  PendRem<LA> pend[kThreads / 32][kPend];
+  int np[kThreads / 32];
+  float blk[kBlk ? kThreads / 32 : 1][kBlk ? kBlkS * kBlkS : 1];
+};
+
+template <int LT, bool MIXED>
+__device__ __forceinline__ void tests_generic(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te,
+                                              TestSmem<LT, MIXED> &sm) {
   constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
   const int l = LT > 0 ? LT : L.level;
   const int level = L.level;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  __shared__ PendRem<LA> s_pend[kThreads / 32][kPend];
-  __shared__ int s_np[kThreads / 32];
   // the staged correlation block of the warp (levels 2-16, mixed precision)
-  constexpr bool kBlk = MIXED && LT >= 2 && LT <= 16;
-  __shared__ float s_blk[kBlk ? kThreads / 32 : 1][kBlk ? kBlkS * kBlkS : 1];
-  float *blk = s_blk[kBlk ? wib : 0];
+  constexpr bool kBlk = TestSmem<LT, MIXED>::kBlk;
+  float *blk = sm.blk[kBlk ? wib : 0];
   int64_t blk_i = -1;  // row and instance of the staged block
   int blk_b = -1;
-  PendRem<LA> *pend = s_pend[wib];
-  int *np = s_np + wib;
+  PendRem<LA> *pend = sm.pend[wib];
+  int *np = sm.np + wib;
   if (lane == 0) *np = 0;
   __syncwarp();
   const unsigned long long total = L.work_prefix[L.count];
@@ -819,8 +825,11 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
 // edge (i, j): their reads of the neighbour list and of row i of cor32 fall into few
 // cache lines and stay in L1 across the edges of row i, and only the reads of row j
 // are scattered. Decisions as test_f32_inc with l = 1 (the closed form of cpuInd.cpp:16-27
-// in FP32), FP64 re-tests as in citest_kernel.
-template <bool MIXED, bool PF>
+// in FP32), FP64 re-tests as in citest_kernel. QO (queue only, mixed precision without
+// an FP64 matrix): an undecided test is only queued, and a full queue is flagged for a
+// rerun as in the set order -- the kernel then holds no inline FP64 re-test, whose
+// registers the interleaved body would otherwise spill for.
+template <bool MIXED, bool PF, bool QO = false>
 __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te) {
   const int level = 1;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -931,8 +940,12 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
             pv_rm = -1.0 - (double)rr;
           } else if (res == 2) {
             if (MIXED) ++retests;
-            if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, &k, 1)))
-              rm = exact_remove_fast<1>(*I, i, j, &k, 1, &pv_rm);
+            if constexpr (QO) {
+              if (!push_retest(L, b, i, j, &k, 1)) atomicOr(&I->g->err, kErrRetestOverflow);
+            } else {
+              if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, &k, 1)))
+                rm = exact_remove_fast<1>(*I, i, j, &k, 1, &pv_rm);
+            }
           }
         }
         float x2n = 0.f, x3n = 0.f;
@@ -1021,31 +1034,311 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
   }
 }
 
+// ---------------------------------------------------------------------------
+// The set order of a level's CI tests (levels 2-16, mixed precision; the kSetOrder
+// kernels, launched from the level set_order_from() on). The flattened index runs over (instance, row i, l-subset S of the row's snapshot neighbours in
+// lexicographic order), and one unit runs the tests (i, j | S) for every live
+// neighbour j outside S, in ascending order. A row of degree d > l has C(d, l) units
+// holding C(d, l) (d - l) = d C(d - 1, l) tests: every test of the edge order once,
+// each in the same FP32 arithmetic -- the Cholesky factor of S and w_i formed as
+// test_f32_inc forms them (along the lexicographic walk, from the lowest changed
+// member on), w_j by the same forward solve -- so the same decisions and the same
+// re-test band. The factor and w_i are formed once per unit instead of once per test:
+// a test costs the forward solve for r_jS (about l^2 / 2 FMAs) instead of the
+// refactored rows (about l^2 / 2 per changed row, and a warp pays for its lane with
+// the most changed rows). Removed edges are skipped when the lane knows of the
+// removal: its own at once, the others' when it enters a row or a tile; unlike the
+// edge order, a unit cannot skip the rest of one edge's tests, so the host picks the
+// order from a level on where removals are rare. Rows of degree up to 64 keep the
+// membership of S and the live neighbours as bit masks; wider rows test membership
+// against the positions and read the live bit per test.
+constexpr int kSetMaskD = 64;
+template <int LT>
+constexpr int kSetBlocks = LT <= 8 ? 2 : 1;  // resident blocks per SM the set-order kernels are compiled for
+
+// Rows ci..l-1 of the Cholesky factor of the S block and of w_i = L_S^-1 r_iS: the
+// operations of test_f32_inc without w_j.
+template <int LA>
+__device__ __forceinline__ void factor_set(const float *__restrict__ C, int64_t stride, int64_t xi, const int *xs,
+                                           int l, int ci, Fact<LA> &F) {
+#pragma unroll (kUnr<LA>)
+  for (int r = 0; r < LA; ++r) {
+    if (r >= ci && r < l) {
+      const int64_t xr = xs[r];
+      float vx = C[xi * stride + xr];
+      float d = 1.0f;
+#pragma unroll (kUnr<LA>)
+      for (int c = 0; c < LA; ++c) {
+        if (c < r) {
+          float v = C[(int64_t)xs[c] * stride + xr];
+#pragma unroll (kUnr<LA>)
+          for (int q = 0; q < LA; ++q)
+            if (q < c) v -= F.Lm[r * (r + 1) / 2 + q] * F.Lm[c * (c + 1) / 2 + q];
+          v *= F.invd[c];
+          F.Lm[r * (r + 1) / 2 + c] = v;
+          d -= v * v;
+          vx -= v * F.wx[c];
+        }
+      }
+      const float id = rsqrtf(fmaxf(d, 1e-30f));
+      F.piv[r] = d;
+      F.invd[r] = id;
+      F.wx[r] = vx * id;
+    }
+  }
+}
+
+// FP32 test of (i, j | S) on the unit's factor: w_j by forward solve, then the tail of
+// test_f32_inc (sx = |w_i|^2 and dmin = the smallest pivot, both in row order, come
+// with the factor). Same return values.
+template <int LA>
+__device__ __forceinline__ int test_set_j(const Inst &I, const float *__restrict__ C, int64_t stride, int64_t xi,
+                                          int64_t xj, const int *xs, int l, const Fact<LA> &F, float sx, float dmin,
+                                          float *rr_out) {
+  float gy[LA], wy[LA];
+#pragma unroll (kUnr<LA>)
+  for (int r = 0; r < LA; ++r)
+    if (r < l) gy[r] = C[xj * stride + xs[r]];
+  const float rij = C[xi * stride + xj];
+  float sy = 0.f, sxy = 0.f;
+#pragma unroll (kUnr<LA>)
+  for (int r = 0; r < LA; ++r)
+    if (r < l) {
+      float vy = gy[r];
+#pragma unroll (kUnr<LA>)
+      for (int c = 0; c < LA; ++c)
+        if (c < r) vy -= F.Lm[r * (r + 1) / 2 + c] * wy[c];
+      wy[r] = vy * F.invd[r];
+      sy += wy[r] * wy[r];
+      sxy += F.wx[r] * wy[r];
+    }
+  const float ax = 1.0f - sx, ay = 1.0f - sy;
+  const float cond = fminf(dmin, fminf(ax, ay));
+  if (!(cond > 1e-3f)) return 2;
+  const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
+  *rr_out = rr;
+  const float dist = rr - I.r_c;
+  const float ke = I.ke_a + (float)(l + 2) * I.ke_b;
+  const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
+  if (!(fabsf(dist) > band)) return 2;
+  return dist < 0.0f ? 1 : 0;
+}
+
+// live bits of row i's snapshot neighbours (bit q: the q-th; d <= kSetMaskD), read by
+// one lane
+__device__ __forceinline__ uint64_t row_live_mask(const Inst &I, int64_t i, int base, int d) {
+  uint64_t m = 0;
+  if (d > kSetMaskD) return m;
+  for (int q = 0; q < d; ++q)
+    if (live_bit(I.adj, I.W, i, I.colidx[base + q])) m |= 1ull << q;
+  return m;
+}
+
+template <int LT>
+__device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *rw_smem, const TuneEntry &te,
+                                          TestSmem<LT, true> &sm) {
+  constexpr int LA = LT;
+  constexpr int l = LT;
+  const int level = L.level;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float *blk = sm.blk[wib];
+  int64_t blk_i = -1;  // row and instance of the staged block
+  int blk_b = -1;
+  uint64_t blk_live = 0;  // live bits of the staged row's neighbours, read when the tile starts
+  PendRem<LA> *pend = sm.pend[wib];
+  int *np = sm.np + wib;
+  if (lane == 0) *np = 0;
+  __syncwarp();
+  const unsigned long long total = L.work_prefix[L.count];
+  if (total == 0) return;
+  const unsigned long long *rw_c = cache_row_work(L, rw_smem);
+  const unsigned long long lanes = (unsigned long long)gridDim.x * blockDim.x;
+  const int m = tile_tests_per_lane(total, lanes, te, true);
+  const unsigned long long per_tile = 32ull * (unsigned long long)m;
+  const unsigned long long nwarps = lanes >> 5;
+  int pos[LA], xs[LA];
+  bool first_tile = true;
+  for (;;) {
+    unsigned long long tile = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    if (!first_tile) {
+      if (lane == 0) tile = nwarps + atomicAdd(&L.lc->tile_next, 1ull);
+      tile = __shfl_sync(0xffffffffu, tile, 0);
+    }
+    first_tile = false;
+    const unsigned long long t0 = tile * per_tile;
+    if (t0 >= total) break;
+    unsigned long long t = t0 + (unsigned long long)lane * m;
+    const unsigned long long tend = min(t + (unsigned long long)m, total);
+    unsigned executed = 0, retests = 0;
+    int b_last = -1;
+    int b = find_inst_u(L.work_prefix, L.count, t0);
+    const Inst *I = inst_of(L, b);
+    unsigned long long base_t = L.work_prefix[b];
+    const int64_t i0 = warp_find_row(rw_c ? rw_c : I->row_work, I->p, t0 - base_t);
+    {  // the block of the tile's first row and its neighbours' live bits (whole warp)
+      const int d0 = I->deg[i0];
+      if (d0 <= kBlkD) {
+        if (i0 != blk_i || b != blk_b) {
+          stage_block(*I, i0, d0, blk);
+          blk_i = i0;
+          blk_b = b;
+        }
+        const int base0 = I->rowptr[i0];
+        const bool lv = lane < d0 && live_bit(I->adj, I->W, i0, I->colidx[base0 + lane]);
+        blk_live = __ballot_sync(0xffffffffu, lv);
+      } else {
+        blk_i = -1;
+        blk_b = -1;
+      }
+    }
+    const bool active = t < tend;
+    const bool same = t < L.work_prefix[b + 1];
+    int64_t i = lane_find_row(rw_c ? rw_c : I->row_work, I->p, i0, (active && same ? t : t0) - base_t, active && same);
+    if (active && !same) {  // the tile runs into the next instance
+      b = find_inst_u(L.work_prefix, L.count, t);
+      I = inst_of(L, b);
+      base_t = L.work_prefix[b];
+      i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
+    }
+    if (active) {
+      int d = I->deg[i];
+      int base = I->rowptr[i];
+      unrank_lex_fast(t - base_t - (rw_c ? rw_c : I->row_work)[i], l, d, pos);
+      bool staged = i == blk_i && b == blk_b;
+      uint64_t live = staged ? blk_live : row_live_mask(*I, i, base, d);
+      int ci = 0;  // lowest member changed since the last unit (factor rows below are valid)
+      Fact<LA> F;
+      for (;;) {
+        // the members' indices into the entries: block-local in the staged block, else
+        // variable ids in the instance's matrix
+        const float *C = staged ? blk : I->cor32;
+        const int64_t stride = staged ? (int64_t)kBlkS : I->p;
+        const int64_t xi = staged ? 0 : i;
+#pragma unroll (kUnr<LA>)
+        for (int q = 0; q < LA; ++q)
+          if (q >= ci) xs[q] = staged ? pos[q] + 1 : I->colidx[base + pos[q]];
+        factor_set<LA>(C, stride, xi, xs, l, ci, F);
+        float sx = 0.f, dmin = 1.f;
+#pragma unroll (kUnr<LA>)
+        for (int r = 0; r < LA; ++r) {
+          dmin = fminf(dmin, F.piv[r]);
+          sx += F.wx[r] * F.wx[r];
+        }
+        // the unit's tests: neighbours q outside S, live as far as the lane knows
+        auto test_q = [&](int q) {
+          const int64_t xj = staged ? (int64_t)(q + 1) : (int64_t)I->colidx[base + q];
+          float rr = 0.f;
+          const int res = test_set_j<LA>(*I, C, stride, xi, xj, xs, l, F, sx, dmin, &rr);
+          ++executed;
+          if (res == 0) return;
+          // removal or re-test: the variable ids of j and S
+          const int64_t j = staged ? (int64_t)I->colidx[base + q] : xj;
+          int ids[LA];
+#pragma unroll (kUnr<LA>)
+          for (int r = 0; r < LA; ++r) ids[r] = staged ? I->colidx[base + pos[r]] : xs[r];
+          bool rm = false;
+          double pv = 0.0;
+          if (res == 1) {
+            // decided in FP32; the p-value is evaluated when the records are read
+            rm = true;
+            pv = -1.0 - (double)rr;
+          } else {
+            // deferred to the FP64 re-test kernel (the set order runs only without an FP64
+            // matrix); a full queue is flagged and the host reruns the skeleton in the edge
+            // order, so the test is never decided here
+            ++retests;
+            if (!push_retest(L, b, i, j, ids, l)) atomicOr(&I->g->err, kErrRetestOverflow);
+          }
+          if (rm) {
+            if (claim_edge(*I, i, j)) push_pending<LA>(pend, np, *I, b, level, i, j, ids, l, pv);
+            if (q < kSetMaskD) live &= ~(1ull << q);
+          }
+        };
+        if (d <= kSetMaskD) {
+          uint64_t in_s = 0;
+#pragma unroll (kUnr<LA>)
+          for (int r = 0; r < LA; ++r) in_s |= 1ull << pos[r];
+          uint64_t todo = live & ~in_s;
+          while (todo) {
+            const int q = __ffsll((long long)todo) - 1;
+            todo &= todo - 1;
+            test_q(q);
+          }
+        } else {
+          for (int q = 0; q < d; ++q) {
+            bool member = false;
+#pragma unroll (kUnr<LA>)
+            for (int r = 0; r < LA; ++r) member |= pos[r] == q;
+            if (member || !live_bit(I->adj, I->W, i, I->colidx[base + q])) continue;
+            test_q(q);
+          }
+        }
+        if (++t >= tend) break;
+        ci = next_lex(l, d, pos);
+        if (ci < 0) {  // the row's last set: the next row with tests, possibly of the next instance
+          if (t >= L.work_prefix[b + 1]) {
+            b = find_inst_u(L.work_prefix, L.count, t);
+            I = inst_of(L, b);
+            base_t = L.work_prefix[b];
+            i = find_row(rw_c ? rw_c : I->row_work, I->p, t - base_t);
+          } else {
+            i = find_row_from(rw_c ? rw_c : I->row_work, I->p, i, t - base_t);
+          }
+          d = I->deg[i];
+          base = I->rowptr[i];
+#pragma unroll (kUnr<LA>)
+          for (int q = 0; q < LA; ++q) pos[q] = q;
+          ci = 0;
+          staged = i == blk_i && b == blk_b;
+          live = staged ? blk_live : row_live_mask(*I, i, base, d);
+        }
+      }
+      b_last = b;
+    }
+    __syncwarp();
+    flush_pending<LA>(L, level, pend, np);
+    const unsigned grp = __match_any_sync(0xffffffffu, b_last);
+    const unsigned ex = __reduce_add_sync(grp, executed);
+    const unsigned rt = __reduce_add_sync(grp, retests);
+    if (b_last >= 0 && lane == __ffs(grp) - 1) {
+      atomicAdd(&inst_of(L, b_last)->ctr[level].tests, (unsigned long long)ex);
+      if (rt) atomicAdd(&inst_of(L, b_last)->ctr[level].retests, (unsigned long long)rt);
+    }
+  }
+}
+
 // One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
 // is the lane-interleaved level-1 body (V: kL1Prefetch loads one step ahead,
 // kL1Chunked runs the chunked body of the higher levels; picked by the tile policy),
-// LT = 2..16 the bodies unrolled for l = LT, LT = 0 the runtime-level body.
+// LT = 2..16 the bodies unrolled for l = LT (V = kSetOrder: in the set order), LT = 0
+// the runtime-level body.
 template <int LT, bool MIXED, int V = kL1Interleaved>
-__global__ void __launch_bounds__(kThreads, LT == 1 && V != kL1Chunked ? 4 : 2)
+__global__ void __launch_bounds__(kThreads, V == kSetOrder ? kSetBlocks<LT> : (LT == 1 && (V & 3) != kL1Chunked ? 4 : 2))
     level_kernel(const __grid_constant__ Launch L) {
   extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
   rebuild_phase(L);
   if (!grid_barrier(L, epoch)) return;
-  scan_phase(L);
+  scan_phase(L, V == kSetOrder);
   if (!grid_barrier(L, epoch)) return;
   const TuneEntry te = tile_policy(L);
-  if (LT == 1 && V != kL1Chunked)  // level 1 keeps the SM's on-chip memory for L1 cache
-    tests_l1<MIXED, V == kL1Prefetch>(L, nullptr, te);
-  else
-    tests_generic<LT, MIXED>(L, LT == 1 ? nullptr : rw_smem, te);
+  if constexpr (V == kSetOrder) {
+    static_assert(MIXED && LT >= 2 && LT <= 16, "the set order runs levels 2-16 in mixed precision");
+    __shared__ TestSmem<LT, true> sm;
+    tests_set<LT>(L, rw_smem, te, sm);
+  } else if constexpr (LT == 1 && (V & 3) != kL1Chunked) {  // level 1 keeps the SM's on-chip memory for L1 cache
+    tests_l1<MIXED, (V & 3) == kL1Prefetch, (V & kQueueOnly) != 0>(L, nullptr, te);
+  } else {
+    __shared__ TestSmem<LT, MIXED> sm;
+    tests_generic<LT, MIXED>(L, LT == 1 ? nullptr : rw_smem, te, sm);
+  }
 }
 
 }  // namespace
 
 // level kernels of levels 9-32 (citest_l9.cu, citest_l13.cu, citest_l17.cu)
-void *level_kernel_9_12(int level, bool mixed);
-void *level_kernel_13_16(int level, bool mixed);
+void *level_kernel_9_12(int level, bool mixed, bool set);
+void *level_kernel_13_16(int level, bool mixed, bool set);
 void *level_kernel_17_up(int level, bool mixed);
 
 }  // namespace hpc

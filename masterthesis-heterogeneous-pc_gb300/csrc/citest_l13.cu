@@ -4,7 +4,16 @@
 
 namespace hpc {
 
-void *level_kernel_13_16(int level, bool mixed) {
+void *level_kernel_13_16(int level, bool mixed, bool set) {
+  if (mixed && set) {
+    switch (level) {
+      case 13: return (void *)level_kernel<13, true, kSetOrder>;
+      case 14: return (void *)level_kernel<14, true, kSetOrder>;
+      case 15: return (void *)level_kernel<15, true, kSetOrder>;
+      case 16: return (void *)level_kernel<16, true, kSetOrder>;
+      default: return nullptr;
+    }
+  }
   switch (level) {
     case 13: return mixed ? (void *)level_kernel<13, true> : (void *)level_kernel<13, false>;
     case 14: return mixed ? (void *)level_kernel<14, true> : (void *)level_kernel<14, false>;

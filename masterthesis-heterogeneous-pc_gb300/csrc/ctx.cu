@@ -93,6 +93,7 @@ cudaStream_t alloc_stream() {
 // Test hooks: the k-th device allocation from now fails (0 = none), and the number of
 // the library's device allocations currently live.
 std::atomic<long long> g_fail_alloc_in{0};
+std::atomic<int> g_set_from{kSetOrderFrom};
 std::atomic<long long> g_live_allocs{0};
 
 template <typename T>
@@ -177,7 +178,9 @@ hpc_status write_inst_table(hpc_ctx *c) {
     I.hi32 = rc >= 1.5 ? 2.f : (float)(rc + d0);
     I.cor64 = (c->cor64_valid && c->cor64) ? c->cor64 + h.cor_off : nullptr;
     I.cor32 = c->cor32 ? c->cor32 + h.cor_off : nullptr;
-    I.Z = c->Z ? c->Z + h.z_off : nullptr;
+    I.Z = c->z_valid ? c->Z + h.z_off : nullptr;
+    I.zh = (!c->z_valid && c->zpair_valid) ? c->zpair + h.z_off : nullptr;
+    I.zl = (!c->z_valid && c->zpair_valid) ? c->zpair + c->ztot + h.z_off : nullptr;
     I.n_z = h.n;
     I.denom = denom_of(c, h.n);
     I.adj = c->adj + h.adj_off;
@@ -202,6 +205,15 @@ hpc_status write_inst_table(hpc_ctx *c) {
   return HPC_OK;
 }
 
+// The lowest set-order level in effect for a context (0: the edge order throughout):
+// the process-wide setting, where the context's re-tests are queued (no FP64 matrix),
+// the set order was not turned off by a re-test queue overflow, and the levels run in
+// a whole-skeleton call (hpc_run_level cannot repeat a run after an overflow).
+int effective_set_from(const hpc_ctx *c) {
+  if (c->opts.precision == HPC_PREC_FP64 || c->cor64_valid || c->set_off || c->level_by_level) return 0;
+  return set_order_from();
+}
+
 Launch make_launch(hpc_ctx *c, int level) {
   Launch L{};
   L.inst = c->inst;
@@ -214,6 +226,9 @@ Launch make_launch(hpc_ctx *c, int level) {
   L.lc = c->lc + level;
   L.rq = c->rq;
   L.rq_cap = c->rq_cap;
+  L.rq_val = c->rq_val;
+  L.rq_done = c->rq_done;
+  L.rq_vcap = c->rq_vcap;
   L.seg_prefix = c->prefixes + 3 * (c->count + 1);
   L.seg = c->seg + (size_t)level * c->total_segs;
   L.row_cache = c->count == 1 && c->ih[0].p + 1 <= kRowCache;
@@ -260,10 +275,15 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   }
   // snapshot rebuild, test-count scan and CI tests in one launch
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  const int l1v = level == 1 ? c->l1v_now : kL1Chunked;
-  if ((s = launch_level(L, c->opts.precision, level == 1 ? c->citest_grid_l1[l1v] : c->citest_grid[level], l1v,
-                        c->stream)) != HPC_OK)
-    return s;
+  const bool set = uses_set_order(effective_set_from(c), level);
+  // level 1: the queue-only build of the interleaved variants where the re-tests are
+  // queued and a queue overflow can be rerun
+  const bool qo = level == 1 && c->l1v_now != kL1Chunked && effective_set_from(c) > 0;
+  const int var = level == 1 ? (qo ? c->l1v_now | kQueueOnly : c->l1v_now) : set ? kSetOrder : kL1Interleaved;
+  const int grid = level == 1 ? (qo ? c->citest_grid_l1q[c->l1v_now] : c->citest_grid_l1[var])
+                   : set      ? c->citest_grid_set[level]
+                              : c->citest_grid[level];
+  if ((s = launch_level(L, c->opts.precision, grid, var, c->stream)) != HPC_OK) return s;
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += queue ? 2 : 1;
@@ -393,10 +413,17 @@ hpc_status global_errors(hpc_ctx *c) {
   return HPC_OK;
 }
 
-bool any_csr_overflow(hpc_ctx *c) {
-  for (int b = 0; b < c->count; ++b)
-    if (c->gctr_host[b].err & kErrCsrOverflow) return true;
-  return false;
+// A run to repeat from level 0: the neighbour lists were too small (the data changed
+// since they were sized), or the set order found the re-test queue full (the rerun
+// keeps the edge order, whose tests re-test inline when the queue is full).
+bool needs_rerun(hpc_ctx *c) {
+  bool again = false;
+  for (int b = 0; b < c->count; ++b) {
+    const int err = c->gctr_host[b].err;
+    if (err & kErrRetestOverflow) c->set_off = true;
+    if (err & (kErrCsrOverflow | kErrRetestOverflow)) again = true;
+  }
+  return again;
 }
 
 bool any_work(hpc_ctx *c, int level) {
@@ -471,6 +498,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
   if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
                        c->graph_version == c->inst_version && c->graph_l1v == c->l1v_now &&
+                       c->graph_set_from == effective_set_from(c) &&
                        c->graph_final == finalize;
     if (!valid) {
       if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -496,6 +524,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
       c->graph_stream = c->stream;
       c->graph_version = c->inst_version;
       c->graph_l1v = c->l1v_now;
+      c->graph_set_from = effective_set_from(c);
       c->graph_final = finalize;
     }
     HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
@@ -588,22 +617,31 @@ GramArgs gram_args(hpc_ctx *c) {
 // level 1 (4.7 M of 1.1e11 at p = 15000), so the queue grows with sum p^2 / 16, from 1 Mi
 // to 16 Mi entries (144 B each). Tests beyond it are re-tested in place.
 long long retest_queue_cap(long long sum_p2) {
-  return std::min<long long>(16ll << 20, std::max<long long>(1ll << 20, sum_p2 / 16));
+  return std::min<long long>(64ll << 20, std::max<long long>(1ll << 20, sum_p2 / 16));
 }
 
 // The deferred FP64 re-test queue, allocated before the first run of a context
 // without an FP64 matrix (tensor-core mode); contexts whose levels run elsewhere (the
 // server's shared launches bring their own queue) never allocate it.
+// queue of `cap` items with its entry scratch and zeroed done counters
+hpc_status alloc_rq(hpc_ctx *c, long long cap) {
+  hpc_status s;
+  if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
+  c->rq_cap = cap;
+  const long long vcap = retest_scratch_entries(cap);
+  if ((s = dev_alloc(&c->rq_val, vcap, "re-test entries")) != HPC_OK) return s;
+  if ((s = dev_alloc(&c->rq_done, cap, "re-test counters")) != HPC_OK) return s;
+  c->rq_vcap = vcap;
+  HPC_CUDA(cudaMemsetAsync(c->rq_done, 0, sizeof(unsigned int) * (size_t)cap, c->stream));
+  ++c->inst_version;  // a captured graph holds the queue pointers
+  return HPC_OK;
+}
+
 hpc_status ensure_rq(hpc_ctx *c) {
   if (c->rq || c->cor64_valid) return HPC_OK;
   long long p2 = 0;
   for (const auto &h : c->ih) p2 += h.p * h.p;
-  const long long cap = retest_queue_cap(p2);
-  hpc_status s;
-  if ((s = dev_alloc(&c->rq, cap, "re-test queue")) != HPC_OK) return s;
-  c->rq_cap = cap;
-  ++c->inst_version;  // a captured graph holds the queue pointer
-  return HPC_OK;
+  return alloc_rq(c, retest_queue_cap(p2));
 }
 
 hpc_status after_correlation(hpc_ctx *c) {
@@ -623,8 +661,16 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
   if ((s = ensure_meta(c)) != HPC_OK) return s;
   long long ztot = 0;
   for (const auto &h : c->ih) ztot += h.n * h.p;
-  if (!c->Z && (s = dev_alloc(&c->Z, ztot, "standardised data")) != HPC_OK) return s;
   const bool tc = c->opts.precision == HPC_PREC_MIXED_TC;
+  // Tensor-core mode with FP32 observations keeps the standardised data as FP32 pairs
+  // (zh + zl, FP64-grade, formed without FP64 arithmetic) instead of FP64: the FP64
+  // entries of the re-tests are dot products of those.
+  const bool pair = tc && f32;
+  c->z_valid = false;
+  c->zpair_valid = false;
+  c->ztot = ztot;
+  if (!pair && !c->Z && (s = dev_alloc(&c->Z, ztot, "standardised data")) != HPC_OK) return s;
+  if (pair && !c->zpair && (s = dev_alloc(&c->zpair, 2 * ztot, "standardised data (FP32 pairs)")) != HPC_OK) return s;
   StdArgs sa = std_args(c);
   HPC_CUDA(cudaEventRecord(c->evc[0], c->stream));
   if (tc) {
@@ -645,8 +691,11 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
                                c->stream));
       HPC_CUDA(cudaStreamSynchronize(c->stream));
     }
-    if ((s = launch_standardise(X, f32, sa, sa.count ? c->total_rows : 0, c->Z, c->tcP, nullptr, c->stream)) != HPC_OK)
+    if ((s = launch_standardise(X, f32, sa, sa.count ? c->total_rows : 0, pair ? nullptr : c->Z,
+                                pair ? c->zpair : nullptr, ztot, c->tcP, c->stream)) != HPC_OK)
       return s;
+    c->z_valid = !pair;
+    c->zpair_valid = pair;
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
     TcArgs ta{};
     ta.count = c->count;
@@ -658,11 +707,13 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
     ta.err = &c->gctr[0].err;
     if ((s = launch_gram_tc(c->cor32, ta, c->tiles_tc, c->stream)) != HPC_OK) return s;
     HPC_CUDA(cudaEventRecord(c->evc[2], c->stream));
-    c->cor64_valid = false;  // FP64 entries come from dot products of Z in the re-test kernels
+    c->cor64_valid = false;  // FP64 entries come from standardised dot products in the re-test kernels
     c->cor32_rounded = false;
     c->timings.launches += 2;
   } else {
-    if ((s = launch_standardise(X, f32, sa, c->total_rows, c->Z, nullptr, nullptr, c->stream)) != HPC_OK) return s;
+    if ((s = launch_standardise(X, f32, sa, c->total_rows, c->Z, nullptr, 0, nullptr, c->stream)) != HPC_OK)
+      return s;
+    c->z_valid = true;
     HPC_CUDA(cudaEventRecord(c->evc[1], c->stream));
     c->cor64_valid = true;
     c->cor32_rounded = true;
@@ -748,6 +799,12 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
 
 }  // namespace
 
+int set_order_from() { return g_set_from.load(); }
+long long retest_scratch_entries(long long cap) { return std::min<long long>(32ll << 20, 3 * cap); }
+bool uses_set_order(int set_from, int level) {
+  return set_from > 0 && level >= 2 && level <= 16 && level >= set_from;
+}
+
 // for the server's shared launches (serve.cu)
 hpc_status ctx_size_after_level0(hpc_ctx *c) {
   bool changed = false;
@@ -800,7 +857,7 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   if (o->precision != HPC_PREC_MIXED_TC) b += p * p * 8;           // cor64
   if (o->precision != HPC_PREC_FP64) b += p * p * 4;               // cor32
   if (o->precision == HPC_PREC_MIXED_TC) b += tc_p_pad(p) * tc_k(n) * 2;      // split operand planes
-  b += n * p * 8;                                                  // standardised data
+  b += n * p * 8;                                                  // standardised data (FP64 or FP32 pairs)
   b += n * p * 4;                                                  // observation staging
   b += p * W * 4 + p * p;                                          // adjacency bits + bytes
   b += (p + 1) * (4 + 4 + 8);                                      // deg, rowptr, row_work
@@ -809,7 +866,10 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
   const int rec_ids = o->max_level < 0 ? HPC_MAX_LEVEL : std::min(std::max(o->max_level, 1), HPC_MAX_LEVEL);
   b += 2 * e * 4 + e * 4 * (int64_t)rec_stride_words(rec_ids);
-  if (o->precision == HPC_PREC_MIXED_TC) b += retest_queue_cap(p * p) * (int64_t)sizeof(RetestItem);
+  if (o->precision == HPC_PREC_MIXED_TC) {
+    const int64_t cap = retest_queue_cap(p * p);
+    b += cap * ((int64_t)sizeof(RetestItem) + 4) + retest_scratch_entries(cap) * 8;  // queue, counters, entries
+  }
   *bytes = b;
   return HPC_OK;
 }
@@ -843,8 +903,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->cor64);
   dev_free(c->cor32);
   dev_free(c->Z);
+  dev_free(c->zpair);
   dev_free(c->tcP);
-  dev_free(c->tcQ);
   dev_free(c->emuD);
   dev_free(c->emuE);
   dev_free(c->tc_maps);
@@ -861,6 +921,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->colidx);
   dev_free(c->recs);
   dev_free(c->rq);
+  dev_free(c->rq_val);
+  dev_free(c->rq_done);
   dev_free(c->ctr);
   dev_free(c->gctr);
   dev_free(c->lc);
@@ -1062,8 +1124,15 @@ hpc_status hpc_get_correlation(hpc_ctx *c, double *C) {
   long long tot = 0;
   for (const auto &h : c->ih) tot += h.p * h.p;
   if (!c->cor64_valid) {
-    // tensor-core mode keeps no FP64 matrix: form it from the standardised data
+    // tensor-core mode keeps no FP64 matrix: form it from the standardised data (FP64
+    // from the FP32 pairs where the context keeps those: the values the re-tests use)
     if (!c->cor64 && (s = dev_alloc(&c->cor64, tot, "cor64")) != HPC_OK) return s;
+    if (!c->z_valid) {
+      if (!c->zpair_valid) return HPC_ERR_STATE;
+      if (!c->Z && (s = dev_alloc(&c->Z, c->ztot, "standardised data")) != HPC_OK) return s;
+      if ((s = launch_pair_to_f64(c->zpair, c->zpair + c->ztot, c->ztot, c->Z, c->stream)) != HPC_OK) return s;
+      c->z_valid = true;
+    }
     if ((s = launch_gram_f64(c->Z, c->cor64, gram_args(c), c->tiles64, c->stream)) != HPC_OK) return s;
     c->cor64_valid = true;
     if ((s = write_inst_table(c)) != HPC_OK) return s;
@@ -1115,9 +1184,12 @@ hpc_status hpc_run_level(hpc_ctx *c, int level, hpc_level_stats *st) {
     bool changed = false;
     if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
   }
-  if ((s = run_levels(c, level, level, false)) != HPC_OK) return s;
+  c->level_by_level = true;
+  s = run_levels(c, level, level, false);
+  c->level_by_level = false;
+  if (s != HPC_OK) return s;
   if ((s = global_errors(c)) != HPC_OK) return s;
-  if (any_csr_overflow(c)) {
+  if (needs_rerun(c)) {
     set_error("neighbour-list buffer too small");
     return HPC_ERR_CAPACITY;
   }
@@ -1142,7 +1214,7 @@ static hpc_status run_chunks(hpc_ctx *c, int first, int top, int *last_run, bool
     else if (first == 0 && c->exhaust_top >= 1) last = std::min(top, c->exhaust_top);
     if ((s = run_levels(c, first, last, known || first == 0, true, true)) != HPC_OK) return s;
     *last_run = last;
-    if (any_csr_overflow(c)) {
+    if (needs_rerun(c)) {
       *overflow = true;
       return HPC_OK;
     }
@@ -1190,7 +1262,7 @@ hpc_status hpc_run_skeleton(hpc_ctx *c, hpc_level_stats *stats, int cap, int *le
   }
   if ((s = ensure_rq(c)) != HPC_OK) return s;
   HPC_CUDA(cudaEventRecord(c->evr[0], c->stream));
-  for (int attempt = 0; attempt < 2; ++attempt) {
+  for (int attempt = 0; attempt < 3; ++attempt) {
     ran = 0;
     for (auto &h : c->ih) h.edges = h.p * (h.p - 1) / 2;
     const bool sized = c->colidx && c->recs;
@@ -1266,7 +1338,7 @@ hpc_status hpc_wait(hpc_ctx *c, hpc_level_stats *stats, int cap, int *levels_run
   if (c->async_pending) {
     c->async_pending = false;
     if ((s = pull_counters(c)) != HPC_OK) return s;
-    if (any_csr_overflow(c)) {
+    if (needs_rerun(c)) {
       // the data changed since the neighbour lists were sized: resize and rerun
       bool changed;
       if ((s = ensure_capacity(c, &changed)) != HPC_OK) return s;
@@ -1612,6 +1684,37 @@ hpc_status hpc_debug_fail_allocation(int64_t k) {
 
 int64_t hpc_debug_live_allocations(void) { return g_live_allocs.load(); }
 
+
+hpc_status hpc_debug_set_retest_queue(hpc_ctx *c, int64_t entries) {
+  hpc_status s = check_ctx(c);
+  if (s != HPC_OK) return s;
+  if (entries < 1) {
+    set_error("re-test queue of %lld entries", (long long)entries);
+    return HPC_ERR_INVALID_ARG;
+  }
+  HPC_CUDA(cudaStreamSynchronize(c->stream));
+  dev_free(c->rq);
+  dev_free(c->rq_val);
+  dev_free(c->rq_done);
+  c->rq = nullptr;
+  c->rq_val = nullptr;
+  c->rq_done = nullptr;
+  if ((s = alloc_rq(c, entries)) != HPC_OK) return s;
+  c->set_off = false;
+  return HPC_OK;
+}
+
+int hpc_debug_set_order_active(hpc_ctx *c) { return c && !c->set_off ? 1 : 0; }
+
+hpc_status hpc_debug_set_order_from(int level) {
+  if (level != 0 && (level < 2 || level > HPC_MAX_LEVEL)) {
+    set_error("set order from level %d: 0 or 2..%d", level, HPC_MAX_LEVEL);
+    return HPC_ERR_INVALID_ARG;
+  }
+  g_set_from.store(level);
+  return HPC_OK;
+}
+
 hpc_status hpc_debug_set_barrier(hpc_ctx *c, int64_t wait_ns, int extra_arrivals) {
   hpc_status s = check_ctx(c);
   if (s != HPC_OK) return s;
@@ -1767,7 +1870,11 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   // at low levels never loads the level-17..32 kernel, whose local-memory stack frame
   // (35 KB per thread) would otherwise be reserved for the whole device
   for (int l = 1; l <= c->rec_ids; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
+  if (o.precision != HPC_PREC_FP64)
+    for (int l = 2; l <= std::min(c->rec_ids, 16); ++l) c->citest_grid_set[l] = citest_grid(o.precision, l, c->device, kSetOrder);
   for (int v = 0; v < 3; ++v) c->citest_grid_l1[v] = citest_grid(o.precision, 1, c->device, v);
+  if (o.precision != HPC_PREC_FP64)
+    for (int v = 0; v < 2; ++v) c->citest_grid_l1q[v] = citest_grid(o.precision, 1, c->device, v | kQueueOnly);
   if (c->rec_ids > 16) retest_setup();  // the re-test kernel of levels 17-32
   if (o.precision != HPC_PREC_MIXED_TC && (s = dev_alloc(&c->cor64, cor, "cor64")) != HPC_OK) return fail(s);
   if (o.precision != HPC_PREC_FP64 && (s = dev_alloc(&c->cor32, cor, "cor32")) != HPC_OK) return fail(s);

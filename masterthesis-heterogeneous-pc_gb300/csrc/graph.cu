@@ -38,10 +38,7 @@ __device__ __noinline__ bool level0_keep_slow(const Launch &L, const Inst &I, in
     return false;  // the FP64 re-test kernel sets the kept bits
   }
   // queue full: serial FP64 dot product here
-  const double *x = I.Z + i * I.n_z, *y = I.Z + j * I.n_z;
-  double sum = 0.0;
-  for (int64_t k = 0; k < I.n_z; ++k) sum = fma(x[k], y[k], sum);
-  return !(calc_pvalue64(sum / I.denom, I.n_obs) >= I.alpha);
+  return !(calc_pvalue64(zdot(I, i, j, 0, 1) / I.denom, I.n_obs) >= I.alpha);
 }
 
 __device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int b, int64_t i, int64_t j, double v64,

@@ -79,6 +79,12 @@ struct TuneEntry {
 // level-1 kernel variants: lanes interleaved over an edge, the same with the next
 // position's entries loaded a step ahead, each lane a chunk of consecutive tests
 constexpr int kL1Interleaved = 0, kL1Prefetch = 1, kL1Chunked = 2;
+// kernel variant of levels 2-16 (mixed precision): the CI tests in the set order
+// (citest.cuh) instead of the edge order (variant 0)
+constexpr int kSetOrder = 3;
+// flag on the level-1 variants kL1Interleaved / kL1Prefetch: undecided tests only
+// queued (mixed precision without an FP64 matrix), as the set order does
+constexpr int kQueueOnly = 8;
 constexpr int kTuneDefaultCap = 64, kTuneDefaultTpl = 4, kTuneDefaultEdgeLanes = 32, kTuneMaxCap = 65536;
 // table of a context: [p bucket][level][degree bucket]; bucket = bit length, capped
 constexpr int kTunePB = 32, kTuneDB = 18;
@@ -96,6 +102,7 @@ constexpr int kSegRows = 256;
 struct SegAgg {
   unsigned long long deg;   // sum of degrees
   unsigned long long work;  // sum of tests per row
+  unsigned long long sets;  // sum of conditioning sets per row (the units of the set order)
   int max_deg;
   int rows;                 // rows with tests
   int over;                 // a row's test count does not fit
@@ -106,6 +113,7 @@ constexpr int kErrWorkOverflow = 2;
 constexpr int kErrCsrOverflow = 4;
 constexpr int kErrTimeout = 8;
 constexpr int kErrBandViolation = 16;
+constexpr int kErrRetestOverflow = 32;  // the set order found the re-test queue full: rerun in the edge order
 
 // Separation-set records on the device, packed: a head (the removed edge i < j, the
 // level and the p-value) and then the context's `rec_ids` separating-variable slots,
@@ -140,7 +148,8 @@ struct Inst {
   float lo32, hi32;       // level 0 on FP32 entries: FP64 re-test inside [lo32, hi32]
   const double *cor64;    // p x p FP64 or null (tensor-core mode: entries from Z)
   const float *cor32;     // p x p FP32 (mixed modes) or null
-  const double *Z;        // standardised data, n_z x p column-major, or null
+  const double *Z;        // FP64 standardised data, n_z x p column-major, or null
+  const float *zh, *zl;   // ... else the same values as FP32 pairs zh + zl (same layout)
   int64_t n_z;
   double denom;           // the Gram's divisor n - 1
   uint32_t *adj;          // live bitmask p x W
@@ -156,6 +165,39 @@ struct Inst {
   DevGlobal *g;
 };
 
+// Sum over samples k = k0, k0 + step, ... < n of z_a[k] * z_b[k], the FP64-standardised
+// variables a and b of one instance. From Z: FP64 FMAs. From the FP32 pairs: each
+// product zh_a zh_b with its exact rounding error (fmaf) and the cross terms, summed
+// with compensation (TwoSum) in FP32 and carried into FP64 every 16 samples -- about
+// 2^-45 relative per block, and FP32 arithmetic instead of this GPU's 1/64-rate FP64.
+__device__ __forceinline__ double zdot(const Inst &I, int64_t a, int64_t b, int64_t k0, int64_t step) {
+  const int64_t n = I.n_z;
+  double s = 0.0;
+  if (I.Z) {
+    const double *x = I.Z + a * n, *y = I.Z + b * n;
+    for (int64_t k = k0; k < n; k += step) s = fma(x[k], y[k], s);
+    return s;
+  }
+  const float *xh = I.zh + a * n, *xl = I.zl + a * n, *yh = I.zh + b * n, *yl = I.zl + b * n;
+  int64_t k = k0;
+  while (k < n) {
+    float sh = 0.f, sl = 0.f;
+#pragma unroll 16
+    for (int u = 0; u < 16 && k < n; ++u, k += step) {
+      const float ah = xh[k], al = xl[k], bh = yh[k], bl = yl[k];
+      const float p = ah * bh;
+      float e = fmaf(ah, bh, -p);
+      e = fmaf(ah, bl, fmaf(al, bh, e));
+      const float t = sh + p;
+      const float bb = t - sh;
+      sl += ((sh - (t - bb)) + (p - bb)) + e;
+      sh = t;
+    }
+    s += (double)sh + (double)sl;
+  }
+  return s;
+}
+
 // One level's launch over all instances, passed by value.
 struct Launch {
   const Inst *inst;
@@ -168,6 +210,9 @@ struct Launch {
   LaunchCounters *lc;               // this level's
   RetestItem *rq;                   // deferred FP64 re-tests
   long long rq_cap;
+  double *rq_val;                   // their entries, rq_vcap doubles of scratch (or null)
+  unsigned int *rq_done;            // entries done per item (rq_cap, zero between launches)
+  long long rq_vcap;
   const long long *seg_prefix;      // scan segments  sum ceil(p / kSegRows) (count + 1)
   SegAgg *seg;                      // this level's segment sums (zeroed before the level)
   int row_cache;                    // the CI tests keep the row offsets in shared memory
@@ -230,8 +275,11 @@ struct StdArgs {                    // grouped standardisation
   const long long *kdim;            // K' per instance (tensor-core layout)
   int ref_compat;
 };
+// Outputs: Z (FP64), or with the split-BF16 planes P either Z or (FP32 samples) the
+// FP32 pairs ZP (zh plane, then zl at + zp_plane elements).
 hpc_status launch_standardise(const void *X, bool f32, const StdArgs &a, long long total_rows, double *Z,
-                              __nv_bfloat16 *P, __nv_bfloat16 *Q, cudaStream_t s);
+                              float *ZP, long long zp_plane, __nv_bfloat16 *P, cudaStream_t s);
+hpc_status launch_pair_to_f64(const float *zh, const float *zl, long long count, double *Z, cudaStream_t s);
 struct GramArgs {                   // grouped FP64 Gram
   int count;
   const long long *tile_prefix;     // 64 x 64 upper-triangle tiles (count + 1)
@@ -298,6 +346,17 @@ TuneEntry tune_get(int p_bucket, int level, int deg_bucket);  // by bucket indic
 // the bytes of the re-test queue a context of sum p^2 would hold
 hpc_status ctx_size_after_level0(hpc_ctx *c);
 long long ctx_retest_queue_bytes(long long sum_p2);
+// entries of re-test scratch for a queue of `cap` items: three per item (a level-1
+// re-test), at most 32 Mi
+long long retest_scratch_entries(long long cap);
+// The lowest level whose CI tests run in the set order (citest.cuh; 0: the edge order at
+// every level), process-wide: kSetOrderFrom unless hpc_debug_set_order_from changed it.
+// uses_set_order: whether a level runs in the set order, given the lowest set-order
+// level in effect (0: none). The set order defers every undecided test to the FP64
+// re-test queue, so it runs only where the re-tests are queued (no FP64 matrix).
+constexpr int kSetOrderFrom = 4;
+int set_order_from();
+bool uses_set_order(int set_from, int level);
 
 // per-instance host bookkeeping
 struct InstHost {
@@ -326,7 +385,11 @@ struct hpc_ctx {
   double *cor64 = nullptr;        // sum p^2 (absent in tensor-core mode unless loaded)
   float *cor32 = nullptr;         // sum p^2 (mixed modes)
   double *Z = nullptr;            // sum n * p
-  __nv_bfloat16 *tcP = nullptr, *tcQ = nullptr;  // split-BF16 operands, sum p_pad * K'
+  bool z_valid = false;           // Z holds the current data's standardised values
+  float *zpair = nullptr;         // the same as FP32 pairs (tensor-core mode, FP32 data): zh | zl planes
+  bool zpair_valid = false;
+  long long ztot = 0;             // sum n * p: the elements of one plane
+  __nv_bfloat16 *tcP = nullptr;   // split-BF16 operands, sum p_pad * K'
   __nv_bfloat16 *emuD = nullptr;  // exact digit planes of the FP64-accurate tensor-core Gram
   int *emuE = nullptr;            // ... and the variables' exponents
   CUtensorMap *tc_maps = nullptr;  // device, 2 per instance
@@ -344,6 +407,9 @@ struct hpc_ctx {
   int rec_ids = HPC_MAX_LEVEL;    // id slots per record: the highest level the context runs
   hpc::RetestItem *rq = nullptr;
   long long rq_cap = 0;
+  double *rq_val = nullptr;       // the re-tests' entries (scratch) and per-item done counters
+  unsigned int *rq_done = nullptr;
+  long long rq_vcap = 0;
   hpc::DevCounters *ctr = nullptr;       // count x (HPC_MAX_LEVEL + 1)
   hpc::DevCounters *ctr_host = nullptr;  // host mirror
   hpc::DevGlobal *gctr = nullptr;        // count
@@ -377,9 +443,14 @@ struct hpc_ctx {
   hpc::TuneEntry tune_force{};
   int p_bucket = 0;
   int citest_grid_l1[3] = {};     // grids of the level-1 kernel variants (kL1*)
+  int citest_grid_l1q[2] = {};    // ... and of the queue-only ones (kL1Interleaved, kL1Prefetch | kQueueOnly)
+  int citest_grid_set[HPC_MAX_LEVEL + 1] = {};  // grids of the set-order kernels (levels 2-16)
   int l1_max_deg = -1;            // level-1 max degree of the last run (keys level 1's kernel choice)
   int l1v_now = 0;                // the level-1 kernel variant of the runs being queued
   int graph_l1v = 0;              // ... and of the captured graph
+  int graph_set_from = 0;         // the set-order levels of the captured graph
+  bool set_off = false;           // the set order turned off (a re-test queue overflow)
+  bool level_by_level = false;    // inside hpc_run_level: the edge order, inline re-tests on overflow
   bool graph_final = false;       // the captured graph ends with the record finalisation
   cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
   cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done

@@ -136,7 +136,7 @@ extern "C" hpc_status hpc_correlation_noalloc_f64(const double *X_dev, int64_t n
   sa.n_pad = &md->n_pad;
   sa.kdim = &md->kdim;
   sa.ref_compat = ref_compat_sd;
-  if ((s = launch_standardise(X_dev, false, sa, p, Z, nullptr, nullptr, st)) != HPC_OK) return s;
+  if ((s = launch_standardise(X_dev, false, sa, p, Z, nullptr, 0, nullptr, st)) != HPC_OK) return s;
   GramArgs ga{};
   ga.count = 1;
   ga.tile_prefix = md->tile_prefix;

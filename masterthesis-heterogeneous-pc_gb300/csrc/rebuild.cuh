@@ -6,10 +6,13 @@
 //            neighbour ids, ascending, into the row's fixed slot of the neighbour-list
 //            buffer -- slots are sized by the degrees after level 0 (degrees only
 //            fall), so no per-level offsets are needed for the lists; the per-segment
-//            sums of d_i and of the row test counts d_i * C(d_i - 1, l) go to SegAgg.
+//            sums of d_i, of the row test counts d_i * C(d_i - 1, l) and of the row
+//            conditioning-set counts C(d_i, l) go to SegAgg.
 //   scan     one block per segment of kSegRows rows: the exclusive prefix of the row
-//            test counts (the CI-test phase's flattened index), each instance's level
-//            summary, and (one block) the prefix of the instances' test counts.
+//            work units -- tests in the edge order, conditioning sets in the set order
+//            (citest.cuh) -- which is the CI-test phase's flattened index, each
+//            instance's level summary, and (one block) the prefix of the instances'
+//            unit counts.
 //
 // Together they replace compactCUTiled (src/independence/compact.cu:4-89), which
 // rebuilds the reference's dense adj_compact rows with one thread block per row.
@@ -76,6 +79,12 @@ __device__ __forceinline__ unsigned long long row_tests(int d, int level, unsign
   return (unsigned long long)d * c;
 }
 
+// conditioning sets of a row of degree d at level l (the set order's units): C(d, l)
+// when the row has tests (d - 1 >= l), else 0. Never above row_tests.
+__device__ __forceinline__ unsigned long long row_sets(int d, int level) {
+  return d - 1 < level ? 0ull : binom_fast(d, level);
+}
+
 __device__ __forceinline__ bool csr_overflow(const Inst &I) { return (long long)I.rowptr[I.p] > I.colidx_cap; }
 
 __device__ __forceinline__ void rebuild_phase(const Launch &L) {
@@ -88,18 +97,19 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
   const long long tend = t + per < R ? t + per : R;
   const int level = L.level;
   long long cur = -1;
-  unsigned long long a_deg = 0, a_work = 0;
+  unsigned long long a_deg = 0, a_work = 0, a_sets = 0;
   int a_max = 0, a_rows = 0, a_over = 0;
   auto flush = [&]() {
     if (cur >= 0 && lane == 0) {
       SegAgg &S = L.seg[cur];
       if (a_deg) atomicAdd(&S.deg, a_deg);
       if (a_work) atomicAdd(&S.work, a_work);
+      if (a_sets) atomicAdd(&S.sets, a_sets);
       if (a_max) atomicMax(&S.max_deg, a_max);
       if (a_rows) atomicAdd(&S.rows, a_rows);
       if (a_over) atomicOr(&S.over, 1);
     }
-    a_deg = a_work = 0;
+    a_deg = a_work = a_sets = 0;
     a_max = a_rows = a_over = 0;
   };
   int b = -1;
@@ -156,18 +166,20 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
     a_max = max(a_max, cnt);
     const unsigned long long w = row_tests(cnt, level, L.row_work_limit, &a_over);
     a_work += w;
+    a_sets += w ? row_sets(cnt, level) : 0ull;
     a_rows += w ? 1 : 0;
   }
   // the warps' last segment sums are merged per block first (the warps of a block
   // take neighbouring rows): one set of global atomics per block and segment
   __shared__ long long s_seg[kLevelThreads / 32];
-  __shared__ unsigned long long s_v[kLevelThreads / 32][2];
+  __shared__ unsigned long long s_v[kLevelThreads / 32][3];
   __shared__ int s_i[kLevelThreads / 32][3];
   const int wid = threadIdx.x >> 5;
   if (lane == 0) {
     s_seg[wid] = cur;
     s_v[wid][0] = a_deg;
     s_v[wid][1] = a_work;
+    s_v[wid][2] = a_sets;
     s_i[wid][0] = a_max;
     s_i[wid][1] = a_rows;
     s_i[wid][2] = a_over;
@@ -179,12 +191,13 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
     bool leader = g >= 0;
     for (int r = 0; r < q && leader; ++r) leader = s_seg[r] != g;
     if (leader) {
-      unsigned long long v0 = 0, v1 = 0;
+      unsigned long long v0 = 0, v1 = 0, v2 = 0;
       int i0 = 0, i1 = 0, i2 = 0;
       for (int r = q; r < kLevelThreads / 32; ++r)
         if (s_seg[r] == g) {
           v0 += s_v[r][0];
           v1 += s_v[r][1];
+          v2 += s_v[r][2];
           i0 = max(i0, s_i[r][0]);
           i1 += s_i[r][1];
           i2 |= s_i[r][2];
@@ -192,6 +205,7 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
       SegAgg &S = L.seg[g];
       if (v0) atomicAdd(&S.deg, v0);
       if (v1) atomicAdd(&S.work, v1);
+      if (v2) atomicAdd(&S.sets, v2);
       if (i0) atomicMax(&S.max_deg, i0);
       if (i1) atomicAdd(&S.rows, i1);
       if (i2) atomicOr(&S.over, 1);
@@ -224,20 +238,23 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long
 }
 
 struct InstSums {
-  unsigned long long deg, work, base;
+  unsigned long long deg, work, units, base;
   int max_deg, rows, over;
 };
 
-// sums over the segments of instance b (one warp); base = work of segments before g
-__device__ __forceinline__ InstSums warp_inst_sums(const Launch &L, int b, long long g) {
+// sums over the segments of instance b (one warp); base = units of segments before g
+// (units: tests, or conditioning sets with `set`)
+__device__ __forceinline__ InstSums warp_inst_sums(const Launch &L, int b, long long g, bool set) {
   const int lane = threadIdx.x & 31;
-  InstSums r{0, 0, 0, 0, 0, 0};
+  InstSums r{0, 0, 0, 0, 0, 0, 0};
   for (long long q = seg_begin(L, b) + lane; q < seg_end(L, b); q += 32) {
     const SegAgg *S = L.seg + q;
     const unsigned long long wk = __ldcg(&S->work);
+    const unsigned long long un = set ? __ldcg(&S->sets) : wk;
     r.deg += __ldcg(&S->deg);
     r.work += wk;
-    if (q < g) r.base += wk;
+    r.units += un;
+    if (q < g) r.base += un;
     r.max_deg = max(r.max_deg, __ldcg(&S->max_deg));
     r.rows += __ldcg(&S->rows);
     r.over |= __ldcg(&S->over);
@@ -246,6 +263,7 @@ __device__ __forceinline__ InstSums warp_inst_sums(const Launch &L, int b, long 
   for (int o = 16; o > 0; o >>= 1) {
     r.deg += __shfl_xor_sync(0xffffffffu, r.deg, o);
     r.work += __shfl_xor_sync(0xffffffffu, r.work, o);
+    r.units += __shfl_xor_sync(0xffffffffu, r.units, o);
     r.base += __shfl_xor_sync(0xffffffffu, r.base, o);
     r.max_deg = max(r.max_deg, __shfl_xor_sync(0xffffffffu, r.max_deg, o));
     r.rows += __shfl_xor_sync(0xffffffffu, r.rows, o);
@@ -254,7 +272,7 @@ __device__ __forceinline__ InstSums warp_inst_sums(const Launch &L, int b, long 
   return r;
 }
 
-__device__ __forceinline__ void scan_phase(const Launch &L) {
+__device__ __forceinline__ void scan_phase(const Launch &L, bool set) {
   __shared__ InstSums s_sum;
   __shared__ int s_bad;
   const int level = L.level;
@@ -271,7 +289,7 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
       if (b < L.count) {
         int over = 0, md = 0;
         for (long long q = seg_begin(L, b); q < seg_end(L, b); ++q) {
-          tot += __ldcg(&L.seg[q].work);
+          tot += set ? __ldcg(&L.seg[q].sets) : __ldcg(&L.seg[q].work);
           over |= __ldcg(&L.seg[q].over);
           md = max(md, __ldcg(&L.seg[q].max_deg));
         }
@@ -295,7 +313,7 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
     const bool valid = r < I.p;
     const int d_row = valid ? __ldcg(I.deg + r) : 0;
     if (threadIdx.x < 32) {
-      const InstSums rs = warp_inst_sums(L, b, g);
+      const InstSums rs = warp_inst_sums(L, b, g, set);
       if (threadIdx.x == 0) {
         s_sum = rs;
         s_bad = (rs.over || csr_overflow(I)) ? 1 : 0;
@@ -305,14 +323,15 @@ __device__ __forceinline__ void scan_phase(const Launch &L) {
     const bool bad = s_bad != 0;
     int over = 0;
     const int d = bad ? 0 : d_row;
-    const unsigned long long w = row_tests(d, level, L.row_work_limit, &over);
+    unsigned long long w = row_tests(d, level, L.row_work_limit, &over);
+    if (set && w) w = row_sets(d, level);
     unsigned long long all;
     const unsigned long long ex = block_exclusive_scan(w, &all);
     if (valid && !bad) I.row_work[r] = s_sum.base + ex;
     if (threadIdx.x == 0 && g == seg_end(L, b) - 1) {
       // last segment of the instance: its level summary
       DevCounters &C = I.ctr[level];
-      if (!bad) I.row_work[I.p] = s_sum.work;
+      if (!bad) I.row_work[I.p] = s_sum.units;
       if (s_sum.over) atomicOr(&I.g->err, kErrWorkOverflow);
       if (csr_overflow(I)) atomicOr(&I.g->err, kErrCsrOverflow);
       C.edges2 = s_sum.deg;

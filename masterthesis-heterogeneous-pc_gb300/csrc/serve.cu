@@ -121,6 +121,10 @@ struct hpc_server {
   long long d_seg_cap = 0;
   RetestItem *d_rq = nullptr;
   long long rq_cap = 0;
+  double *d_rqv = nullptr;         // the re-tests' entry scratch and done counters
+  long long rqv_cap = 0;
+  unsigned int *d_rqd = nullptr;
+  long long rqd_cap = 0;
   int *d_levels = nullptr;
   long long d_levels_cap = 0;
   StepCounters *d_out = nullptr;
@@ -129,6 +133,7 @@ struct hpc_server {
   long long d_tune_cap = 0;
   long long tune_version = -1;
   int grid[kLevels] = {};
+  int grid_set[kLevels] = {};  // set-order kernels (levels 2-16)
   int grid_l1 = 0;
 };
 
@@ -245,6 +250,9 @@ hpc_status step(hpc_server *sv) {
     L.lc = sv->d_lc + gi;
     L.rq = sv->d_rq;
     L.rq_cap = sv->rq_cap;
+    L.rq_val = sv->d_rqv;
+    L.rq_done = sv->d_rqd;
+    L.rq_vcap = sv->rqv_cap;
     L.seg = sv->d_seg + g.seg_off;
     L.row_cache = g.count == 1 && g.pmax + 1 <= kRowCache;
     L.total_rows = g.rows;
@@ -263,8 +271,10 @@ hpc_status step(hpc_server *sv) {
       if ((s = launch_degrees(L, g.rows, sv->st)) != HPC_OK) return s;
       if ((s = launch_scan(L, sv->st)) != HPC_OK) return s;
     } else {
-      const int grid = g.level == 1 ? sv->grid_l1 : sv->grid[g.level];
-      if ((s = launch_level(L, sv->opts.precision, grid, kL1Interleaved, sv->st)) != HPC_OK) return s;
+      const bool set = tc && uses_set_order(set_order_from(), g.level);
+      const int grid = g.level == 1 ? sv->grid_l1 : set ? sv->grid_set[g.level] : sv->grid[g.level];
+      if ((s = launch_level(L, sv->opts.precision, grid, set ? kSetOrder : kL1Interleaved, sv->st)) != HPC_OK)
+        return s;
       if (tc && (s = launch_retest(L, sv->sms, sv->st)) != HPC_OK) return s;
     }
   }
@@ -289,7 +299,7 @@ bool advance(hpc_server *sv, Request *r) {
   const int l = r->next;
   const DevCounters &C = c->ctr_host[l];
   const int err = c->gctr_host[0].err;
-  if (err & (kErrTimeout | kErrRecOverflow | kErrWorkOverflow | kErrCsrOverflow)) {
+  if (err & (kErrTimeout | kErrRecOverflow | kErrWorkOverflow | kErrCsrOverflow | kErrRetestOverflow)) {
     r->status = (err & kErrTimeout) ? HPC_ERR_TIMEOUT : HPC_ERR_CAPACITY;
     return true;
   }
@@ -409,12 +419,18 @@ hpc_status hpc_server_create(hpc_server **out, const hpc_server_opts *opts) {
   }
   const int top = o.max_level < 0 ? HPC_MAX_LEVEL : o.max_level;
   for (int l = 2; l <= top; ++l) sv->grid[l] = citest_grid(o.precision, l, o.device);
+  if (o.precision != HPC_PREC_FP64)
+    for (int l = 2; l <= std::min(top, 16); ++l) sv->grid_set[l] = citest_grid(o.precision, l, o.device, kSetOrder);
   if (top >= 1) sv->grid_l1 = citest_grid(o.precision, 1, o.device, kL1Interleaved);
   if (top > 16) retest_setup();
   if (o.precision == HPC_PREC_MIXED_TC) {
     // the shared FP64 re-test queue of every launch (4 Mi entries; a full queue re-tests
     // in place)
     hpc_status s = grow(&sv->d_rq, &sv->rq_cap, 4ll << 20, sv->st);
+    if (s == HPC_OK) s = grow(&sv->d_rqv, &sv->rqv_cap, retest_scratch_entries(4ll << 20), sv->st);
+    if (s == HPC_OK) s = grow(&sv->d_rqd, &sv->rqd_cap, 4ll << 20, sv->st);
+    if (s == HPC_OK && cudaMemsetAsync(sv->d_rqd, 0, sizeof(unsigned int) * (size_t)sv->rqd_cap, sv->st) != cudaSuccess)
+      s = HPC_ERR_CUDA;
     if (s != HPC_OK) {
       cudaStreamDestroy(sv->st);
       delete sv;
@@ -507,7 +523,8 @@ hpc_status hpc_server_destroy(hpc_server *sv) {
   for (Request *r : sv->done) delete r;
   cudaSetDevice(sv->opts.device);
   for (void *p : {(void *)sv->stage, (void *)sv->d_inst, (void *)sv->d_pre, (void *)sv->d_work, (void *)sv->d_lc,
-                  (void *)sv->d_seg, (void *)sv->d_rq, (void *)sv->d_levels, (void *)sv->d_out, (void *)sv->d_tune})
+                  (void *)sv->d_seg, (void *)sv->d_rq, (void *)sv->d_rqv, (void *)sv->d_rqd, (void *)sv->d_levels,
+                  (void *)sv->d_out, (void *)sv->d_tune})
     if (p) cudaFreeAsync(p, sv->st);
   cudaStreamSynchronize(sv->st);
   cudaStreamDestroy(sv->st);

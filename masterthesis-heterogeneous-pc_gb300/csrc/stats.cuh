@@ -22,6 +22,16 @@ HPC_HD double calc_pvalue64(double r_in, int n) {
   return 2.0 * (erfc(absz / 1.41421356237309504880) / 2.0);
 }
 
+// The same formula in FP32, for the record p-value of a removal decided in FP32 from
+// its FP32 |r| (which carries FP32 rounding anyway; a removal's p-value is at least
+// alpha, far from FP32's underflow): log1pf / erfcf instead of their FP64 versions on
+// this GPU's 1/64-rate FP64 pipe.
+HPC_HD float calc_pvalue32(float r_in, int n) {
+  const float r = isnan(r_in) ? 0.f : fminf(0.9999999f, fabsf(r_in));
+  const float absz = sqrtf((float)n - 3.0f) * 0.5f * log1pf(2.0f * r / (1.0f - r));
+  return erfcf(absz * 0.707106781186547524f);
+}
+
 // closed-form level-1 partial correlation (cpuInd.cpp:16-27)
 HPC_HD double pval_l1_64(double x1, double x2, double x3, int n) {
   double r = (x1 - x2 * x3) / sqrt((1.0 - x3 * x3) * (1.0 - x2 * x2));

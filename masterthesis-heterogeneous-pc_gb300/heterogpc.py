@@ -120,6 +120,9 @@ _SIGS = {
     "hpc_debug_fail_allocation": (C.c_int, [C.c_int64]),
     "hpc_debug_live_allocations": (C.c_int64, []),
     "hpc_debug_set_barrier": (C.c_int, [C.c_void_p, C.c_int64, C.c_int]),
+    "hpc_debug_set_order_from": (C.c_int, [C.c_int]),
+    "hpc_debug_set_retest_queue": (C.c_int, [C.c_void_p, C.c_int64]),
+    "hpc_debug_set_order_active": (C.c_int, [C.c_void_p]),
     "hpc_sem_generate": (C.c_int, [C.POINTER(SemParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hpc_server_opts_default": (C.c_int, [C.POINTER(ServerOpts)]),
     "hpc_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(ServerOpts)]),
@@ -178,6 +181,15 @@ def tune_save(path):
 
 def tune_load(path):
     _check(lib().hpc_tune_load(os.fsencode(path)))
+
+
+SET_ORDER_DEFAULT = 4  # the library's default lowest set-order level (kSetOrderFrom)
+
+
+def set_order_from(level):
+    """The lowest level whose CI tests run in the set order, 0 for the edge order at every
+    level (hpc_debug_set_order_from; process-wide). Both orders give the same skeleton."""
+    _check(lib().hpc_debug_set_order_from(int(level)))
 
 
 def _params(c):
@@ -577,6 +589,14 @@ class SkeletonBatch:
         k = C.c_int(0)
         _check(lib().hpc_batch_level_stats(self._h, idx, arr, cap, C.byref(k)))
         return [arr[i].as_dict() for i in range(k.value)]
+
+    def set_retest_queue(self, entries):
+        """Test hook (hpc_debug_set_retest_queue): a re-test queue of `entries` entries."""
+        _check(lib().hpc_debug_set_retest_queue(self._h, int(entries)))
+
+    def set_order_active(self):
+        """Test hook: whether the context still runs levels in the set order."""
+        return bool(lib().hpc_debug_set_order_active(self._h))
 
     def run_async(self):
         """Queue the whole batch's skeleton and return (hpc_run_skeleton_async)."""
