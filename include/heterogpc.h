@@ -360,7 +360,7 @@ hpc_status hpc_debug_set_barrier(hpc_ctx *ctx, int64_t wait_ns, int extra_arriva
 /* hpc_debug_set_order_from(level): the lowest level whose CI tests run in the set order
  * (one Cholesky factor of a conditioning set serves every neighbour outside it), 2..32,
  * or 0 for the edge order (each test factors its own set) at every level; process-wide,
- * read when a level is launched. Both orders give the same skeleton; the default is 4. */
+ * read when a level is launched. Both orders give the same skeleton; the default is 3. */
 hpc_status hpc_debug_set_order_from(int level);
 /* hpc_debug_set_retest_queue(ctx, entries): replace the context's FP64 re-test queue by
  * one of `entries` entries (so that a test can make it overflow). When a set-order level

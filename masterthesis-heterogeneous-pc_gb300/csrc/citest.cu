@@ -27,7 +27,18 @@ __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count
         h->pmax = (double)calc_pvalue32((float)(-1.0 - h->pmax), I.n_obs);
         continue;
       }
-      const double pv = exact_pvalue<HPC_MAX_LEVEL>(I, h->i, h->j, rec + kRecHeadWords, h->level);
+      // level 1: the closed form from the three entries (what exact_pvalue evaluates
+      // there, without its matrix in local memory); else the general path, its arrays
+      // sized by the level
+      double pv;
+      const int l = h->level;
+      if (l == 1) {
+        const int64_t k = rec[kRecHeadWords];
+        pv = pval_l1_64(I.cor64[h->i * I.p + h->j], I.cor64[h->i * I.p + k], I.cor64[h->j * I.p + k], I.n_obs);
+      } else {
+        pv = l <= 16 ? exact_pvalue<16>(I, h->i, h->j, rec + kRecHeadWords, l)
+                     : exact_pvalue<HPC_MAX_LEVEL>(I, h->i, h->j, rec + kRecHeadWords, l);
+      }
       h->pmax = pv;
       if (!(pv >= I.alpha)) atomicOr(&I.g->err, kErrBandViolation);
     }
@@ -48,33 +59,28 @@ __global__ void gather_records_kernel(const Inst *__restrict__ inst, int count, 
   }
 }
 
-// Records of all instances in the packed form of hpc_batch_get_records_packed: record
-// r (instance b with pre[b] <= r < pre[b + 1]) has level l, found from the instance's
-// removals per level (records are appended level by level, so an instance's records of
-// level l follow those of lower levels), and goes to word
-//   inst_words[b] + sum_{l' < l} deleted(l') * w(l') + (rank within level l) * w(l),
-// w(l) = 6 + 2 ceil(l / 2). One warp per record.
-__global__ void pack_records_kernel(const Inst *__restrict__ inst, int count, const long long *__restrict__ pre,
-                                    const long long *__restrict__ inst_words, long long total,
+// Records of all instances in the packed form of hpc_batch_get_records_packed. The host
+// cuts them into segments, one per (instance, level) with removals: an instance's
+// records are appended level by level, so a segment is a contiguous run of `count`
+// records from record `src` of instance `inst` (rec_stride words each), and it goes to
+// the contiguous words from `dst`, w = 6 + 2 ceil(l / 2) words per record (head, l ids,
+// -1 padding). One block per segment, its threads over the segment's output words
+// (coalesced writes, no per-record search).
+__global__ void pack_records_kernel(const Inst *__restrict__ inst, const RecSegment *__restrict__ seg, int nseg,
                                     int32_t *__restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < total; r += nw) {
-    const int b = find_inst(pre, count, r);
-    const Inst &I = inst[b];
-    const long long rr = r - pre[b];
-    long long cum = 0, words = inst_words[b];
-    int l = 1;
-    for (; l <= HPC_MAX_LEVEL; ++l) {
-      const long long d = (long long)I.ctr[l].deleted;
-      if (rr < cum + d) break;
-      cum += d;
-      words += d * (long long)(6 + ((l + 1) & ~1));
-    }
+  for (int g = blockIdx.x; g < nseg; g += gridDim.x) {
+    const RecSegment S = seg[g];
+    const Inst &I = inst[S.inst];
+    const int l = S.level;
     const int w = 6 + ((l + 1) & ~1);
-    const int32_t *src = I.recs + rr * (long long)I.rec_stride;
-    int32_t *dst = out + words + (rr - cum) * (long long)w;
-    for (int q = lane; q < w; q += 32) dst[q] = q < 6 + l ? src[q] : -1;
+    const long long words = S.count * (long long)w;
+    const int32_t *src = I.recs + S.src * (long long)I.rec_stride;
+    int32_t *dst = out + S.dst;
+    for (long long t = threadIdx.x; t < words; t += blockDim.x) {
+      const long long r = t / w;
+      const int q = (int)(t - r * w);
+      dst[t] = q < 6 + l ? src[r * I.rec_stride + q] : -1;
+    }
   }
 }
 
@@ -127,8 +133,132 @@ __device__ __forceinline__ void retest_decide(const Launch &L, const Inst &I, co
   if (decide_of_r(I, r, nan_p, &pv) && claim_edge(I, i, j)) write_record(I, L.level, i, j, it->ids, l, pv);
 }
 
+// Levels 1-4 (K = l + 2 <= 6 variables): one warp per item, every lane accumulating the
+// E = K(K - 1) / 2 products over its samples (k = lane, lane + 32, ...) in passes of
+// kRetestPass entries (the accumulators of a pass stay in registers), so that each of
+// the K columns is read once per item instead of once per entry it takes part in (2E
+// column reads in the entry-parallel form). Above level 4 the entry-parallel form is
+// faster (measured on C4: a re-test's 28-45 entries spread over as many warps beat one
+// warp stepping through the columns, and the column form's registers halve occupancy). The products are
+// summed as in zdot: the FP32 pairs' products with their exact rounding errors and cross
+// terms, compensated in FP32 and carried into FP64 every 16 samples of a lane.
+constexpr int kRetestPass = 16;
+constexpr int kColumnTop = 4;  // the highest level re-tested by columns
+
+// (r, c) of entry e of the upper triangle of a K x K matrix, row by row
+__host__ __device__ constexpr int entry_row(int e, int K) {
+  int r = 0;
+  while (e >= K - 1 - r) {
+    e -= K - 1 - r;
+    ++r;
+  }
+  return r;
+}
+__host__ __device__ constexpr int entry_col(int e, int K) {
+  int r = 0;
+  while (e >= K - 1 - r) {
+    e -= K - 1 - r;
+    ++r;
+  }
+  return r + 1 + e;
+}
+
+// one pass: entries E0 .. E0 + EN - 1, written to the warp's matrix M (K x K) by lane 0
+template <int K, int E0, int EN>
+__device__ __forceinline__ void retest_columns_pass(const Inst &I, const float *const *ch, int64_t lo_off,
+                                                    double *M) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n = I.n_z;
+  double acc[EN];
+#pragma unroll
+  for (int e = 0; e < EN; ++e) acc[e] = 0.0;
+  for (int64_t k0 = lane; k0 < n; k0 += 32 * 16) {
+    float sh[EN], sl[EN];
+#pragma unroll
+    for (int e = 0; e < EN; ++e) sh[e] = sl[e] = 0.f;
+    // the products of one sample's loaded values
+    auto add = [&](const float *ah, const float *al) {
+      int e = 0;
+#pragma unroll
+      for (int r = 0; r < K; ++r)
+#pragma unroll
+        for (int c = r + 1; c < K; ++c, ++e) {
+          if (e < E0 || e >= E0 + EN) continue;
+          const int x = e - E0;
+          const float p = ah[r] * ah[c];
+          float er = fmaf(ah[r], ah[c], -p);
+          er = fmaf(ah[r], al[c], fmaf(al[r], ah[c], er));
+          const float t = sh[x] + p;
+          const float bb = t - sh[x];
+          sl[x] += ((sh[x] - (t - bb)) + (p - bb)) + er;
+          sh[x] = t;
+        }
+    };
+    // two samples at a time, both loaded before the arithmetic (no bounds test between)
+#pragma unroll 1
+    for (int u = 0; u < 16; u += 2) {
+      const int64_t k = k0 + 32 * u;
+      if (k + 32 < n) {
+        float ah[2][K], al[2][K];
+#pragma unroll
+        for (int v = 0; v < 2; ++v)
+#pragma unroll
+          for (int r = 0; r < K; ++r) {
+            ah[v][r] = ch[r][k + 32 * v];
+            al[v][r] = ch[r][k + 32 * v + lo_off];
+          }
+        add(ah[0], al[0]);
+        add(ah[1], al[1]);
+      } else if (k < n) {
+        float ah[K], al[K];
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+          ah[r] = ch[r][k];
+          al[r] = ch[r][k + lo_off];
+        }
+        add(ah, al);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < EN; ++e) acc[e] += (double)sh[e] + (double)sl[e];
+  }
+#pragma unroll
+  for (int e = 0; e < EN; ++e) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], o);
+    if (lane == 0) {
+      const int r = entry_row(E0 + e, K), c = entry_col(E0 + e, K);
+      M[r * K + c] = M[c * K + r] = acc[e] / I.denom;
+    }
+  }
+}
+
+template <int K, int E0>
+__device__ __forceinline__ void retest_columns_passes(const Inst &I, const float *const *ch, int64_t lo_off,
+                                                      double *M) {
+  constexpr int E = K * (K - 1) / 2;
+  if constexpr (E0 < E) {
+    constexpr int EN = E - E0 < kRetestPass ? E - E0 : kRetestPass;
+    retest_columns_pass<K, E0, EN>(I, ch, lo_off, M);
+    retest_columns_passes<K, E0 + kRetestPass>(I, ch, lo_off, M);
+  }
+}
+
+// the item's matrix M (K x K, the warp's shared memory) from its columns
+template <int K>
+__device__ __forceinline__ void retest_item_columns(const Inst &I, const RetestItem *it, double *M) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n = I.n_z;
+  const float *ch[K];
+  const int64_t lo_off = I.zl - I.zh;  // the zl plane, at a fixed distance from zh
+#pragma unroll
+  for (int r = 0; r < K; ++r) ch[r] = I.zh + retest_var(it, r) * n;
+  if (lane < K) M[lane * K + lane] = 1.0;
+  retest_columns_passes<K, 0>(I, ch, lo_off, M);
+}
+
 template <int KM>
-__global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_constant__ Launch L) {
+__global__ void __launch_bounds__(kRetestWarps * 32, 2) retest_kernel(const __grid_constant__ Launch L) {
   extern __shared__ double retest_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int l = L.level;
@@ -152,15 +282,36 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_
     }
     return;
   }
+  if (l <= kColumnTop) {
+    // an item per warp from its columns (instances with FP32-pair data; FP64 Z takes
+    // the general path below)
+    for (unsigned long long q = warp; q < count; q += nwarps) {
+      const RetestItem *it = L.rq + q;
+      const Inst &I = *inst_of(L, it->inst);
+      if (!I.zh || !live_bit(I.adj, I.W, it->i, it->j)) continue;
+      switch (l) {
+        case 1: retest_item_columns<3>(I, it, M); break;
+        case 2: retest_item_columns<4>(I, it, M); break;
+        case 3: retest_item_columns<5>(I, it, M); break;
+        default: retest_item_columns<6>(I, it, M); break;
+      }
+      __syncwarp();
+      if (lane == 0) retest_decide<KM>(L, I, it, l, M);
+      __syncwarp();
+    }
+  }
   const int E = k * (k - 1) / 2;
+  // the items not taken above run entry by entry (the first W of them) or a warp each
+  const bool by_columns = l <= kColumnTop;
   const unsigned long long W =
-      L.rq_val ? min(count, (unsigned long long)(L.rq_vcap / E)) : 0ull;  // items run entry by entry
+      L.rq_val ? min(count, (unsigned long long)(L.rq_vcap / E)) : 0ull;
   const unsigned long long units = W * (unsigned long long)E;
   for (unsigned long long u = warp; u < units; u += nwarps) {
     const unsigned long long q = u / (unsigned long long)E;
     const int e = (int)(u - q * (unsigned long long)E);
     const RetestItem *it = L.rq + q;
     const Inst &I = *inst_of(L, it->inst);
+    if (by_columns && I.zh) continue;  // decided above
     const int64_t i = it->i, j = it->j;
     if (live_bit(I.adj, I.W, i, j)) {  // else removed meanwhile: nothing to compute
       int r, c;
@@ -196,6 +347,7 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_
   for (unsigned long long q = W + warp; q < count; q += nwarps) {
     const RetestItem *it = L.rq + q;
     const Inst &I = *inst_of(L, it->inst);
+    if (by_columns && I.zh) continue;                    // decided above
     if (!live_bit(I.adj, I.W, it->i, it->j)) continue;  // removed by another test meanwhile
     for (int r = 0; r < k; ++r) {
       if (lane == 0) M[r * k + r] = 1.0;
@@ -212,7 +364,7 @@ __global__ void __launch_bounds__(kRetestWarps * 32) retest_kernel(const __grid_
 
 template <bool MIXED>
 void *kernel_for(int level, int l1_variant) {
-  if (MIXED && l1_variant == kSetOrder && level >= 2 && level <= 16) {
+  if (MIXED && l1_variant == kSetOrder && level >= 2 && level <= kSetTop) {
     switch (level) {
       case 2: return (void *)level_kernel<2, true, kSetOrder>;
       case 3: return (void *)level_kernel<3, true, kSetOrder>;
@@ -221,7 +373,10 @@ void *kernel_for(int level, int l1_variant) {
       case 6: return (void *)level_kernel<6, true, kSetOrder>;
       case 7: return (void *)level_kernel<7, true, kSetOrder>;
       case 8: return (void *)level_kernel<8, true, kSetOrder>;
-      default: return level <= 12 ? level_kernel_9_12(level, true, true) : level_kernel_13_16(level, true, true);
+      default:
+        return level <= 12 ? level_kernel_9_12(level, true, true)
+               : level <= 16 ? level_kernel_13_16(level, true, true)
+                             : level_kernel_17_24_set(level);
     }
   }
   switch (level) {
@@ -294,11 +449,9 @@ hpc_status launch_gather_records(const Inst *inst, int count, const long long *p
   return HPC_OK;
 }
 
-hpc_status launch_pack_records(const Inst *inst, int count, const long long *prefix, const long long *inst_words,
-                               long long total, int32_t *out, cudaStream_t s) {
-  if (total <= 0) return HPC_OK;
-  const long long blocks = std::min<long long>((total + 7) / 8, 152 * 8);
-  pack_records_kernel<<<(unsigned)blocks, 256, 0, s>>>(inst, count, prefix, inst_words, total, out);
+hpc_status launch_pack_records(const Inst *inst, const RecSegment *seg, int nseg, int32_t *out, cudaStream_t s) {
+  if (nseg <= 0) return HPC_OK;
+  pack_records_kernel<<<(unsigned)std::min(nseg, 152 * 16), 256, 0, s>>>(inst, seg, nseg, out);
   HPC_LAUNCH_CHECK("pack_records_kernel");
   return HPC_OK;
 }

@@ -46,6 +46,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "internal.cuh"
 #include "rebuild.cuh"
 #include "stats.cuh"
@@ -59,7 +61,7 @@ constexpr int kThreads = kLevelThreads;
 // 1-16 (LA = the level); the runtime-level kernel of levels 17-32 (LA = HPC_MAX_LEVEL)
 // keeps them rolled, which bounds its code size and compile time.
 template <int LA>
-constexpr int kUnr = LA <= 16 ? (LA > 0 ? LA : 1) : 1;
+constexpr int kUnr = LA <= kSetTop ? (LA > 0 ? LA : 1) : 1;
 
 __device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, int64_t j) {
   const volatile uint32_t *w = adj + i * W + (j >> 5);
@@ -641,11 +643,12 @@ __device__ __forceinline__ void skip_tiles_of_edge(const Launch &L, unsigned lon
 }
 
 // Shared memory of a level kernel's CI-test phase: per warp, the pending removals and
-// (levels 2-16, mixed precision) the staged correlation block.
+// (mixed precision: levels 2-16 of the edge order, every set-order level) the staged
+// correlation block.
 template <int LT, bool MIXED>
 struct TestSmem {
   static constexpr int LA = LT > 0 ? LT : HPC_MAX_LEVEL;
-  static constexpr bool kBlk = MIXED && LT >= 2 && LT <= 16;
+  static constexpr bool kBlk = MIXED && LT >= 2 && LT <= kSetTop;
   PendRem<LA> pend[kThreads / 32][kPend];
   int np[kThreads / 32];
   float blk[kBlk ? kThreads / 32 : 1][kBlk ? kBlkS * kBlkS : 1];
@@ -1035,7 +1038,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 }
 
 // ---------------------------------------------------------------------------
-// The set order of a level's CI tests (levels 2-16, mixed precision; the kSetOrder
+// The set order of a level's CI tests (levels 2-24, mixed precision; the kSetOrder
 // kernels, launched from the level set_order_from() on). The flattened index runs over (instance, row i, l-subset S of the row's snapshot neighbours in
 // lexicographic order), and one unit runs the tests (i, j | S) for every live
 // neighbour j outside S, in ascending order. A row of degree d > l has C(d, l) units
@@ -1054,23 +1057,24 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 // against the positions and read the live bit per test.
 constexpr int kSetMaskD = 64;
 template <int LT>
-constexpr int kSetBlocks = LT <= 8 ? 2 : 1;  // resident blocks per SM the set-order kernels are compiled for
+constexpr int kSetBlocks = LT <= 10 ? 2 : 1;  // resident blocks per SM the set-order kernels are compiled for
 
 // Rows ci..l-1 of the Cholesky factor of the S block and of w_i = L_S^-1 r_iS: the
 // operations of test_f32_inc without w_j.
-template <int LA>
-__device__ __forceinline__ void factor_set(const float *__restrict__ C, int64_t stride, int64_t xi, const int *xs,
-                                           int l, int ci, Fact<LA> &F) {
+// IdxT: int for the staged block in shared memory, int64_t for the instance's matrix.
+template <int LA, typename IdxT>
+__device__ __forceinline__ void factor_set(const float *__restrict__ C, IdxT stride, IdxT xi, const int *xs, int l,
+                                           int ci, Fact<LA> &F) {
 #pragma unroll (kUnr<LA>)
   for (int r = 0; r < LA; ++r) {
     if (r >= ci && r < l) {
-      const int64_t xr = xs[r];
+      const IdxT xr = xs[r];
       float vx = C[xi * stride + xr];
       float d = 1.0f;
 #pragma unroll (kUnr<LA>)
       for (int c = 0; c < LA; ++c) {
         if (c < r) {
-          float v = C[(int64_t)xs[c] * stride + xr];
+          float v = C[(IdxT)xs[c] * stride + xr];
 #pragma unroll (kUnr<LA>)
           for (int q = 0; q < LA; ++q)
             if (q < c) v -= F.Lm[r * (r + 1) / 2 + q] * F.Lm[c * (c + 1) / 2 + q];
@@ -1091,9 +1095,9 @@ __device__ __forceinline__ void factor_set(const float *__restrict__ C, int64_t 
 // FP32 test of (i, j | S) on the unit's factor: w_j by forward solve, then the tail of
 // test_f32_inc (sx = |w_i|^2 and dmin = the smallest pivot, both in row order, come
 // with the factor). Same return values.
-template <int LA>
-__device__ __forceinline__ int test_set_j(const Inst &I, const float *__restrict__ C, int64_t stride, int64_t xi,
-                                          int64_t xj, const int *xs, int l, const Fact<LA> &F, float sx, float dmin,
+template <int LA, typename IdxT>
+__device__ __forceinline__ int test_set_j(const Inst &I, const float *__restrict__ C, IdxT stride, IdxT xi, IdxT xj,
+                                          const int *xs, int l, const Fact<LA> &F, float sx, float dmin,
                                           float *rr_out) {
   float gy[LA], wy[LA];
 #pragma unroll (kUnr<LA>)
@@ -1208,16 +1212,19 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
       uint64_t live = staged ? blk_live : row_live_mask(*I, i, base, d);
       int ci = 0;  // lowest member changed since the last unit (factor rows below are valid)
       Fact<LA> F;
-      for (;;) {
-        // the members' indices into the entries: block-local in the staged block, else
-        // variable ids in the instance's matrix
-        const float *C = staged ? blk : I->cor32;
-        const int64_t stride = staged ? (int64_t)kBlkS : I->p;
-        const int64_t xi = staged ? 0 : i;
+      // one unit: the factor of S (rows from ci on), then the tests. ST: the row's block
+      // is staged (entries from shared memory by block-local index, 32-bit index
+      // arithmetic), else the instance's matrix by variable id
+      auto unit = [&](auto staged_c) {
+        constexpr bool ST = decltype(staged_c)::value;
+        using IdxT = typename std::conditional<ST, int, int64_t>::type;
+        const float *C = ST ? blk : I->cor32;
+        const IdxT stride = ST ? (IdxT)kBlkS : (IdxT)I->p;
+        const IdxT xi = ST ? (IdxT)0 : (IdxT)i;
 #pragma unroll (kUnr<LA>)
         for (int q = 0; q < LA; ++q)
-          if (q >= ci) xs[q] = staged ? pos[q] + 1 : I->colidx[base + pos[q]];
-        factor_set<LA>(C, stride, xi, xs, l, ci, F);
+          if (q >= ci) xs[q] = ST ? pos[q] + 1 : I->colidx[base + pos[q]];
+        factor_set<LA, IdxT>(C, stride, xi, xs, l, ci, F);
         float sx = 0.f, dmin = 1.f;
 #pragma unroll (kUnr<LA>)
         for (int r = 0; r < LA; ++r) {
@@ -1226,16 +1233,16 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
         }
         // the unit's tests: neighbours q outside S, live as far as the lane knows
         auto test_q = [&](int q) {
-          const int64_t xj = staged ? (int64_t)(q + 1) : (int64_t)I->colidx[base + q];
+          const IdxT xj = ST ? (IdxT)(q + 1) : (IdxT)I->colidx[base + q];
           float rr = 0.f;
-          const int res = test_set_j<LA>(*I, C, stride, xi, xj, xs, l, F, sx, dmin, &rr);
+          const int res = test_set_j<LA, IdxT>(*I, C, stride, xi, xj, xs, l, F, sx, dmin, &rr);
           ++executed;
           if (res == 0) return;
           // removal or re-test: the variable ids of j and S
-          const int64_t j = staged ? (int64_t)I->colidx[base + q] : xj;
+          const int64_t j = ST ? (int64_t)I->colidx[base + q] : (int64_t)xj;
           int ids[LA];
 #pragma unroll (kUnr<LA>)
-          for (int r = 0; r < LA; ++r) ids[r] = staged ? I->colidx[base + pos[r]] : xs[r];
+          for (int r = 0; r < LA; ++r) ids[r] = ST ? I->colidx[base + pos[r]] : xs[r];
           bool rm = false;
           double pv = 0.0;
           if (res == 1) {
@@ -1254,7 +1261,7 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
             if (q < kSetMaskD) live &= ~(1ull << q);
           }
         };
-        if (d <= kSetMaskD) {
+        if (ST || d <= kSetMaskD) {
           uint64_t in_s = 0;
 #pragma unroll (kUnr<LA>)
           for (int r = 0; r < LA; ++r) in_s |= 1ull << pos[r];
@@ -1273,6 +1280,12 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
             test_q(q);
           }
         }
+      };
+      for (;;) {
+        if (staged)
+          unit(std::true_type{});
+        else
+          unit(std::false_type{});
         if (++t >= tend) break;
         ci = next_lex(l, d, pos);
         if (ci < 0) {  // the row's last set: the next row with tests, possibly of the next instance
@@ -1310,8 +1323,8 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
 // One level l >= 1: rebuild | grid barrier | scan | grid barrier | CI tests. LT = 1
 // is the lane-interleaved level-1 body (V: kL1Prefetch loads one step ahead,
 // kL1Chunked runs the chunked body of the higher levels; picked by the tile policy),
-// LT = 2..16 the bodies unrolled for l = LT (V = kSetOrder: in the set order), LT = 0
-// the runtime-level body.
+// LT = 2..16 the bodies unrolled for l = LT (V = kSetOrder: in the set order, LT up to
+// kSetTop), LT = 0 the runtime-level body.
 template <int LT, bool MIXED, int V = kL1Interleaved>
 __global__ void __launch_bounds__(kThreads, V == kSetOrder ? kSetBlocks<LT> : (LT == 1 && (V & 3) != kL1Chunked ? 4 : 2))
     level_kernel(const __grid_constant__ Launch L) {
@@ -1323,7 +1336,7 @@ __global__ void __launch_bounds__(kThreads, V == kSetOrder ? kSetBlocks<LT> : (L
   if (!grid_barrier(L, epoch)) return;
   const TuneEntry te = tile_policy(L);
   if constexpr (V == kSetOrder) {
-    static_assert(MIXED && LT >= 2 && LT <= 16, "the set order runs levels 2-16 in mixed precision");
+    static_assert(MIXED && LT >= 2 && LT <= kSetTop, "the set order runs levels 2-24 in mixed precision");
     __shared__ TestSmem<LT, true> sm;
     tests_set<LT>(L, rw_smem, te, sm);
   } else if constexpr (LT == 1 && (V & 3) != kL1Chunked) {  // level 1 keeps the SM's on-chip memory for L1 cache
@@ -1339,6 +1352,7 @@ __global__ void __launch_bounds__(kThreads, V == kSetOrder ? kSetBlocks<LT> : (L
 // level kernels of levels 9-32 (citest_l9.cu, citest_l13.cu, citest_l17.cu)
 void *level_kernel_9_12(int level, bool mixed, bool set);
 void *level_kernel_13_16(int level, bool mixed, bool set);
+void *level_kernel_17_24_set(int level);
 void *level_kernel_17_up(int level, bool mixed);
 
 }  // namespace hpc

@@ -61,8 +61,20 @@ struct ColScalars {
   float mh, ml, ih, il, jh, jl;
 };
 
-// Block-wide total of one FP64 value per warp (lane 0 has stored it in red[warp]):
-// thread 0 only.
+// Block-wide total of the warps' FP32 pairs (lane 0 of warp w stored them in rh[w],
+// rl[w]), compensated in FP32, converted to FP64 once: thread 0 only. (Every FP64 warp
+// instruction occupies the SM's FP64 unit for 16 cycles, whether one lane or 32 use it.)
+__device__ __forceinline__ double warp_totals(const float *rh, const float *rl) {
+  float h = 0.f, l = 0.f;
+#pragma unroll
+  for (int w = 0; w < kStdThreads / 32; ++w) {
+    float s, e;
+    two_sum(h, rh[w], s, e);
+    h = s;
+    l += rl[w] + e;
+  }
+  return (double)h + (double)l;
+}
 __device__ __forceinline__ double warp_totals(const double *red) {
   double t = 0.0;
 #pragma unroll
@@ -71,16 +83,15 @@ __device__ __forceinline__ double warp_totals(const double *red) {
 }
 
 __device__ __forceinline__ void finish_scalars(double ss, long long n, int ref_compat, ColScalars &S) {
-  double sd;
+  // z = (x - mean) * (1 / sd): one multiply per sample instead of a division; 1 / sd by
+  // rsqrt of the variance (within an ulp of 1 / sqrt, fewer FP64 instructions than a
+  // square root and a division)
   if (ref_compat)  // corHelper.cu:75: sqrtf of (sum / (dim - 1.f))
-    sd = (double)sqrtf((float)(ss / (double)((float)n - 1.f)));
+    S.inv_sd = 1.0 / (double)sqrtf((float)(ss / (double)((float)n - 1.f)));
   else
-    sd = sqrt(ss / (double)(n - 1));
-  // z = (x - mean) * (1 / sd): one multiply per sample instead of a division; the values
-  // differ from (x - mean) / sd by at most an ulp
-  S.inv_sd = 1.0 / sd;
+    S.inv_sd = rsqrt(ss / (double)(n - 1));
   const double denom = ref_compat ? (double)((float)n - 1.f) : (double)(n - 1);
-  S.scale = 1.0 / sqrt(denom);
+  S.scale = rsqrt(denom);
   const double inv = S.inv_sd * S.scale;
   S.ih = (float)inv;
   S.il = (float)(inv - (double)S.ih);
@@ -94,7 +105,7 @@ __device__ __forceinline__ void finish_scalars(double ss, long long n, int ref_c
 // SD loop skip them.
 __device__ __forceinline__ void column_scalars(const float *__restrict__ x, long long n, int ref_compat,
                                                ColScalars &S) {
-  __shared__ double red[kStdThreads / 32];
+  __shared__ float rh[kStdThreads / 32], rl[kStdThreads / 32];
   __shared__ long long redc[kStdThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float sh = 0.f, sl = 0.f;
@@ -112,14 +123,15 @@ __device__ __forceinline__ void column_scalars(const float *__restrict__ x, long
   warp_sum_pair(sh, sl);
   cnt = __reduce_add_sync(0xffffffffu, cnt);
   if (lane == 0) {
-    red[wid] = (double)sh + (double)sl;
+    rh[wid] = sh;
+    rl[wid] = sl;
     redc[wid] = cnt;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     long long c = 0;
     for (int w = 0; w < kStdThreads / 32; ++w) c += redc[w];
-    S.mean = warp_totals(red) / (double)c;
+    S.mean = warp_totals(rh, rl) / (double)c;
     S.mh = (float)S.mean;
     S.ml = (float)(S.mean - (double)S.mh);
   }
@@ -142,10 +154,13 @@ __device__ __forceinline__ void column_scalars(const float *__restrict__ x, long
     }
   }
   warp_sum_pair(qh, ql);
-  __syncthreads();  // red is reused
-  if (lane == 0) red[wid] = (double)qh + (double)ql;
+  __syncthreads();  // rh, rl are reused
+  if (lane == 0) {
+    rh[wid] = qh;
+    rl[wid] = ql;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) finish_scalars(warp_totals(red), n, ref_compat, S);
+  if (threadIdx.x == 0) finish_scalars(warp_totals(rh, rl), n, ref_compat, S);
   __syncthreads();
 }
 

@@ -802,7 +802,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
 int set_order_from() { return g_set_from.load(); }
 long long retest_scratch_entries(long long cap) { return std::min<long long>(32ll << 20, 3 * cap); }
 bool uses_set_order(int set_from, int level) {
-  return set_from > 0 && level >= 2 && level <= 16 && level >= set_from;
+  return set_from > 0 && level >= 2 && level <= kSetTop && level >= set_from;
 }
 
 // for the server's shared launches (serve.cu)
@@ -935,6 +935,7 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->tune_dev);
   dev_free(c->rec_stage);
   dev_free(c->rec_prefix_dev);
+  dev_free(c->rec_seg);
   delete[] c->ctr_host;
   delete[] c->gctr_host;
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -1539,15 +1540,28 @@ hpc_status hpc_batch_get_records_packed(hpc_ctx *c, int32_t *out, int64_t cap_wo
     if ((s = dev_alloc(&c->rec_stage, words, "record staging")) != HPC_OK) return s;
     c->rec_stage_words = words;
   }
-  if (!c->rec_prefix_dev && (s = dev_alloc(&c->rec_prefix_dev, 2 * (c->count + 1), "record prefix")) != HPC_OK)
-    return s;
-  std::vector<long long> both(pre);
-  both.insert(both.end(), wpre.begin(), wpre.end());
-  HPC_CUDA(cudaMemcpyAsync(c->rec_prefix_dev, both.data(), sizeof(long long) * both.size(), cudaMemcpyHostToDevice,
+  // one segment per (instance, level) with removals: a contiguous run of records
+  std::vector<RecSegment> segs;
+  for (int b = 0; b < c->count; ++b) {
+    long long src = 0, dst = wpre[b];
+    for (int l = 1; l < kLevels && l < c->next_level; ++l) {
+      const long long d = (long long)c->ctr_host[(size_t)b * kLevels + l].deleted;
+      if (d == 0) continue;
+      segs.push_back(RecSegment{src, d, dst, b, l});
+      src += d;
+      dst += d * (6 + ((l + 1) & ~1));
+    }
+  }
+  if ((long long)segs.size() > c->rec_seg_cap) {
+    dev_free(c->rec_seg);
+    c->rec_seg = nullptr;
+    c->rec_seg_cap = 0;
+    if ((s = dev_alloc(&c->rec_seg, (int64_t)segs.size(), "record segments")) != HPC_OK) return s;
+    c->rec_seg_cap = (long long)segs.size();
+  }
+  HPC_CUDA(cudaMemcpyAsync(c->rec_seg, segs.data(), sizeof(RecSegment) * segs.size(), cudaMemcpyHostToDevice,
                            c->stream));
-  if ((s = launch_pack_records(c->inst, c->count, c->rec_prefix_dev, c->rec_prefix_dev + c->count + 1, total,
-                               c->rec_stage, c->stream)) != HPC_OK)
-    return s;
+  if ((s = launch_pack_records(c->inst, c->rec_seg, (int)segs.size(), c->rec_stage, c->stream)) != HPC_OK) return s;
   c->timings.launches += 1;
   HPC_CUDA(cudaMemcpyAsync(out, c->rec_stage, sizeof(int32_t) * (size_t)std::min<long long>(cap_words, words),
                            cudaMemcpyDeviceToHost, c->stream));
@@ -1871,7 +1885,8 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   // (35 KB per thread) would otherwise be reserved for the whole device
   for (int l = 1; l <= c->rec_ids; ++l) c->citest_grid[l] = citest_grid(o.precision, l, c->device);
   if (o.precision != HPC_PREC_FP64)
-    for (int l = 2; l <= std::min(c->rec_ids, 16); ++l) c->citest_grid_set[l] = citest_grid(o.precision, l, c->device, kSetOrder);
+    for (int l = 2; l <= std::min(c->rec_ids, kSetTop); ++l)
+      c->citest_grid_set[l] = citest_grid(o.precision, l, c->device, kSetOrder);
   for (int v = 0; v < 3; ++v) c->citest_grid_l1[v] = citest_grid(o.precision, 1, c->device, v);
   if (o.precision != HPC_PREC_FP64)
     for (int v = 0; v < 2; ++v) c->citest_grid_l1q[v] = citest_grid(o.precision, 1, c->device, v | kQueueOnly);

@@ -82,6 +82,7 @@ constexpr int kL1Interleaved = 0, kL1Prefetch = 1, kL1Chunked = 2;
 // kernel variant of levels 2-16 (mixed precision): the CI tests in the set order
 // (citest.cuh) instead of the edge order (variant 0)
 constexpr int kSetOrder = 3;
+constexpr int kSetTop = 24;  // the highest level with a set-order kernel (unrolled for its level)
 // flag on the level-1 variants kL1Interleaved / kL1Prefetch: undecided tests only
 // queued (mixed precision without an FP64 matrix), as the set order does
 constexpr int kQueueOnly = 8;
@@ -179,23 +180,29 @@ __device__ __forceinline__ double zdot(const Inst &I, int64_t a, int64_t b, int6
     return s;
   }
   const float *xh = I.zh + a * n, *xl = I.zl + a * n, *yh = I.zh + b * n, *yl = I.zl + b * n;
+  // one block of up to 16 samples: products compensated into (sh, sl)
+  auto add = [&](int64_t k, float &sh, float &sl) {
+    const float ah = xh[k], al = xl[k], bh = yh[k], bl = yl[k];
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, fmaf(al, bh, e));
+    const float t = sh + p;
+    const float bb = t - sh;
+    sl += ((sh - (t - bb)) + (p - bb)) + e;
+    sh = t;
+  };
   int64_t k = k0;
-  while (k < n) {
+  // full blocks: no bounds test inside, so that all 64 loads of a block issue before the
+  // arithmetic that waits for them
+  for (; k + 15 * step < n; k += 16 * step) {
     float sh = 0.f, sl = 0.f;
-#pragma unroll 16
-    for (int u = 0; u < 16 && k < n; ++u, k += step) {
-      const float ah = xh[k], al = xl[k], bh = yh[k], bl = yl[k];
-      const float p = ah * bh;
-      float e = fmaf(ah, bh, -p);
-      e = fmaf(ah, bl, fmaf(al, bh, e));
-      const float t = sh + p;
-      const float bb = t - sh;
-      sl += ((sh - (t - bb)) + (p - bb)) + e;
-      sh = t;
-    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) add(k + u * step, sh, sl);
     s += (double)sh + (double)sl;
   }
-  return s;
+  float sh = 0.f, sl = 0.f;
+  for (; k < n; k += step) add(k, sh, sl);
+  return s + ((double)sh + (double)sl);
 }
 
 // One level's launch over all instances, passed by value.
@@ -329,8 +336,14 @@ hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s);
 hpc_status launch_gather_records(const Inst *inst, int count, const long long *prefix, long long total, int stride,
                                  int32_t *out, cudaStream_t s);
 // every instance's records in the packed form of hpc_batch_get_records_packed
-hpc_status launch_pack_records(const Inst *inst, int count, const long long *prefix, const long long *inst_words,
-                               long long total, int32_t *out, cudaStream_t s);
+// one (instance, level) run of records for the packed copy (pack_records_kernel)
+struct RecSegment {
+  long long src;    // first record, within the instance
+  long long count;  // records
+  long long dst;    // first output word
+  int inst, level;
+};
+hpc_status launch_pack_records(const Inst *inst, const RecSegment *seg, int nseg, int32_t *out, cudaStream_t s);
 int citest_grid(int precision, int level, int device, int l1_variant = kL1Interleaved);
 
 // process-wide tile-policy table (tune.cu)
@@ -354,7 +367,7 @@ long long retest_scratch_entries(long long cap);
 // uses_set_order: whether a level runs in the set order, given the lowest set-order
 // level in effect (0: none). The set order defers every undecided test to the FP64
 // re-test queue, so it runs only where the re-tests are queued (no FP64 matrix).
-constexpr int kSetOrderFrom = 4;
+constexpr int kSetOrderFrom = 3;
 int set_order_from();
 bool uses_set_order(int set_from, int level);
 
@@ -473,4 +486,6 @@ struct hpc_ctx {
   int32_t *rec_stage = nullptr;
   long long rec_stage_words = 0;
   long long *rec_prefix_dev = nullptr;  // 2 x (count + 1): record and packed-word prefixes
+  hpc::RecSegment *rec_seg = nullptr;  // segments of the packed record copy
+  long long rec_seg_cap = 0;
 };

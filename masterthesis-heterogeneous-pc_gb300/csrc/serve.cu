@@ -420,7 +420,7 @@ hpc_status hpc_server_create(hpc_server **out, const hpc_server_opts *opts) {
   const int top = o.max_level < 0 ? HPC_MAX_LEVEL : o.max_level;
   for (int l = 2; l <= top; ++l) sv->grid[l] = citest_grid(o.precision, l, o.device);
   if (o.precision != HPC_PREC_FP64)
-    for (int l = 2; l <= std::min(top, 16); ++l) sv->grid_set[l] = citest_grid(o.precision, l, o.device, kSetOrder);
+    for (int l = 2; l <= std::min(top, kSetTop); ++l) sv->grid_set[l] = citest_grid(o.precision, l, o.device, kSetOrder);
   if (top >= 1) sv->grid_l1 = citest_grid(o.precision, 1, o.device, kL1Interleaved);
   if (top > 16) retest_setup();
   if (o.precision == HPC_PREC_MIXED_TC) {

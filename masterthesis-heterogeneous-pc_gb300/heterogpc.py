@@ -183,7 +183,7 @@ def tune_load(path):
     _check(lib().hpc_tune_load(os.fsencode(path)))
 
 
-SET_ORDER_DEFAULT = 4  # the library's default lowest set-order level (kSetOrderFrom)
+SET_ORDER_DEFAULT = 3  # the library's default lowest set-order level (kSetOrderFrom)
 
 
 def set_order_from(level):

@@ -21,7 +21,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["citest_l17.cu", "citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
+CU_SOURCES = ["citest_l17s.cu", "citest_l17.cu", "citest_l13.cu", "citest_l9.cu", "citest.cu", "ctx.cu", "correlation.cu", "graph.cu", "gram_tc.cu",
               "noalloc.cu", "tune.cu", "compat.cu", "serve.cu", "gram_emu.cu"]
 HOST_SOURCES = ["semgen.cpp"]
 
