@@ -25,6 +25,7 @@ Other workloads (--workload): c1, c2 (single instances), c3 (wide, hub-heavy), c
 not shard without an exchange step).
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -533,7 +534,12 @@ def run_c4(args, wl):
     rec_cap = rec_words + 65536
     recs_h = torch.empty(rec_cap, dtype=torch.int32, pin_memory=True)
     e2e_t = []
-    for k in range(args.warmup + args.steps):
+    e2e_steps = max(args.steps, 10)  # host wall clock: more steps than the device-timed loop
+    # the interpreter's cyclic garbage collector stays off while host wall time is taken
+    # (a collection pass is the harness's pause, not the library's)
+    gc.collect()
+    gc.disable()
+    for k in range(args.warmup + e2e_steps):
         t0 = time.perf_counter()
         bt.add_observations_ptr(host.data_ptr(), np.float32)
         bt.run()
@@ -556,6 +562,7 @@ def run_c4(args, wl):
         t1 = time.perf_counter()
         phase.append((t1 - t0) * 1e3)
         t0 = t1
+    gc.enable()
     e2e = {"value": bt.count * len(e2e_t) / sum(e2e_t), "unit": "skeletons/s", "h2d_bytes_per_step": total_obs * 4,
            "d2h_bytes_per_step": words * 4 + rec_words * 4,
            "path": "hpc_correlation_f32 (host observations, pinned) + hpc_run_skeleton + "
@@ -580,7 +587,7 @@ def run_c4(args, wl):
                           % (lv_dom, lv_dom, bt.count),
                 "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (hbm_gbs, burst)",
-                "traffic": traffic_from_profile("c4_level_kernel_l%d" % lv_dom),
+                "traffic": c4_scaled_traffic(lv_dom, st),
                 "algorithmic_bytes_per_launch": int(lb.get(lv_dom, 0)), "launch_ms": test_ms[lv_dom],
                 "all_levels": {"algorithmic_bytes": int(all_b), "kernel_ms": all_ms,
                                "frac": all_b / 1e9 / (all_ms / 1e3) / peaks["hbm_gbs"] if all_ms > 0 else None},
@@ -608,7 +615,9 @@ def run_c4(args, wl):
             "e2e_speedup_vs_plain": e2e["value"] / plain["skeletons_per_sec"],
             "parity": parity, "clocks": clk, "tile_policy": tuned,
             "kernel_ms": {"standardise": t_k["standardise_ms"], "gram": t_k["gram_ms"],
-                          "levels": {str(l): test_ms[l] for l in range(len(test_ms)) if test_ms[l] > 0}},
+                          "levels": {str(l): test_ms[l] for l in range(len(test_ms)) if test_ms[l] > 0},
+                          "retests": {str(l): t_k["retest_ms"][l] for l in range(len(test_ms))
+                                      if t_k["retest_ms"][l] > 0}},
             "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
                         "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
                         "retests": s_["retests"], "edges_after": s_["edges_after"]} for s_ in st]}
@@ -852,6 +861,24 @@ def citest_bytes(adjs, levels_stats, lane_bytes=4):
         rebuild = (p * ((p + 31) // 32) + int(d.sum()) + 2 * p) * 4 + (p + 1) * 8
         out.append(st["executed_tests"] * lane_bytes * l * (l + 3) // 2 + edge_bytes + rebuild)
     return out
+
+
+def c4_scaled_traffic(level, stats):
+    """DRAM bytes of the c4 level kernel per launch: the capture of the same kernel on the
+    first 64 instances (profiles/ncu_traffic.json), scaled by this run's executed tests
+    of the level over the capture's (the kernel's traffic grows with the tests it runs);
+    None without a capture of that level."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        ent = json.load(f).get("c4_64_level_kernel_l%d" % level)
+    if not ent:
+        return None
+    ex = [s_["executed_tests"] for s_ in stats if s_["level"] == level]
+    if not ex or not ent.get("executed_tests"):
+        return None
+    return ent["dram_bytes_per_launch"] * ex[0] / ent["executed_tests"]
 
 
 def traffic_from_profile(kernel):
@@ -1139,7 +1166,7 @@ def main():
     roofline = {"kernel": "level_kernel<1> (level 1: rebuild, scan, CI tests; mixed)", "bound": "hbm",
                 "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (hbm_gbs)",
-                "traffic": traffic_from_profile("level_kernel_l1"),
+                "traffic": traffic_from_profile("%s_level_kernel_l1" % args.workload),
                 "algorithmic_bytes_per_launch": int(bytes_l[1]), "launch_ms": l1_ms,
                 "all_levels": {"algorithmic_bytes": int(sum(bytes_l)), "kernel_ms": float(sum(test_ms[1:len(lst)]))}}
     gram_flops = n * p * (p + 1)  # FP64 Gram, upper triangle incl. diagonal

@@ -92,6 +92,7 @@ typedef struct hpc_timings {
   double test_ms[HPC_MAX_LEVEL + 1];     /* CI-test kernel of the level */
   int64_t launches;                      /* kernels launched by this context so far */
   double skeleton_ms;                    /* last hpc_run_skeleton as a whole */
+  double retest_ms[HPC_MAX_LEVEL + 1];   /* FP64 re-test kernel of the level (tensor-core mode) */
 } hpc_timings;
 
 typedef struct hpc_ctx hpc_ctx;

@@ -214,6 +214,23 @@ int effective_set_from(const hpc_ctx *c) {
   return set_order_from();
 }
 
+// Whether level l runs in the set order: from the lowest set-order level in effect, and
+// only where the largest degree at the level's start in the context's last run (else
+// the level before it; unknown before a first run) fits kSetDegMax.
+bool set_at(const hpc_ctx *c, int level) {
+  if (!uses_set_order(effective_set_from(c), level)) return false;
+  int d = c->deg_seen[level];
+  if (d < 0) d = c->deg_seen[level - 1];
+  return d <= kSetDegMax;
+}
+
+unsigned int set_mask(const hpc_ctx *c, int last) {
+  unsigned int m = 0;
+  for (int l = 2; l <= last && l <= kSetTop; ++l)
+    if (set_at(c, l)) m |= 1u << l;
+  return m;
+}
+
 Launch make_launch(hpc_ctx *c, int level) {
   Launch L{};
   L.inst = c->inst;
@@ -275,7 +292,7 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
   }
   // snapshot rebuild, test-count scan and CI tests in one launch
   if (timed) HPC_CUDA(cudaEventRecord(ev[1], c->stream));
-  const bool set = uses_set_order(effective_set_from(c), level);
+  const bool set = set_at(c, level);
   // level 1: the queue-only build of the interleaved variants where the re-tests are
   // queued and a queue overflow can be rerun
   const bool qo = level == 1 && c->l1v_now != kL1Chunked && effective_set_from(c) > 0;
@@ -284,6 +301,7 @@ hpc_status enqueue_level(hpc_ctx *c, int level, bool timed) {
                    : set      ? c->citest_grid_set[level]
                               : c->citest_grid[level];
   if ((s = launch_level(L, c->opts.precision, grid, var, c->stream)) != HPC_OK) return s;
+  if (timed) HPC_CUDA(cudaEventRecord(ev[3], c->stream));
   if (queue && (s = launch_retest(L, c->sm_count, c->stream)) != HPC_OK) return s;
   if (timed) HPC_CUDA(cudaEventRecord(ev[2], c->stream));
   c->timings.launches += queue ? 2 : 1;
@@ -361,10 +379,16 @@ hpc_level_stats level_stats_of(hpc_ctx *c, int level, int only) {
 hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
   hpc_level_stats st = level_stats_of(c, level, -1);
   if (level == 1) c->l1_max_deg = st.max_degree;
-  float t_all = 0.f, t_snap = 0.f, t_test = 0.f;
+  if (level >= 1) c->deg_seen[level] = st.max_degree;
+  float t_all = 0.f, t_snap = 0.f, t_test = 0.f, t_re = 0.f;
   if (!c->last_run_graph) {
     HPC_CUDA(cudaEventElapsedTime(&t_snap, c->evl[level][0], c->evl[level][1]));
-    HPC_CUDA(cudaEventElapsedTime(&t_test, c->evl[level][1], c->evl[level][2]));
+    if (level >= 1) {  // the level kernel, then its re-tests
+      HPC_CUDA(cudaEventElapsedTime(&t_test, c->evl[level][1], c->evl[level][3]));
+      HPC_CUDA(cudaEventElapsedTime(&t_re, c->evl[level][3], c->evl[level][2]));
+    } else {
+      HPC_CUDA(cudaEventElapsedTime(&t_test, c->evl[level][1], c->evl[level][2]));
+    }
     HPC_CUDA(cudaEventElapsedTime(&t_all, c->evl[level][0], level < HPC_MAX_LEVEL && level + 1 < c->next_level
                                                                 ? c->evl[level + 1][0] : c->evl[level][2]));
   }
@@ -372,6 +396,7 @@ hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
   c->timings.level_ms[level] = t_all;
   c->timings.compact_ms[level] = t_snap;
   c->timings.test_ms[level] = t_test;
+  c->timings.retest_ms[level] = t_re;
   for (int b = 0; b < c->count; ++b) {
     const DevCounters &h = c->ctr_host[(size_t)b * kLevels + level];
     c->ih[b].edges = level == 0 ? (int64_t)(h.edges2 / 2) : (int64_t)(h.edges2 / 2) - (int64_t)h.deleted;
@@ -498,7 +523,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
   if (use_graph && c->graphs_enabled && first == 0 && capturable(c->stream)) {
     const bool valid = c->graph && c->graph_top == last && c->graph_stream == c->stream &&
                        c->graph_version == c->inst_version && c->graph_l1v == c->l1v_now &&
-                       c->graph_set_from == effective_set_from(c) &&
+                       c->graph_set_mask == set_mask(c, last) &&
                        c->graph_final == finalize;
     if (!valid) {
       if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -524,7 +549,7 @@ hpc_status run_levels(hpc_ctx *c, int first, int last, bool use_graph, bool wait
       c->graph_stream = c->stream;
       c->graph_version = c->inst_version;
       c->graph_l1v = c->l1v_now;
-      c->graph_set_from = effective_set_from(c);
+      c->graph_set_mask = set_mask(c, last);
       c->graph_final = finalize;
     }
     HPC_CUDA(cudaGraphLaunch(c->graph, c->stream));
@@ -1869,6 +1894,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
     return HPC_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  std::fill(std::begin(c->deg_seen), std::end(c->deg_seen), -1);
   bool ev_ok = true;
   for (auto &ev : c->evc) ev_ok = ev_ok && cudaEventCreate(&ev) == cudaSuccess;
   for (auto &ev : c->evr) ev_ok = ev_ok && cudaEventCreate(&ev) == cudaSuccess;

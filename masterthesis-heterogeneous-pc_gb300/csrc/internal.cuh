@@ -368,6 +368,9 @@ long long retest_scratch_entries(long long cap);
 // level in effect (0: none). The set order defers every undecided test to the FP64
 // re-test queue, so it runs only where the re-tests are queued (no FP64 matrix).
 constexpr int kSetOrderFrom = 3;
+// ... and only where the level's largest degree fits the set order's 64-bit masks:
+// wider rows (hubs) are where the edge order's early exit on removed edges pays most
+constexpr int kSetDegMax = 64;
 int set_order_from();
 bool uses_set_order(int set_from, int level);
 
@@ -461,12 +464,13 @@ struct hpc_ctx {
   int l1_max_deg = -1;            // level-1 max degree of the last run (keys level 1's kernel choice)
   int l1v_now = 0;                // the level-1 kernel variant of the runs being queued
   int graph_l1v = 0;              // ... and of the captured graph
-  int graph_set_from = 0;         // the set-order levels of the captured graph
+  unsigned int graph_set_mask = 0;  // the set-order levels of the captured graph (bit l)
+  int deg_seen[HPC_MAX_LEVEL + 1];  // largest degree at each level's start in the last run (-1: unknown)
   bool set_off = false;           // the set order turned off (a re-test queue overflow)
   bool level_by_level = false;    // inside hpc_run_level: the edge order, inline re-tests on overflow
   bool graph_final = false;       // the captured graph ends with the record finalisation
   cudaEvent_t evc[4] = {nullptr, nullptr, nullptr, nullptr};  // correlation phases
-  cudaEvent_t evl[HPC_MAX_LEVEL + 1][3] = {};  // per level: start, snapshot done, tests done
+  cudaEvent_t evl[HPC_MAX_LEVEL + 1][4] = {};  // per level: start, kernel start, re-tests done, kernel done
   cudaEvent_t evr[2] = {nullptr, nullptr};      // whole skeleton run
   bool cor_timed = false;
   hpc_timings timings{};

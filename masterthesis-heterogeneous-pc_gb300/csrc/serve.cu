@@ -185,6 +185,7 @@ hpc_status step(hpc_server *sv) {
     int level, first, count;
     long long pre_off, seg_off, words, tiles, rows, segs;
     int64_t pmax;
+    int prev_deg;  // largest degree at the previous level's start over the group (the set-order choice)
   };
   std::vector<Group> groups;
   long long segs_all = 0;
@@ -192,7 +193,7 @@ hpc_status step(hpc_server *sv) {
     const int l = act[order[q]]->next;
     int e = q;
     while (e < A && act[order[e]]->next == l) ++e;
-    Group g{l, q, e - q, (long long)pre.size(), segs_all, 0, 0, 0, 0, 0};
+    Group g{l, q, e - q, (long long)pre.size(), segs_all, 0, 0, 0, 0, 0, 0};
     pre.resize(pre.size() + 4 * (size_t)(g.count + 1));
     long long *wp = pre.data() + g.pre_off, *tp = wp + (g.count + 1), *rp = tp + (g.count + 1),
               *sp = rp + (g.count + 1);
@@ -210,6 +211,7 @@ hpc_status step(hpc_server *sv) {
       g.rows += h.p;
       g.segs += (h.p + kSegRows - 1) / kSegRows;
       g.pmax = std::max<int64_t>(g.pmax, h.p);
+      g.prev_deg = std::max(g.prev_deg, l >= 2 ? r->ctx->ctr_host[l - 1].max_deg : 0);
       r->batch_size = std::max(r->batch_size, g.count);
     }
     wp[g.count] = g.words;
@@ -271,7 +273,7 @@ hpc_status step(hpc_server *sv) {
       if ((s = launch_degrees(L, g.rows, sv->st)) != HPC_OK) return s;
       if ((s = launch_scan(L, sv->st)) != HPC_OK) return s;
     } else {
-      const bool set = tc && uses_set_order(set_order_from(), g.level);
+      const bool set = tc && uses_set_order(set_order_from(), g.level) && g.prev_deg <= kSetDegMax;
       const int grid = g.level == 1 ? sv->grid_l1 : set ? sv->grid_set[g.level] : sv->grid[g.level];
       if ((s = launch_level(L, sv->opts.precision, grid, set ? kSetOrder : kL1Interleaved, sv->st)) != HPC_OK)
         return s;
