@@ -539,15 +539,21 @@ def run_c4(args, wl):
     # (a collection pass is the harness's pause, not the library's)
     gc.collect()
     gc.disable()
+    e2e_calls = []  # host time until each call returned (the skeleton and result calls wait for the GPU)
     for k in range(args.warmup + e2e_steps):
         t0 = time.perf_counter()
         bt.add_observations_ptr(host.data_ptr(), np.float32)
-        bt.run()
+        t1 = time.perf_counter()
+        lv_run = bt.run()
+        t2 = time.perf_counter()
         bt.adjacency_bits_into(bits_h.data_ptr(), words)
         w = bt.records_packed_into(recs_h.data_ptr(), rec_cap)
         torch.cuda.synchronize()
+        t3 = time.perf_counter()
         if k >= args.warmup:
-            e2e_t.append(time.perf_counter() - t0)
+            e2e_t.append(t3 - t0)
+            e2e_calls.append([round(1e3 * (t1 - t0), 2), round(1e3 * (t2 - t1), 2), round(1e3 * (t3 - t2), 2),
+                              round(bt.timings()["skeleton_ms"], 2), len(lv_run)])
         rec_words = int(w[-1])
     # one more step with a device sync after every call: where the host wall time goes
     # (not part of the value)
@@ -568,6 +574,8 @@ def run_c4(args, wl):
            "path": "hpc_correlation_f32 (host observations, pinned) + hpc_run_skeleton + "
                    "hpc_batch_get_adjacency_bits + hpc_batch_get_records_packed (pinned), host wall clock per step",
            "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t), "step_ms": [round(1e3 * t, 2) for t in e2e_t],
+           "step_calls_ms": {"order": ["correlation call", "skeleton call", "results", "skeleton device ms",
+                                       "levels"], "steps": e2e_calls},
            "phases_ms": {"correlation_from_host": phase[0], "skeleton": phase[1], "adjacency_bits": phase[2],
                          "records_packed": phase[3], "note": "one extra step, device synchronised after each call"}}
 

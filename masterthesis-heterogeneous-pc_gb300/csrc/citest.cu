@@ -247,14 +247,33 @@ __device__ __forceinline__ void retest_columns_passes(const Inst &I, const float
 // the item's matrix M (K x K, the warp's shared memory) from its columns
 template <int K>
 __device__ __forceinline__ void retest_item_columns(const Inst &I, const RetestItem *it, double *M) {
+  constexpr int E = K * (K - 1) / 2;
+  static_assert(E <= 32, "one lane per entry");
   const int lane = threadIdx.x & 31;
   const int64_t n = I.n_z;
+  if (lane < K) M[lane * K + lane] = 1.0;
+  // lane e: entry e -- formed by an earlier re-test? then no column is read
+  int er = 0, ec = 0;
+  int64_t va = 0, vb = 0;
+  double v = 0.0;
+  bool have = true;
+  if (lane < E) {
+    entry_rc(lane, K, er, ec);
+    va = retest_var(it, er);
+    vb = retest_var(it, ec);
+    have = ecache_get(I, va, vb, &v);
+  }
+  if (__all_sync(0xffffffffu, have)) {
+    if (lane < E) M[er * K + ec] = M[ec * K + er] = v;
+    return;
+  }
   const float *ch[K];
   const int64_t lo_off = I.zl - I.zh;  // the zl plane, at a fixed distance from zh
 #pragma unroll
   for (int r = 0; r < K; ++r) ch[r] = I.zh + retest_var(it, r) * n;
-  if (lane < K) M[lane * K + lane] = 1.0;
   retest_columns_passes<K, 0>(I, ch, lo_off, M);
+  __syncwarp();
+  if (lane < E && !have) ecache_put(I, va, vb, M[er * K + ec]);
 }
 
 template <int KM>
@@ -273,7 +292,11 @@ __global__ void __launch_bounds__(kRetestWarps * 32, 2) retest_kernel(const __gr
       const RetestItem *it = L.rq + q;
       const Inst &I = *inst_of(L, it->inst);
       const int64_t i = it->i, j = it->j;
-      const double r = warp_dot(I, i, j) / I.denom;
+      double r;
+      if (!ecache_get(I, i, j, &r)) {
+        r = warp_dot(I, i, j) / I.denom;
+        if (lane == 0) ecache_put(I, i, j, r);
+      }
       double pv;
       if (lane == 0 && !decide_of_r(I, r, false, &pv)) {  // kept: both triangles' bits
         atomicOr(I.adj + i * I.W + (j >> 5), 1u << (j & 31));
@@ -316,7 +339,12 @@ __global__ void __launch_bounds__(kRetestWarps * 32, 2) retest_kernel(const __gr
     if (live_bit(I.adj, I.W, i, j)) {  // else removed meanwhile: nothing to compute
       int r, c;
       entry_rc(e, k, r, c);
-      const double v = warp_dot(I, retest_var(it, r), retest_var(it, c)) / I.denom;
+      const int64_t va = retest_var(it, r), vb = retest_var(it, c);
+      double v;
+      if (!ecache_get(I, va, vb, &v)) {
+        v = warp_dot(I, va, vb) / I.denom;
+        if (lane == 0) ecache_put(I, va, vb, v);
+      }
       if (lane == 0) L.rq_val[q * (unsigned long long)E + e] = v;
     }
     unsigned last = 0;
@@ -352,7 +380,12 @@ __global__ void __launch_bounds__(kRetestWarps * 32, 2) retest_kernel(const __gr
     for (int r = 0; r < k; ++r) {
       if (lane == 0) M[r * k + r] = 1.0;
       for (int c2 = r + 1; c2 < k; ++c2) {
-        const double v = warp_dot(I, retest_var(it, r), retest_var(it, c2)) / I.denom;
+        const int64_t va = retest_var(it, r), vb = retest_var(it, c2);
+        double v;
+        if (!ecache_get(I, va, vb, &v)) {
+          v = warp_dot(I, va, vb) / I.denom;
+          if (lane == 0) ecache_put(I, va, vb, v);
+        }
         if (lane == 0) M[r * k + c2] = M[c2 * k + r] = v;
       }
     }

@@ -73,7 +73,11 @@ __device__ __forceinline__ bool live_bit(const uint32_t *adj, int W, int64_t i, 
 // reference reads cor[row * p + col].
 __device__ __forceinline__ double exact_entry(const Inst &I, int64_t x, int64_t y) {
   if (I.cor64) return I.cor64[x * I.p + y];
-  return zdot(I, x, y, 0, 1) / I.denom;
+  double v;
+  if (ecache_get(I, x, y, &v)) return v;
+  v = zdot(I, x, y, 0, 1) / I.denom;
+  ecache_put(I, x, y, v);
+  return v;
 }
 
 // FP64 partial correlation of a k x k submatrix M (row-major, ordered i, j, S;
@@ -1057,7 +1061,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
 // against the positions and read the live bit per test.
 constexpr int kSetMaskD = 64;
 template <int LT>
-constexpr int kSetBlocks = LT <= 10 ? 2 : 1;  // resident blocks per SM the set-order kernels are compiled for
+constexpr int kSetBlocks = LT <= 11 ? 2 : 1;  // resident blocks per SM the set-order kernels are compiled for
 
 // Rows ci..l-1 of the Cholesky factor of the S block and of w_i = L_S^-1 r_iS: the
 // operations of test_f32_inc without w_j.

@@ -181,6 +181,9 @@ hpc_status write_inst_table(hpc_ctx *c) {
     I.Z = c->z_valid ? c->Z + h.z_off : nullptr;
     I.zh = (!c->z_valid && c->zpair_valid) ? c->zpair + h.z_off : nullptr;
     I.zl = (!c->z_valid && c->zpair_valid) ? c->zpair + c->ztot + h.z_off : nullptr;
+    I.ec = (c->ecache && I.zh) ? c->ecache + h.cor_off : nullptr;
+    I.ev = (c->ecache && I.zh) ? c->evalid : nullptr;
+    I.ev_off = h.cor_off;
     I.n_z = h.n;
     I.denom = denom_of(c, h.n);
     I.adj = c->adj + h.adj_off;
@@ -696,6 +699,19 @@ hpc_status correlation_device(hpc_ctx *c, const void *X, bool f32) {
   c->ztot = ztot;
   if (!pair && !c->Z && (s = dev_alloc(&c->Z, ztot, "standardised data")) != HPC_OK) return s;
   if (pair && !c->zpair && (s = dev_alloc(&c->zpair, 2 * ztot, "standardised data (FP32 pairs)")) != HPC_OK) return s;
+  if (pair) {
+    // the re-tests' entry store: sum p^2 doubles (instance b at its cor_off) and one bit
+    // each, the bits cleared for the new data
+    long long ent = 0;
+    for (const auto &h : c->ih) ent = std::max(ent, h.cor_off + h.p * h.p);
+    const long long words = (ent + 31) / 32 + 1;
+    if (!c->ecache) {
+      if ((s = dev_alloc(&c->ecache, ent, "re-test entries")) != HPC_OK) return s;
+      if ((s = dev_alloc(&c->evalid, words, "re-test entry bits")) != HPC_OK) return s;
+      c->evalid_words = words;
+    }
+    HPC_CUDA(cudaMemsetAsync(c->evalid, 0, sizeof(uint32_t) * (size_t)c->evalid_words, c->stream));
+  }
   StdArgs sa = std_args(c);
   HPC_CUDA(cudaEventRecord(c->evc[0], c->stream));
   if (tc) {
@@ -882,6 +898,7 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   if (o->precision != HPC_PREC_MIXED_TC) b += p * p * 8;           // cor64
   if (o->precision != HPC_PREC_FP64) b += p * p * 4;               // cor32
   if (o->precision == HPC_PREC_MIXED_TC) b += tc_p_pad(p) * tc_k(n) * 2;      // split operand planes
+  if (o->precision == HPC_PREC_MIXED_TC) b += p * p * 8 + p * p / 8 + 8;     // re-test entry store and its bits
   b += n * p * 8;                                                  // standardised data (FP64 or FP32 pairs)
   b += n * p * 4;                                                  // observation staging
   b += p * W * 4 + p * p;                                          // adjacency bits + bytes
@@ -929,6 +946,8 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->cor32);
   dev_free(c->Z);
   dev_free(c->zpair);
+  dev_free(c->ecache);
+  dev_free(c->evalid);
   dev_free(c->tcP);
   dev_free(c->emuD);
   dev_free(c->emuE);

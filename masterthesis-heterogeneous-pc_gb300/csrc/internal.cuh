@@ -151,6 +151,9 @@ struct Inst {
   const float *cor32;     // p x p FP32 (mixed modes) or null
   const double *Z;        // FP64 standardised data, n_z x p column-major, or null
   const float *zh, *zl;   // ... else the same values as FP32 pairs zh + zl (same layout)
+  double *ec;             // FP64 entries the re-tests formed (p x p, entry (a, b) at min * p + max), or null
+  uint32_t *ev;           // ... and which of them are there: bit ev_off + index of the context's bitmap
+  int64_t ev_off;
   int64_t n_z;
   double denom;           // the Gram's divisor n - 1
   uint32_t *adj;          // live bitmask p x W
@@ -165,6 +168,27 @@ struct Inst {
   DevCounters *ctr;       // [HPC_MAX_LEVEL + 1]
   DevGlobal *g;
 };
+
+// The re-tests' FP64 entries, kept per instance once formed (the same entries recur in
+// the re-tests of one edge and of neighbouring conditioning sets): entry (a, b) at
+// min * p + max, present when its bit is set. The value is stored, fenced, then the bit
+// set; a reader that sees the bit fences before reading the value.
+__device__ __forceinline__ bool ecache_get(const Inst &I, int64_t a, int64_t b, double *v) {
+  if (!I.ec) return false;
+  const int64_t idx = (a < b ? a : b) * I.p + (a < b ? b : a), bit = I.ev_off + idx;
+  const uint32_t w = __ldcg(I.ev + (bit >> 5));
+  if (!((w >> (bit & 31)) & 1u)) return false;
+  __threadfence();
+  *v = __ldcg(I.ec + idx);
+  return true;
+}
+__device__ __forceinline__ void ecache_put(const Inst &I, int64_t a, int64_t b, double v) {
+  if (!I.ec) return;
+  const int64_t idx = (a < b ? a : b) * I.p + (a < b ? b : a), bit = I.ev_off + idx;
+  __stcg(I.ec + idx, v);
+  __threadfence();
+  atomicOr(I.ev + (bit >> 5), 1u << (bit & 31));
+}
 
 // Sum over samples k = k0, k0 + step, ... < n of z_a[k] * z_b[k], the FP64-standardised
 // variables a and b of one instance. From Z: FP64 FMAs. From the FP32 pairs: each
@@ -402,6 +426,9 @@ struct hpc_ctx {
   float *cor32 = nullptr;         // sum p^2 (mixed modes)
   double *Z = nullptr;            // sum n * p
   bool z_valid = false;           // Z holds the current data's standardised values
+  double *ecache = nullptr;       // FP64 entries formed by the re-tests, sum p^2 (tensor-core mode)
+  uint32_t *evalid = nullptr;     // ... validity bits, cleared with every correlation
+  long long evalid_words = 0;
   float *zpair = nullptr;         // the same as FP32 pairs (tensor-core mode, FP32 data): zh | zl planes
   bool zpair_valid = false;
   long long ztot = 0;             // sum n * p: the elements of one plane

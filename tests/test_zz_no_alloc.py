@@ -92,3 +92,34 @@ def test_noalloc_rejects_oversize_inputs():
     st = hg.lib().hpc_correlation_noalloc_f64(C.c_void_p(Xd.data_ptr()), n, p, 0, C.c_void_p(Cd.data_ptr()), None)
     assert st == 7  # HPC_ERR_CAPACITY
     assert b"allocation-free limit" in hg.lib().hpc_last_error_string()
+
+
+def test_noalloc_captured_into_a_graph_and_replayed():
+    """The call only enqueues kernels on the caller's stream (its shapes are written by a
+    one-thread kernel, nothing is copied from host memory), so after a first call outside
+    any capture it can be captured into a CUDA graph; each replay computes the
+    correlation of the observations then in the input buffer."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    p, n = 64, 900
+    Xd = torch.from_numpy(hg.sem_generate(p, n, hg.GRAPH_ER, 3.0, seed=7)).to(dev)
+    Cd = torch.full((p, p), float("nan"), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize()
+    assert _noalloc(Xd, p, n, Cd, stream.cuda_stream) == 0, hg.lib().hpc_last_error_string()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        st = _noalloc(Xd, p, n, Cd, stream.cuda_stream)
+    assert st == 0, hg.lib().hpc_last_error_string()
+    for seed in (8, 9):
+        Xd.copy_(torch.from_numpy(hg.sem_generate(p, n, hg.GRAPH_ER, 3.0, seed=seed)).to(dev))
+        Cd.fill_(float("nan"))
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        got = Cd.cpu().numpy()
+        want = _reference_correlation(Xd, p, n)
+        assert np.isfinite(got).all()
+        assert np.abs(got - want).max() <= TOL
