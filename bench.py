@@ -574,6 +574,7 @@ def run_c4(args, wl):
            "path": "hpc_correlation_f32 (host observations, pinned) + hpc_run_skeleton + "
                    "hpc_batch_get_adjacency_bits + hpc_batch_get_records_packed (pinned), host wall clock per step",
            "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t), "step_ms": [round(1e3 * t, 2) for t in e2e_t],
+           "median_ms_per_step": 1e3 * statistics.median(e2e_t),
            "step_calls_ms": {"order": ["correlation call", "skeleton call", "results", "skeleton device ms",
                                        "levels"], "steps": e2e_calls},
            "phases_ms": {"correlation_from_host": phase[0], "skeleton": phase[1], "adjacency_bits": phase[2],
