@@ -482,7 +482,7 @@ def run_c4(args, wl):
     for _ in range(args.warmup):
         queue_step()
         bt.wait()
-    tuned = autotune_setup(args, bt, None, 2)
+    tuned = autotune_setup(args, bt, None, 3)
     queue_step()
     bt.wait()
     torch.cuda.synchronize()
@@ -529,56 +529,20 @@ def run_c4(args, wl):
     # correlation, all levels, record p-values, D2H of every adjacency bitmask and all
     # separation-set records
     words = int(bt.adjacency_words()[-1])
-    bits_h = torch.empty(words, dtype=torch.int32, pin_memory=True)
     rec_words = int(bt.packed_words()[-1])
     rec_cap = rec_words + 65536
-    recs_h = torch.empty(rec_cap, dtype=torch.int32, pin_memory=True)
-    e2e_t = []
     e2e_steps = max(args.steps, 10)  # host wall clock: more steps than the device-timed loop
-    # the interpreter's cyclic garbage collector stays off while host wall time is taken
-    # (a collection pass is the harness's pause, not the library's)
-    gc.collect()
-    gc.disable()
-    e2e_calls = []  # host time until each call returned (the skeleton and result calls wait for the GPU)
-    for k in range(args.warmup + e2e_steps):
-        t0 = time.perf_counter()
-        bt.add_observations_ptr(host.data_ptr(), np.float32)
-        t1 = time.perf_counter()
-        lv_run = bt.run()
-        t2 = time.perf_counter()
-        bt.adjacency_bits_into(bits_h.data_ptr(), words)
-        w = bt.records_packed_into(recs_h.data_ptr(), rec_cap)
-        torch.cuda.synchronize()
-        t3 = time.perf_counter()
-        if k >= args.warmup:
-            e2e_t.append(t3 - t0)
-            e2e_calls.append([round(1e3 * (t1 - t0), 2), round(1e3 * (t2 - t1), 2), round(1e3 * (t3 - t2), 2),
-                              round(bt.timings()["skeleton_ms"], 2), len(lv_run)])
-        rec_words = int(w[-1])
-    # one more step with a device sync after every call: where the host wall time goes
-    # (not part of the value)
-    phase = []
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for call in (lambda: bt.add_observations_ptr(host.data_ptr(), np.float32), bt.run,
-                 lambda: bt.adjacency_bits_into(bits_h.data_ptr(), words),
-                 lambda: bt.records_packed_into(recs_h.data_ptr(), rec_cap)):
-        call()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        phase.append((t1 - t0) * 1e3)
-        t0 = t1
-    gc.enable()
-    e2e = {"value": bt.count * len(e2e_t) / sum(e2e_t), "unit": "skeletons/s", "h2d_bytes_per_step": total_obs * 4,
-           "d2h_bytes_per_step": words * 4 + rec_words * 4,
-           "path": "hpc_correlation_f32 (host observations, pinned) + hpc_run_skeleton + "
-                   "hpc_batch_get_adjacency_bits + hpc_batch_get_records_packed (pinned), host wall clock per step",
-           "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t), "step_ms": [round(1e3 * t, 2) for t in e2e_t],
-           "median_ms_per_step": 1e3 * statistics.median(e2e_t),
-           "step_calls_ms": {"order": ["correlation call", "skeleton call", "results", "skeleton device ms",
-                                       "levels"], "steps": e2e_calls},
-           "phases_ms": {"correlation_from_host": phase[0], "skeleton": phase[1], "adjacency_bits": phase[2],
-                         "records_packed": phase[3], "note": "one extra step, device synchronised after each call"}}
+    e2e_serial = c4_e2e_serial(args, bt, host, words, rec_cap, e2e_steps)
+    # pipelined: a second context of the same shapes on its own stream, the two taking
+    # steps in turn, so that step k+1's observations are copied (and correlated) while
+    # step k's skeleton runs
+    stream2 = torch.cuda.Stream(device=dev)
+    bt2 = hg.SkeletonBatch(ps, ns, alphas, max_level=wl["max_level"], precision=hg.PREC_MIXED_TC)
+    bt2.set_stream(stream2.cuda_stream)
+    e2e = c4_e2e_pipelined(args, [bt, bt2], host, words, rec_cap, e2e_steps, ps)
+    e2e["serial"] = e2e_serial
+    bt2.close()
+    torch.cuda.set_stream(stream)
 
     # the plain single-instance FP64 path on the same instances, like for like
     plain = c4_plain_path(wl, hg, torch, stream, ps, ns, alphas, Xd, bt.obs_off, flush)
@@ -626,13 +590,126 @@ def run_c4(args, wl):
             "kernel_ms": {"standardise": t_k["standardise_ms"], "gram": t_k["gram_ms"],
                           "levels": {str(l): test_ms[l] for l in range(len(test_ms)) if test_ms[l] > 0},
                           "retests": {str(l): t_k["retest_ms"][l] for l in range(len(test_ms))
-                                      if t_k["retest_ms"][l] > 0}},
+                                      if t_k["retest_ms"][l] > 0},
+                          "level_phases": {"order": ["neighbour-list rebuild", "test-count scan"],
+                                           "levels": {str(l): [round(t_k["rebuild_ms"][l], 4),
+                                                               round(t_k["scan_ms"][l], 4)]
+                                                      for l in range(len(test_ms)) if test_ms[l] > 0}}},
             "levels": [{"level": s_["level"], "max_degree": s_["max_degree"],
                         "potential_tests": s_["potential_tests"], "executed_tests": s_["executed_tests"],
                         "retests": s_["retests"], "edges_after": s_["edges_after"]} for s_ in st]}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = c4_cpu_baseline(wl, bt.count)
     print(json.dumps(line), flush=True)
+
+
+def c4_e2e_serial(args, bt, host, words, rec_cap, steps):
+    """One context, one step after the other: the host wall time of correlation call,
+    skeleton call and result reads per step (the skeleton call waits for the copy, the
+    correlation and every level)."""
+    import torch
+    bits_h = torch.empty(words, dtype=torch.int32, pin_memory=True)
+    recs_h = torch.empty(rec_cap, dtype=torch.int32, pin_memory=True)
+    e2e_t, calls = [], []
+    # the interpreter's cyclic garbage collector stays off while host wall time is taken
+    # (a collection pass is the harness's pause, not the library's)
+    gc.collect()
+    gc.disable()
+    rec_words = 0
+    for k in range(args.warmup + steps):
+        t0 = time.perf_counter()
+        bt.add_observations_ptr(host.data_ptr(), np.float32)
+        t1 = time.perf_counter()
+        lv_run = bt.run()
+        t2 = time.perf_counter()
+        bt.adjacency_bits_into(bits_h.data_ptr(), words)
+        w = bt.records_packed_into(recs_h.data_ptr(), rec_cap)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_t.append(t3 - t0)
+            calls.append([round(1e3 * (t1 - t0), 2), round(1e3 * (t2 - t1), 2), round(1e3 * (t3 - t2), 2),
+                          round(bt.timings()["skeleton_ms"], 2), len(lv_run)])
+        rec_words = int(w[-1])
+    # one more step with a device sync after every call: where the host wall time goes
+    phase = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for call in (lambda: bt.add_observations_ptr(host.data_ptr(), np.float32), bt.run,
+                 lambda: bt.adjacency_bits_into(bits_h.data_ptr(), words),
+                 lambda: bt.records_packed_into(recs_h.data_ptr(), rec_cap)):
+        call()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        phase.append((t1 - t0) * 1e3)
+        t0 = t1
+    gc.enable()
+    return {"value": bt.count * len(e2e_t) / sum(e2e_t), "unit": "skeletons/s",
+            "h2d_bytes_per_step": int(host.numel()) * 4, "d2h_bytes_per_step": words * 4 + rec_words * 4,
+            "path": "one context: hpc_correlation_f32 (host observations, pinned) + hpc_run_skeleton + "
+                    "hpc_batch_get_adjacency_bits + hpc_batch_get_records_packed (pinned), host wall clock per step",
+            "ms_per_step": 1e3 * sum(e2e_t) / len(e2e_t), "median_ms_per_step": 1e3 * statistics.median(e2e_t),
+            "step_ms": [round(1e3 * t, 2) for t in e2e_t],
+            "step_calls_ms": {"order": ["correlation call", "skeleton call", "results", "skeleton device ms",
+                                        "levels"], "steps": calls},
+            "phases_ms": {"correlation_from_host": phase[0], "skeleton": phase[1], "adjacency_bits": phase[2],
+                          "records_packed": phase[3], "note": "one extra step, device synchronised after each call"}}
+
+
+def c4_e2e_pipelined(args, ctxs, host, words, rec_cap, steps, ps):
+    """Two contexts of the same shapes, each on its own stream, taking steps in turn:
+    step k+1's hpc_correlation_f32 (pinned host observations; the call returns once the
+    copy, standardisation and Gram are queued) is issued before step k's hpc_run_skeleton,
+    so that the copy runs while step k's levels do. Every step still copies all of its
+    observations to the device and reads its adjacency bitmasks and records back; the
+    value is steps over the wall time of the whole loop."""
+    import torch
+    bits_h = [torch.empty(words, dtype=torch.int32, pin_memory=True) for _ in ctxs]
+    recs_h = [torch.empty(rec_cap, dtype=torch.int32, pin_memory=True) for _ in ctxs]
+    for _ in range(max(2, args.warmup)):  # both contexts warm (staging, graphs, queues)
+        for c in ctxs:
+            c.add_observations_ptr(host.data_ptr(), np.float32)
+            c.run()
+    torch.cuda.synchronize()
+    gc.collect()
+    gc.disable()
+    ends = []
+    rec_words = 0
+    t_start = time.perf_counter()
+    ctxs[0].add_observations_ptr(host.data_ptr(), np.float32)
+    for k in range(steps):
+        cur, nxt = k % 2, (k + 1) % 2
+        if k + 1 < steps:
+            ctxs[nxt].add_observations_ptr(host.data_ptr(), np.float32)
+        ctxs[cur].run()
+        ctxs[cur].adjacency_bits_into(bits_h[cur].data_ptr(), words)
+        w = ctxs[cur].records_packed_into(recs_h[cur].data_ptr(), rec_cap)
+        rec_words = int(w[-1])
+        ends.append(time.perf_counter())
+    torch.cuda.synchronize()
+    t_end = time.perf_counter()
+    gc.enable()
+    total = t_end - t_start
+    step_ms = [1e3 * (b - a) for a, b in zip([t_start] + ends[:-1], ends)]
+    # the host copies of the last step of each context against the committed oracle results
+    gold = c4_golden()
+    parity = None
+    if gold and ctxs[0].count == len(gold["instances"]):
+        off = ctxs[0].adjacency_words()
+        same = []
+        for i in range(len(ctxs)):
+            bits = bits_h[i].numpy().view(np.uint32)
+            same.append(sum(int(c4_adj_sha(bits_to_matrix(bits[off[b]:off[b + 1]], int(ps[b]))) == g["adj_sha256"])
+                            for b, g in enumerate(gold["instances"])))
+        parity = {"instances_equal_to_oracle": same, "instances": ctxs[0].count,
+                  "note": "last step of each context, from the pinned host copies"}
+    return {"value": ctxs[0].count * steps / total, "unit": "skeletons/s",
+            "h2d_bytes_per_step": int(host.numel()) * 4, "d2h_bytes_per_step": words * 4 + rec_words * 4,
+            "path": "two contexts in turn, one host thread: hpc_correlation_f32 of step k+1 (host observations, "
+                    "pinned) queued before hpc_run_skeleton of step k, then hpc_batch_get_adjacency_bits + "
+                    "hpc_batch_get_records_packed (pinned) of step k; host wall clock of the whole loop",
+            "ms_per_step": 1e3 * total / steps, "median_ms_per_step": statistics.median(step_ms),
+            "step_ms": [round(t, 2) for t in step_ms], "steps": steps, "parity": parity}
 
 
 def c4_adj_sha(adj):

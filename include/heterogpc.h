@@ -93,6 +93,8 @@ typedef struct hpc_timings {
   int64_t launches;                      /* kernels launched by this context so far */
   double skeleton_ms;                    /* last hpc_run_skeleton as a whole */
   double retest_ms[HPC_MAX_LEVEL + 1];   /* FP64 re-test kernel of the level (tensor-core mode) */
+  double rebuild_ms[HPC_MAX_LEVEL + 1];  /* level kernel, neighbour-list rebuild phase (device timer) */
+  double scan_ms[HPC_MAX_LEVEL + 1];     /* level kernel, test-count scan phase (device timer) */
 } hpc_timings;
 
 typedef struct hpc_ctx hpc_ctx;
@@ -226,9 +228,9 @@ hpc_status hpc_tune_load(const char *path);
 /* Forces one policy on every level of the context's runs (NULL = the table again). */
 hpc_status hpc_ctx_set_tune(hpc_ctx *ctx, const hpc_tune_params *force);
 /* Autotuner: runs the context's skeleton (on its current correlation, kernel by
- * kernel) once per candidate policy and repetition, times every level's CI-test
- * kernel with CUDA events, and stores for each level the fastest candidate under the
- * level's key. cands/ncands: the candidates (NULL = the built-in grid: tile_cap
+ * kernel) once per candidate policy in each of `reps` rounds, times every level's
+ * CI-test kernel with CUDA events, and stores for each level the candidate with the
+ * smallest median time under the level's key. cands/ncands: the candidates (NULL = the built-in grid: tile_cap
  * 16, 64, 256, 1024 x tiles_per_lane 2, 4, 8 x level-1 kernel interleaved,
  * interleaved with prefetch, chunked). chosen (optional,
  * HPC_MAX_LEVEL + 1 entries) receives each level's choice (zeros for levels not run);

@@ -505,6 +505,10 @@ __device__ __forceinline__ bool claim_edge(const Inst &I, int64_t i, int64_t j) 
   const uint32_t old = atomicAnd(I.adj + lo * I.W + (hi >> 5), ~bit);
   if (!(old & bit)) return false;  // another test removed it first
   atomicAnd(I.adj + hi * I.W + (lo >> 5), ~(1u << (lo & 31)));
+  if (I.dirty) {  // both rows' neighbour lists are stale from here on
+    I.dirty[lo] = 1;
+    I.dirty[hi] = 1;
+  }
   return true;
 }
 
@@ -1334,10 +1338,14 @@ __global__ void __launch_bounds__(kThreads, V == kSetOrder ? kSetBlocks<LT> : (L
     level_kernel(const __grid_constant__ Launch L) {
   extern __shared__ unsigned long long rw_smem[];  // kRowCache entries
   unsigned int epoch = 0;
+  const bool stamp = blockIdx.x == 0 && threadIdx.x == 0;  // the phase times
+  if (stamp) L.lc->t_entry = globaltimer_ns();
   rebuild_phase(L);
   if (!grid_barrier(L, epoch)) return;
+  if (stamp) L.lc->t_rebuilt = globaltimer_ns();
   scan_phase(L, V == kSetOrder);
   if (!grid_barrier(L, epoch)) return;
+  if (stamp) L.lc->t_scanned = globaltimer_ns();
   const TuneEntry te = tile_policy(L);
   if constexpr (V == kSetOrder) {
     static_assert(MIXED && LT >= 2 && LT <= kSetTop, "the set order runs levels 2-24 in mixed precision");
@@ -1349,6 +1357,8 @@ __global__ void __launch_bounds__(kThreads, V == kSetOrder ? kSetBlocks<LT> : (L
     __shared__ TestSmem<LT, MIXED> sm;
     tests_generic<LT, MIXED>(L, LT == 1 ? nullptr : rw_smem, te, sm);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(&L.lc->t_end, globaltimer_ns());
 }
 
 }  // namespace

@@ -198,9 +198,14 @@ hpc_status write_inst_table(hpc_ctx *c) {
     I.rec_stride = rec_stride_words(c->rec_ids);
     I.ctr = c->ctr + (size_t)b * kLevels;
     I.g = c->gctr + b;
+    I.dirty = c->row_dirty ? c->row_dirty + h.row_off : nullptr;
+    I.snap_epoch = c->snap_epoch;
   }
   if (c->inst_host.size() == t.size() && std::memcmp(c->inst_host.data(), t.data(), sizeof(Inst) * t.size()) == 0)
     return HPC_OK;  // unchanged: captured graphs stay valid
+  // a new table (new arrays or capacities) invalidates every neighbour-list snapshot
+  ++c->snap_epoch;
+  for (auto &I : t) I.snap_epoch = c->snap_epoch;
   c->inst_host = t;
   HPC_CUDA(cudaMemcpyAsync(c->inst, c->inst_host.data(), sizeof(Inst) * t.size(), cudaMemcpyHostToDevice, c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
@@ -268,6 +273,8 @@ Launch make_launch(hpc_ctx *c, int level) {
 hpc_status pull_counters(hpc_ctx *c) {
   HPC_CUDA(cudaMemcpyAsync(c->ctr_host, c->ctr, sizeof(DevCounters) * (size_t)c->count * kLevels,
                            cudaMemcpyDeviceToHost, c->stream));
+  if (!c->last_run_graph)  // the level kernels' phase times
+    HPC_CUDA(cudaMemcpyAsync(c->lc_host, c->lc, sizeof(LaunchCounters) * kLevels, cudaMemcpyDeviceToHost, c->stream));
   HPC_CUDA(cudaMemcpyAsync(c->gctr_host, c->gctr, sizeof(DevGlobal) * (size_t)c->count, cudaMemcpyDeviceToHost,
                            c->stream));
   HPC_CUDA(cudaStreamSynchronize(c->stream));
@@ -400,6 +407,13 @@ hpc_status collect_level(hpc_ctx *c, int level, hpc_level_stats *out) {
   c->timings.compact_ms[level] = t_snap;
   c->timings.test_ms[level] = t_test;
   c->timings.retest_ms[level] = t_re;
+  {  // phases of the level kernel by %globaltimer (kernel-by-kernel runs)
+    const LaunchCounters &lc = c->lc_host[level];
+    const bool ok = !c->last_run_graph && level >= 1 && lc.t_entry && lc.t_rebuilt >= lc.t_entry &&
+                    lc.t_scanned >= lc.t_rebuilt;
+    c->timings.rebuild_ms[level] = ok ? 1e-6 * (double)(lc.t_rebuilt - lc.t_entry) : 0.0;
+    c->timings.scan_ms[level] = ok ? 1e-6 * (double)(lc.t_scanned - lc.t_rebuilt) : 0.0;
+  }
   for (int b = 0; b < c->count; ++b) {
     const DevCounters &h = c->ctr_host[(size_t)b * kLevels + level];
     c->ih[b].edges = level == 0 ? (int64_t)(h.edges2 / 2) : (int64_t)(h.edges2 / 2) - (int64_t)h.deleted;
@@ -902,7 +916,7 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n, const hpc_opts *o, int64_t *b
   b += n * p * 8;                                                  // standardised data (FP64 or FP32 pairs)
   b += n * p * 4;                                                  // observation staging
   b += p * W * 4 + p * p;                                          // adjacency bits + bytes
-  b += (p + 1) * (4 + 4 + 8);                                      // deg, rowptr, row_work
+  b += (p + 1) * (4 + 4 + 8 + 1);                                  // deg, rowptr, row_work, stale-row marks
   b += (int64_t)(HPC_MAX_LEVEL + 1) * ((p + kSegRows - 1) / kSegRows) * (int64_t)sizeof(SegAgg);  // scan sums
   // neighbour lists and records are sized after level 0; budget an average degree of 64
   const int64_t e = std::min<int64_t>(p * (p - 1) / 2, p * 32);
@@ -962,6 +976,7 @@ hpc_status hpc_ctx_destroy(hpc_ctx *c) {
   dev_free(c->deg);
   dev_free(c->rowptr);
   dev_free(c->row_work);
+  dev_free(c->row_dirty);
   dev_free(c->colidx);
   dev_free(c->recs);
   dev_free(c->rq);
@@ -1067,30 +1082,41 @@ hpc_status hpc_autotune(hpc_ctx *c, const hpc_tune_params *cands, int ncands, in
   const bool graphs = c->graphs_enabled;
   const TuneEntry force0 = c->tune_force;
   c->graphs_enabled = false;  // kernel by kernel: every level's kernels are timed
-  double best_ms[kLevels];
+  // every candidate's level times, the candidates taken in turn within each round (so
+  // that a drift over the tuning run touches them alike); per level the candidate with
+  // the smallest median over the rounds wins, not the one with the luckiest sample
+  std::vector<std::vector<double>> ms_of(grid.size() * kLevels);
   int best[kLevels], max_deg[kLevels];
   for (int l = 0; l < kLevels; ++l) {
-    best_ms[l] = 1e300;
     best[l] = -1;
     max_deg[l] = -1;
   }
   hpc_level_stats st[kLevels];
-  for (size_t q = 0; q < grid.size() && s == HPC_OK; ++q) {
-    c->tune_force = tune_entry_of(grid[q]);
-    ++c->inst_version;
-    for (int r = 0; r < reps && s == HPC_OK; ++r) {
+  for (int r = 0; r < reps && s == HPC_OK; ++r) {
+    for (size_t q = 0; q < grid.size() && s == HPC_OK; ++q) {
+      c->tune_force = tune_entry_of(grid[q]);
+      ++c->inst_version;
       int ran = 0;
       if ((s = hpc_ctx_reset(c)) != HPC_OK) break;
       if ((s = hpc_run_skeleton(c, st, kLevels, &ran)) != HPC_OK) break;
       for (int k = 0; k < ran; ++k) {
         const int l = st[k].level;
         if (l < 1 || st[k].potential_tests == 0) continue;
-        const double ms = c->timings.test_ms[l];
         max_deg[l] = st[k].max_degree;
-        if (ms < best_ms[l]) {
-          best_ms[l] = ms;
-          best[l] = (int)q;
-        }
+        ms_of[q * kLevels + l].push_back(c->timings.test_ms[l]);
+      }
+    }
+  }
+  for (int l = 0; l < kLevels && s == HPC_OK; ++l) {
+    double best_ms = 1e300;
+    for (size_t q = 0; q < grid.size(); ++q) {
+      std::vector<double> v = ms_of[q * kLevels + l];
+      if (v.empty()) continue;
+      std::sort(v.begin(), v.end());
+      const double med = v.size() % 2 ? v[v.size() / 2] : 0.5 * (v[v.size() / 2 - 1] + v[v.size() / 2]);
+      if (med < best_ms) {
+        best_ms = med;
+        best[l] = (int)q;
       }
     }
   }
@@ -1942,6 +1968,7 @@ hpc_status create(hpc_ctx **out, int count, const int64_t *p, const int64_t *n, 
   if ((s = dev_alloc(&c->deg, rows, "degrees")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->rowptr, rows, "row offsets")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->row_work, rows, "row work")) != HPC_OK) return fail(s);
+  if ((s = dev_alloc(&c->row_dirty, rows, "stale-row marks")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->ctr, (int64_t)count * kLevels, "level counters")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->gctr, count, "counters")) != HPC_OK) return fail(s);
   if ((s = dev_alloc(&c->lc, kLevels, "launch counters")) != HPC_OK) return fail(s);

@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(const __grid_constan
       C.deleted = 0;
       C.band_violations = 0;
       C.rec_begin = I.g->rec_count;
+      I.g->snap = 0;  // a new CSR layout: every neighbour list is extracted at level 1
       L.work_prefix[b] = 0;
       if (b == L.count - 1) L.work_prefix[L.count] = 0;
     }

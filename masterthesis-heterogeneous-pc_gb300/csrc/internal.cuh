@@ -54,6 +54,10 @@ struct DevCounters {
 // Instance-wide device counters.
 struct DevGlobal {
   unsigned long long rec_count;    // separation-set records written (cumulative)
+  // the neighbour-list snapshot: Inst::snap_epoch while every row's list in colidx
+  // matches the adjacency except the rows marked in Inst::dirty, else 0 (set by the
+  // scan phase after a rebuild, cleared by level 0 and by every counter reset)
+  unsigned long long snap;
   int err;                         // error bits (kErr*)
   int pad;
 };
@@ -65,6 +69,9 @@ struct LaunchCounters {
   unsigned int bar;                // grid-barrier arrivals of the level kernel
   int max_deg;                     // largest degree at the level start over all instances
   int pad;
+  // %globaltimer (ns) of the level kernel's phases: block 0 at entry, after the rebuild
+  // and after the scan; the last block to finish its tests
+  unsigned long long t_entry, t_rebuilt, t_scanned, t_end;
 };
 
 // Tile policy of a level's CI tests (set by the autotuner, else the defaults):
@@ -161,6 +168,8 @@ struct Inst {
   int *rowptr;            // snapshot CSR offsets (p + 1)
   int *colidx;            // snapshot neighbour ids, ascending per row
   long long colidx_cap;
+  uint8_t *dirty;         // per row: nonzero when the row lost an edge since its list was extracted
+  unsigned long long snap_epoch;  // nonzero; changes whenever the table (pointers, capacities) does
   unsigned long long *row_work;  // exclusive prefix of tests per row (p + 1)
   int32_t *recs;          // packed records (RecHead + rec_ids slots each)
   long long rec_cap;      // records
@@ -458,6 +467,9 @@ struct hpc_ctx {
   hpc::DevGlobal *gctr = nullptr;        // count
   hpc::DevGlobal *gctr_host = nullptr;
   hpc::LaunchCounters *lc = nullptr;     // HPC_MAX_LEVEL + 1
+  hpc::LaunchCounters lc_host[HPC_MAX_LEVEL + 1] = {};  // host mirror (phase times of timed runs)
+  uint8_t *row_dirty = nullptr;          // sum (p + 1): rows whose neighbour list is stale
+  unsigned long long snap_epoch = 0;     // of the instance table last written
   hpc::Inst *inst = nullptr;             // device table (count)
   std::vector<hpc::Inst> inst_host;      // the table last written
   long long *prefixes = nullptr;         // device: word, tile, row, segment prefixes (4 x (count + 1))

@@ -87,6 +87,55 @@ __device__ __forceinline__ unsigned long long row_sets(int d, int level) {
 
 __device__ __forceinline__ bool csr_overflow(const Inst &I) { return (long long)I.rowptr[I.p] > I.colidx_cap; }
 
+// Row i's neighbour list from its adjacency row (whole warp, converged), written
+// ascending at its CSR slot; returns the degree (warp-uniform).
+__device__ __forceinline__ int extract_row(const Inst &I, int64_t i) {
+  const int lane = threadIdx.x & 31;
+  // the row's first 128 words and its slot offset in one round trip
+  const uint32_t *words = I.adj + i * I.W;
+  const int W = I.W;
+  uint32_t pre[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) pre[q] = q * 32 + lane < W ? words[q * 32 + lane] : 0u;
+  int *out = I.colidx + I.rowptr[i];
+  int cnt = 0;
+  auto emit = [&](uint32_t word, int w) {
+    const int c = __popc(word);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int pos = cnt + incl - c;
+    while (word) {
+      const int bit = __ffs(word) - 1;
+      out[pos++] = w * 32 + bit;
+      word &= word - 1;
+    }
+    cnt += __shfl_sync(0xffffffffu, incl, 31);
+  };
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (q * 32 < W) emit(pre[q], q * 32 + lane);
+  for (int w0 = 128; w0 < W; w0 += 32) emit(w0 + lane < W ? words[w0 + lane] : 0u, w0 + lane);
+  return cnt;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// The level's neighbour-list snapshot and its per-segment sums (degrees, tests,
+// conditioning sets, rows with tests). A warp takes a contiguous range of rows, 32 at a
+// time (a lane each, within one instance and segment). A row's list is extracted again
+// (whole warp) only when it may have changed: every row of an instance whose snapshot is
+// not current (after level 0, a reset or a new instance table), else the rows that lost
+// an edge since their last extraction (marked by claim_edge); the other rows keep their
+// lists and degrees. Rows of an instance whose lists overflow their capacity are left
+// alone (the scan phase flags it; the host resizes and reruns).
 __device__ __forceinline__ void rebuild_phase(const Launch &L) {
   const int lane = threadIdx.x & 31;
   const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -115,8 +164,8 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
   int b = -1;
   const Inst *I = nullptr;
   long long r0 = 0, r1 = 0, g0 = 0;
-  bool skip = false;
-  for (; t < tend; ++t) {
+  bool skip = false, current = false;
+  while (t < tend) {
     if (b < 0 || t >= r1) {
       b = L.count == 1 ? 0 : find_inst(L.row_prefix, L.count, t);
       I = inst_of(L, b);
@@ -124,50 +173,40 @@ __device__ __forceinline__ void rebuild_phase(const Launch &L) {
       r1 = row_end(L, b);
       g0 = seg_begin(L, b);
       skip = csr_overflow(*I);  // flagged by the scan phase; the host resizes and reruns
+      current = !skip && I->dirty && __ldcg(&I->g->snap) == I->snap_epoch;
     }
-    const int64_t i = t - r0;
-    const long long g = g0 + i / kSegRows;
+    const int64_t i0 = t - r0;
+    const long long g = g0 + i0 / kSegRows;
     if (g != cur) {
       flush();
       cur = g;
     }
-    // the row's first 128 words, its slot offset and the overflow flag in one round trip
-    const uint32_t *words = I->adj + i * I->W;
-    const int W = I->W;
-    uint32_t pre[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) pre[q] = q * 32 + lane < W ? words[q * 32 + lane] : 0u;
-    const int slot = I->rowptr[i];
-    if (skip) continue;
-    int *out = I->colidx + slot;
-    int cnt = 0;
-    auto emit = [&](uint32_t word, int w) {
-      const int c = __popc(word);
-      int incl = c;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-      }
-      int pos = cnt + incl - c;
-      while (word) {
-        const int bit = __ffs(word) - 1;
-        out[pos++] = w * 32 + bit;
-        word &= word - 1;
-      }
-      cnt += __shfl_sync(0xffffffffu, incl, 31);
-    };
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (q * 32 < W) emit(pre[q], q * 32 + lane);
-    for (int w0 = 128; w0 < W; w0 += 32) emit(w0 + lane < W ? words[w0 + lane] : 0u, w0 + lane);
-    if (lane == 0) I->deg[i] = cnt;
-    a_deg += (unsigned long long)cnt;
-    a_max = max(a_max, cnt);
-    const unsigned long long w = row_tests(cnt, level, L.row_work_limit, &a_over);
-    a_work += w;
-    a_sets += w ? row_sets(cnt, level) : 0ull;
-    a_rows += w ? 1 : 0;
+    const long long seg_end_row = r0 + (i0 / kSegRows + 1) * kSegRows;
+    const int n = (int)min(32ll, min(tend, min(r1, seg_end_row)) - t);
+    const int64_t i = i0 + lane;
+    const bool mine = lane < n && !skip;
+    const bool stale = mine && (!current || I->dirty[i] != 0);
+    int cnt = mine && !stale ? I->deg[i] : 0;
+    unsigned todo = __ballot_sync(0xffffffffu, stale);
+    while (todo) {
+      const int q = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int c = extract_row(*I, i0 + q);
+      if (lane == q) cnt = c;
+    }
+    if (stale) {
+      I->deg[i] = cnt;
+      if (I->dirty) I->dirty[i] = 0;
+    }
+    int over = 0;
+    const unsigned long long w = mine ? row_tests(cnt, level, L.row_work_limit, &over) : 0ull;
+    a_deg += warp_sum_u64(mine ? (unsigned long long)cnt : 0ull);
+    a_work += warp_sum_u64(w);
+    a_sets += warp_sum_u64(w ? row_sets(cnt, level) : 0ull);
+    a_max = max(a_max, __reduce_max_sync(0xffffffffu, mine ? cnt : 0));
+    a_rows += (int)__reduce_add_sync(0xffffffffu, w ? 1u : 0u);
+    a_over |= (int)__reduce_or_sync(0xffffffffu, (unsigned)over);
+    t += n;
   }
   // the warps' last segment sums are merged per block first (the warps of a block
   // take neighbouring rows): one set of global atomics per block and segment
@@ -332,6 +371,8 @@ __device__ __forceinline__ void scan_phase(const Launch &L, bool set) {
       // last segment of the instance: its level summary
       DevCounters &C = I.ctr[level];
       if (!bad) I.row_work[I.p] = s_sum.units;
+      // the lists just rebuilt are the instance's snapshot (unless they overflowed)
+      I.g->snap = bad || s_sum.over ? 0ull : I.snap_epoch;
       if (s_sum.over) atomicOr(&I.g->err, kErrWorkOverflow);
       if (csr_overflow(I)) atomicOr(&I.g->err, kErrCsrOverflow);
       C.edges2 = s_sum.deg;

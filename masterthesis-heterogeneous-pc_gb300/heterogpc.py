@@ -51,12 +51,14 @@ class Timings(C.Structure):
     _fields_ = [("standardise_ms", C.c_double), ("gram_ms", C.c_double), ("convert_ms", C.c_double),
                 ("level_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("compact_ms", C.c_double * (HPC_MAX_LEVEL + 1)),
                 ("test_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("launches", C.c_int64),
-                ("skeleton_ms", C.c_double), ("retest_ms", C.c_double * (HPC_MAX_LEVEL + 1))]
+                ("skeleton_ms", C.c_double), ("retest_ms", C.c_double * (HPC_MAX_LEVEL + 1)),
+                ("rebuild_ms", C.c_double * (HPC_MAX_LEVEL + 1)), ("scan_ms", C.c_double * (HPC_MAX_LEVEL + 1))]
 
     def as_dict(self):
         return {"standardise_ms": self.standardise_ms, "gram_ms": self.gram_ms, "convert_ms": self.convert_ms,
                 "level_ms": list(self.level_ms), "compact_ms": list(self.compact_ms), "test_ms": list(self.test_ms),
-                "launches": self.launches, "skeleton_ms": self.skeleton_ms, "retest_ms": list(self.retest_ms)}
+                "launches": self.launches, "skeleton_ms": self.skeleton_ms, "retest_ms": list(self.retest_ms),
+                "rebuild_ms": list(self.rebuild_ms), "scan_ms": list(self.scan_ms)}
 
 
 class ServerOpts(C.Structure):

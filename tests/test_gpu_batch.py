@@ -88,3 +88,45 @@ def test_whole_batch_result_copies():
                                                                           in one]
         assert [pm for *_, pm in packed[b]] == [pm for *_, pm in one]
         assert [lev for _, _, lev, _, _ in packed[b]] == sorted(lev for _, _, lev, _, _ in packed[b])
+
+
+def test_batch_new_data_on_the_same_context_matches_oracle():
+    """The neighbour lists a context keeps between levels (rows are extracted again only
+    where an edge was removed) belong to one skeleton: new observations of the same
+    shapes, and then the first ones again, must each give the oracle's skeletons, run
+    whole and level by level."""
+    ps, ns, alphas, Xs = make_batch(12, seed=5)
+    rng = np.random.default_rng(55)
+    degs = rng.uniform(1, 5, len(ps))
+    Ys = [hg.sem_generate(int(p), int(n), hg.GRAPH_ER, float(d), 2, 0.1, 1.0, 9000 + b, dtype=np.float32)
+          for b, (p, n, d) in enumerate(zip(ps, ns, degs))]
+    bt = hg.SkeletonBatch(ps, ns, alphas, max_level=8, precision=hg.PREC_MIXED_TC)
+    for data in (Xs, Ys, Xs):
+        bt.add_observations(bt.pack(data))
+        wants = [orc.run(orc.correlation(data[b].astype(np.float64)), int(ns[b]), float(alphas[b]), 8)
+                 for b in range(bt.count)]
+        bt.run()
+        for b in range(bt.count):
+            assert np.array_equal(bt.adjacency(b), wants[b].adj), b
+        bt.reset()
+        for level in range(9):
+            bt.calc_level(level)
+        for b in range(bt.count):
+            assert np.array_equal(bt.adjacency(b), wants[b].adj), ("level by level", b)
+
+
+def test_batch_level_phase_times():
+    """Kernel-by-kernel runs report the level kernels' rebuild and scan phases (device
+    timer), within the kernel's own time."""
+    ps, ns, alphas, Xs = make_batch(16, seed=7)
+    bt = hg.SkeletonBatch(ps, ns, alphas, max_level=4, precision=hg.PREC_MIXED_TC)
+    bt.add_observations(bt.pack(Xs))
+    bt.set_graphs(False)
+    st = bt.run()
+    t = bt.timings()
+    ran = [s["level"] for s in st if s["level"] >= 1]
+    assert ran
+    for level in ran:
+        assert t["rebuild_ms"][level] > 0.0, level
+        assert t["scan_ms"][level] >= 0.0, level
+        assert t["rebuild_ms"][level] + t["scan_ms"][level] <= t["test_ms"][level] + 5e-3, level
