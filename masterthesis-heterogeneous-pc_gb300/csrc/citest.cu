@@ -194,29 +194,35 @@ __device__ __forceinline__ void retest_columns_pass(const Inst &I, const float *
           sh[x] = t;
         }
     };
-    // two samples at a time, both loaded before the arithmetic (no bounds test between)
+    // S samples at a time, all loaded before the arithmetic (no bounds test between):
+    // the loop is bound by its round trips to memory, so a round trip carries as many
+    // samples as the registers allow
+    constexpr int S = K <= 4 ? 8 : K == 5 ? 4 : 2;
 #pragma unroll 1
-    for (int u = 0; u < 16; u += 2) {
+    for (int u = 0; u < 16; u += S) {
       const int64_t k = k0 + 32 * u;
-      if (k + 32 < n) {
-        float ah[2][K], al[2][K];
+      if (k + 32 * (S - 1) < n) {
+        float ah[S][K], al[S][K];
 #pragma unroll
-        for (int v = 0; v < 2; ++v)
+        for (int v = 0; v < S; ++v)
 #pragma unroll
           for (int r = 0; r < K; ++r) {
             ah[v][r] = ch[r][k + 32 * v];
             al[v][r] = ch[r][k + 32 * v + lo_off];
           }
-        add(ah[0], al[0]);
-        add(ah[1], al[1]);
-      } else if (k < n) {
-        float ah[K], al[K];
 #pragma unroll
-        for (int r = 0; r < K; ++r) {
-          ah[r] = ch[r][k];
-          al[r] = ch[r][k + lo_off];
+        for (int v = 0; v < S; ++v) add(ah[v], al[v]);
+      } else {
+#pragma unroll 1
+        for (int v = 0; v < S && k + 32 * v < n; ++v) {  // the ragged end, a sample at a time
+          float ah[K], al[K];
+#pragma unroll
+          for (int r = 0; r < K; ++r) {
+            ah[r] = ch[r][k + 32 * v];
+            al[r] = ch[r][k + 32 * v + lo_off];
+          }
+          add(ah, al);
         }
-        add(ah, al);
       }
     }
 #pragma unroll

@@ -499,13 +499,17 @@ struct PendRem {
   int32_t ids[LA > 0 ? LA : 1];
 };
 
+// MARK: the removal marks both rows' neighbour lists stale (every removal outside level
+// 1, whose launch leaves the snapshot invalid instead: its 4 M removals on C4 made the
+// marks cost a third of the level-1 kernel)
+template <bool MARK = true>
 __device__ __forceinline__ bool claim_edge(const Inst &I, int64_t i, int64_t j) {
   const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
   const uint32_t bit = 1u << (hi & 31);
   const uint32_t old = atomicAnd(I.adj + lo * I.W + (hi >> 5), ~bit);
   if (!(old & bit)) return false;  // another test removed it first
   atomicAnd(I.adj + hi * I.W + (lo >> 5), ~(1u << (lo & 31)));
-  if (I.dirty) {  // both rows' neighbour lists are stale from here on
+  if (MARK && I.dirty) {  // both rows' neighbour lists are stale from here on
     I.dirty[lo] = 1;
     I.dirty[hi] = 1;
   }
@@ -773,7 +777,7 @@ __device__ __forceinline__ void tests_generic(const Launch &L, unsigned long lon
             if (!(MIXED && !I->cor64 && push_retest(L, b, i, j, ids, l))) rm = exact_remove_fast<LA>(*I, i, j, ids, l, &pv);
           }
           if (rm) {
-            if (claim_edge(*I, i, j)) {
+            if (claim_edge<LT != 1>(*I, i, j)) {
               push_pending<LA>(pend, np, *I, b, level, i, j, ids, l, pv);
               skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
             }
@@ -974,7 +978,7 @@ __device__ __forceinline__ void tests_l1(const Launch &L, unsigned long long *rw
             const unsigned grp = __match_any_sync(act, (unsigned)(t - (unsigned long long)rank));
             const unsigned rmask = rall & grp;
             if (rmask) {
-              if (lane == __ffs(rmask) - 1 && claim_edge(*I, i, j)) {
+              if (lane == __ffs(rmask) - 1 && claim_edge<false>(*I, i, j)) {
                 push_pending<1>(pend, np, *I, b, level, i, j, &k, 1, pv_rm);
                 skip_tiles_of_edge(L, t - rank + c, t0 + per_tile, per_tile, nwarps);
               }

@@ -371,8 +371,9 @@ __device__ __forceinline__ void scan_phase(const Launch &L, bool set) {
       // last segment of the instance: its level summary
       DevCounters &C = I.ctr[level];
       if (!bad) I.row_work[I.p] = s_sum.units;
-      // the lists just rebuilt are the instance's snapshot (unless they overflowed)
-      I.g->snap = bad || s_sum.over ? 0ull : I.snap_epoch;
+      // the lists just rebuilt are the instance's snapshot (unless they overflowed, or the
+      // level is 1, whose removals do not mark their rows)
+      I.g->snap = bad || s_sum.over || level == 1 ? 0ull : I.snap_epoch;
       if (s_sum.over) atomicOr(&I.g->err, kErrWorkOverflow);
       if (csr_overflow(I)) atomicOr(&I.g->err, kErrCsrOverflow);
       C.edges2 = s_sum.deg;
