@@ -1104,6 +1104,23 @@ __device__ __forceinline__ void factor_set(const float *__restrict__ C, IdxT str
   }
 }
 
+// The tail of test_f32_inc on a test's sums: sx = |w_i|^2, sy = |w_j|^2, sxy = w_i.w_j
+// and dmin = the smallest pivot of S. 0: keep, 1: remove (FP32-decided, |r| in *rr_out),
+// 2: inside the re-test band.
+__device__ __forceinline__ int set_decide(const Inst &I, int l, float sx, float dmin, float rij, float sy, float sxy,
+                                          float *rr_out) {
+  const float ax = 1.0f - sx, ay = 1.0f - sy;
+  const float cond = fminf(dmin, fminf(ax, ay));
+  if (!(cond > 1e-3f)) return 2;
+  const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
+  *rr_out = rr;
+  const float dist = rr - I.r_c;
+  const float ke = I.ke_a + (float)(l + 2) * I.ke_b;
+  const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
+  if (!(fabsf(dist) > band)) return 2;
+  return dist < 0.0f ? 1 : 0;
+}
+
 // FP32 test of (i, j | S) on the unit's factor: w_j by forward solve, then the tail of
 // test_f32_inc (sx = |w_i|^2 and dmin = the smallest pivot, both in row order, come
 // with the factor). Same return values.
@@ -1128,17 +1145,52 @@ __device__ __forceinline__ int test_set_j(const Inst &I, const float *__restrict
       sy += wy[r] * wy[r];
       sxy += F.wx[r] * wy[r];
     }
-  const float ax = 1.0f - sx, ay = 1.0f - sy;
-  const float cond = fminf(dmin, fminf(ax, ay));
-  if (!(cond > 1e-3f)) return 2;
-  const float rr = fabsf(rij - sxy) * rsqrtf(ax * ay);
-  *rr_out = rr;
-  const float dist = rr - I.r_c;
-  const float ke = I.ke_a + (float)(l + 2) * I.ke_b;
-  const float band = I.margin_r + 8.0f * __fdividef(ke, cond);
-  if (!(fabsf(dist) > band)) return 2;
-  return dist < 0.0f ? 1 : 0;
+  return set_decide(I, l, sx, dmin, rij, sy, sxy, rr_out);
 }
+
+// Two tests (i, j1 | S) and (i, j2 | S) of one unit side by side: each in exactly the
+// operations of test_set_j, the two dependency chains of the forward solves interleaved
+// (the single solve leaves the issue slots waiting on its own results).
+template <int LA, typename IdxT>
+__device__ __forceinline__ void test_set_j2(const Inst &I, const float *__restrict__ C, IdxT stride, IdxT xi,
+                                            IdxT xj1, IdxT xj2, const int *xs, int l, const Fact<LA> &F, float sx,
+                                            float dmin, int *res1, int *res2, float *rr1, float *rr2) {
+  float g1[LA], g2[LA], w1[LA], w2[LA];
+#pragma unroll (kUnr<LA>)
+  for (int r = 0; r < LA; ++r)
+    if (r < l) {
+      g1[r] = C[xj1 * stride + xs[r]];
+      g2[r] = C[xj2 * stride + xs[r]];
+    }
+  const float rij1 = C[xi * stride + xj1], rij2 = C[xi * stride + xj2];
+  float sy1 = 0.f, sxy1 = 0.f, sy2 = 0.f, sxy2 = 0.f;
+#pragma unroll (kUnr<LA>)
+  for (int r = 0; r < LA; ++r)
+    if (r < l) {
+      float v1 = g1[r], v2 = g2[r];
+#pragma unroll (kUnr<LA>)
+      for (int c = 0; c < LA; ++c)
+        if (c < r) {
+          const float lrc = F.Lm[r * (r + 1) / 2 + c];
+          v1 -= lrc * w1[c];
+          v2 -= lrc * w2[c];
+        }
+      w1[r] = v1 * F.invd[r];
+      w2[r] = v2 * F.invd[r];
+      sy1 += w1[r] * w1[r];
+      sxy1 += F.wx[r] * w1[r];
+      sy2 += w2[r] * w2[r];
+      sxy2 += F.wx[r] * w2[r];
+    }
+  *res1 = set_decide(I, l, sx, dmin, rij1, sy1, sxy1, rr1);
+  *res2 = set_decide(I, l, sx, dmin, rij2, sy2, sxy2, rr2);
+}
+
+// Levels whose set-order tests run in pairs: 3-5 (measured on C4 against the single
+// loop, level by level: 10 % faster at level 3, 3 % at 5, even at 4; 7-9 % slower at 6-7
+// and 3-7 % at 12-14, where the second solve's registers crowd the schedule; 9-11 spill).
+template <int LA>
+constexpr bool kSetPairs = LA <= 5;
 
 // live bits of row i's snapshot neighbours (bit q: the q-th; d <= kSetMaskD), read by
 // one lane
@@ -1244,10 +1296,9 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
           sx += F.wx[r] * F.wx[r];
         }
         // the unit's tests: neighbours q outside S, live as far as the lane knows
-        auto test_q = [&](int q) {
-          const IdxT xj = ST ? (IdxT)(q + 1) : (IdxT)I->colidx[base + q];
-          float rr = 0.f;
-          const int res = test_set_j<LA, IdxT>(*I, C, stride, xi, xj, xs, l, F, sx, dmin, &rr);
+        // a test's outcome: a removal claims the edge (and the lane forgets j for its
+        // later units), an undecided test goes to the re-test queue
+        auto finish_q = [&](int q, IdxT xj, int res, float rr) {
           ++executed;
           if (res == 0) return;
           // removal or re-test: the variable ids of j and S
@@ -1273,15 +1324,42 @@ __device__ __forceinline__ void tests_set(const Launch &L, unsigned long long *r
             if (q < kSetMaskD) live &= ~(1ull << q);
           }
         };
+        auto xj_of = [&](int q) -> IdxT { return ST ? (IdxT)(q + 1) : (IdxT)I->colidx[base + q]; };
+        auto test_q = [&](int q) {
+          const IdxT xj = xj_of(q);
+          float rr = 0.f;
+          const int res = test_set_j<LA, IdxT>(*I, C, stride, xi, xj, xs, l, F, sx, dmin, &rr);
+          finish_q(q, xj, res, rr);
+        };
         if (ST || d <= kSetMaskD) {
           uint64_t in_s = 0;
 #pragma unroll (kUnr<LA>)
           for (int r = 0; r < LA; ++r) in_s |= 1ull << pos[r];
           uint64_t todo = live & ~in_s;
-          while (todo) {
-            const int q = __ffsll((long long)todo) - 1;
-            todo &= todo - 1;
-            test_q(q);
+          if constexpr (kSetPairs<LA>) {
+            // in pairs, the outcomes taken in the order of the single loop
+            while (todo) {
+              const int q1 = __ffsll((long long)todo) - 1;
+              todo &= todo - 1;
+              if (!todo) {
+                test_q(q1);
+                break;
+              }
+              const int q2 = __ffsll((long long)todo) - 1;
+              todo &= todo - 1;
+              const IdxT x1 = xj_of(q1), x2 = xj_of(q2);
+              int res1, res2;
+              float rr1 = 0.f, rr2 = 0.f;
+              test_set_j2<LA, IdxT>(*I, C, stride, xi, x1, x2, xs, l, F, sx, dmin, &res1, &res2, &rr1, &rr2);
+              finish_q(q1, x1, res1, rr1);
+              finish_q(q2, x2, res2, rr2);
+            }
+          } else {
+            while (todo) {
+              const int q = __ffsll((long long)todo) - 1;
+              todo &= todo - 1;
+              test_q(q);
+            }
           }
         } else {
           for (int q = 0; q < d; ++q) {
