@@ -11,11 +11,17 @@ namespace {
 // p-values of the removals decided in FP32 (negative pmax), for every instance's
 // records: FP64 re-evaluation where the instance has an FP64 matrix -- a result below
 // alpha flags kErrBandViolation (the FP32 error bound did not hold) -- else the formula
-// in FP32 on the stored FP32 |r|. Run at the end of every skeleton run.
+// in FP32 on the stored FP32 |r|. Run at the end of every skeleton run. The instances
+// run side by side, a group of gridDim / count blocks (at least one) each: taking them
+// one after another over the whole grid cost a chain of dependent loads per instance
+// (0.8 ms for the 512 instances of C4).
 __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count) {
-  const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-  const unsigned long long nthreads = (unsigned long long)gridDim.x * blockDim.x;
-  for (int b = 0; b < count; ++b) {
+  if (count <= 0) return;
+  const unsigned per = max(1u, gridDim.x / (unsigned)count);  // blocks per instance
+  const unsigned groups = gridDim.x / per;
+  const unsigned long long tid = (blockIdx.x % per) * (unsigned long long)blockDim.x + threadIdx.x;
+  const unsigned long long nthreads = (unsigned long long)per * blockDim.x;
+  for (int b = (int)(blockIdx.x / per); b < count; b += (int)groups) {
     const Inst &I = inst[b];
     unsigned long long end = I.g->rec_count;
     if (end > (unsigned long long)I.rec_cap) end = (unsigned long long)I.rec_cap;
@@ -474,7 +480,7 @@ hpc_status launch_retest(const Launch &L, int sms, cudaStream_t s) {
 }
 
 hpc_status launch_finalize_records(const Inst *inst, int count, cudaStream_t s) {
-  finalize_records_kernel<<<152 * 2, 128, 0, s>>>(inst, count);
+  finalize_records_kernel<<<152 * 4, 128, 0, s>>>(inst, count);
   HPC_LAUNCH_CHECK("finalize_records_kernel");
   return HPC_OK;
 }

@@ -63,19 +63,35 @@ __device__ __forceinline__ bool level0_keep(const Launch &L, const Inst &I, int 
 // loads issued together) -- and each row's ballot is its word; warp 0 then transposes
 // the tile with 32 more ballots and writes both triangles (the diagonal tile as the
 // union of the two).
+// A block takes a contiguous run of tiles: the instance is searched once per run (and
+// where the run crosses into the next instance), and the tile coordinates step along
+// the row-major order instead of being recomputed by a square root per tile.
 constexpr int kL0Threads = 128;
 __global__ void __launch_bounds__(kL0Threads) level0_kernel(const __grid_constant__ Launch L, long long total) {
   __shared__ uint32_t s_word[32];
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int b = L.count == 1 ? 0 : find_inst(L.tile_prefix, L.count, t);
+  const long long per = (total + gridDim.x - 1) / gridDim.x;
+  const long long t0 = blockIdx.x * per, t1 = min(t0 + per, total);
+  int b = -1;
+  long long tb1 = 0;     // first tile of the next instance
+  int64_t TI = 0, w = 0;  // (TI, w), w <= TI: the tile, row-major over the lower triangle of tiles
+  for (long long t = t0; t < t1; ++t) {
+    if (b < 0 || t >= tb1) {
+      b = L.count == 1 ? 0 : find_inst(L.tile_prefix, L.count, t);
+      const long long tb0 = L.count == 1 ? 0 : L.tile_prefix[b];
+      tb1 = L.count == 1 ? total : L.tile_prefix[b + 1];
+      const long long lt = t - tb0;
+      // an FP32 estimate of the triangular root, corrected in integers
+      TI = (int64_t)((sqrtf(8.0f * (float)lt + 1.0f) - 1.0f) * 0.5f);
+      if (TI < 0) TI = 0;
+      while (TI > 0 && TI * (TI + 1) / 2 > lt) --TI;
+      while ((TI + 1) * (TI + 2) / 2 <= lt) ++TI;
+      w = lt - TI * (TI + 1) / 2;
+    } else if (++w > TI) {
+      ++TI;
+      w = 0;
+    }
     const Inst &I = *inst_of(L, b);
-    const long long lt = t - (L.count == 1 ? 0 : L.tile_prefix[b]);
-    // lt -> (TI, w), w <= TI, row-major over the lower triangle of tiles
-    int64_t TI = (int64_t)((sqrt(8.0 * (double)lt + 1.0) - 1.0) * 0.5);
-    while (TI * (TI + 1) / 2 > lt) --TI;
-    while ((TI + 1) * (TI + 2) / 2 <= lt) ++TI;
-    const int64_t w = lt - TI * (TI + 1) / 2;
     const int64_t j = w * 32 + lane;
     double v64[8];
     float v32[8];
