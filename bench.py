@@ -531,17 +531,21 @@ def run_c4(args, wl):
     words = int(bt.adjacency_words()[-1])
     rec_words = int(bt.packed_words()[-1])
     rec_cap = rec_words + 65536
-    e2e_steps = max(args.steps, 10)  # host wall clock: more steps than the device-timed loop
+    e2e_steps = max(args.steps, 20)  # host wall clock: more steps than the device-timed loop
     e2e_serial = c4_e2e_serial(args, bt, host, words, rec_cap, e2e_steps)
-    # pipelined: a second context of the same shapes on its own stream, the two taking
-    # steps in turn, so that step k+1's observations are copied (and correlated) while
-    # step k's skeleton runs
-    stream2 = torch.cuda.Stream(device=dev)
-    bt2 = hg.SkeletonBatch(ps, ns, alphas, max_level=wl["max_level"], precision=hg.PREC_MIXED_TC)
-    bt2.set_stream(stream2.cuda_stream)
-    e2e = c4_e2e_pipelined(args, [bt, bt2], host, words, rec_cap, e2e_steps, ps)
+    # pipelined: two more contexts of the same shapes, each on its own stream, the three
+    # taking steps in turn, so that a step's observations are copied (and correlated)
+    # while the two steps before it run their skeletons
+    extra = []
+    for _ in range(2):
+        st_x = torch.cuda.Stream(device=dev)
+        bt_x = hg.SkeletonBatch(ps, ns, alphas, max_level=wl["max_level"], precision=hg.PREC_MIXED_TC)
+        bt_x.set_stream(st_x.cuda_stream)
+        extra.append((st_x, bt_x))
+    e2e = c4_e2e_pipelined(args, [bt] + [b_ for _, b_ in extra], host, words, rec_cap, e2e_steps, ps)
     e2e["serial"] = e2e_serial
-    bt2.close()
+    for _, b_ in extra:
+        b_.close()
     torch.cuda.set_stream(stream)
 
     # the plain single-instance FP64 path on the same instances, like for like
@@ -657,16 +661,18 @@ def c4_e2e_serial(args, bt, host, words, rec_cap, steps):
 
 
 def c4_e2e_pipelined(args, ctxs, host, words, rec_cap, steps, ps):
-    """Two contexts of the same shapes, each on its own stream, taking steps in turn:
-    step k+1's hpc_correlation_f32 (pinned host observations; the call returns once the
-    copy, standardisation and Gram are queued) is issued before step k's hpc_run_skeleton,
-    so that the copy runs while step k's levels do. Every step still copies all of its
-    observations to the device and reads its adjacency bitmasks and records back; the
-    value is steps over the wall time of the whole loop."""
+    """D = len(ctxs) contexts of the same shapes, each on its own stream, taking steps in
+    turn from one host thread: step k + D - 1's hpc_correlation_f32 (pinned host
+    observations; the call returns once the copy, standardisation and Gram are queued) is
+    issued before step k's hpc_run_skeleton, on the context whose step k - 1 results were
+    just read, so that every copy has D - 1 skeleton steps to finish in. Every step still
+    copies all of its observations to the device and reads its adjacency bitmasks and
+    records back; the value is steps over the wall time of the whole loop."""
     import torch
+    D = len(ctxs)
     bits_h = [torch.empty(words, dtype=torch.int32, pin_memory=True) for _ in ctxs]
     recs_h = [torch.empty(rec_cap, dtype=torch.int32, pin_memory=True) for _ in ctxs]
-    for _ in range(max(2, args.warmup)):  # both contexts warm (staging, graphs, queues)
+    for _ in range(max(2, args.warmup)):  # every context warm (staging, graphs, queues)
         for c in ctxs:
             c.add_observations_ptr(host.data_ptr(), np.float32)
             c.run()
@@ -676,11 +682,12 @@ def c4_e2e_pipelined(args, ctxs, host, words, rec_cap, steps, ps):
     ends = []
     rec_words = 0
     t_start = time.perf_counter()
-    ctxs[0].add_observations_ptr(host.data_ptr(), np.float32)
+    for k in range(min(D - 1, steps)):  # the first D - 1 steps' inputs
+        ctxs[k].add_observations_ptr(host.data_ptr(), np.float32)
     for k in range(steps):
-        cur, nxt = k % 2, (k + 1) % 2
-        if k + 1 < steps:
-            ctxs[nxt].add_observations_ptr(host.data_ptr(), np.float32)
+        cur = k % D
+        if k + D - 1 < steps:
+            ctxs[(k + D - 1) % D].add_observations_ptr(host.data_ptr(), np.float32)
         ctxs[cur].run()
         ctxs[cur].adjacency_bits_into(bits_h[cur].data_ptr(), words)
         w = ctxs[cur].records_packed_into(recs_h[cur].data_ptr(), rec_cap)
@@ -705,9 +712,9 @@ def c4_e2e_pipelined(args, ctxs, host, words, rec_cap, steps, ps):
                   "note": "last step of each context, from the pinned host copies"}
     return {"value": ctxs[0].count * steps / total, "unit": "skeletons/s",
             "h2d_bytes_per_step": int(host.numel()) * 4, "d2h_bytes_per_step": words * 4 + rec_words * 4,
-            "path": "two contexts in turn, one host thread: hpc_correlation_f32 of step k+1 (host observations, "
+            "path": "%d contexts in turn, one host thread: hpc_correlation_f32 of step k+%d (host observations, "
                     "pinned) queued before hpc_run_skeleton of step k, then hpc_batch_get_adjacency_bits + "
-                    "hpc_batch_get_records_packed (pinned) of step k; host wall clock of the whole loop",
+                    "hpc_batch_get_records_packed (pinned) of step k; host wall clock of the whole loop" % (D, D - 1),
             "ms_per_step": 1e3 * total / steps, "median_ms_per_step": statistics.median(step_ms),
             "step_ms": [round(t, 2) for t in step_ms], "steps": steps, "parity": parity}
 
