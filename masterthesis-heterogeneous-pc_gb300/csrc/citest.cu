@@ -14,7 +14,7 @@ namespace {
 // in FP32 on the stored FP32 |r|. Run at the end of every skeleton run. The instances
 // run side by side, a group of gridDim / count blocks (at least one) each: taking them
 // one after another over the whole grid cost a chain of dependent loads per instance
-// (0.8 ms for the 512 instances of C4).
+// (0.8 ms for a batch of 512 instances of p 20-800).
 __global__ void finalize_records_kernel(const Inst *__restrict__ inst, int count) {
   if (count <= 0) return;
   const unsigned per = max(1u, gridDim.x / (unsigned)count);  // blocks per instance
@@ -144,8 +144,9 @@ __device__ __forceinline__ void retest_decide(const Launch &L, const Inst &I, co
 // kRetestPass entries (the accumulators of a pass stay in registers), so that each of
 // the K columns is read once per item instead of once per entry it takes part in (2E
 // column reads in the entry-parallel form). Above level 4 the entry-parallel form is
-// faster (measured on C4: a re-test's 28-45 entries spread over as many warps beat one
-// warp stepping through the columns, and the column form's registers halve occupancy). The products are
+// faster (measured on a batch of 512 instances of p 20-800: a re-test's 28-45 entries
+// spread over as many warps beat one warp stepping through the columns, and the column
+// form's registers halve occupancy). The products are
 // summed as in zdot: the FP32 pairs' products with their exact rounding errors and cross
 // terms, compensated in FP32 and carried into FP64 every 16 samples of a lane.
 constexpr int kRetestPass = 16;

@@ -500,8 +500,8 @@ struct PendRem {
 };
 
 // MARK: the removal marks both rows' neighbour lists stale (every removal outside level
-// 1, whose launch leaves the snapshot invalid instead: its 4 M removals on C4 made the
-// marks cost a third of the level-1 kernel)
+// 1, whose launch leaves the snapshot invalid instead: its 4 M removals on a batch of 512
+// instances of p 20-800 made the marks cost a third of the level-1 kernel)
 template <bool MARK = true>
 __device__ __forceinline__ bool claim_edge(const Inst &I, int64_t i, int64_t j) {
   const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
@@ -1186,9 +1186,10 @@ __device__ __forceinline__ void test_set_j2(const Inst &I, const float *__restri
   *res2 = set_decide(I, l, sx, dmin, rij2, sy2, sxy2, rr2);
 }
 
-// Levels whose set-order tests run in pairs: 3-5 (measured on C4 against the single
-// loop, level by level: 10 % faster at level 3, 3 % at 5, even at 4; 7-9 % slower at 6-7
-// and 3-7 % at 12-14, where the second solve's registers crowd the schedule; 9-11 spill).
+// Levels whose set-order tests run in pairs: 3-5 (measured on a batch of 512 instances of
+// p 20-800 against the single loop, level by level: 10 % faster at level 3, 3 % at 5,
+// even at 4; 7-9 % slower at 6-7 and 3-7 % at 12-14, where the second solve's registers
+// crowd the schedule; 9-11 spill).
 template <int LA>
 constexpr bool kSetPairs = LA <= 5;
 
