@@ -132,8 +132,12 @@ hpc_status hpc_ctx_footprint(int64_t p, int64_t n_obs, const hpc_opts *opts, int
  * (src/correlation/corOwn.cuh:3, src/correlation/corOwn.cu:10-48).
  * X is column-major n_obs x p (each variable's samples contiguous), exactly the
  * arma::mat layout returned by CSVParser::read_csv_to_mat (src/util/csv_parser.cpp:64-77).
- * Host pointers are copied to the device inside the call; *_device variants take
- * device pointers already resident in HBM. */
+ * Host pointers are copied to the device on the context's stream: from pageable memory
+ * the call returns once the data has left the caller's buffer; from pinned (page-locked)
+ * memory it returns once the copy, the standardisation and the Gram are queued, and the
+ * caller keeps X_host unchanged until a later call on the context that waits for its
+ * stream (hpc_run_skeleton, hpc_wait, a result read) has returned. *_device variants
+ * take device pointers already resident in HBM. */
 hpc_status hpc_correlation_f64(hpc_ctx *ctx, const double *X_host);
 hpc_status hpc_correlation_f32(hpc_ctx *ctx, const float *X_host);
 hpc_status hpc_correlation_device_f64(hpc_ctx *ctx, const double *X_dev);
